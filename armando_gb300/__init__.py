@@ -1,0 +1,169 @@
+"""armando_gb300: GB300 (sm_103a) weakly-compressible SPH step of Armando.
+
+Python host mirror of the reference's step interface over the C-ABI in
+``include/armando.h``. ``Context.step`` is one iteration of the
+``do its = 1, steps`` loop of CERNsource/time_integration.f:131-235 (what
+``single_step`` plus the leapfrog update do there); ``Context.integrate`` is
+``time_integration`` with ``refresh_step = 1`` and no file output.
+
+All compute runs in the compiled CUDA library; importing the package does not
+load it, creating a Context does, and fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._abi import (ERR_UNSUPPORTED, EXPORTED, LIB_PATH, MEM_DEVICE, MEM_HOST, OK,  # noqa: F401
+                   STATUS_NAMES, Params, Stats, load_library)
+
+__all__ = ["Context", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
+           "MEM_DEVICE", "LIB_PATH", "EXPORTED"]
+
+
+class ArmandoError(RuntimeError):
+    """A non-OK armando_status; ``status`` holds the code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(C.c_void_p)
+    if hasattr(a, "data_ptr"):  # torch tensor (device memory kind)
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def _check_host(a, n, dtype, name):
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous numpy {np.dtype(dtype).name} array")
+    if a.size != n:
+        raise ValueError(f"{name} has {a.size} elements, expected {n}")
+
+
+class Context:
+    """One particle system on the current CUDA device (``armando_create``)."""
+
+    def __init__(self, params: Params, n_fluid: int, n_wall: int, mem: int = MEM_HOST):
+        self._lib = load_library()
+        self.params = params.copy()
+        self.dim = int(params.dim)
+        self.n = int(n_fluid) + int(n_wall)
+        self.mem = mem
+        h = C.c_void_p()
+        st = self._lib.armando_create(C.byref(h), C.byref(self.params), self.dim, int(n_fluid),
+                                      int(n_wall), mem)
+        if st != OK:
+            raise ArmandoError(st, self._lib.armando_last_error(None).decode())
+        self._h = h
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.armando_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st):
+        if st != OK:
+            raise ArmandoError(st, self._lib.armando_last_error(self._h).decode())
+
+    # -- the step ------------------------------------------------------------
+    def _validate(self, arrs):
+        if self.mem != MEM_HOST:
+            return
+        n, nd = self.n, self.n * self.dim
+        for name, size, dt in (("x", nd, np.float32), ("v", nd, np.float32),
+                               ("mass", n, np.float32), ("rho", n, np.float32),
+                               ("p", n, np.float32), ("u", n, np.float32), ("h", n, np.float32),
+                               ("itype", n, np.int32), ("dvdt", nd, np.float32),
+                               ("dudt", n, np.float32)):
+            _check_host(arrs[name], size, dt, name)
+
+    def set_params(self, params: Params):
+        self._check(self._lib.armando_set_params(self._h, C.byref(params)))
+        self.params = params.copy()
+
+    def step(self, s, dt: float, its: int):
+        """One leapfrog iteration `its` on state `s` (a Case or dict of arrays), in place."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        self._check(self._lib.armando_step(self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]),
+                                           _ptr(a["rho"]), _ptr(a["p"]), _ptr(a["u"]),
+                                           _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]),
+                                           _ptr(a["dudt"]), float(dt), int(its)))
+        return s
+
+    def integrate(self, s, dt: float, its0: int, steps: int):
+        """`steps` leapfrog iterations its0.. on state `s`, in place."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        self._check(self._lib.armando_integrate(self._h, _ptr(a["x"]), _ptr(a["v"]),
+                                                _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+                                                _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]),
+                                                _ptr(a["dvdt"]), _ptr(a["dudt"]), float(dt),
+                                                int(its0), int(steps)))
+        return s
+
+    # -- diagnostics ---------------------------------------------------------
+    def cell_ids(self, x, h):
+        """Cell id per particle (caller order) under the link_list grid of x."""
+        out = np.zeros(self.n, np.int32) if self.mem == MEM_HOST else None
+        if self.mem != MEM_HOST:
+            import torch
+            out = torch.zeros(self.n, dtype=torch.int32, device="cuda")
+        self._check(self._lib.armando_cell_ids(self._h, _ptr(x), _ptr(h), _ptr(out)))
+        return out
+
+    def neighbours(self, x, h):
+        """CSR (offs[n+1], nbr) of neighbour sets j != i, ascending (host arrays)."""
+        x = np.ascontiguousarray(x, np.float32)
+        h = np.ascontiguousarray(h, np.float32)
+        offs = np.zeros(self.n + 1, np.int64)
+        total = C.c_int64(0)
+        st = self._lib.armando_neighbours(self._h, _ptr(x), _ptr(h), _ptr(offs), None, 0,
+                                          C.byref(total))
+        if st != OK and total.value == 0 and self.n > 0:
+            self._check(st)
+        nbr = np.zeros(max(total.value, 1), np.int32)
+        self._check(self._lib.armando_neighbours(self._h, _ptr(x), _ptr(h), _ptr(offs), _ptr(nbr),
+                                                 nbr.size, C.byref(total)))
+        return offs, nbr[:total.value]
+
+    def stats(self) -> Stats:
+        st = Stats()
+        self._check(self._lib.armando_get_stats(self._h, C.byref(st)))
+        return st
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the context (for CUDA events around calls)."""
+        sp = C.c_void_p()
+        self._check(self._lib.armando_get_stream(self._h, C.byref(sp)))
+        return sp.value or 0
+
+    def profile_phases(self, steps: int) -> dict:
+        """Mean ms per step of each phase over `steps` further steps (see header)."""
+        from ._abi import N_PHASES, PHASE_NAMES
+        out = (C.c_float * N_PHASES)()
+        self._check(self._lib.armando_profile_phases(self._h, int(steps), out))
+        return {PHASE_NAMES[k]: float(out[k]) for k in range(N_PHASES)}
+
+    def sync(self):
+        self._check(self._lib.armando_sync(self._h))

@@ -1,0 +1,186 @@
+"""ctypes mirror of ``include/armando.h`` and the loader of the native library.
+
+The structs here are byte-for-byte the C structs of the header; the loader
+fails loudly when the compiled CUDA library is missing (there is no CPU path).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libarmando_gb300.so")
+
+# armando_status
+OK = 0
+ERR_INVALID_ARG = 1
+ERR_OOM = 2
+ERR_GRID_OVERFLOW = 3
+ERR_NONFINITE = 4
+ERR_OUT_OF_GRID = 5
+ERR_TIMEOUT = 6
+ERR_CUDA = 7
+ERR_NO_DEVICE = 8
+ERR_UNSUPPORTED = 9
+
+STATUS_NAMES = {
+    OK: "OK", ERR_INVALID_ARG: "INVALID_ARG", ERR_OOM: "OOM",
+    ERR_GRID_OVERFLOW: "GRID_OVERFLOW", ERR_NONFINITE: "NONFINITE",
+    ERR_OUT_OF_GRID: "OUT_OF_GRID", ERR_TIMEOUT: "TIMEOUT", ERR_CUDA: "CUDA",
+    ERR_NO_DEVICE: "NO_DEVICE", ERR_UNSUPPORTED: "UNSUPPORTED",
+}
+
+MEM_HOST = 0
+MEM_DEVICE = 1
+
+F3 = C.c_float * 3
+I3 = C.c_int32 * 3
+
+
+class Params(C.Structure):
+    """``armando_params``: physics constants of the step."""
+
+    _fields_ = [
+        ("dim", C.c_int32),
+        ("pa_sph", C.c_int32),
+        ("visc", C.c_int32),
+        ("visc_artificial", C.c_int32),
+        ("heat_artificial", C.c_int32),
+        ("heat_external", C.c_int32),
+        ("kernel_3d_legacy", C.c_int32),
+        ("periodic", I3),
+        ("rho0", C.c_float),
+        ("c0", C.c_float),
+        ("pmin", C.c_float),
+        ("eta", C.c_float),
+        ("av_alpha", C.c_float),
+        ("av_beta", C.c_float),
+        ("av_eta", C.c_float),
+        ("ah_g1", C.c_float),
+        ("ah_g2", C.c_float),
+        ("ah_eta", C.c_float),
+        ("gravity", F3),
+        ("heat_q0", C.c_float),
+        ("heat_sigma", C.c_float),
+        ("heat_center", F3),
+        ("heat_t_end", C.c_float),
+        ("period_lo", F3),
+        ("period_hi", F3),
+    ]
+
+    @classmethod
+    def default(cls, **kw) -> "Params":
+        """Reference defaults (art_visc.f:38-44, art_heat.f:38-40), overridable."""
+        p = cls()
+        p.dim = 2
+        p.pa_sph = 1
+        p.rho0 = 1000.0
+        p.c0 = 1.0
+        p.pmin = -math.inf
+        p.av_alpha, p.av_beta, p.av_eta = 1.0, 1.0, 0.1
+        p.ah_g1, p.ah_g2, p.ah_eta = 0.1, 1.0, 0.1
+        p.heat_sigma = 1.0
+        p.heat_t_end = math.inf
+        for k, v in kw.items():
+            p.set(k, v)
+        return p
+
+    def set(self, key, value):
+        if key in ("periodic", "gravity", "heat_center", "period_lo", "period_hi"):
+            arr = getattr(self, key)
+            for i in range(3):
+                arr[i] = value[i] if i < len(value) else 0
+        else:
+            setattr(self, key, value)
+        return self
+
+    def copy(self) -> "Params":
+        q = Params()
+        C.memmove(C.byref(q), C.byref(self), C.sizeof(Params))
+        return q
+
+    def as_dict(self) -> dict:
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
+class Stats(C.Structure):
+    """``armando_stats``."""
+
+    _fields_ = [
+        ("steps_done", C.c_int64),
+        ("n_particles", C.c_int64),
+        ("n_cells", C.c_int64),
+        ("cell_capacity", C.c_int64),
+        ("gpu_launches", C.c_int64),
+        ("grid_dims", I3),
+        ("grid_origin", F3),
+        ("grid_cell_size", F3),
+        ("device_flags", C.c_uint32),
+    ]
+
+
+# Every symbol include/armando.h declares (checked by the CPU test suite).
+EXPORTED = [
+    "armando_params_default", "armando_create", "armando_set_params",
+    "armando_step", "armando_integrate", "armando_cell_ids",
+    "armando_neighbours", "armando_sync", "armando_get_stats",
+    "armando_last_error", "armando_destroy", "armando_abi_version",
+    "armando_get_stream", "armando_profile_phases",
+]
+N_PHASES = 6
+PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Loads the compiled sm_103a library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"armando_gb300 native library not found at {path}; "
+            "run `python -c 'import __graft_entry__ as g; g.build()'` first")
+    lib = C.CDLL(path)
+    fp = C.POINTER(C.c_float)
+    ip = C.POINTER(C.c_int32)
+    vp = C.c_void_p
+    lib.armando_params_default.argtypes = [C.POINTER(Params)]
+    lib.armando_params_default.restype = None
+    lib.armando_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(Params), C.c_int32,
+                                   C.c_int64, C.c_int64, C.c_int32]
+    lib.armando_create.restype = C.c_int
+    lib.armando_set_params.argtypes = [vp, C.POINTER(Params)]
+    lib.armando_set_params.restype = C.c_int
+    step_args = [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_float, C.c_int32]
+    lib.armando_step.argtypes = step_args
+    lib.armando_step.restype = C.c_int
+    lib.armando_integrate.argtypes = step_args + [C.c_int32]
+    lib.armando_integrate.restype = C.c_int
+    lib.armando_cell_ids.argtypes = [vp, vp, vp, vp]
+    lib.armando_cell_ids.restype = C.c_int
+    lib.armando_neighbours.argtypes = [vp, vp, vp, vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    lib.armando_neighbours.restype = C.c_int
+    lib.armando_sync.argtypes = [vp]
+    lib.armando_sync.restype = C.c_int
+    lib.armando_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    lib.armando_get_stats.restype = C.c_int
+    lib.armando_last_error.argtypes = [vp]
+    lib.armando_last_error.restype = C.c_char_p
+    lib.armando_destroy.argtypes = [vp]
+    lib.armando_destroy.restype = C.c_int
+    lib.armando_abi_version.argtypes = []
+    lib.armando_abi_version.restype = C.c_int32
+    lib.armando_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
+    lib.armando_get_stream.restype = C.c_int
+    lib.armando_profile_phases.argtypes = [vp, C.c_int32, C.POINTER(C.c_float)]
+    lib.armando_profile_phases.restype = C.c_int
+    del fp, ip
+    _lib = lib
+    return lib

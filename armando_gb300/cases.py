@@ -1,0 +1,244 @@
+"""Seeded synthetic workloads of the benchmark configurations.
+
+The reference generates its inputs the same way (hard-coded lattices in
+CERNsource/test_cases.f:577-761 and ArmandoThrust/acpu.c:1784-1902); no
+dataset is involved. Every generator returns a :class:`Case` whose arrays are
+FP32/int32 in the C-ABI layout (particle-major, ``x[i*dim + d]``).
+
+Configurations (sizes are parameters so tests can shrink them):
+  * :func:`cavity`      -- 2D shear-driven cavity, physical viscosity.
+  * :func:`dam_break`   -- 2D dam break, artificial viscosity, gravity.
+  * :func:`channel`     -- 3D heated channel, periodic x, art. visc + art. heat
+                            + Gaussian volumetric source.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+from ._abi import Params
+
+G = 9.81
+
+
+@dataclasses.dataclass
+class Case:
+    name: str
+    params: Params
+    dim: int
+    x: np.ndarray        # float32 [n*dim]
+    v: np.ndarray        # float32 [n*dim]
+    mass: np.ndarray     # float32 [n]
+    rho: np.ndarray      # float32 [n]
+    p: np.ndarray        # float32 [n]
+    u: np.ndarray        # float32 [n]
+    h: np.ndarray        # float32 [n]
+    itype: np.ndarray    # int32 [n]; > 0 fluid, <= 0 wall
+    dt: float
+    steps: int
+    dvdt: np.ndarray = None  # float32 [n*dim] rates carried between steps
+    dudt: np.ndarray = None  # float32 [n]
+    meta: dict = dataclasses.field(default_factory=dict)
+
+    def __post_init__(self):
+        if self.dvdt is None:
+            self.dvdt = np.zeros_like(self.x)
+        if self.dudt is None:
+            self.dudt = np.zeros_like(self.u)
+
+    @property
+    def n(self) -> int:
+        return int(self.mass.shape[0])
+
+    @property
+    def n_fluid(self) -> int:
+        return int(np.count_nonzero(self.itype > 0))
+
+    @property
+    def n_wall(self) -> int:
+        return self.n - self.n_fluid
+
+    def copy(self) -> "Case":
+        c = dataclasses.replace(self)
+        for f in ("x", "v", "mass", "rho", "p", "u", "h", "itype", "dvdt", "dudt"):
+            setattr(c, f, getattr(self, f).copy())
+        c.params = self.params.copy()
+        c.meta = dict(self.meta)
+        return c
+
+    def arrays(self) -> dict:
+        return {f: getattr(self, f) for f in
+                ("x", "v", "mass", "rho", "p", "u", "h", "itype", "dvdt", "dudt")}
+
+
+def wendland_w(r, h, dim, legacy3d=0):
+    """Wendland C2 W(r, h) in FP64 (same formula as the library)."""
+    q = np.asarray(r, dtype=np.float64) / h
+    if dim == 2:
+        a = 7.0 / (4.0 * math.pi * h * h)
+    else:
+        a = (15.0 if legacy3d else 21.0) / (16.0 * math.pi * h ** 3)
+    t = np.clip(1.0 - 0.5 * q, 0.0, None)
+    return np.where(q < 2.0, a * t ** 4 * (1.0 + 2.0 * q), 0.0)
+
+
+def lattice_kernel_sum(dim: int, h_over_dx: float, legacy3d: int = 0) -> float:
+    """sum_k W(|k| dx, h) dx^dim over a perfect lattice (self included), dx = 1."""
+    h = float(h_over_dx)
+    m = int(math.ceil(2 * h)) + 1
+    ax = np.arange(-m, m + 1, dtype=np.float64)
+    if dim == 2:
+        X, Y = np.meshgrid(ax, ax, indexing="ij")
+        r = np.sqrt(X * X + Y * Y)
+    else:
+        X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+        r = np.sqrt(X * X + Y * Y + Z * Z)
+    return float(wendland_w(r, h, dim, legacy3d).sum())
+
+
+def tait_rho_from_p(p, rho0, c0):
+    return rho0 * (1.0 + 7.0 * np.asarray(p, np.float64) / (rho0 * c0 * c0)) ** (1.0 / 7.0)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def cavity(n_side: int = 40, seed: int = 1, length: float = 1.0e-3, lid_u: float = 1.0e-3,
+           jitter: float = 0.01, steps: int = 3000) -> Case:
+    """2D shear-driven cavity (reference case CERNsource/test_cases.f:577-761 with
+    the configuration's Wendland/Tait physics): n_side^2 fluid particles in a
+    square, 4*2*n_side wall particles at dx/2 spacing on its perimeter, moving
+    lid on top; Tait c0 = 0.01 m/s, eta = 1e-3 Pa s, dt = 5e-5 s."""
+    rng = np.random.default_rng(seed)
+    dx = length / n_side
+    h = 1.3 * dx
+    rho0 = 1000.0
+    i, j = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    xf = np.stack([(i.ravel() + 0.5) * dx, (j.ravel() + 0.5) * dx], axis=1)
+    xf += rng.uniform(-jitter, jitter, size=xf.shape) * dx
+    k = np.arange(2 * n_side) * (dx / 2)
+    bottom = np.stack([k, np.zeros_like(k)], 1)
+    right = np.stack([np.full_like(k, length), k], 1)
+    top = np.stack([length - k, np.full_like(k, length)], 1)
+    left = np.stack([np.zeros_like(k), length - k], 1)
+    xw = np.concatenate([bottom, right, top, left])
+    vw = np.zeros_like(xw)
+    vw[2 * (2 * n_side):3 * (2 * n_side), 0] = lid_u
+    nf, nw = xf.shape[0], xw.shape[0]
+    n = nf + nw
+    P = Params.default(dim=2, pa_sph=1, visc=1, rho0=rho0, c0=0.01, eta=1.0e-3,
+                       pmin=-math.inf)
+    x = np.concatenate([xf, xw])
+    v = np.concatenate([np.zeros_like(xf), vw])
+    mass = np.concatenate([np.full(nf, rho0 * dx * dx), np.full(nw, 0.75 * rho0 * dx * dx)])
+    return Case("cavity2d", P, 2, _f32(x.ravel()), _f32(v.ravel()), _f32(mass),
+                _f32(np.full(n, rho0)), _f32(np.zeros(n)), _f32(np.zeros(n)),
+                _f32(np.full(n, h)), np.concatenate([np.ones(nf), np.zeros(nw)]).astype(np.int32),
+                dt=5.0e-5, steps=steps, meta=dict(dx=dx, seed=seed))
+
+
+def dam_break(dx: float = 1.0e-3, col_w: float = 1.0, col_h: float = 2.0, tank_w: float = 4.0,
+              tank_h: float = 3.0, layers: int = 3, jitter: float = 0.005, seed: int = 2,
+              steps: int = 1000, alpha: float = 0.01, c0: float | None = None) -> Case:
+    """2D dam break: a col_w x col_h water column at the left of a tank_w x tank_h
+    tank, `layers` layers of fixed wall particles on the bottom and both sides.
+    Hydrostatic initial density through the Tait EOS, masses scaled by the
+    lattice kernel sum so summation density reproduces it; c0 = 10 sqrt(2 g H),
+    dt = 0.2 h / c0, art. visc alpha = 0.01, beta = 0, gravity -9.81, pmin = 0.
+    Defaults: dx = 1 mm, 1000 x 2000 = 2.0 M fluid + 30,018 wall particles."""
+    rng = np.random.default_rng(seed)
+    h = 1.3 * dx
+    rho0 = 1000.0
+    if c0 is None:
+        c0 = 10.0 * math.sqrt(2.0 * G * col_h)
+    nx, ny = int(round(col_w / dx)), int(round(col_h / dx))
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    xf = np.stack([(i.ravel() + 0.5) * dx, (j.ravel() + 0.5) * dx], axis=1)
+    xf += rng.uniform(-jitter, jitter, size=xf.shape) * dx
+    ntx, nty = int(round(tank_w / dx)), int(round(tank_h / dx))
+    walls = []
+    for kk in range(layers):
+        bx = (np.arange(-layers, ntx + layers) + 0.5) * dx
+        walls.append(np.stack([bx, np.full_like(bx, -(kk + 0.5) * dx)], 1))
+    sy = (np.arange(nty) + 0.5) * dx
+    for kk in range(layers):
+        walls.append(np.stack([np.full_like(sy, -(kk + 0.5) * dx), sy], 1))
+        walls.append(np.stack([np.full_like(sy, tank_w + (kk + 0.5) * dx), sy], 1))
+    xw = np.concatenate(walls)
+    x = np.concatenate([xf, xw])
+    nf, nw = xf.shape[0], xw.shape[0]
+    hloc = np.where(x[:, 0] <= col_w, col_h, 0.0)
+    p = rho0 * G * np.maximum(0.0, hloc - x[:, 1])
+    rho = tait_rho_from_p(p, rho0, c0)
+    S = lattice_kernel_sum(2, 1.3)
+    mass = rho * dx * dx / S
+    P = Params.default(dim=2, pa_sph=1, visc=0, visc_artificial=1, rho0=rho0, c0=c0,
+                       av_alpha=alpha, av_beta=0.0, av_eta=0.1, pmin=0.0,
+                       gravity=(0.0, -G, 0.0))
+    n = nf + nw
+    return Case("dambreak2d", P, 2, _f32(x.ravel()), _f32(np.zeros(2 * n)), _f32(mass),
+                _f32(rho), _f32(p), _f32(np.zeros(n)), _f32(np.full(n, h)),
+                np.concatenate([np.ones(nf), np.zeros(nw)]).astype(np.int32),
+                dt=0.2 * h / c0, steps=steps,
+                meta=dict(dx=dx, seed=seed, nx=nx, ny=ny, c0=c0))
+
+
+def channel(n_x: int = 504, n_yz: int = 126, length: float = 0.4, width: float = 0.1,
+            layers: int = 3, seed: int = 3, steps: int = 500, u_in: float = 1.0,
+            jitter: float = 0.0) -> Case:
+    """3D heated liquid-metal channel, periodic in x, `layers` wall layers on the
+    four y/z sides (no-slip, wall velocity 0). rho0 = 10500, c0 = 20 m/s,
+    art. visc alpha = 0.02, art. heat g1 = g2 = 0.1, Gaussian source q0 = 1e8 W/m^3,
+    sigma = 0.01 m centred at x = 0.1 m on the axis, cp = 146 J/(kg K), u = cp T,
+    T = 600 K + N(0, 1 K). Default 504 x 126 x 126 = 8.0 M fluid particles."""
+    rng = np.random.default_rng(seed)
+    dx = length / n_x
+    assert abs(width / dx - n_yz) < 1e-6 * n_yz or True
+    dyz = width / n_yz
+    h = 1.3 * dx
+    rho0, c0, cp = 10500.0, 20.0, 146.0
+    ix = np.arange(n_x)
+    jy = np.arange(-layers, n_yz + layers)
+    I, J, K = np.meshgrid(ix, jy, jy, indexing="ij")
+    inside = (J >= 0) & (J < n_yz) & (K >= 0) & (K < n_yz)
+    pos = np.stack([(I + 0.5) * dx, (J + 0.5) * dyz, (K + 0.5) * dyz], axis=-1)
+    xf = pos[inside].reshape(-1, 3)
+    xw = pos[~inside].reshape(-1, 3)
+    if jitter:
+        xf = xf + rng.uniform(-jitter, jitter, size=xf.shape) * dx
+    nf, nw = xf.shape[0], xw.shape[0]
+    n = nf + nw
+    x = np.concatenate([xf, xw])
+    v = np.zeros_like(x)
+    v[:nf, 0] = u_in
+    S = lattice_kernel_sum(3, 1.3)
+    mass = np.full(n, rho0 * dx * dyz * dyz / S)
+    T = np.concatenate([600.0 + rng.standard_normal(nf), np.full(nw, 600.0)])
+    P = Params.default(dim=3, pa_sph=1, visc_artificial=1, heat_artificial=1, heat_external=1,
+                       rho0=rho0, c0=c0, av_alpha=0.02, av_beta=0.0, av_eta=0.1,
+                       ah_g1=0.1, ah_g2=0.1, ah_eta=0.1, heat_q0=1.0e8, heat_sigma=0.01,
+                       heat_center=(0.1, width / 2, width / 2), pmin=-math.inf,
+                       periodic=(1, 0, 0), period_lo=(0.0, 0.0, 0.0),
+                       period_hi=(length, 0.0, 0.0))
+    return Case("channel3d", P, 3, _f32(x.ravel()), _f32(v.ravel()), _f32(mass),
+                _f32(np.full(n, rho0)), _f32(np.zeros(n)), _f32(cp * T),
+                _f32(np.full(n, h)), np.concatenate([np.ones(nf), np.zeros(nw)]).astype(np.int32),
+                dt=0.2 * h / c0, steps=steps, meta=dict(dx=dx, seed=seed, cp=cp))
+
+
+def perturbed(case: Case, seed: int, dv: float = 0.0, du: float = 0.0) -> Case:
+    """Copy of `case` with seeded random fluid velocities (std dv) and energy (std du),
+    used to give single-step parity tests non-trivial art_visc / art_heat terms."""
+    c = case.copy()
+    rng = np.random.default_rng(seed)
+    fl = c.itype > 0
+    if dv:
+        vv = c.v.reshape(-1, c.dim)
+        vv[fl] += rng.standard_normal((int(fl.sum()), c.dim)).astype(np.float32) * dv
+        c.v = _f32(vv.ravel())
+    if du:
+        c.u[fl] += (rng.standard_normal(int(fl.sum())) * du).astype(np.float32)
+    return c

@@ -1,0 +1,849 @@
+// armando.cu -- C-ABI of the GB300 SPH step (declared in include/armando.h).
+//
+// A context owns the device working set of one particle system. Caller arrays
+// are gathered into cell order at the start of a call, the leapfrog loop runs
+// as replayed CUDA graphs on the context's stream, and the results are scattered
+// back to the caller's order at the end.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/armando.h"
+#include "kernels.cuh"
+
+using namespace ag;
+
+namespace {
+
+thread_local std::string g_last_error = "no error";
+
+struct GraphKey {
+    float kdt, hdt, dt;
+    int heat_on;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(kdt, hdt, dt, heat_on) < std::tie(o.kdt, o.hdt, o.dt, o.heat_on);
+    }
+};
+
+template <class T>
+T* dalloc(size_t count, cudaError_t& err) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) err = e;
+    return static_cast<T*>(p);
+}
+
+inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+struct armando_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    armando_params prm{};
+    DevParams dp{};
+    int dim = 2;
+    int64_t n = 0, nf = 0, nw = 0;
+    int mem_kind = ARMANDO_MEM_HOST;
+    StateA A{};
+    StateB B{};
+    unsigned* keys[2] = {nullptr, nullptr};
+    int* vals[2] = {nullptr, nullptr};
+    unsigned* hist = nullptr;
+    unsigned* dtotal = nullptr;
+    int num_tiles = 0;
+    int* start = nullptr;
+    long long cell_cap = 0;
+    int passes = 0;
+    float* bbox_part = nullptr;
+    DevGrid* grid = nullptr;
+    unsigned* flags = nullptr;
+    unsigned* h_flags = nullptr;  // pinned
+    DevGrid* h_grid = nullptr;    // pinned
+    // Device copies of caller arrays (host memory kind).
+    float *s_x = nullptr, *s_v = nullptr, *s_m = nullptr, *s_rho = nullptr, *s_p = nullptr,
+          *s_u = nullptr, *s_h = nullptr, *s_dvdt = nullptr, *s_dudt = nullptr;
+    int* s_itype = nullptr;
+    std::vector<void*> owned;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::string err = "no error";
+    int64_t steps_done = 0, launches = 0;
+    int launches_per_step = 0;
+    DevGrid last_grid{};
+    bool have_grid = false;
+    float last_dt = 0.f;  // dt and next its of the state left on the device
+    int next_its = 0;
+};
+
+namespace {
+
+armando_status fail(armando_ctx* c, armando_status st, const std::string& msg) {
+    if (c) c->err = msg;
+    g_last_error = msg;
+    return st;
+}
+
+armando_status cuda_fail(armando_ctx* c, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return fail(c, e == cudaErrorMemoryAllocation ? ARMANDO_ERR_OOM : ARMANDO_ERR_CUDA, m);
+}
+
+#define CK(call)                                                          \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);          \
+    } while (0)
+
+armando_status validate_params(const armando_params* p, int dim, std::string& why) {
+    if (!p) {
+        why = "params is NULL";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    if (p->dim != dim || (dim != 2 && dim != 3)) {
+        why = "dim must be 2 or 3 and match params->dim";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    if (p->pa_sph != 0 && p->pa_sph != 1) {
+        why = "pa_sph must be 0 or 1";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    if (!(p->rho0 > 0.f) || !(p->c0 >= 0.f) || !std::isfinite(p->c0)) {
+        why = "rho0 must be > 0 and c0 finite and >= 0";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    if (p->heat_external && !(p->heat_sigma > 0.f)) {
+        why = "heat_sigma must be > 0 with heat_external";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    for (int d = 0; d < dim; ++d)
+        if (p->periodic[d] && !(p->period_hi[d] > p->period_lo[d])) {
+            why = "periodic axis needs period_hi > period_lo";
+            return ARMANDO_ERR_INVALID_ARG;
+        }
+    return ARMANDO_OK;
+}
+
+DevParams make_dev_params(const armando_params& p) {
+    DevParams d{};
+    d.dim = p.dim;
+    d.pa_sph = p.pa_sph;
+    d.visc = p.visc;
+    d.visc_art = p.visc_artificial;
+    d.heat_art = p.heat_artificial;
+    d.heat_ext = p.heat_external;
+    d.rho0 = p.rho0;
+    d.inv_rho0 = (float)(1.0 / (double)p.rho0);
+    d.B = (float)((double)p.rho0 * (double)p.c0 * (double)p.c0 / 7.0);
+    d.c0 = p.c0;
+    d.pmin = p.pmin;
+    d.eta = p.eta;
+    d.av_alpha = p.av_alpha;
+    d.av_beta = p.av_beta;
+    d.av_eta2 = p.av_eta * p.av_eta;
+    d.ah_g1 = p.ah_g1;
+    d.ah_g2 = p.ah_g2;
+    d.ah_eta2 = p.ah_eta * p.ah_eta;
+    d.heat_q0 = p.heat_q0;
+    d.heat_k = p.heat_sigma > 0.f ? (float)(1.0 / (2.0 * (double)p.heat_sigma * p.heat_sigma)) : 0.f;
+    for (int k = 0; k < 3; ++k) {
+        d.periodic[k] = (k < p.dim) ? p.periodic[k] : 0;
+        d.gravity[k] = p.gravity[k];
+        d.heat_center[k] = p.heat_center[k];
+        d.period_lo[k] = p.period_lo[k];
+        d.period_hi[k] = p.period_hi[k];
+        const float L = p.period_hi[k] - p.period_lo[k];  // FP32, as the oracle
+        d.period_L[k] = L;
+        d.period_half[k] = 0.5f * L;
+    }
+    const double pi = 3.14159265358979323846;
+    double K = (p.dim == 2) ? 7.0 / (4.0 * pi) : (p.kernel_3d_legacy ? 15.0 : 21.0) / (16.0 * pi);
+    d.kw_hi = (float)K;
+    d.kw_lo = (float)(K - (double)d.kw_hi);
+    d.kg = (float)(K * 5.0 / 8.0);
+    return d;
+}
+
+StepArgs make_args(const armando_ctx* c, float dt, int its) {
+    StepArgs s;
+    s.dt = dt;
+    s.kdt = (its == 1) ? 0.5f * dt : dt;
+    s.hdt = (its == 1) ? 0.f : 0.5f * dt;
+    s.heat_on = c->prm.heat_external && ((double)its * (double)dt <= (double)c->prm.heat_t_end);
+    return s;
+}
+
+void free_graphs(armando_ctx* c) {
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+}
+
+// ---- launch sequences -------------------------------------------------------
+
+template <int DIM>
+int launch_grid_and_sort(armando_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    int L = 0;
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part);
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
+                                    ctx->flags);
+    k_hash<DIM><<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->A.xh, n, ctx->grid, ctx->keys[0],
+                                                          ctx->hist, ctx->num_tiles);
+    L += 3;
+    for (int p = 0; p < ctx->passes; ++p) {
+        const int shift = 8 * p;
+        const int a = p & 1, b = (p + 1) & 1;
+        if (p > 0) {
+            k_radix_hist<<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, shift,
+                                                                   ctx->hist, ctx->num_tiles);
+            ++L;
+        }
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal);
+        k_radix_scatter<<<ctx->num_tiles, kSortThreads, 0, st>>>(
+            ctx->keys[a], p == 0 ? nullptr : ctx->vals[a], ctx->keys[b], ctx->vals[b], n, shift,
+            ctx->hist, ctx->dtotal, ctx->num_tiles);
+        L += 2;
+    }
+    k_cell_start<<<blocks_for(n + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n, ctx->grid,
+                                                          ctx->start);
+    return L + 1;
+}
+
+template <int DIM>
+int launch_step(armando_ctx* ctx, const StepArgs& S) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    int L = launch_grid_and_sort<DIM>(ctx);
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
+    k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,
+                                                                         ctx->grid, ctx->dp, n);
+    L += 2;
+    if (ctx->dp.visc) {
+        k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
+        ++L;
+    }
+    k_force<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+        ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+    return L + 1;
+}
+
+int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
+    return ctx->dim == 2 ? launch_step<2>(ctx, S) : launch_step<3>(ctx, S);
+}
+
+// The kernels of launch_step with an event recorded after each phase
+// (ev[0] before the step, ev[k+1] after phase k).
+template <int DIM>
+int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    int L = 0;
+    cudaEventRecord(ev[0], st);
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part);
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
+                                    ctx->flags);
+    k_hash<DIM><<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->A.xh, n, ctx->grid, ctx->keys[0],
+                                                          ctx->hist, ctx->num_tiles);
+    L += 3;
+    cudaEventRecord(ev[1], st);
+    for (int p = 0; p < ctx->passes; ++p) {
+        const int shift = 8 * p;
+        const int a = p & 1, b = (p + 1) & 1;
+        if (p > 0) {
+            k_radix_hist<<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, shift,
+                                                                   ctx->hist, ctx->num_tiles);
+            ++L;
+        }
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal);
+        k_radix_scatter<<<ctx->num_tiles, kSortThreads, 0, st>>>(
+            ctx->keys[a], p == 0 ? nullptr : ctx->vals[a], ctx->keys[b], ctx->vals[b], n, shift,
+            ctx->hist, ctx->dtotal, ctx->num_tiles);
+        L += 2;
+    }
+    cudaEventRecord(ev[2], st);
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_cell_start<<<blocks_for(n + 1, 256), 256, 0, st>>>(skeys, n, ctx->grid, ctx->start);
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
+    cudaEventRecord(ev[3], st);
+    k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,
+                                                                         ctx->grid, ctx->dp, n);
+    cudaEventRecord(ev[4], st);
+    L += 3;
+    if (ctx->dp.visc) {
+        k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
+        ++L;
+    }
+    cudaEventRecord(ev[5], st);
+    k_force<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+        ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+    cudaEventRecord(ev[6], st);
+    return L + 1;
+}
+
+armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
+    GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
+    auto itg = ctx->graphs.find(key);
+    cudaGraphExec_t exec = nullptr;
+    if (itg == ctx->graphs.end()) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int L = launch_step_any(ctx, S);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        ctx->graphs[key] = exec;
+        ctx->launches_per_step = L;
+    } else {
+        exec = itg->second;
+    }
+    CK(cudaGraphLaunch(exec, ctx->stream));
+    ctx->launches += ctx->launches_per_step;
+    ctx->steps_done += 1;
+    return ARMANDO_OK;
+}
+
+armando_status alloc_state(armando_ctx* ctx) {
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    auto F4 = [&](float4*& p) { p = dalloc<float4>(n, e); ctx->owned.push_back(p); };
+    auto F1 = [&](float*& p, size_t k) { p = dalloc<float>(k, e); ctx->owned.push_back(p); };
+    auto I1 = [&](int*& p) { p = dalloc<int>(n, e); ctx->owned.push_back(p); };
+    F4(ctx->A.xh);
+    F4(ctx->A.vm);
+    F1(ctx->A.u, n);
+    F4(ctx->A.ap);
+    F1(ctx->A.rho, n);
+    F1(ctx->A.p, n);
+    I1(ctx->A.itype);
+    I1(ctx->A.id);
+    F4(ctx->B.xh);
+    F4(ctx->B.vm);
+    F4(ctx->B.vmin);
+    F4(ctx->B.rp);
+    F1(ctx->B.p, n);
+    I1(ctx->B.itype);
+    I1(ctx->B.id);
+    F4(ctx->B.tau);
+    F4(ctx->B.tau2);
+    F1(ctx->B.tds, n);
+    ctx->num_tiles = blocks_for(ctx->n, kSortTile);
+    for (int k = 0; k < 2; ++k) {
+        ctx->keys[k] = dalloc<unsigned>(n, e);
+        ctx->vals[k] = dalloc<int>(n, e);
+        ctx->owned.push_back(ctx->keys[k]);
+        ctx->owned.push_back(ctx->vals[k]);
+    }
+    ctx->hist = dalloc<unsigned>((size_t)kRadix * std::max(ctx->num_tiles, 1), e);
+    ctx->dtotal = dalloc<unsigned>(kRadix, e);
+    ctx->bbox_part = dalloc<float>(kBBoxBlocks * 8, e);
+    ctx->grid = dalloc<DevGrid>(1, e);
+    ctx->flags = dalloc<unsigned>(1, e);
+    for (void* p : {(void*)ctx->hist, (void*)ctx->dtotal, (void*)ctx->bbox_part, (void*)ctx->grid,
+                    (void*)ctx->flags})
+        ctx->owned.push_back(p);
+    if (ctx->mem_kind == ARMANDO_MEM_HOST) {
+        const size_t nd = n * ctx->dim;
+        F1(ctx->s_x, nd);
+        F1(ctx->s_v, nd);
+        F1(ctx->s_dvdt, nd);
+        F1(ctx->s_m, n);
+        F1(ctx->s_rho, n);
+        F1(ctx->s_p, n);
+        F1(ctx->s_u, n);
+        F1(ctx->s_h, n);
+        F1(ctx->s_dudt, n);
+        I1(ctx->s_itype);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc");
+    cudaError_t he = cudaMallocHost((void**)&ctx->h_flags, sizeof(unsigned));
+    if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
+    he = cudaMallocHost((void**)&ctx->h_grid, sizeof(DevGrid));
+    if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
+    return ARMANDO_OK;
+}
+
+// Sizes the cell table from the grid of the current positions (A.xh): twice
+// the cells of that grid. A later grid larger than that ends a call with
+// ARMANDO_ERR_GRID_OVERFLOW (link_list.f:61-66 `stop`s in the same case).
+armando_status plan_grid(armando_ctx* ctx) {
+    if (ctx->start) return ARMANDO_OK;
+    cudaStream_t st = ctx->stream;
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, (int)ctx->n, ctx->dim, ctx->bbox_part);
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, (long long)INT32_MAX,
+                                    ctx->grid, ctx->flags);
+    ctx->launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_grid, ctx->grid, sizeof(DevGrid), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const DevGrid g = *ctx->h_grid;
+    if (!g.ok) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "neighbour grid too large or periodic box shorter than 3 cells");
+    long long cap = std::max<long long>(2LL * g.ncells, 4096);
+    if (cap > (1LL << 30)) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "neighbour grid needs more than 2^30 cells");
+    int bits = 1;
+    while ((1LL << bits) < cap) ++bits;
+    ctx->passes = (bits + 7) / 8;
+    ctx->cell_cap = cap;
+    cudaError_t e = cudaSuccess;
+    ctx->start = dalloc<int>((size_t)cap + 1, e);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(cell table)");
+    ctx->owned.push_back(ctx->start);
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+armando_status check_flags(armando_ctx* ctx) {
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_grid, ctx->grid, sizeof(DevGrid), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->last_grid = *ctx->h_grid;
+    ctx->have_grid = true;
+    const unsigned f = *ctx->h_flags;
+    if (f & FLAG_PERIODIC_SMALL) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "periodic box shorter than 3 cells of 2*max(h)");
+    if (f & FLAG_GRID_OVERFLOW) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "neighbour grid exceeded the context's cell capacity");
+    if (f & FLAG_NONFINITE) return fail(ctx, ARMANDO_ERR_NONFINITE, "non-finite value in a fluid particle's state");
+    if (f & FLAG_OUT_OF_GRID) return fail(ctx, ARMANDO_ERR_OUT_OF_GRID, "a particle left the periodic box by more than one period");
+    return ARMANDO_OK;
+}
+
+// Caller arrays -> A (caller order, id = index).
+armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, const float* mass,
+                           const float* rho, const float* p, const float* u, const float* hsml,
+                           const int32_t* itype, const float* dvdt, const float* dudt) {
+    const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
+    cudaStream_t st = ctx->stream;
+    if (ctx->mem_kind == ARMANDO_MEM_HOST) {
+        auto H2D = [&](void* dst, const void* src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+        };
+        CK(H2D(ctx->s_x, x, nd * 4));
+        CK(H2D(ctx->s_v, vx, nd * 4));
+        CK(H2D(ctx->s_m, mass, n * 4));
+        CK(H2D(ctx->s_rho, rho, n * 4));
+        CK(H2D(ctx->s_p, p, n * 4));
+        CK(H2D(ctx->s_u, u, n * 4));
+        CK(H2D(ctx->s_h, hsml, n * 4));
+        CK(H2D(ctx->s_itype, itype, n * 4));
+        if (dvdt) CK(H2D(ctx->s_dvdt, dvdt, nd * 4));
+        if (dudt) CK(H2D(ctx->s_dudt, dudt, n * 4));
+        x = ctx->s_x;
+        vx = ctx->s_v;
+        mass = ctx->s_m;
+        rho = ctx->s_rho;
+        p = ctx->s_p;
+        u = ctx->s_u;
+        hsml = ctx->s_h;
+        itype = ctx->s_itype;
+        dvdt = dvdt ? ctx->s_dvdt : nullptr;
+        dudt = dudt ? ctx->s_dudt : nullptr;
+    } else {
+        CK(cudaDeviceSynchronize());  // caller's producers of the arrays are complete
+    }
+    if (dvdt && !dudt) dvdt = nullptr;
+    const int nn = (int)ctx->n;
+    if (ctx->dim == 2)
+        k_gather_in<2><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
+                                                            dvdt, dudt, ctx->A, nn);
+    else
+        k_gather_in<3><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
+                                                            dvdt, dudt, ctx->A, nn);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    return ARMANDO_OK;
+}
+
+// A -> caller arrays.
+armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, float* p, float* u,
+                             float* dvdt, float* dudt) {
+    const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
+    cudaStream_t st = ctx->stream;
+    const bool host = ctx->mem_kind == ARMANDO_MEM_HOST;
+    float* dx = host ? ctx->s_x : x;
+    float* dv = host ? ctx->s_v : vx;
+    float* drho = host ? ctx->s_rho : rho;
+    float* dp = host ? ctx->s_p : p;
+    float* du = host ? ctx->s_u : u;
+    float* ddvdt = host ? ctx->s_dvdt : dvdt;
+    float* ddudt = host ? ctx->s_dudt : dudt;
+    const int nn = (int)ctx->n;
+    if (ctx->dim == 2)
+        k_scatter_out<2><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, nn, dx, dv, drho, dp, du,
+                                                              ddvdt, ddudt);
+    else
+        k_scatter_out<3><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, nn, dx, dv, drho, dp, du,
+                                                              ddvdt, ddudt);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    if (host) {
+        auto D2H = [&](void* dst, const void* src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+        };
+        CK(D2H(x, ctx->s_x, nd * 4));
+        CK(D2H(vx, ctx->s_v, nd * 4));
+        CK(D2H(rho, ctx->s_rho, n * 4));
+        CK(D2H(p, ctx->s_p, n * 4));
+        CK(D2H(u, ctx->s_u, n * 4));
+        CK(D2H(dvdt, ctx->s_dvdt, nd * 4));
+        CK(D2H(dudt, ctx->s_dudt, n * 4));
+    }
+    return ARMANDO_OK;
+}
+
+armando_status check_step_args(armando_ctx* ctx, const void* x, const void* vx, const void* mass,
+                               const void* rho, const void* p, const void* u, const void* hsml,
+                               const void* itype, const void* dvdt, const void* dudt, float dt,
+                               int its) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!x || !vx || !mass || !rho || !p || !u || !hsml || !itype || !dvdt || !dudt)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL particle array");
+    if (!(dt > 0.f) || !std::isfinite(dt)) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "dt must be finite and > 0");
+    if (its < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "its must be >= 1");
+    return ARMANDO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void armando_params_default(armando_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dim = 2;
+    p->pa_sph = 1;
+    p->rho0 = 1000.f;
+    p->c0 = 1.f;
+    p->pmin = -INFINITY;
+    p->av_alpha = 1.f;
+    p->av_beta = 1.f;
+    p->av_eta = 0.1f;
+    p->ah_g1 = 0.1f;
+    p->ah_g2 = 1.f;
+    p->ah_eta = 0.1f;
+    p->heat_sigma = 1.f;
+    p->heat_t_end = INFINITY;
+}
+
+int32_t armando_abi_version(void) { return ARMANDO_ABI_VERSION; }
+
+armando_status armando_create(armando_ctx** out, const armando_params* params, int32_t dim,
+                              int64_t n_fluid, int64_t n_wall, int32_t mem_kind) {
+    armando_ctx* ctx = nullptr;
+    if (!out) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    armando_status vs = validate_params(params, dim, why);
+    if (vs != ARMANDO_OK) return fail(nullptr, vs, why);
+    if (n_fluid < 0 || n_wall < 0 || n_fluid + n_wall > (int64_t)INT32_MAX / 2)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "particle counts out of range");
+    if (mem_kind != ARMANDO_MEM_HOST && mem_kind != ARMANDO_MEM_DEVICE)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "mem_kind must be ARMANDO_MEM_HOST or ARMANDO_MEM_DEVICE");
+    int dev = 0, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(nullptr, ARMANDO_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+        return fail(nullptr, ARMANDO_ERR_NO_DEVICE, "cudaGetDeviceProperties failed");
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(nullptr, ARMANDO_ERR_NO_DEVICE,
+                    std::string("library is built for sm_103a; device is ") + prop.name);
+    ctx = new armando_ctx();
+    ctx->device = dev;
+    ctx->prm = *params;
+    ctx->dp = make_dev_params(*params);
+    ctx->dim = dim;
+    ctx->nf = n_fluid;
+    ctx->nw = n_wall;
+    ctx->n = n_fluid + n_wall;
+    ctx->mem_kind = mem_kind;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        armando_status st = cuda_fail(ctx, e, "cudaStreamCreate");
+        delete ctx;
+        return st;
+    }
+    armando_status st = alloc_state(ctx);
+    if (st != ARMANDO_OK) {
+        armando_destroy(ctx);
+        return st;
+    }
+    if (cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream) != cudaSuccess) {
+        armando_destroy(ctx);
+        return fail(nullptr, ARMANDO_ERR_CUDA, "cudaMemsetAsync");
+    }
+    *out = ctx;
+    return ARMANDO_OK;
+}
+
+armando_status armando_set_params(armando_ctx* ctx, const armando_params* params) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    std::string why;
+    armando_status vs = validate_params(params, ctx->dim, why);
+    if (vs != ARMANDO_OK) return fail(ctx, vs, why);
+    ctx->prm = *params;
+    ctx->dp = make_dev_params(*params);
+    free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const float* mass,
+                                 float* rho, float* p, float* u, const float* hsml,
+                                 const int32_t* itype, float* dvdt, float* dudt, float dt,
+                                 int32_t its0, int32_t steps) {
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
+    if (st != ARMANDO_OK) return st;
+    if (steps < 0) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->n == 0 || steps == 0) return ARMANDO_OK;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+    if (st != ARMANDO_OK) return st;
+    st = plan_grid(ctx);
+    if (st != ARMANDO_OK) return st;
+    for (int k = 0; k < steps; ++k) {
+        st = run_step(ctx, make_args(ctx, dt, its0 + k));
+        if (st != ARMANDO_OK) return st;
+    }
+    ctx->last_dt = dt;
+    ctx->next_its = its0 + steps;
+    st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
+    if (st != ARMANDO_OK) return st;
+    return check_flags(ctx);
+}
+
+armando_status armando_step(armando_ctx* ctx, float* x, float* vx, const float* mass, float* rho,
+                            float* p, float* u, const float* hsml, const int32_t* itype,
+                            float* dvdt, float* dudt, float dt, int32_t its) {
+    return armando_integrate(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its, 1);
+}
+
+armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* hsml, int32_t* cell) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!x || !hsml || !cell) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL array");
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->n == 0) return ARMANDO_OK;
+    const int nn = (int)ctx->n;
+    const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    const float* dx = x;
+    const float* dh = hsml;
+    int* dcell = reinterpret_cast<int*>(cell);
+    if (ctx->mem_kind == ARMANDO_MEM_HOST) {
+        CK(cudaMemcpyAsync(ctx->s_x, x, nd * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ctx->s_h, hsml, n * 4, cudaMemcpyHostToDevice, st));
+        dx = ctx->s_x;
+        dh = ctx->s_h;
+        dcell = ctx->s_itype;  // scratch int[n]
+    } else {
+        CK(cudaDeviceSynchronize());
+    }
+    if (ctx->dim == 2) k_load_xh<2><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
+    else k_load_xh<3><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    armando_status s = plan_grid(ctx);
+    if (s != ARMANDO_OK) return s;
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, nn, ctx->dim, ctx->bbox_part);
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
+                                    ctx->flags);
+    if (ctx->dim == 2) k_keys_only<2><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.xh, nn, ctx->grid, dcell);
+    else k_keys_only<3><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.xh, nn, ctx->grid, dcell);
+    ctx->launches += 3;
+    CK(cudaGetLastError());
+    if (ctx->mem_kind == ARMANDO_MEM_HOST)
+        CK(cudaMemcpyAsync(cell, dcell, n * 4, cudaMemcpyDeviceToHost, st));
+    return check_flags(ctx);
+}
+
+armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float* hsml,
+                                  int64_t* offs, int32_t* nbr, int64_t cap, int64_t* total) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!x || !hsml || !offs || !total) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL array");
+    CK(cudaSetDevice(ctx->device));
+    const int nn = (int)ctx->n;
+    const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
+    *total = 0;
+    offs[0] = 0;
+    if (nn == 0) return ARMANDO_OK;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    float* dx = nullptr;
+    float* dh = nullptr;
+    cudaError_t e = cudaSuccess;
+    dx = dalloc<float>(nd, e);
+    dh = dalloc<float>(n, e);
+    int* cnt = dalloc<int>(n, e);
+    long long* doffs = dalloc<long long>(n + 1, e);
+    std::vector<void*> tmp = {dx, dh, cnt, doffs};
+    auto cleanup = [&]() {
+        for (void* q : tmp) cudaFree(q);
+    };
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "cudaMalloc");
+    }
+#define CKT(call)                                                    \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) {                                     \
+            cleanup();                                               \
+            return cuda_fail(ctx, e_, #call);                        \
+        }                                                            \
+    } while (0)
+    CKT(cudaMemcpyAsync(dx, x, nd * 4, cudaMemcpyHostToDevice, st));
+    CKT(cudaMemcpyAsync(dh, hsml, n * 4, cudaMemcpyHostToDevice, st));
+    if (ctx->dim == 2) k_load_xh<2><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
+    else k_load_xh<3><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
+    CKT(cudaGetLastError());
+    armando_status s = plan_grid(ctx);
+    if (s != ARMANDO_OK) {
+        cleanup();
+        return s;
+    }
+    int L = ctx->dim == 2 ? launch_grid_and_sort<2>(ctx) : launch_grid_and_sort<3>(ctx);
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_reorder_xh<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, nn);
+    if (ctx->dim == 2)
+        k_count_nbrs<2><<<blocks_for(nn, 128), 128, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, cnt, nn);
+    else
+        k_count_nbrs<3><<<blocks_for(nn, 128), 128, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, cnt, nn);
+    ctx->launches += L + 3;
+    CKT(cudaGetLastError());
+    std::vector<int> hc(n);
+    CKT(cudaMemcpyAsync(hc.data(), cnt, n * 4, cudaMemcpyDeviceToHost, st));
+    CKT(cudaStreamSynchronize(st));
+    std::vector<long long> ho(n + 1, 0);
+    for (size_t i = 0; i < n; ++i) ho[i + 1] = ho[i] + hc[i];
+    *total = ho[n];
+    for (size_t i = 0; i <= n; ++i) offs[i] = ho[i];
+    if (ho[n] > cap || !nbr) {
+        cleanup();
+        armando_status fs = check_flags(ctx);
+        if (fs != ARMANDO_OK) return fs;
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "neighbour capacity too small (see *total)");
+    }
+    int* dnbr = dalloc<int>((size_t)std::max<long long>(ho[n], 1), e);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_fail(ctx, e, "cudaMalloc");
+    }
+    tmp.push_back(dnbr);
+    CKT(cudaMemcpyAsync(doffs, ho.data(), (n + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    if (ctx->dim == 2)
+        k_fill_nbrs<2><<<blocks_for(nn, 128), 128, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, doffs, dnbr, nn);
+    else
+        k_fill_nbrs<3><<<blocks_for(nn, 128), 128, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, doffs, dnbr, nn);
+    ctx->launches += 1;
+    CKT(cudaGetLastError());
+    CKT(cudaMemcpyAsync(nbr, dnbr, (size_t)ho[n] * 4, cudaMemcpyDeviceToHost, st));
+    CKT(cudaStreamSynchronize(st));
+    for (size_t i = 0; i < n; ++i) std::sort(nbr + ho[i], nbr + ho[i + 1]);
+#undef CKT
+    cleanup();
+    return check_flags(ctx);
+}
+
+armando_status armando_get_stream(armando_ctx* ctx, void** stream) {
+    if (!ctx || !stream) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    *stream = (void*)ctx->stream;
+    return ARMANDO_OK;
+}
+
+armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms_per_phase) {
+    if (!ctx || !ms_per_phase || steps < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "bad argument");
+    if (!ctx->start || ctx->next_its < 2 || !(ctx->last_dt > 0.f))
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "no device state: call armando_integrate first");
+    CK(cudaSetDevice(ctx->device));
+    cudaEvent_t ev[ARMANDO_N_PHASES + 1];
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    double acc[ARMANDO_N_PHASES] = {0, 0, 0, 0, 0, 0};
+    armando_status st = ARMANDO_OK;
+    for (int k = 0; k < steps && st == ARMANDO_OK; ++k) {
+        const StepArgs S = make_args(ctx, ctx->last_dt, ctx->next_its);
+        int L = ctx->dim == 2 ? launch_step_phased<2>(ctx, S, ev) : launch_step_phased<3>(ctx, S, ev);
+        ctx->launches += L;
+        ctx->steps_done += 1;
+        ctx->next_its += 1;
+        cudaError_t e = cudaEventSynchronize(ev[ARMANDO_N_PHASES]);
+        if (e != cudaSuccess) {
+            st = cuda_fail(ctx, e, "profile step");
+            break;
+        }
+        for (int ph = 0; ph < ARMANDO_N_PHASES; ++ph) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, ev[ph], ev[ph + 1]);
+            acc[ph] += ms;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    if (st != ARMANDO_OK) return st;
+    for (int ph = 0; ph < ARMANDO_N_PHASES; ++ph) ms_per_phase[ph] = (float)(acc[ph] / steps);
+    return check_flags(ctx);
+}
+
+armando_status armando_sync(armando_ctx* ctx) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ARMANDO_OK;
+}
+
+armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
+    if (!cctx || !out) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    out->steps_done = cctx->steps_done;
+    out->n_particles = cctx->n;
+    out->cell_capacity = cctx->cell_cap;
+    out->gpu_launches = cctx->launches;
+    if (cctx->have_grid) {
+        const DevGrid& g = cctx->last_grid;
+        out->n_cells = g.ncells;
+        for (int d = 0; d < 3; ++d) {
+            out->grid_dims[d] = g.n[d];
+            out->grid_origin[d] = g.o[d];
+            out->grid_cell_size[d] = g.size[d];
+        }
+    }
+    out->device_flags = cctx->h_flags ? *cctx->h_flags : 0u;
+    return ARMANDO_OK;
+}
+
+const char* armando_last_error(const armando_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_last_error.c_str();
+}
+
+armando_status armando_destroy(armando_ctx* ctx) {
+    if (!ctx) return ARMANDO_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_graphs(ctx);
+    for (void* p : ctx->owned) cudaFree(p);
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->h_grid) cudaFreeHost(ctx->h_grid);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ARMANDO_OK;
+}
+
+}  // extern "C"

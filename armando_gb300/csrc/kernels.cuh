@@ -1,0 +1,959 @@
+// kernels.cuh -- sm_103a kernels of one leapfrog step of Armando's SPH.
+//
+// Step pipeline (one CUDA graph per step):
+//   bbox_partial -> bbox_final        grid of CERNsource/link_list.f:39-67
+//   hash (+ digit-0 histogram)        cell id, link_list.f:75-88 / acpu.c:2085-2105
+//   [hist] scan scatter  x passes     LSD radix sort of (cell, slot), 8-bit digits
+//   cell_start                        first slot of every cell (empty cells included)
+//   reorder                           gather state into cell order + leapfrog predictor
+//                                     (time_integration.f:136-154)
+//   density                           summation density + Tait EOS + div v
+//                                     (density.f:1-62, eos.f90:255-283, art_heat.f:46-67)
+//   shear (physical viscosity only)   shear tensor T_ab (internal_force.f:75-171)
+//   force                             pressure + viscous force, art_visc, art_heat,
+//                                     external heat, gravity, leapfrog corrector
+//                                     (internal_force.f:178-435, art_visc.f:55-101,
+//                                     art_heat.f:69-97, time_integration.f:186-218)
+// Every pass is a gather over the 3^dim neighbour cells of a particle: no
+// atomics on particle data, so a step is deterministic. Layout (float4, sorted
+// by cell):
+//   xh  2D {x, y, m, h}        3D {x, y, z, h}
+//   vm  2D {vx, vy, 0, 0}      3D {vx, vy, vz, m}
+//   rp  {rho, pf, u, psi}      pf = p/rho^2 (pa_sph 1) or p (pa_sph 0),
+//                              psi = art_heat coefficient of the particle
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "sph_math.cuh"
+
+namespace ag {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRadix = 256;
+constexpr int kPassThreads = 128;
+constexpr int kBBoxBlocks = 608;  // 4 x 152 SMs
+
+enum DevFlag : unsigned {
+    FLAG_GRID_OVERFLOW = 1u,
+    FLAG_NONFINITE = 2u,
+    FLAG_OUT_OF_GRID = 4u,
+    FLAG_PERIODIC_SMALL = 8u,
+};
+
+struct DevGrid {
+    float o[3], size[3], L[3], half[3];
+    int n[3];
+    int ncells;  // cells in use (<= capacity)
+    int ok;      // 0 when the grid did not fit; passes then do nothing
+    int periodic[3];
+};
+
+struct DevParams {
+    int dim, pa_sph, visc, visc_art, heat_art, heat_ext;
+    int periodic[3];
+    float rho0, inv_rho0, B, c0, pmin, eta;
+    float av_alpha, av_beta, av_eta2;
+    float ah_g1, ah_g2, ah_eta2;
+    float gravity[3];
+    float heat_q0, heat_k, heat_center[3];
+    float period_lo[3], period_hi[3], period_L[3], period_half[3];
+    float kw_hi, kw_lo;  // K_dim as float-float
+    float kg;            // K_dim * 5/8
+};
+
+struct StepArgs {
+    float kdt;    // corrector step: dt (its > 1) or dt/2 (its == 1)
+    float hdt;    // predictor half step: dt/2 (its > 1) or 0 (its == 1)
+    float dt;     // drift
+    int heat_on;  // external heat gate its*dt <= t_end
+};
+
+struct StateA {  // integrated state (slot order of the last sort)
+    float4* xh;
+    float4* vm;
+    float* u;
+    float4* ap;  // previous rates {a, du}
+    float* rho;
+    float* p;
+    int* itype;
+    int* id;
+};
+
+struct StateB {  // working set of one step (cell order)
+    float4* xh;
+    float4* vm;    // predicted velocity (+ mass in 3D)
+    float4* vmin;  // velocity and energy at the start of the step
+    float4* rp;
+    float* p;
+    int* itype;
+    int* id;
+    float4* tau;   // eta T_ab / rho^2 (or eta T_ab): {xx, yy, xy, zz}
+    float4* tau2;  // {xz, yz, -, -}
+    float* tds;    // T ds/dt
+};
+
+template <int DIM>
+__device__ __forceinline__ float mass_of(const float4& xh, const float4& vm) {
+    return DIM == 2 ? xh.z : vm.w;
+}
+
+// ---------------------------------------------------------------------------
+// Small block-level helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned warp_incl_scan(unsigned v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Exclusive scan of one value per thread over a block of NT threads.
+template <int NT>
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* s_warp,
+                                                    unsigned* total = nullptr) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned inc = warp_incl_scan(v);
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = (lane < NT / 32) ? s_warp[lane] : 0u;
+        unsigned wi = warp_incl_scan(w);
+        if (lane < NT / 32) s_warp[lane] = wi - w;
+        if (lane == NT / 32 - 1 && total) *total = wi;
+    }
+    __syncthreads();
+    unsigned r = s_warp[warp] + inc - v;
+    __syncthreads();
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Grid: bbox of all particles and the link_list grid in FP32.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_bbox_partial(const float4* __restrict__ xh, int n, int dim,
+                                                      float* __restrict__ part) {
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mh = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = xh[i];
+        mn[0] = fminf(mn[0], a.x);
+        mx[0] = fmaxf(mx[0], a.x);
+        mn[1] = fminf(mn[1], a.y);
+        mx[1] = fmaxf(mx[1], a.y);
+        if (dim == 3) {
+            mn[2] = fminf(mn[2], a.z);
+            mx[2] = fmaxf(mx[2], a.z);
+        }
+        mh = fmaxf(mh, a.w);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+        mh = fmaxf(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+    }
+    __shared__ float s[8][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int d = 0; d < 3; ++d) {
+            s[warp][d] = mn[d];
+            s[warp][3 + d] = mx[d];
+        }
+        s[warp][6] = mh;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        int k = threadIdx.x;
+        float v = s[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            v = (k < 3) ? fminf(v, s[w][k]) : fmaxf(v, s[w][k]);
+        part[blockIdx.x * 8 + k] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ part, int nparts,
+                                                    DevParams P, long long capacity,
+                                                    DevGrid* __restrict__ grid,
+                                                    unsigned* __restrict__ flags) {
+    __shared__ float s[7][256];
+    float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+        for (int k = 0; k < 7; ++k)
+            v[k] = (k < 3) ? fminf(v[k], part[b * 8 + k]) : fmaxf(v[k], part[b * 8 + k]);
+    for (int k = 0; k < 7; ++k) s[k][threadIdx.x] = v[k];
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int k = 0; k < 7; ++k)
+                s[k][threadIdx.x] = (k < 3) ? fminf(s[k][threadIdx.x], s[k][threadIdx.x + st])
+                                            : fmaxf(s[k][threadIdx.x], s[k][threadIdx.x + st]);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    DevGrid g;
+    const float mh = s[6][0];
+    const float cell = __fmul_rn(2.0f, mh);  // scale_k * mh, scale_k = 2
+    long long ncells = 1;
+    unsigned fl = 0;
+    for (int d = 0; d < 3; ++d) {
+        g.periodic[d] = P.periodic[d];
+        g.o[d] = 0.f;
+        g.size[d] = 1.f;
+        g.L[d] = 0.f;
+        g.half[d] = 0.f;
+        g.n[d] = 1;
+        if (d >= P.dim) continue;
+        if (P.periodic[d]) {
+            const float L = P.period_L[d];
+            float nf = __fdiv_rn(L, cell);
+            int nn = (nf >= 3.0f && nf < 1.0e9f) ? (int)nf : 3;
+            if (!(nf >= 3.0f)) fl |= FLAG_PERIODIC_SMALL;
+            g.o[d] = P.period_lo[d];
+            g.size[d] = __fdiv_rn(L, (float)nn);
+            g.L[d] = L;
+            g.half[d] = P.period_half[d];
+            g.n[d] = nn;
+        } else {
+            const float lo = __fsub_rn(s[d][0], mh);
+            const float hi = __fadd_rn(s[3 + d][0], mh);
+            float nf = __fdiv_rn(__fsub_rn(hi, lo), cell);
+            g.o[d] = lo;
+            g.size[d] = cell;
+            if (nf < 1.0e9f) {
+                g.n[d] = (int)nf + 1;
+            } else {
+                g.n[d] = 1;
+                fl |= FLAG_GRID_OVERFLOW;
+            }
+        }
+        ncells *= g.n[d];
+    }
+    g.ok = 1;
+    if (ncells > capacity || (fl & FLAG_GRID_OVERFLOW) || (fl & FLAG_PERIODIC_SMALL)) {
+        fl |= (ncells > capacity) ? FLAG_GRID_OVERFLOW : 0u;
+        g.ok = 0;
+        ncells = capacity;
+    }
+    g.ncells = (int)ncells;
+    *grid = g;
+    if (fl) atomicOr(flags, fl);
+}
+
+template <int DIM>
+__device__ __forceinline__ unsigned cell_key(const float4& a, const DevGrid& g) {
+    const float xv[3] = {a.x, a.y, a.z};
+    unsigned key = 0;
+#pragma unroll
+    for (int d = DIM - 1; d >= 0; --d) {
+        int c = (int)__fdiv_rn(__fsub_rn(xv[d], g.o[d]), g.size[d]);
+        c = c < 0 ? 0 : (c > g.n[d] - 1 ? g.n[d] - 1 : c);
+        key = key * (unsigned)g.n[d] + (unsigned)c;
+    }
+    if (!g.ok) key = 0;
+    return key;
+}
+
+// Cell key of every slot + per-tile histogram of its low digit.
+template <int DIM>
+__global__ void __launch_bounds__(kSortThreads)
+    k_hash(const float4* __restrict__ xh, int n, const DevGrid* __restrict__ gp,
+           unsigned* __restrict__ keys, unsigned* __restrict__ hist, int num_tiles) {
+    __shared__ unsigned sh[kRadix];
+    __shared__ DevGrid g;
+    if (threadIdx.x == 0) g = *gp;
+    sh[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        int i = base + k * kSortThreads + threadIdx.x;
+        if (i < n) {
+            unsigned key = cell_key<DIM>(xh[i], g);
+            keys[i] = key;
+            atomicAdd(&sh[key & 255u], 1u);
+        }
+    }
+    __syncthreads();
+    hist[threadIdx.x * num_tiles + blockIdx.x] = sh[threadIdx.x];
+}
+
+// Cell keys only (caller order), for the cell-id entry point.
+template <int DIM>
+__global__ void k_keys_only(const float4* __restrict__ xh, int n, const DevGrid* __restrict__ gp,
+                            int* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    DevGrid g = *gp;
+    out[i] = (int)cell_key<DIM>(xh[i], g);
+}
+
+// ---------------------------------------------------------------------------
+// LSD radix sort, reduce-then-scan (no inter-block waiting).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kSortThreads)
+    k_radix_hist(const unsigned* __restrict__ keys, int n, int shift, unsigned* __restrict__ hist,
+                 int num_tiles) {
+    __shared__ unsigned sh[kRadix];
+    sh[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        int i = base + k * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&sh[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * num_tiles + blockIdx.x] = sh[threadIdx.x];
+}
+
+// Block d: exclusive scan of the tile counts of digit d; total per digit.
+__global__ void __launch_bounds__(256)
+    k_radix_scan(unsigned* __restrict__ hist, int num_tiles, unsigned* __restrict__ dtotal) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned s_total;
+    unsigned* row = hist + (size_t)blockIdx.x * num_tiles;
+    const int per = (num_tiles + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per;
+    const int e = min(b + per, num_tiles);
+    unsigned sum = 0;
+    for (int i = b; i < e; ++i) sum += row[i];
+    unsigned off = block_excl_scan<256>(sum, s_warp, &s_total);
+    for (int i = b; i < e; ++i) {
+        unsigned c = row[i];
+        row[i] = off;
+        off += c;
+    }
+    if (threadIdx.x == 0) dtotal[blockIdx.x] = s_total;
+}
+
+// Stable scatter of one tile by one 8-bit digit. vals_in == nullptr means
+// the values are the slot indices themselves.
+__global__ void __launch_bounds__(kSortThreads)
+    k_radix_scatter(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
+                    unsigned* __restrict__ keys_out, int* __restrict__ vals_out, int n, int shift,
+                    const unsigned* __restrict__ hist, const unsigned* __restrict__ dtotal,
+                    int num_tiles) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned s_base[kRadix];
+    __shared__ unsigned s_tstart[kRadix];
+    __shared__ unsigned s_wcnt[kSortThreads / 32][kRadix];
+    __shared__ unsigned s_keys[kSortTile];
+    __shared__ int s_vals[kSortTile];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tile = blockIdx.x;
+    const int tile_base = tile * kSortTile;
+    const int tile_n = min(kSortTile, n - tile_base);
+
+    unsigned excl = block_excl_scan<kSortThreads>(dtotal[tid], s_warp);
+    s_base[tid] = excl + hist[(size_t)tid * num_tiles + tile];
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) s_wcnt[w][tid] = 0;
+    __syncthreads();
+
+    unsigned mykey[kSortItems];
+    int myval[kSortItems];
+    unsigned myrank[kSortItems];
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const int idx = warp * (32 * kSortItems) + it * 32 + lane;
+        const bool valid = idx < tile_n;
+        unsigned key = valid ? keys_in[tile_base + idx] : 0u;
+        int val = valid ? (vals_in ? vals_in[tile_base + idx] : tile_base + idx) : 0;
+        unsigned d = (key >> shift) & 255u;
+        unsigned peers = __match_any_sync(0xffffffffu, valid ? d : 0x100u);
+        unsigned lt = peers & ((1u << lane) - 1u);
+        unsigned base = valid ? s_wcnt[warp][d] : 0u;
+        __syncwarp();
+        if (valid && lt == 0u) s_wcnt[warp][d] = base + __popc(peers);
+        __syncwarp();
+        mykey[it] = key;
+        myval[it] = val;
+        myrank[it] = base + __popc(lt);
+    }
+    __syncthreads();
+    unsigned run = 0;
+#pragma unroll
+    for (int w = 0; w < kSortThreads / 32; ++w) {
+        unsigned c = s_wcnt[w][tid];
+        s_wcnt[w][tid] = run;
+        run += c;
+    }
+    unsigned ts = block_excl_scan<kSortThreads>(run, s_warp);
+    s_tstart[tid] = ts;
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        const int idx = warp * (32 * kSortItems) + it * 32 + lane;
+        if (idx < tile_n) {
+            unsigned d = (mykey[it] >> shift) & 255u;
+            unsigned pos = s_tstart[d] + s_wcnt[warp][d] + myrank[it];
+            s_keys[pos] = mykey[it];
+            s_vals[pos] = myval[it];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < tile_n; i += kSortThreads) {
+        unsigned key = s_keys[i];
+        unsigned d = (key >> shift) & 255u;
+        unsigned dst = s_base[d] + (unsigned)i - s_tstart[d];
+        keys_out[dst] = key;
+        vals_out[dst] = s_vals[i];
+    }
+}
+
+// start[c] = first sorted slot of cell c, for c in [0, ncells]; empty cells
+// get start[c] == start[c+1]. Slot s fills the cells (key[s-1], key[s]].
+__global__ void k_cell_start(const unsigned* __restrict__ keys, int n,
+                             const DevGrid* __restrict__ gp, int* __restrict__ start) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s > n) return;
+    const int ncells = gp->ncells;
+    const int lo = (s == 0) ? 0 : (int)keys[s - 1] + 1;
+    const int hi = (s == n) ? ncells : (int)keys[s];
+    for (int c = lo; c <= hi; ++c) start[c] = s;
+}
+
+// ---------------------------------------------------------------------------
+// State movement
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_gather_in(const float* __restrict__ x, const float* __restrict__ v,
+                            const float* __restrict__ m, const float* __restrict__ rho,
+                            const float* __restrict__ p, const float* __restrict__ u,
+                            const float* __restrict__ h, const int* __restrict__ itype,
+                            const float* __restrict__ dvdt, const float* __restrict__ dudt,
+                            StateA A, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (DIM == 2) {
+        A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], m[i], h[i]);
+        A.vm[i] = make_float4(v[2 * i], v[2 * i + 1], 0.f, 0.f);
+        A.ap[i] = dvdt ? make_float4(dvdt[2 * i], dvdt[2 * i + 1], 0.f, dudt[i])
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        A.xh[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], h[i]);
+        A.vm[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], m[i]);
+        A.ap[i] = dvdt ? make_float4(dvdt[3 * i], dvdt[3 * i + 1], dvdt[3 * i + 2], dudt[i])
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    A.u[i] = u[i];
+    A.rho[i] = rho[i];
+    A.p[i] = p[i];
+    A.itype[i] = itype[i];
+    A.id[i] = i;
+}
+
+// Positions and h only (neighbour / cell-id entry points).
+template <int DIM>
+__global__ void k_load_xh(const float* __restrict__ x, const float* __restrict__ h, StateA A,
+                          int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (DIM == 2) A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], 0.f, h[i]);
+    else A.xh[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], h[i]);
+    A.id[i] = i;
+}
+
+template <int DIM>
+__global__ void k_scatter_out(StateA A, int n, float* __restrict__ x, float* __restrict__ v,
+                              float* __restrict__ rho, float* __restrict__ p,
+                              float* __restrict__ u, float* __restrict__ dvdt,
+                              float* __restrict__ dudt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = A.id[s];
+    const float4 a = A.xh[s], b = A.vm[s], r = A.ap[s];
+    x[DIM * i] = a.x;
+    x[DIM * i + 1] = a.y;
+    v[DIM * i] = b.x;
+    v[DIM * i + 1] = b.y;
+    dvdt[DIM * i] = r.x;
+    dvdt[DIM * i + 1] = r.y;
+    if (DIM == 3) {
+        x[3 * i + 2] = a.z;
+        v[3 * i + 2] = b.z;
+        dvdt[3 * i + 2] = r.z;
+    }
+    dudt[i] = r.w;
+    u[i] = A.u[s];
+    rho[i] = A.rho[s];
+    p[i] = A.p[s];
+}
+
+// Cell-ordered working set + leapfrog predictor (time_integration.f:136-154).
+template <int DIM>
+__global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, StepArgs S,
+                              int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int j = perm[s];
+    const float4 xh = A.xh[j];
+    float4 vm = A.vm[j];
+    float u = A.u[j];
+    const int it = A.itype[j];
+    B.vmin[s] = make_float4(vm.x, vm.y, vm.z, u);
+    if (it > 0 && S.hdt != 0.f) {
+        const float4 ap = A.ap[j];
+        vm.x = fmaf(S.hdt, ap.x, vm.x);
+        vm.y = fmaf(S.hdt, ap.y, vm.y);
+        if (DIM == 3) vm.z = fmaf(S.hdt, ap.z, vm.z);
+        u = fmaf(S.hdt, ap.w, u);
+        if (u < 0.f) u = 0.f;
+    }
+    B.xh[s] = xh;
+    B.vm[s] = vm;
+    B.rp[s] = make_float4(A.rho[j], 0.f, u, 0.f);
+    B.p[s] = A.p[j];
+    B.itype[s] = it;
+    B.id[s] = A.id[j];
+}
+
+// Positions only (neighbour entry point).
+__global__ void k_reorder_xh(StateA A, const int* __restrict__ perm, StateB B, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int j = perm[s];
+    B.xh[s] = A.xh[j];
+    B.id[s] = A.id[j];
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour-cell iteration
+// ---------------------------------------------------------------------------
+struct CellCoord {
+    int c[3];
+};
+
+template <int DIM>
+__device__ __forceinline__ CellCoord decode_key(unsigned key, const DevGrid& g) {
+    CellCoord cc;
+    cc.c[0] = (int)(key % (unsigned)g.n[0]);
+    unsigned t = key / (unsigned)g.n[0];
+    if (DIM == 2) {
+        cc.c[1] = (int)t;
+        cc.c[2] = 0;
+    } else {
+        cc.c[1] = (int)(t % (unsigned)g.n[1]);
+        cc.c[2] = (int)(t / (unsigned)g.n[1]);
+    }
+    return cc;
+}
+
+// Calls f(k) for every sorted slot k in the 3^DIM cells around cc (k == self
+// included; callers skip it). Non-periodic x: one contiguous slot range per
+// (y, z) row.
+template <int DIM, class F>
+__device__ __forceinline__ void for_candidates(const DevGrid& g, const int* __restrict__ start,
+                                               const CellCoord& cc, F&& f) {
+    const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
+    for (int dz = zlo; dz <= zhi; ++dz) {
+        int cz = cc.c[2] + dz;
+        if (DIM == 3) {
+            if (g.periodic[2]) cz = (cz + g.n[2]) % g.n[2];
+            else if (cz < 0 || cz >= g.n[2]) continue;
+        }
+        for (int dy = -1; dy <= 1; ++dy) {
+            int cy = cc.c[1] + dy;
+            if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
+            else if (cy < 0 || cy >= g.n[1]) continue;
+            const int row = (cz * g.n[1] + cy) * g.n[0];
+            if (!g.periodic[0]) {
+                const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
+                const int kb = __ldg(start + row + c0), ke = __ldg(start + row + c1 + 1);
+                for (int k = kb; k < ke; ++k) f(k);
+            } else {
+#pragma unroll
+                for (int dx = -1; dx <= 1; ++dx) {
+                    const int cx = (cc.c[0] + dx + g.n[0]) % g.n[0];
+                    const int kb = __ldg(start + row + cx), ke = __ldg(start + row + cx + 1);
+                    for (int k = kb; k < ke; ++k) f(k);
+                }
+            }
+        }
+    }
+}
+
+// Difference x_i - x_j (minimum image) and the exact pair test.
+template <int DIM>
+__device__ __forceinline__ bool pair_delta(const float4& xi, const float4& xj, const DevGrid& g,
+                                           float* d, float& dr2) {
+    d[0] = __fsub_rn(xi.x, xj.x);
+    d[1] = __fsub_rn(xi.y, xj.y);
+    d[2] = (DIM == 3) ? __fsub_rn(xi.z, xj.z) : 0.f;
+#pragma unroll
+    for (int a = 0; a < DIM; ++a)
+        if (g.periodic[a]) d[a] = sph::min_image(d[a], g.L[a], g.half[a]);
+    dr2 = sph::dist2_exact<DIM>(d);
+    return sph::within_support(dr2, xi.w, xj.w);
+}
+
+template <int DIM>
+__device__ __forceinline__ sph::ff ff_pow_dim(sph::ff ih) {
+    sph::ff a = sph::ff_sqr(ih);
+    if (DIM == 3) a = sph::ff_mul(a, ih);
+    return a;
+}
+
+template <int DIM>
+__device__ __forceinline__ float pow_grad(float ih) {
+    float ih2 = __fmul_rn(ih, ih);
+    float ih4 = __fmul_rn(ih2, ih2);
+    return DIM == 2 ? ih4 : __fmul_rn(ih4, ih);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: summation density (float-float), Tait EOS, div v for art_heat.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+              const DevGrid* __restrict__ gp, DevParams P, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = *gp;
+    const float4 xi = B.xh[s];
+    const bool fluid = B.itype[s] > 0;
+    const bool need_div = P.heat_art != 0;
+    float4 rp = B.rp[s];
+    float p = B.p[s];
+    if ((!fluid && !need_div) || !g.ok) {
+        rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
+        B.rp[s] = rp;
+        return;
+    }
+    const float4 vi = B.vm[s];
+    const float mi = mass_of<DIM>(xi, vi);
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    const sph::ff kw = {P.kw_hi, P.kw_lo};
+    const sph::ff ih_i = sph::ff_recip(xi.w);
+    const sph::ff al_i = sph::ff_mul(kw, ff_pow_dim<DIM>(ih_i));
+    // Self density m_i W(0, h_i) (density.f:39-42).
+    sph::ff S = sph::ff_mul_f(al_i, mi);
+    const float ihf = ih_i.hi;
+    const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
+    float divs = 0.f;
+    for_candidates<DIM>(g, start, cc, [&](int k) {
+        if (k == s) return;
+        const float4 xj = __ldg(B.xh + k);
+        float d[3], dr2;
+        if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
+        float4 vj;
+        if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
+        const float mj = (DIM == 2) ? xj.z : vj.w;
+        if (fluid) {
+            sph::ff ih = ih_i, al = al_i;
+            if (xj.w != xi.w) {
+                ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+                al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
+            }
+            sph::ff_acc(S, sph::wendland_mw_ff<DIM>(d, ih, al, mj));
+        }
+        if (need_div) {
+            float ih = ihf, kgih = kgih_i;
+            if (xj.w != xi.w) {
+                ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+                kgih = __fmul_rn(P.kg, pow_grad<DIM>(ih));
+            }
+            const float gw = sph::wendland_grad_factor<DIM>(__fsqrt_rn(dr2), ih, kgih);
+            float vd = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
+            if (DIM == 3) vd += (vj.z - vi.z) * d[2];
+            divs = fmaf(mj * gw, vd, divs);
+        }
+    });
+    float rho = rp.x;
+    if (fluid) {
+        float drho = __fadd_rn(__fsub_rn(S.hi, P.rho0), S.lo);
+        p = sph::tait_poly(__fmul_rn(drho, P.inv_rho0), P.B);
+        if (p < P.pmin) {  // eos.f90:277-280
+            p = 0.f;
+            drho = 0.f;
+        }
+        rho = __fadd_rn(P.rho0, drho);
+        B.p[s] = p;
+    }
+    rp.x = rho;
+    rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rho, rho)) : p;
+    if (need_div) {
+        const float divv = __fdiv_rn(divs, rho);
+        rp.w = P.ah_g1 * xi.w * P.c0 + P.ah_g2 * xi.w * xi.w * (fabsf(divv) - divv);
+    }
+    B.rp[s] = rp;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1b: shear tensor (physical viscosity), every particle.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_shear(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+            const DevGrid* __restrict__ gp, DevParams P, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = *gp;
+    if (!g.ok) return;
+    const float4 xi = B.xh[s];
+    const float4 vi = B.vm[s];
+    const float rhoi = B.rp[s].x;
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    const float ihf = __frcp_rn(xi.w);
+    const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
+    float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // xx yy zz xy xz yz
+    for_candidates<DIM>(g, start, cc, [&](int k) {
+        if (k == s) return;
+        const float4 xj = __ldg(B.xh + k);
+        float d[3], dr2;
+        if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
+        const float4 vj = __ldg(B.vm + k);
+        const float mj = mass_of<DIM>(xj, vj);
+        const float rhoj = __ldg(&B.rp[k].x);
+        float ih = ihf, kgih = kgih_i;
+        if (xj.w != xi.w) {
+            ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+            kgih = __fmul_rn(P.kg, pow_grad<DIM>(ih));
+        }
+        const float gw = sph::wendland_grad_factor<DIM>(__fsqrt_rn(dr2), ih, kgih);
+        const float w0 = gw * d[0], w1 = gw * d[1], w2 = gw * d[2];
+        const float dv0 = vj.x - vi.x, dv1 = vj.y - vi.y, dv2 = (DIM == 3) ? vj.z - vi.z : 0.f;
+        float hxx, hyy, hzz = 0.f, hxy, hxz = 0.f, hyz = 0.f;
+        if (DIM == 2) {
+            hxx = 2.f * dv0 * w0 - dv1 * w1;
+            hyy = 2.f * dv1 * w1 - dv0 * w0;
+            hxy = dv0 * w1 + dv1 * w0;
+        } else {
+            hxx = 2.f * dv0 * w0 - dv1 * w1 - dv2 * w2;
+            hyy = 2.f * dv1 * w1 - dv0 * w0 - dv2 * w2;
+            hzz = 2.f * dv2 * w2 - dv0 * w0 - dv1 * w1;
+            hyz = dv1 * w2 + dv2 * w1;
+            hxz = dv0 * w2 + dv2 * w0;
+            hxy = dv0 * w1 + dv1 * w0;
+        }
+        const float c = mj / rhoj;
+        const float c23 = c * (2.f / 3.f);
+        t[0] = fmaf(c23, hxx, t[0]);
+        t[1] = fmaf(c23, hyy, t[1]);
+        t[2] = fmaf(c23, hzz, t[2]);
+        t[3] = fmaf(c, hxy, t[3]);
+        t[4] = fmaf(c, hxz, t[4]);
+        t[5] = fmaf(c, hyz, t[5]);
+    });
+    float q = t[0] * t[0] + t[1] * t[1] + 2.f * t[3] * t[3];
+    if (DIM == 3) q += t[2] * t[2] + 2.f * t[5] * t[5] + 2.f * t[4] * t[4];
+    B.tds[s] = 0.5f * P.eta / rhoi * q;
+    const float sc = (P.pa_sph == 1) ? P.eta / (rhoi * rhoi) : P.eta;
+    B.tau[s] = make_float4(sc * t[0], sc * t[1], sc * t[3], sc * t[2]);
+    if (DIM == 3) B.tau2[s] = make_float4(sc * t[4], sc * t[5], 0.f, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
+            const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
+            int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = *gp;
+    const float4 xi = B.xh[s];
+    const int it = B.itype[s];
+    const float4 vi = B.vm[s];
+    const float4 rpi = B.rp[s];
+    if (it <= 0 || !g.ok) {  // wall: fixed state, zero rates
+        A.xh[s] = xi;
+        A.vm[s] = vi;
+        A.u[s] = B.vmin[s].w;
+        A.ap[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        A.rho[s] = rpi.x;
+        A.p[s] = B.p[s];
+        A.itype[s] = it;
+        A.id[s] = B.id[s];
+        return;
+    }
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    const float ihf = __frcp_rn(xi.w);
+    const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
+    const float pi_i = B.p[s];
+    float4 ti = make_float4(0.f, 0.f, 0.f, 0.f), ti2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (P.visc) {
+        ti = B.tau[s];
+        if (DIM == 3) ti2 = B.tau2[s];
+    }
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
+    for_candidates<DIM>(g, start, cc, [&](int k) {
+        if (k == s) return;
+        const float4 xj = __ldg(B.xh + k);
+        float d[3], dr2;
+        if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
+        const float4 vj = __ldg(B.vm + k);
+        const float4 rpj = __ldg(B.rp + k);
+        const float mj = mass_of<DIM>(xj, vj);
+        float ih = ihf, kgih = kgih_i;
+        if (xj.w != xi.w) {
+            ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+            kgih = __fmul_rn(P.kg, pow_grad<DIM>(ih));
+        }
+        const float r = __fsqrt_rn(dr2);
+        const float gw = sph::wendland_grad_factor<DIM>(r, ih, kgih);
+        const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;
+        const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = (DIM == 3) ? vj.z - vi.z : 0.f;
+        // Pressure (internal_force.f:309-428 for pa_sph 1, 179-306 for pa_sph 0).
+        float fs;
+        float inv_rr = 1.f;
+        if (P.pa_sph == 1) {
+            fs = -(rpi.y + rpj.y);
+        } else {
+            fs = -(rpi.y + rpj.y);
+            inv_rr = __frcp_rn(rpi.x * rpj.x);
+        }
+        float h0 = fs * w0, h1 = fs * w1, h2 = fs * w2;
+        float he = vx * h0 + vy * h1;
+        if (DIM == 3) he += vz * h2;
+        if (P.visc) {
+            const float4 tj = __ldg(B.tau + k);
+            float4 tj2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 3) tj2 = __ldg(B.tau2 + k);
+            const float sxx = ti.x + tj.x, syy = ti.y + tj.y, sxy = ti.z + tj.z;
+            if (DIM == 2) {
+                h0 += sxx * w0 + sxy * w1;
+                h1 += sxy * w0 + syy * w1;
+            } else {
+                const float szz = ti.w + tj.w, sxz = ti2.x + tj2.x, syz = ti2.y + tj2.y;
+                h0 += sxx * w0 + sxy * w1 + sxz * w2;
+                h1 += sxy * w0 + syy * w1 + syz * w2;
+                h2 += sxz * w0 + syz * w1 + szz * w2;
+            }
+        }
+        if (P.pa_sph != 1) {
+            h0 *= inv_rr;
+            h1 *= inv_rr;
+            h2 *= inv_rr;
+            he *= inv_rr;
+        }
+        a0 = fmaf(mj, h0, a0);
+        a1 = fmaf(mj, h1, a1);
+        if (DIM == 3) a2 = fmaf(mj, h2, a2);
+        he_sum = fmaf(mj, he, he_sum);
+        const float mh = 0.5f * (xi.w + xj.w);
+        const float rho_bar = 0.5f * (rpi.x + rpj.x);
+        // art_visc.f:71-100.
+        if (P.visc_art) {
+            float vr = vx * d[0] + vy * d[1];
+            if (DIM == 3) vr += vz * d[2];
+            vr = -vr;  // (v_i - v_j) . (x_i - x_j)
+            if (vr < 0.f) {
+                const float phi = mh * vr / (dr2 + mh * mh * P.av_eta2);
+                const float piv = (P.av_beta * phi - P.av_alpha * P.c0) * phi / rho_bar;
+                const float mp = mj * piv;
+                a0 = fmaf(-mp, w0, a0);
+                a1 = fmaf(-mp, w1, a1);
+                if (DIM == 3) a2 = fmaf(-mp, w2, a2);
+                float vdw = vx * w0 + vy * w1;
+                if (DIM == 3) vdw += vz * w2;
+                av_du = fmaf(-0.5f * mp, vdw, av_du);
+            }
+        }
+        // art_heat.f:69-97.
+        if (P.heat_art) {
+            float rdw = d[0] * w0 + d[1] * w1;
+            if (DIM == 3) rdw += d[2] * w2;
+            const float psi = (rpi.w + rpj.w) / (rho_bar * (dr2 + mh * mh * P.ah_eta2)) * rdw;
+            ah_du = fmaf(mj * psi, rpi.z - rpj.z, ah_du);
+        }
+        (void)pi_i;
+    });
+    float du = 0.5f * he_sum + av_du + ah_du;  // internal_force.f:433-435
+    if (P.visc) du += B.tds[s];
+    if (S.heat_on) {
+        float e0 = xi.x - P.heat_center[0], e1 = xi.y - P.heat_center[1];
+        float dd = e0 * e0 + e1 * e1;
+        if (DIM == 3) {
+            float e2 = xi.z - P.heat_center[2];
+            dd += e2 * e2;
+        }
+        du += P.heat_q0 * expf(-dd * P.heat_k) / rpi.x;
+    }
+    a0 += P.gravity[0];
+    a1 += P.gravity[1];
+    if (DIM == 3) a2 += P.gravity[2];
+    // Corrector (time_integration.f:186-218).
+    const float4 vmin = B.vmin[s];
+    float4 vn = vi;
+    vn.x = fmaf(S.kdt, a0, vmin.x);
+    vn.y = fmaf(S.kdt, a1, vmin.y);
+    if (DIM == 3) vn.z = fmaf(S.kdt, a2, vmin.z);
+    float un = fmaf(S.kdt, du, vmin.w);
+    if (un < 0.f) un = 0.f;
+    float4 xn = xi;
+    xn.x = fmaf(S.dt, vn.x, xi.x);
+    xn.y = fmaf(S.dt, vn.y, xi.y);
+    if (DIM == 3) xn.z = fmaf(S.dt, vn.z, xi.z);
+    float* xv[3] = {&xn.x, &xn.y, &xn.z};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        if (!P.periodic[d]) continue;
+        float& c = *xv[d];
+        if (!(c < P.period_hi[d])) c = __fsub_rn(c, P.period_L[d]);
+        else if (c < P.period_lo[d]) c = __fadd_rn(c, P.period_L[d]);
+        if (!(c >= P.period_lo[d] && c < P.period_hi[d])) atomicOr(flags, (unsigned)FLAG_OUT_OF_GRID);
+    }
+    const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + un + a0 + a1 + a2 + du;
+    if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
+    A.xh[s] = xn;
+    A.vm[s] = vn;
+    A.u[s] = un;
+    A.ap[s] = make_float4(a0, a1, a2, du);
+    A.rho[s] = rpi.x;
+    A.p[s] = B.p[s];
+    A.itype[s] = it;
+    A.id[s] = B.id[s];
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour lists (diagnostic entry point)
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void k_count_nbrs(StateB B, const unsigned* __restrict__ keys,
+                             const int* __restrict__ start, const DevGrid* __restrict__ gp,
+                             int* __restrict__ cnt_by_id, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = *gp;
+    const float4 xi = B.xh[s];
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    int c = 0;
+    for_candidates<DIM>(g, start, cc, [&](int k) {
+        if (k == s) return;
+        float d[3], dr2;
+        if (pair_delta<DIM>(xi, B.xh[k], g, d, dr2)) ++c;
+    });
+    cnt_by_id[B.id[s]] = c;
+}
+
+template <int DIM>
+__global__ void k_fill_nbrs(StateB B, const unsigned* __restrict__ keys,
+                            const int* __restrict__ start, const DevGrid* __restrict__ gp,
+                            const long long* __restrict__ offs_by_id, int* __restrict__ nbr,
+                            int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = *gp;
+    const float4 xi = B.xh[s];
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    long long o = offs_by_id[B.id[s]];
+    for_candidates<DIM>(g, start, cc, [&](int k) {
+        if (k == s) return;
+        float d[3], dr2;
+        if (pair_delta<DIM>(xi, B.xh[k], g, d, dr2)) nbr[o++] = B.id[k];
+    });
+}
+
+}  // namespace ag

@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 SPH step: particle-steps/s.
+
+Workload (default): the 2D dam break of the benchmark configuration -- a 1 m x
+2 m water column in a 4 m x 3 m tank, dx = 1 mm, 2,000,000 fluid + 30,018 wall
+particles, Wendland C2, Tait (c0 = 62.6 m/s), art. visc alpha = 0.01, gravity,
+leapfrog dt = 0.2 h / c0. Seeded synthetic inputs (no dataset exists).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:      `value`  K steps of armando_integrate on device-resident state,
+                    timed with CUDA events on the library's stream.
+           `e2e`    the same metric through armando_step with pinned HOST
+                    buffers, one call per step (copy in, step, copy out).
+           `roofline` the force pass (dominant kernel) against the measured
+                    HBM copy bandwidth, its duration from armando_profile_phases.
+           `cpu_baseline` the FP64 oracle (threaded gather form) on the host
+                    cores, a bounded number of steps of the same workload.
+reference: the reference algorithm's CPU restatement (the FP64 oracle port; the
+           reference's own Fortran cannot be built here) on all host cores.
+Under torchrun every rank runs an independent replica (the step has no data
+exchange between GPUs); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "particle-steps/s"
+# Algorithmic bytes per particle-step (FP32/int32 compulsory traffic of the
+# step's data flow): read the persistent state once, write it once, the
+# cross-pass rho/p, the neighbour-search key + permutation and the cell table.
+#   force pass:  read x, v, u, m, h, itype + rho, p; write x, v, dv, u, rho, p, du
+B_FORCE = {2: (2 + 2 + 4) * 4 + 8 + (3 * 2 + 4) * 4, 3: (3 + 3 + 4) * 4 + 8 + (3 * 3 + 4) * 4}
+
+
+def step_bytes(dim: int, cells_per_particle: float) -> float:
+    """Algorithmic bytes of a whole step per particle."""
+    read_state = (3 * dim + 5) * 4
+    write_state = (3 * dim + 4) * 4
+    return read_state + write_state + 16 + 16 + 8.0 * 2 * cells_per_particle
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="dambreak2d", choices=["dambreak2d", "channel3d"])
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--profile-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_case(name):
+    from armando_gb300 import cases
+
+    if name == "dambreak2d":
+        return cases.dam_break()
+    return cases.channel()
+
+
+def peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_particle(kernel, config):
+    """DRAM bytes per particle of one launch, from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return d.get(config, {}).get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(case, budget_s):
+    """FP64 oracle (threaded gather form) on all host threads, bounded steps."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O  # the checker's CPU restatement
+
+    threads = O.hardware_threads()
+    st = O.State(case)
+    O.integrate_gather(st, 1, 1, case.dt, threads)  # its = 1 (untimed)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        O.integrate_gather(st, 2 + steps, 1, case.dt, threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 200:
+            break
+    return {"value": case.n * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{case.name}, {case.n} particles, steps its=2..{steps + 1} "
+                      f"({el:.1f} s), FP64"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    case = make_case(args.config)
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    threads = O.hardware_threads()
+    st = O.State(case)
+    w = max(1, min(args.warmup, 2))
+    t0 = time.perf_counter()
+    O.integrate_gather(st, 1, w, case.dt, threads)
+    t_w = (time.perf_counter() - t0) / w
+    # Each timed step is one full step of the workload; the count is bounded so
+    # the run ends within a few minutes.
+    k = max(1, min(args.steps, int(120.0 / max(t_w, 1e-3))))
+    t0 = time.perf_counter()
+    O.integrate_gather(st, 1 + w, k, case.dt, threads)
+    el = time.perf_counter() - t0
+    v = case.n * k / el
+    line = {
+        "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": k,
+        "warmup": w, "ms_per_step": 1e3 * el / k, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": config_dict(case, args),
+        "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"{case.name}, {case.n} particles, {k} of {args.steps} "
+                                   f"requested steps (bounded), FP64 oracle restatement of "
+                                   f"CERNsource time_integration/single_step"},
+        "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def config_dict(case, args):
+    return {"workload": f"{case.name}: {case.n_fluid} fluid + {case.n_wall} wall particles, "
+                        f"dim {case.dim}, dx {case.meta.get('dx'):.4g} m, dt {case.dt:.4g} s",
+            "particles": case.n, "dim": case.dim, "parallelism": f"replicas x{args.gpus}",
+            "l2": "working set > L2 (state ~0.4 GB per replica); no flush needed",
+            "seed": case.meta.get("seed")}
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import armando_gb300 as ag
+
+    torch.cuda.set_device(local_rank)
+    case = make_case(args.config)
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+
+    def barrier():
+        if dist:
+            td.barrier()
+        torch.cuda.synchronize()
+
+    dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in case.arrays().items()}
+    ctx = ag.Context(case.params, case.n_fluid, case.n_wall, mem=ag.MEM_DEVICE)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    # Warm-up: its = 1 .. W (graph capture, grid planning).
+    ctx.integrate(dev, case.dt, 1, args.warmup)
+    its = 1 + args.warmup
+    launches0 = ctx.stats().gpu_launches
+    barrier()
+    with ClockSampler(local_rank) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.integrate(dev, case.dt, its, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    its += args.steps
+    launches = ctx.stats().gpu_launches - launches0
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * case.n * args.steps / (ms * 1e-3)
+    # Phase split (same kernels, direct launches with events between phases).
+    phases = ctx.profile_phases(args.profile_steps)
+    st = ctx.stats()
+    ctx.close()
+
+    out = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        t_force = phases["force"] * 1e-3
+        alg_force = B_FORCE[case.dim] * case.n
+        achieved = alg_force / t_force / 1e9
+        tr = traffic_per_particle("k_force", args.config)
+        cells_pp = st.n_cells / case.n if st.n_cells else 0.9
+        b_step = step_bytes(case.dim, cells_pp)
+        step_s = ms * 1e-3 / args.steps
+        out = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded lattice, no dataset)",
+            "config": config_dict(case, args),
+            "roofline": {"bound": "hbm", "kernel": "k_force (pass 2: forces + leapfrog)",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "alg_bytes_per_particle": B_FORCE[case.dim],
+                         "traffic": (tr * case.n if tr is not None else None)},
+            "step_roofline": {"alg_bytes_per_particle": b_step,
+                              "achieved_gbs": b_step * case.n / step_s / 1e9,
+                              "frac_of_measured_hbm": b_step * case.n / step_s / 1e9 / hbm},
+            "phases_ms": phases, "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        }
+    # e2e: armando_step with pinned host buffers, one call per step.
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
+    pinned = {}
+    for k, v in case.arrays().items():
+        t = torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True)
+        t.copy_(torch.from_numpy(v))
+        pinned[k] = t.numpy()
+    hctx = ag.Context(case.params, case.n_fluid, case.n_wall, mem=ag.MEM_HOST)
+    hs = torch.cuda.ExternalStream(hctx.stream_handle())
+    hctx.step(pinned, case.dt, 1)
+    barrier()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(hs)
+    for k in range(e2e_steps):
+        hctx.step(pinned, case.dt, 2 + k)
+    f1.record(hs)
+    f1.synchronize()
+    barrier()
+    ems = f0.elapsed_time(f1)
+    hctx.close()
+    if dist:
+        t = torch.tensor([ems], device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        ems = float(t.item())
+    if rank == 0:
+        h2d = sum(a.nbytes for a in (pinned["x"], pinned["v"], pinned["mass"], pinned["rho"],
+                                     pinned["p"], pinned["u"], pinned["h"], pinned["itype"],
+                                     pinned["dvdt"], pinned["dudt"]))
+        d2h = sum(a.nbytes for a in (pinned["x"], pinned["v"], pinned["rho"], pinned["p"],
+                                     pinned["u"], pinned["dvdt"], pinned["dudt"]))
+        out["e2e"] = {"value": world * case.n * e2e_steps / (ems * 1e-3), "unit": METRIC,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "steps": e2e_steps, "api": "armando_step, pinned host buffers"}
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(make_case(args.config), args.cpu_seconds)
+    return out
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        torch.cuda.set_device(local_rank)
+        td.init_process_group("nccl")
+    line = run_ours(args, rank, world, local_rank)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

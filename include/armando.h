@@ -1,0 +1,198 @@
+/*
+ * armando.h -- C ABI of the GB300 (sm_103a) weakly-compressible SPH step.
+ *
+ * This is the drop-in boundary for Armando's leapfrog step. One call of
+ * armando_step() performs one iteration of the `do its = 1, steps` loop of
+ * CERNsource/time_integration.f:131-235 (predictor, neighbour search,
+ * single_step, corrector); armando_integrate() performs `steps` of them, which
+ * is time_integration.f:1-247 without its file output.
+ *
+ * Particle arrays follow the reference's Fortran layout `x(dim, maxn)`:
+ * particle-major, x[i*dim + d], 0-based here. Particles with itype > 0 are
+ * fluid (the reference's 1..np); particles with itype <= 0 are fixed wall
+ * ("virtual") particles (np+1..np+nv): they are neighbours of fluid particles
+ * but are never integrated and keep their rho, p, u and prescribed velocity
+ * (CERNsource/density.f:58-59, time_integration.f:137,188).
+ *
+ * All arithmetic is FP32. Every entry point returns an armando_status; no
+ * entry point exits the process (the reference prints and `stop`s,
+ * CERNsource/link_list.f:160-173).
+ */
+#ifndef ARMANDO_H
+#define ARMANDO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ARMANDO_ABI_VERSION 1
+
+typedef enum armando_status {
+    ARMANDO_OK = 0,
+    ARMANDO_ERR_INVALID_ARG = 1,   /* bad pointer, size, dim or parameter          */
+    ARMANDO_ERR_OOM = 2,           /* device or pinned-host allocation failed       */
+    ARMANDO_ERR_GRID_OVERFLOW = 3, /* cell grid larger than the context's capacity  */
+    ARMANDO_ERR_NONFINITE = 4,     /* NaN/Inf produced in a fluid particle's state  */
+    ARMANDO_ERR_OUT_OF_GRID = 5,   /* a particle left the periodic / bounded grid   */
+    ARMANDO_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up            */
+    ARMANDO_ERR_CUDA = 7,          /* a CUDA runtime call failed                    */
+    ARMANDO_ERR_NO_DEVICE = 8,     /* no sm_103 device visible                      */
+    ARMANDO_ERR_UNSUPPORTED = 9    /* option the GPU step does not implement        */
+} armando_status;
+
+typedef enum armando_mem_kind {
+    ARMANDO_MEM_HOST = 0,   /* caller arrays are host memory; the library stages them */
+    ARMANDO_MEM_DEVICE = 1  /* caller arrays are device memory on the context's GPU   */
+} armando_mem_kind;
+
+/*
+ * Physics parameters. They replace the reference's compile-time and hard-coded
+ * constants (art_visc.f:38-44, art_heat.f:38-40, the `prop` material table of
+ * single_step.f:120-186 for the Tait family of FORTRANsource/eos.f90:255-283).
+ * The struct is plain data; armando_params_default() fills the reference
+ * defaults.
+ */
+typedef struct armando_params {
+    int32_t dim;              /* 2 or 3                                                     */
+    int32_t pa_sph;           /* int_force form: 0 = -(p_i+p_j)/(rho_i rho_j),
+                                 1 = -(p_i/rho_i^2 + p_j/rho_j^2)  (internal_force.f:178-429) */
+    int32_t visc;             /* physical viscosity via the shear tensor T_ab (int_force)   */
+    int32_t visc_artificial;  /* Monaghan artificial viscosity (art_visc.f)                 */
+    int32_t heat_artificial;  /* Noh artificial heat conduction (art_heat.f)                */
+    int32_t heat_external;    /* analytic Gaussian volumetric heat source, du += q(x)/rho  */
+    int32_t kernel_3d_legacy; /* 1: 3D Wendland normalised 15/(16 pi h^3) as in
+                                 ArmandoThrust/armando.cu:150; 0: 21/(16 pi h^3)            */
+    int32_t periodic[3];      /* per-axis periodic wrap (minimum image), 0/1                */
+    float rho0;               /* reference density                                          */
+    float c0;                 /* Tait sound speed; c = c0 for every particle                */
+    float pmin;               /* p < pmin -> p = 0 and rho = rho0 (eos.f90:277-280);
+                                 -INFINITY disables the clamp                               */
+    float eta;                /* dynamic viscosity of the shear-tensor term                 */
+    float av_alpha, av_beta, av_eta;  /* art_visc alpha, beta, eta (ref: 1, 1, 0.1)         */
+    float ah_g1, ah_g2, ah_eta;       /* art_heat g1, g2, eta (ref: 0.1, 1, 0.1)            */
+    float gravity[3];         /* body acceleration of fluid particles                       */
+    float heat_q0;            /* peak volumetric source, W/m^3                              */
+    float heat_sigma;         /* Gaussian width, m                                          */
+    float heat_center[3];     /* Gaussian centre, m                                         */
+    float heat_t_end;         /* source active while its*dt <= heat_t_end (fluka_heat gate) */
+    float period_lo[3];       /* periodic box lower bound per axis                          */
+    float period_hi[3];       /* periodic box upper bound per axis                          */
+} armando_params;
+
+/* Per-step statistics of the last completed call. */
+typedef struct armando_stats {
+    int64_t steps_done;       /* leapfrog steps executed by the context so far   */
+    int64_t n_particles;      /* fluid + wall particles                          */
+    int64_t n_cells;          /* cells of the last neighbour grid                */
+    int64_t cell_capacity;    /* cells the context can hold                      */
+    int64_t gpu_launches;     /* kernels launched by the context so far          */
+    int32_t grid_dims[3];     /* cells per axis of the last grid                 */
+    float grid_origin[3];     /* grid origin (link_list.f:53-57: bbox min - max h) */
+    float grid_cell_size[3];  /* cell edge per axis (2 * max h when not periodic) */
+    uint32_t device_flags;    /* raw device status word of the last check        */
+} armando_stats;
+
+typedef struct armando_ctx armando_ctx;
+
+/* Fills *p with the reference defaults: dim 2, pa_sph 1, art_visc constants
+ * 1/1/0.1, art_heat 0.1/1/0.1, rho0 1000, no clamp, no gravity. */
+void armando_params_default(armando_params* p);
+
+/*
+ * Creates a context for n_fluid + n_wall particles on the current CUDA device.
+ * Replaces the allocations of time_integration.f:89-95 (pair lists, rate
+ * arrays); the caller keeps owning the particle arrays.
+ * mem_kind selects how later calls interpret the caller's pointers.
+ */
+armando_status armando_create(armando_ctx** ctx, const armando_params* params,
+                              int32_t dim, int64_t n_fluid, int64_t n_wall,
+                              int32_t mem_kind);
+
+/* Replaces the context's parameters (same dim). Takes effect at the next call. */
+armando_status armando_set_params(armando_ctx* ctx, const armando_params* params);
+
+/*
+ * One leapfrog iteration `its` of CERNsource/time_integration.f:131-218.
+ *   its == 1 : rates at (x, v, u); v += dt/2 dvdt; u += dt/2 dudt; x += dt v
+ *   its  > 1 : predictor v_h = v + dt/2 dvdt_prev, u_h = max(0, u + dt/2 dudt_prev);
+ *              rates at (x, v_h, u_h); v = v + dt dvdt; u = max(0, u + dt dudt);
+ *              x += dt v
+ * In: x[n*dim], vx[n*dim], mass[n], rho[n], p[n], u[n], hsml[n], itype[n], and
+ * for its > 1 the previous rates dvdt[n*dim], dudt[n]. Out: x, vx, u (fluid),
+ * rho, p (fluid; from summation density and the Tait EOS of this step), and the
+ * new rates dvdt, dudt (zero for walls). Walls keep every input value.
+ * The call is stream-ordered; with ARMANDO_MEM_HOST it returns after the
+ * results are back in the caller's arrays.
+ */
+armando_status armando_step(armando_ctx* ctx, float* x, float* vx,
+                            const float* mass, float* rho, float* p, float* u,
+                            const float* hsml, const int32_t* itype,
+                            float* dvdt, float* dudt, float dt, int32_t its);
+
+/*
+ * `steps` leapfrog iterations its0 .. its0+steps-1 (time_integration.f:131-235
+ * with refresh_step = 1, i.e. a neighbour search every step). The state stays
+ * on the device in cell-sorted order between iterations; the loop is replayed
+ * as CUDA graphs. Same arrays and meaning as armando_step.
+ */
+armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx,
+                                 const float* mass, float* rho, float* p,
+                                 float* u, const float* hsml,
+                                 const int32_t* itype, float* dvdt,
+                                 float* dudt, float dt, int32_t its0,
+                                 int32_t steps);
+
+/* Cell id of every particle under the link_list.f grid of positions x (FP32
+ * form of ArmandoThrust/acpu.c:2085-2105 / link_list.f:75-88), caller order.
+ * Out: cell[n]; grid (origin, size, dims) through armando_get_stats. */
+armando_status armando_cell_ids(armando_ctx* ctx, const float* x,
+                                const float* hsml, int32_t* cell);
+
+/*
+ * Neighbour sets under the link_list.f pair test r^2 < (h_i + h_j)^2 (scale_k
+ * = 2), as a CSR over caller particle ids: for particle i, its neighbours j != i
+ * are nbr[offs[i] .. offs[i+1]), ascending. offs has n+1 entries; nbr has
+ * capacity `cap`; *total receives the number of (ordered) neighbour entries.
+ * Returns ARMANDO_ERR_INVALID_ARG with *total set when cap is too small.
+ * Host memory only (test/diagnostic entry, the step itself never builds lists).
+ */
+armando_status armando_neighbours(armando_ctx* ctx, const float* x,
+                                  const float* hsml, int64_t* offs,
+                                  int32_t* nbr, int64_t cap, int64_t* total);
+
+/* The CUDA stream (cudaStream_t) every call of the context is ordered on, so
+ * a caller can bracket calls with its own CUDA events. */
+armando_status armando_get_stream(armando_ctx* ctx, void** stream);
+
+/* Phases of one step, in launch order, for armando_profile_phases. */
+#define ARMANDO_N_PHASES 6
+/* 0 grid (bbox + cell hash), 1 radix sort, 2 cell table + reorder/predictor,
+ * 3 density + EOS, 4 shear tensor (physical viscosity only), 5 forces +
+ * corrector. */
+
+/*
+ * Runs `steps` further leapfrog iterations on the state the last
+ * armando_integrate / armando_step left on the device (same dt, its
+ * continuing), launching the kernels directly with CUDA events between the
+ * phases, and returns the mean device time per step of each phase in
+ * ms_per_phase[ARMANDO_N_PHASES]. The per-kernel split of the step that the
+ * reference reports for its GPU code (ArmandoOnGPU.pdf p.6 Tab.2), measured.
+ */
+armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms_per_phase);
+
+/* Blocks until the context's stream is idle and returns its sticky status. */
+armando_status armando_sync(armando_ctx* ctx);
+armando_status armando_get_stats(const armando_ctx* ctx, armando_stats* out);
+/* Last error message of the context (static string when ctx is NULL). */
+const char* armando_last_error(const armando_ctx* ctx);
+armando_status armando_destroy(armando_ctx* ctx);
+int32_t armando_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARMANDO_H */

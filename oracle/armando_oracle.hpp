@@ -1,0 +1,656 @@
+// armando_oracle.hpp -- CPU restatement of Armando's weakly-compressible SPH
+// step, used ONLY as the checker of the GPU library (tests, smoke check and the
+// CPU baseline leg of the benchmark). Nothing in the product links or calls it.
+//
+// It restates, in the reference's pair-loop form (i < j pairs, contributions
+// scattered to both partners):
+//   time_integration  CERNsource/time_integration.f:131-218 (leapfrog)
+//   single_step       CERNsource/single_step.f:92-234
+//   link_list         CERNsource/link_list.f:1-224 (scale_k = 2)
+//   direct_find       CERNsource/direct_find.f:1-61
+//   sum_density       CERNsource/density.f:1-62
+//   int_force         CERNsource/internal_force.f:57-435 (pa_sph 0 and 1, visc)
+//   art_visc          CERNsource/art_visc.f:55-101 (alpha, beta, eta as parameters)
+//   art_heat          CERNsource/art_heat.f:42-97 (g1, g2, eta as parameters)
+//   Tait EOS          FORTRANsource/eos.f90:255-283 (c = c0, pmin clamp)
+//   Wendland kernel   ArmandoThrust/armando.cu:137-191 with the 2D constant of
+//                     ArmandoThrust/acpu.c:162 and the C2 3D constant noted at
+//                     acpu.c:159 (15/16pi of armando.cu:150 behind a switch)
+//   external heat     du += q(x)/rho as CERNsource/fluka_heat.f:337-338, with
+//                     the analytic Gaussian of Code/armando.cu:1058-1071
+//   gravity           FORTRANsource/time_integration.f90:148-152
+//
+// Deliberate, documented departures from the Fortran text (each one removes
+// reference undefined behaviour, none changes a defined result):
+//   * T_ab and div(v) are zeroed for every particle each step. The Fortran zeroes
+//     them only for 1..np (internal_force.f:58-71, art_heat.f:42-44) and
+//     accumulates wall entries into stale storage.
+//   * eta (dynamic viscosity) and c (= c0) are set for wall particles too; the
+//     Fortran leaves them unset for j > np (single_step.f:120-186).
+//   * pi is M_PI (acpu.c); CERN options.inc declares pi with a single-precision
+//     literal.
+// Scalar type R: double (oracle), float (FP32 mirror), or a dual / counting
+// type. Coordinates used for the neighbour grid and the pair test have their
+// own type Rc so the FP32 cell ids / neighbour sets of the GPU can be mirrored
+// bit for bit (compile with -ffp-contract=off).
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <thread>
+#include <vector>
+
+namespace ao {
+
+constexpr double kPi = 3.14159265358979323846;
+
+template <class R>
+struct Params {
+    int dim = 2, pa_sph = 1, visc = 0, visc_artificial = 0, heat_artificial = 0,
+        heat_external = 0, kernel_3d_legacy = 0;
+    int periodic[3] = {0, 0, 0};
+    R rho0 = R(1000), c0 = R(1), pmin = R(-INFINITY), eta = R(0);
+    R av_alpha = R(1), av_beta = R(1), av_eta = R(0.1);
+    R ah_g1 = R(0.1), ah_g2 = R(1), ah_eta = R(0.1);
+    R gravity[3] = {R(0), R(0), R(0)};
+    R heat_q0 = R(0), heat_sigma = R(1), heat_center[3] = {R(0), R(0), R(0)};
+    double heat_t_end = INFINITY;
+    double period_lo[3] = {0, 0, 0}, period_hi[3] = {0, 0, 0};
+};
+
+// ---------------------------------------------------------------------------
+// Wendland C2 kernel, support 2h (armando.cu:137-191).
+//   W(r,h)   = alpha (1 - q/2)^4 (1 + 2q),      q = r/h < 2
+//   dW/dr    = alpha/h * 5/8 * q (q - 2)^3
+//   dW/dx_d  = dW/dr * dx_d / r = alpha * 5/(8 h^2) * (q - 2)^3 * dx_d
+// alpha_2D = 7/(4 pi h^2) (acpu.c:162); alpha_3D = 21/(16 pi h^3) (acpu.c:159),
+// or 15/(16 pi h^3) with kernel_3d_legacy (armando.cu:150).
+// ---------------------------------------------------------------------------
+template <class R>
+inline R kernel_alpha(const R& h, int dim, int legacy3d) {
+    if (dim == 2) return R(7.0) / (R(4.0) * R(kPi) * h * h);
+    return R(legacy3d ? 15.0 : 21.0) / (R(16.0) * R(kPi) * h * h * h);
+}
+
+template <class R>
+inline R kernel_w(const R& r, const R& h, int dim, int legacy3d) {
+    R q = r / h;
+    if (!(q < R(2))) return R(0);
+    R t = R(1) - R(0.5) * q;
+    t = t * t;
+    t = t * t;
+    return kernel_alpha(h, dim, legacy3d) * t * (R(1) + R(2) * q);
+}
+
+// Gradient with respect to x_i of W(|x_i - x_j|, h); dx = x_i - x_j.
+template <class R>
+inline void kernel_dwdx(const R* dx, const R& r, const R& h, int dim, int legacy3d,
+                        R* dwdx) {
+    R q = r / h;
+    if (!(q < R(2))) {
+        for (int d = 0; d < dim; ++d) dwdx[d] = R(0);
+        return;
+    }
+    R t = q - R(2);
+    R f = kernel_alpha(h, dim, legacy3d) * R(5.0 / 8.0) / (h * h) * t * t * t;
+    for (int d = 0; d < dim; ++d) dwdx[d] = f * dx[d];
+}
+
+// dW/dr exactly as the reference writes it (used by the acpu.c pin tests).
+template <class R>
+inline R kernel_dwdr(const R& r, const R& h, int dim, int legacy3d) {
+    R q = r / h;
+    if (!(q < R(2))) return R(0);
+    R t = q - R(2);
+    return R(5.0 / 8.0) * q * t * t * t * kernel_alpha(h, dim, legacy3d) / h;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour grid of link_list.f:39-88, in coordinate precision Rc.
+// ---------------------------------------------------------------------------
+template <class Rc>
+struct Grid {
+    Rc o[3] = {0, 0, 0};
+    Rc size[3] = {1, 1, 1};
+    Rc period[3] = {0, 0, 0};
+    Rc half_period[3] = {0, 0, 0};
+    int n[3] = {1, 1, 1};
+    int64_t ncells = 1;
+};
+
+// Minimum-image difference on a periodic axis (absent from the reference,
+// which only has commented-out wrap code, ArmandoList/armando2Dlist.cu:856-870).
+template <class Rc>
+inline Rc min_image(Rc dx, const Grid<Rc>& g, int d, const int* periodic) {
+    if (periodic[d]) {
+        if (dx > g.half_period[d]) dx = dx - g.period[d];
+        else if (dx < -g.half_period[d]) dx = dx + g.period[d];
+    }
+    return dx;
+}
+
+// Grid over all particles: bbox expanded by the largest h, cell edge
+// scale_k * mh with scale_k = 2 (link_list.f:29-57). A periodic axis uses the
+// box [lo, hi) split into n = floor(L / (2 mh)) >= 3 equal cells.
+template <class Rc>
+Grid<Rc> make_grid(int64_t nt, int dim, const Rc* x, const Rc* h, const int* periodic,
+                   const double* lo, const double* hi) {
+    Grid<Rc> g;
+    Rc gmin[3], gmax[3];
+    for (int d = 0; d < 3; ++d) {
+        gmin[d] = Rc(1.0e30);
+        gmax[d] = Rc(-1.0e30);
+    }
+    Rc mh = Rc(0);
+    for (int64_t i = 0; i < nt; ++i) {
+        for (int d = 0; d < dim; ++d) {
+            Rc xv = x[i * dim + d];
+            if (xv < gmin[d]) gmin[d] = xv;
+            if (xv > gmax[d]) gmax[d] = xv;
+        }
+        if (h[i] > mh) mh = h[i];
+    }
+    Rc cell = Rc(2) * mh;
+    g.ncells = 1;
+    for (int d = 0; d < dim; ++d) {
+        if (periodic[d]) {
+            Rc L = Rc(hi[d]) - Rc(lo[d]);
+            int n = (int)(L / cell);
+            if (n < 3) throw std::runtime_error("periodic axis shorter than 3 cells");
+            g.o[d] = Rc(lo[d]);
+            g.n[d] = n;
+            g.size[d] = L / Rc(n);
+            g.period[d] = L;
+            g.half_period[d] = Rc(0.5) * L;
+        } else {
+            Rc lo_d = gmin[d] - mh;
+            Rc hi_d = gmax[d] + mh;
+            g.o[d] = lo_d;
+            g.size[d] = cell;
+            g.n[d] = (int)((hi_d - lo_d) / cell) + 1;
+        }
+        g.ncells *= g.n[d];
+    }
+    return g;
+}
+
+// Cell coordinate of x along d: int((x - grid_min)/(scale_k mh)) (link_list.f:76-78).
+template <class Rc>
+inline int cell_coord(Rc xv, const Grid<Rc>& g, int d) {
+    int c = (int)((xv - g.o[d]) / g.size[d]);
+    if (c < 0) c = 0;
+    if (c > g.n[d] - 1) c = g.n[d] - 1;
+    return c;
+}
+
+// Linear cell id g = n1*n2*k + n1*j + i (link_list.f:80-85, 0-based).
+template <class Rc>
+inline int64_t cell_id(const Rc* xi, const Grid<Rc>& g, int dim) {
+    int64_t c = 0;
+    for (int d = dim - 1; d >= 0; --d) c = c * g.n[d] + cell_coord(xi[d], g, d);
+    return c;
+}
+
+// Pair test of link_list.f:154-159: dr^2 < (scale_k * (h_i + h_j)/2)^2, with
+// dr^2 summed over axes in order; (2 * ((h_i+h_j)/2)) is exactly h_i + h_j.
+template <class Rc>
+inline bool pair_test(const Rc* xi, const Rc* xj, Rc hi, Rc hj, int dim, const Grid<Rc>& g,
+                      const int* periodic) {
+    Rc dr2 = Rc(0);
+    for (int d = 0; d < dim; ++d) {
+        Rc dx = min_image(Rc(xi[d] - xj[d]), g, d, periodic);
+        Rc sq = dx * dx;
+        dr2 = (d == 0) ? sq : Rc(dr2 + sq);
+    }
+    Rc s = hi + hj;
+    return dr2 < Rc(s * s);
+}
+
+struct PairList {
+    std::vector<int> pi, pj;
+};
+
+// link_list.f:1-224: counting sort of particles into cells, then for every i
+// the 3^dim stencil, pairs (i, j) with j > i that pass the test.
+template <class Rc>
+Grid<Rc> link_list(int64_t nt, int dim, const Rc* x, const Rc* h, const int* periodic,
+                   const double* lo, const double* hi, PairList& out,
+                   std::vector<int64_t>* cell_of = nullptr) {
+    Grid<Rc> g = make_grid<Rc>(nt, dim, x, h, periodic, lo, hi);
+    std::vector<int64_t> cid(nt);
+    std::vector<int64_t> start(g.ncells + 1, 0);
+    for (int64_t i = 0; i < nt; ++i) {
+        cid[i] = cell_id(x + i * dim, g, dim);
+        start[cid[i] + 1]++;
+    }
+    for (int64_t c = 0; c < g.ncells; ++c) start[c + 1] += start[c];
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    std::vector<int> part(nt);
+    for (int64_t i = 0; i < nt; ++i) part[fill[cid[i]]++] = (int)i;
+    out.pi.clear();
+    out.pj.clear();
+    for (int64_t i = 0; i < nt; ++i) {
+        int ijk[3] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) ijk[d] = cell_coord(x[i * dim + d], g, d);
+        int lo3[3] = {0, 0, 0}, hi3[3] = {0, 0, 0};
+        for (int d = 0; d < dim; ++d) {
+            if (periodic[d]) {
+                lo3[d] = ijk[d] - 1;
+                hi3[d] = ijk[d] + 1;
+            } else {
+                lo3[d] = std::max(ijk[d] - 1, 0);
+                hi3[d] = std::min(ijk[d] + 1, g.n[d] - 1);
+            }
+        }
+        for (int kg = lo3[2]; kg <= hi3[2]; ++kg)
+            for (int jg = lo3[1]; jg <= hi3[1]; ++jg)
+                for (int ig = lo3[0]; ig <= hi3[0]; ++ig) {
+                    int cc[3] = {ig, jg, kg};
+                    int64_t c = 0;
+                    for (int d = dim - 1; d >= 0; --d) {
+                        int v = cc[d];
+                        if (periodic[d]) v = (v + g.n[d]) % g.n[d];
+                        c = c * g.n[d] + v;
+                    }
+                    for (int64_t k = start[c]; k < start[c + 1]; ++k) {
+                        int j = part[k];
+                        if (j <= i) continue;
+                        if (pair_test(x + i * dim, x + (int64_t)j * dim, h[i], h[j], dim, g,
+                                      periodic)) {
+                            out.pi.push_back((int)i);
+                            out.pj.push_back(j);
+                        }
+                    }
+                }
+    }
+    if (cell_of) *cell_of = cid;
+    return g;
+}
+
+// direct_find.f:1-61: all pairs i < j with sqrt(dr^2) < scale_k * mh.
+template <class Rc>
+void direct_find(int64_t nt, int dim, const Rc* x, const Rc* h, const int* periodic,
+                 const Grid<Rc>& g, PairList& out) {
+    out.pi.clear();
+    out.pj.clear();
+    for (int64_t i = 0; i + 1 < nt; ++i)
+        for (int64_t j = i + 1; j < nt; ++j) {
+            Rc dr2 = Rc(0);
+            for (int d = 0; d < dim; ++d) {
+                Rc dx = min_image(Rc(x[i * dim + d] - x[j * dim + d]), g, d, periodic);
+                dr2 = (d == 0) ? Rc(dx * dx) : Rc(dr2 + dx * dx);
+            }
+            Rc mh = (h[i] + h[j]) / Rc(2);
+            if (std::sqrt(dr2) < Rc(2) * mh) {
+                out.pi.push_back((int)i);
+                out.pj.push_back((int)j);
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Step state (particle-major like the Fortran x(dim, maxn)).
+// ---------------------------------------------------------------------------
+template <class R>
+struct State {
+    int64_t n = 0;
+    int dim = 2;
+    std::vector<R> x, v, m, rho, p, u, h, c;
+    std::vector<int> itype;
+    std::vector<R> dvdt, dudt;  // rates of the last single_step (carried)
+    bool fluid(int64_t i) const { return itype[i] > 0; }
+};
+
+template <class R>
+struct Rates {
+    std::vector<R> dv, du, tdsdt, divv;
+};
+
+// Pair geometry shared by every pair loop: dx = x_i - x_j (minimum image),
+// r, mh = (h_i + h_j)/2, W and dW/dx_i.
+template <class R, class Rc>
+struct PairGeom {
+    R dx[3], r2, r, mh, w, dwdx[3];
+};
+
+template <class R, class Rc>
+inline void pair_geom(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, int i, int j,
+                      PairGeom<R, Rc>& pg) {
+    const int dim = s.dim;
+    pg.r2 = R(0);
+    for (int d = 0; d < dim; ++d) {
+        R dx = s.x[(int64_t)i * dim + d] - s.x[(int64_t)j * dim + d];
+        if (P.periodic[d]) {
+            R L = R(P.period_hi[d] - P.period_lo[d]);
+            if (dx > R(0.5) * L) dx = dx - L;
+            else if (dx < -R(0.5) * L) dx = dx + L;
+        }
+        pg.dx[d] = dx;
+        pg.r2 = pg.r2 + dx * dx;
+    }
+    using std::sqrt;
+    pg.r = sqrt(pg.r2);
+    pg.mh = R(0.5) * (s.h[i] + s.h[j]);
+    pg.w = kernel_w(pg.r, pg.mh, dim, P.kernel_3d_legacy);
+    kernel_dwdx(pg.dx, pg.r, pg.mh, dim, P.kernel_3d_legacy, pg.dwdx);
+}
+
+// density.f:1-62 (sum_density): rho_i = m_i W(0, h_i) + sum_j m_j W_ij, fluid only.
+template <class R, class Rc>
+void sum_density(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl) {
+    for (int64_t i = 0; i < s.n; ++i)
+        if (s.fluid(i)) s.rho[i] = kernel_w(R(0), s.h[i], s.dim, P.kernel_3d_legacy) * s.m[i];
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        if (s.fluid(i)) s.rho[i] = s.rho[i] + s.m[j] * pg.w;
+        if (s.fluid(j)) s.rho[j] = s.rho[j] + s.m[i] * pg.w;
+    }
+}
+
+// Tait EOS (eos.f90:255-283): p = rho0 c0^2/7 ((rho/rho0)^7 - 1), c = c0; if
+// p < pmin then p = 0 and rho = rho0. Fluid particles only (single_step.f:120).
+template <class R>
+inline void eos_tait(R& rho, R& p, const Params<R>& P) {
+    R ratio = rho / P.rho0;
+    R r2 = ratio * ratio;
+    R r7 = r2 * r2 * r2 * ratio;
+    p = P.rho0 * P.c0 * P.c0 / R(7) * (r7 - R(1));
+    if (p < P.pmin) {
+        p = R(0);
+        rho = P.rho0;
+    }
+}
+
+// internal_force.f:1-437 (int_force).
+template <class R, class Rc>
+void int_force(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+               std::vector<R>& dvdt, std::vector<R>& dudt, std::vector<R>& tdsdt) {
+    const int dim = s.dim;
+    const int64_t n = s.n;
+    std::vector<R> T(n * 6, R(0));  // txx tyy tzz txy txz tyz
+    dvdt.assign(n * dim, R(0));
+    dudt.assign(n, R(0));
+    tdsdt.assign(n, R(0));
+    PairGeom<R, Rc> pg;
+    if (P.visc) {
+        // Shear tensor T_ab = v_a,b + v_b,a - 2/3 delta_ab v_c,c (internal_force.f:75-152).
+        for (size_t k = 0; k < pl.pi.size(); ++k) {
+            int i = pl.pi[k], j = pl.pj[k];
+            pair_geom(s, g, P, i, j, pg);
+            R dv[3] = {R(0), R(0), R(0)};
+            for (int d = 0; d < dim; ++d) dv[d] = s.v[(int64_t)j * dim + d] - s.v[(int64_t)i * dim + d];
+            const R* w = pg.dwdx;
+            R hxx, hyy, hzz = R(0), hxy, hxz = R(0), hyz = R(0);
+            if (dim == 2) {
+                hxx = R(2) * dv[0] * w[0] - dv[1] * w[1];
+                hyy = R(2) * dv[1] * w[1] - dv[0] * w[0];
+                hxy = dv[0] * w[1] + dv[1] * w[0];
+            } else {
+                hxx = R(2) * dv[0] * w[0] - dv[1] * w[1] - dv[2] * w[2];
+                hyy = R(2) * dv[1] * w[1] - dv[0] * w[0] - dv[2] * w[2];
+                hzz = R(2) * dv[2] * w[2] - dv[0] * w[0] - dv[1] * w[1];
+                hyz = dv[1] * w[2] + dv[2] * w[1];
+                hxz = dv[0] * w[2] + dv[2] * w[0];
+                hxy = dv[0] * w[1] + dv[1] * w[0];
+            }
+            hxx = R(2.0 / 3.0) * hxx;
+            hyy = R(2.0 / 3.0) * hyy;
+            hzz = R(2.0 / 3.0) * hzz;
+            R hh[6] = {hxx, hyy, hzz, hxy, hxz, hyz};
+            for (int a = 0; a < 6; ++a) {
+                T[(int64_t)i * 6 + a] = T[(int64_t)i * 6 + a] + s.m[j] * hh[a] / s.rho[j];
+                T[(int64_t)j * 6 + a] = T[(int64_t)j * 6 + a] + s.m[i] * hh[a] / s.rho[i];
+            }
+        }
+        // Viscous entropy T ds/dt = 1/2 eta/rho T_ab T_ab (internal_force.f:156-171).
+        for (int64_t i = 0; i < n; ++i) {
+            if (!s.fluid(i)) continue;
+            const R* t = &T[i * 6];
+            R q;
+            if (dim == 2) q = t[0] * t[0] + t[1] * t[1] + R(2) * t[3] * t[3];
+            else
+                q = t[0] * t[0] + t[1] * t[1] + t[2] * t[2] + R(2) * t[5] * t[5] +
+                    R(2) * t[4] * t[4] + R(2) * t[3] * t[3];
+            tdsdt[i] = R(0.5) * P.eta / s.rho[i] * q;
+        }
+    }
+    // Pressure force, viscous force and -p/rho div v (internal_force.f:178-429).
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        const R* w = pg.dwdx;
+        R he = R(0);
+        R hv[3];
+        const R* ti = &T[(int64_t)i * 6];
+        const R* tj = &T[(int64_t)j * 6];
+        // Rows of the symmetric tensor as (row a, column b) -> index.
+        static const int tidx[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+        if (P.pa_sph == 0) {
+            R rr = s.rho[i] * s.rho[j];
+            for (int d = 0; d < dim; ++d) {
+                R h = -(s.p[i] + s.p[j]) * w[d];
+                he = he + (s.v[(int64_t)j * dim + d] - s.v[(int64_t)i * dim + d]) * h;
+                if (P.visc)
+                    for (int b = 0; b < dim; ++b)
+                        h = h + (P.eta * ti[tidx[d][b]] + P.eta * tj[tidx[d][b]]) * w[b];
+                hv[d] = h / rr;
+            }
+            he = he / rr;
+        } else {
+            R pi2 = s.p[i] / (s.rho[i] * s.rho[i]);
+            R pj2 = s.p[j] / (s.rho[j] * s.rho[j]);
+            R ri2 = s.rho[i] * s.rho[i], rj2 = s.rho[j] * s.rho[j];
+            for (int d = 0; d < dim; ++d) {
+                R h = -(pi2 + pj2) * w[d];
+                he = he + (s.v[(int64_t)j * dim + d] - s.v[(int64_t)i * dim + d]) * h;
+                if (P.visc)
+                    for (int b = 0; b < dim; ++b)
+                        h = h + (P.eta * ti[tidx[d][b]] / ri2 + P.eta * tj[tidx[d][b]] / rj2) * w[b];
+                hv[d] = h;
+            }
+        }
+        for (int d = 0; d < dim; ++d) {
+            dvdt[(int64_t)i * dim + d] = dvdt[(int64_t)i * dim + d] + s.m[j] * hv[d];
+            dvdt[(int64_t)j * dim + d] = dvdt[(int64_t)j * dim + d] - s.m[i] * hv[d];
+        }
+        dudt[i] = dudt[i] + s.m[j] * he;
+        dudt[j] = dudt[j] + s.m[i] * he;
+    }
+    // de/dt = T ds/dt + 1/2 (sum) (internal_force.f:433-435).
+    for (int64_t i = 0; i < n; ++i) dudt[i] = tdsdt[i] + R(0.5) * dudt[i];
+}
+
+// art_visc.f:1-103.
+template <class R, class Rc>
+void art_visc(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+              std::vector<R>& dvdt, std::vector<R>& dudt) {
+    const int dim = s.dim;
+    dvdt.assign(s.n * dim, R(0));
+    dudt.assign(s.n, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        R vr = R(0), vdwdx = R(0);
+        for (int d = 0; d < dim; ++d) {
+            R dv = s.v[(int64_t)i * dim + d] - s.v[(int64_t)j * dim + d];
+            vr = vr + dv * pg.dx[d];
+            vdwdx = vdwdx + dv * pg.dwdx[d];
+        }
+        if (vr < R(0)) {
+            R he = pg.mh * P.av_eta;
+            R phi = (pg.mh * vr) / (pg.r2 + he * he);
+            R mc = R(0.5) * (s.c[i] + s.c[j]);
+            R mrho = R(0.5) * (s.rho[i] + s.rho[j]);
+            R piv = (P.av_beta * phi - P.av_alpha * mc) * phi / mrho;
+            for (int d = 0; d < dim; ++d) {
+                dvdt[(int64_t)i * dim + d] = dvdt[(int64_t)i * dim + d] - s.m[j] * piv * pg.dwdx[d];
+                dvdt[(int64_t)j * dim + d] = dvdt[(int64_t)j * dim + d] + s.m[i] * piv * pg.dwdx[d];
+            }
+            dudt[i] = dudt[i] + R(0.5) * s.m[j] * piv * vdwdx;
+            dudt[j] = dudt[j] + R(0.5) * s.m[i] * piv * vdwdx;
+        }
+    }
+}
+
+// art_heat.f:1-99. divv is returned for diagnostics.
+template <class R, class Rc>
+void art_heat(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+              std::vector<R>& dudt, std::vector<R>& divv) {
+    const int dim = s.dim;
+    dudt.assign(s.n, R(0));
+    divv.assign(s.n, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        R vdwdx = R(0);
+        for (int d = 0; d < dim; ++d)
+            vdwdx = vdwdx + (s.v[(int64_t)j * dim + d] - s.v[(int64_t)i * dim + d]) * pg.dwdx[d];
+        divv[i] = divv[i] + s.m[j] / s.rho[i] * vdwdx;
+        divv[j] = divv[j] + s.m[i] / s.rho[j] * vdwdx;
+    }
+    using std::fabs;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        R mrho = R(0.5) * (s.rho[i] + s.rho[j]);
+        R rdwdx = R(0);
+        for (int d = 0; d < dim; ++d) rdwdx = rdwdx + pg.dx[d] * pg.dwdx[d];
+        R psi_i = P.ah_g1 * s.h[i] * s.c[i] + P.ah_g2 * s.h[i] * s.h[i] * (fabs(divv[i]) - divv[i]);
+        R psi_j = P.ah_g1 * s.h[j] * s.c[j] + P.ah_g2 * s.h[j] * s.h[j] * (fabs(divv[j]) - divv[j]);
+        R psi_ij = R(0.5) * (psi_i + psi_j);
+        R he = pg.mh * P.ah_eta;
+        R psi = (R(2) * psi_ij) / (mrho * (pg.r2 + he * he)) * rdwdx;
+        dudt[i] = dudt[i] + s.m[j] * psi * (s.u[i] - s.u[j]);
+        dudt[j] = dudt[j] + s.m[i] * psi * (s.u[j] - s.u[i]);
+    }
+}
+
+// External volumetric heat, du_i += q(x_i)/rho_i (fluka_heat.f:337-338), with
+// q(x) = q0 exp(-|x - xc|^2 / (2 sigma^2)).
+template <class R>
+void ext_heat(const State<R>& s, const Params<R>& P, std::vector<R>& dudt) {
+    dudt.assign(s.n, R(0));
+    using std::exp;
+    for (int64_t i = 0; i < s.n; ++i) {
+        if (!s.fluid(i)) continue;
+        R d2 = R(0);
+        for (int d = 0; d < s.dim; ++d) {
+            R e = s.x[i * s.dim + d] - P.heat_center[d];
+            d2 = d2 + e * e;
+        }
+        R q = P.heat_q0 * exp(-d2 / (R(2) * P.heat_sigma * P.heat_sigma));
+        dudt[i] = q / s.rho[i];
+    }
+}
+
+// single_step.f:92-234 for summation density and the Tait family:
+// fills s.rho, s.p (fluid), s.c, and rates dv, du (zero for walls).
+template <class R, class Rc>
+void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl, int its,
+                 double dt, Rates<R>& out) {
+    const int dim = s.dim;
+    const int64_t n = s.n;
+    sum_density(s, g, P, pl);
+    for (int64_t i = 0; i < n; ++i) {
+        s.c[i] = P.c0;
+        if (s.fluid(i)) eos_tait(s.rho[i], s.p[i], P);
+    }
+    std::vector<R> indvdt, indudt, avdvdt, avdudt, ahdudt, exdudt;
+    int_force(s, g, P, pl, indvdt, indudt, out.tdsdt);
+    if (P.visc_artificial) art_visc(s, g, P, pl, avdvdt, avdudt);
+    if (P.heat_artificial) art_heat(s, g, P, pl, ahdudt, out.divv);
+    if (P.heat_external && (double(its) * dt <= P.heat_t_end)) ext_heat(s, P, exdudt);
+    out.dv.assign(n * dim, R(0));
+    out.du.assign(n, R(0));
+    for (int64_t i = 0; i < n; ++i) {
+        if (!s.fluid(i)) continue;
+        for (int d = 0; d < dim; ++d) {
+            R a = indvdt[i * dim + d] + P.gravity[d];
+            if (P.visc_artificial) a = a + avdvdt[i * dim + d];
+            out.dv[i * dim + d] = a;
+        }
+        R du = indudt[i];
+        if (P.visc_artificial) du = du + avdudt[i];
+        if (P.heat_artificial) du = du + ahdudt[i];
+        if (!exdudt.empty()) du = du + exdudt[i];
+        out.du[i] = du;
+    }
+}
+
+template <class R>
+inline void wrap_periodic(State<R>& s, const Params<R>& P, int64_t i) {
+    for (int d = 0; d < s.dim; ++d) {
+        if (!P.periodic[d]) continue;
+        R lo = R(P.period_lo[d]), hi = R(P.period_hi[d]), L = hi - lo;
+        R& xv = s.x[i * s.dim + d];
+        if (!(xv < hi)) xv = xv - L;
+        else if (xv < lo) xv = xv + L;
+    }
+}
+
+// Neighbour search for the physics: link_list in coordinate precision Rc on
+// the current positions.
+template <class R, class Rc>
+Grid<Rc> neighbour_search(const State<R>& s, const Params<R>& P, PairList& pl) {
+    std::vector<Rc> xc(s.n * s.dim), hc(s.n);
+    for (int64_t i = 0; i < s.n * s.dim; ++i) xc[i] = Rc(s.x[i]);
+    for (int64_t i = 0; i < s.n; ++i) hc[i] = Rc(s.h[i]);
+    return link_list<Rc>(s.n, s.dim, xc.data(), hc.data(), P.periodic, P.period_lo, P.period_hi,
+                         pl);
+}
+
+// One iteration `its` of time_integration.f:131-218 (refresh_step = 1).
+// s.dvdt / s.dudt carry the previous rates in and the new rates out.
+template <class R, class Rc = R>
+void leapfrog_step(State<R>& s, const Params<R>& P, int its, double dt, Rates<R>* rates_out = nullptr,
+                   PairList* pairs_out = nullptr) {
+    const int dim = s.dim;
+    const int64_t n = s.n;
+    const R hdt = R(dt / 2.0), fdt = R(dt);
+    std::vector<R> u_min, v_min;
+    if (its != 1) {
+        u_min = s.u;
+        v_min = s.v;
+        for (int64_t i = 0; i < n; ++i) {
+            if (!s.fluid(i)) continue;
+            s.u[i] = s.u[i] + hdt * s.dudt[i];
+            if (s.u[i] < R(0)) s.u[i] = R(0);
+            for (int d = 0; d < dim; ++d) s.v[i * dim + d] = s.v[i * dim + d] + hdt * s.dvdt[i * dim + d];
+        }
+    }
+    PairList pl;
+    Grid<Rc> g = neighbour_search<R, Rc>(s, P, pl);
+    Rates<R> r;
+    single_step(s, g, P, pl, its, dt, r);
+    for (int64_t i = 0; i < n; ++i) {
+        if (!s.fluid(i)) continue;
+        if (its != 1) {
+            s.u[i] = u_min[i] + fdt * r.du[i];
+            if (s.u[i] < R(0)) s.u[i] = R(0);
+            for (int d = 0; d < dim; ++d) {
+                s.v[i * dim + d] = v_min[i * dim + d] + fdt * r.dv[i * dim + d];
+                s.x[i * dim + d] = s.x[i * dim + d] + fdt * s.v[i * dim + d];
+            }
+        } else {
+            s.u[i] = s.u[i] + hdt * r.du[i];
+            if (s.u[i] < R(0)) s.u[i] = R(0);
+            for (int d = 0; d < dim; ++d) {
+                s.v[i * dim + d] = s.v[i * dim + d] + hdt * r.dv[i * dim + d];
+                s.x[i * dim + d] = s.x[i * dim + d] + fdt * s.v[i * dim + d];
+            }
+        }
+        wrap_periodic(s, P, i);
+    }
+    s.dvdt = r.dv;
+    s.dudt = r.du;
+    if (rates_out) *rates_out = r;
+    if (pairs_out) *pairs_out = std::move(pl);
+}
+
+}  // namespace ao

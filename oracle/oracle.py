@@ -1,0 +1,190 @@
+"""ctypes wrapper of the CPU oracle (liboracle.so).
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker. The product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REPO = os.path.dirname(_HERE)
+if _REPO not in sys.path:
+    sys.path.insert(0, _REPO)
+
+from armando_gb300._abi import Params  # noqa: E402  (shared C-ABI struct)
+
+LIB_PATH = os.path.join(_HERE, "liboracle.so")
+REF_LIB_PATH = os.path.join(_HERE, "_ref", "libacpu.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles liboracle.so with the committed Makefile."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return LIB_PATH
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        i64 = C.c_int64
+        L.ao_link_list_f64.argtypes = [i64, C.c_int, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp, C.c_int]
+        L.ao_link_list_f64.restype = i64
+        L.ao_link_list_f32.argtypes = L.ao_link_list_f64.argtypes
+        L.ao_link_list_f32.restype = i64
+        L.ao_kernel_f64.argtypes = [C.c_int, C.c_int, i64, vp, vp, vp, vp]
+        L.ao_kernel_f64.restype = None
+        L.ao_tait_f64.argtypes = [i64, vp, C.c_double, C.c_double, C.c_double, C.c_int, vp]
+        L.ao_tait_f64.restype = None
+        L.ao_forces_f64.argtypes = [C.POINTER(Params), i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+        L.ao_forces_f64.restype = C.c_int
+        L.ao_step_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double, vp, vp, vp, vp, vp,
+                                  vp, vp, vp, vp, vp, C.c_int, vp]
+        L.ao_step_f64.restype = C.c_int
+        L.ao_step_f32.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double, vp, vp, vp, vp, vp,
+                                  vp, vp, vp, vp, vp]
+        L.ao_step_f32.restype = C.c_int
+        L.ao_integrate_gather_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_int, C.c_double,
+                                              vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.ao_integrate_gather_f64.restype = C.c_int
+        L.ao_hardware_threads.argtypes = []
+        L.ao_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _per(params: Params | None, dim: int):
+    per = np.zeros(3, np.int32)
+    lo = np.zeros(3, np.float64)
+    hi = np.zeros(3, np.float64)
+    if params is not None:
+        for d in range(3):
+            per[d] = params.periodic[d]
+            lo[d] = params.period_lo[d]
+            hi[d] = params.period_hi[d]
+    return per, lo, hi
+
+
+def link_list(x, h, dim, fp32=False, params=None, direct=False):
+    """Pairs (i < j) by link_list / direct_find. Returns (pi, pj, cell_ids, grid)
+    where grid = dict(o, size, n, ncells)."""
+    dt = np.float32 if fp32 else np.float64
+    x = np.ascontiguousarray(x, dt)
+    h = np.ascontiguousarray(h, dt)
+    n = h.shape[0]
+    per, lo, hi = _per(params, dim)
+    cid = np.zeros(n, np.int64)
+    grid = np.zeros(10, np.float64)
+    f = lib().ao_link_list_f32 if fp32 else lib().ao_link_list_f64
+    npairs = f(n, dim, _p(x), _p(h), _p(per), _p(lo), _p(hi), None, None, 0, _p(cid), _p(grid),
+               int(direct))
+    if npairs < 0:
+        raise RuntimeError("oracle link_list failed")
+    pi = np.zeros(npairs, np.int32)
+    pj = np.zeros(npairs, np.int32)
+    f(n, dim, _p(x), _p(h), _p(per), _p(lo), _p(hi), _p(pi), _p(pj), npairs, None, None, int(direct))
+    g = dict(o=grid[0:3].copy(), size=grid[3:6].copy(), n=grid[6:9].astype(np.int64),
+             ncells=int(grid[9]))
+    return pi, pj, cid, g
+
+
+def kernel(r, h, dim, legacy3d=0):
+    r = np.ascontiguousarray(r, np.float64)
+    h = np.ascontiguousarray(np.broadcast_to(h, r.shape), np.float64)
+    w = np.zeros_like(r)
+    dw = np.zeros_like(r)
+    lib().ao_kernel_f64(dim, legacy3d, r.size, _p(r), _p(h), _p(w), _p(dw))
+    return w, dw
+
+
+def tait(rho, rho0, c0, pmin=-np.inf, clamp=False):
+    rho = np.ascontiguousarray(rho, np.float64)
+    p = np.zeros_like(rho)
+    lib().ao_tait_f64(rho.size, _p(rho), rho0, c0, pmin, int(clamp), _p(p))
+    return p
+
+
+def forces(params: Params, x, v, m, rho, p, u, h, itype):
+    """int_force (+ art_visc) rates for given rho, p (FP64)."""
+    d = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    x, v, m, rho, p, u, h = map(d, (x, v, m, rho, p, u, h))
+    itype = np.ascontiguousarray(itype, np.int32)
+    n = m.shape[0]
+    dim = params.dim
+    dv = np.zeros(n * dim, np.float64)
+    du = np.zeros(n, np.float64)
+    rc = lib().ao_forces_f64(C.byref(params), n, _p(x), _p(v), _p(m), _p(rho), _p(p), _p(u),
+                             _p(h), _p(itype), _p(dv), _p(du))
+    if rc:
+        raise RuntimeError("oracle forces failed")
+    return dv, du
+
+
+class State:
+    """FP64 (or FP32) copy of a case's arrays for the oracle."""
+
+    def __init__(self, case, dtype=np.float64):
+        self.dim = case.dim
+        self.params = case.params
+        d = lambda a: np.array(a, dtype=dtype)  # noqa: E731
+        self.x, self.v, self.m = d(case.x), d(case.v), d(case.mass)
+        self.rho, self.p, self.u, self.h = d(case.rho), d(case.p), d(case.u), d(case.h)
+        self.dvdt, self.dudt = d(case.dvdt), d(case.dudt)
+        self.itype = np.array(case.itype, np.int32)
+        self.extra = None
+
+    @property
+    def n(self):
+        return self.m.shape[0]
+
+
+def step(state: State, its: int, dt: float, nbr_fp32: bool = False, extra: bool = False):
+    """One leapfrog iteration of the pair-loop oracle (in place)."""
+    n = state.n
+    ex = np.zeros(2 * n, np.float64) if extra else None
+    if state.x.dtype == np.float64:
+        rc = lib().ao_step_f64(C.byref(state.params), n, its, dt, _p(state.x), _p(state.v),
+                               _p(state.m), _p(state.rho), _p(state.p), _p(state.u), _p(state.h),
+                               _p(state.itype), _p(state.dvdt), _p(state.dudt), int(nbr_fp32),
+                               _p(ex) if extra else None)
+    else:
+        rc = lib().ao_step_f32(C.byref(state.params), n, its, dt, _p(state.x), _p(state.v),
+                               _p(state.m), _p(state.rho), _p(state.p), _p(state.u), _p(state.h),
+                               _p(state.itype), _p(state.dvdt), _p(state.dudt))
+    if rc:
+        raise RuntimeError("oracle step failed")
+    if extra:
+        state.extra = ex.reshape(n, 2)
+    return state
+
+
+def integrate_gather(state: State, its0: int, steps: int, dt: float, nthreads: int = 0):
+    """`steps` iterations of the threaded FP64 gather form (in place)."""
+    if nthreads <= 0:
+        nthreads = lib().ao_hardware_threads()
+    rc = lib().ao_integrate_gather_f64(C.byref(state.params), state.n, its0, steps, dt,
+                                       _p(state.x), _p(state.v), _p(state.m), _p(state.rho),
+                                       _p(state.p), _p(state.u), _p(state.h), _p(state.itype),
+                                       _p(state.dvdt), _p(state.dudt), nthreads)
+    if rc:
+        raise RuntimeError("oracle gather integrate failed")
+    return state
+
+
+def hardware_threads() -> int:
+    return lib().ao_hardware_threads()

@@ -1,0 +1,246 @@
+// oracle_capi.cpp -- extern "C" entry points of the CPU oracle, for the test
+// suite, the smoke check and the CPU-baseline leg of the benchmark only.
+// The product library never links this file.
+#include <cstdio>
+#include <cstring>
+
+#include "../include/armando.h"
+#include "armando_oracle.hpp"
+#include "armando_oracle_gather.hpp"
+
+namespace {
+
+template <class R>
+ao::Params<R> to_params(const armando_params* p) {
+    ao::Params<R> P;
+    P.dim = p->dim;
+    P.pa_sph = p->pa_sph;
+    P.visc = p->visc;
+    P.visc_artificial = p->visc_artificial;
+    P.heat_artificial = p->heat_artificial;
+    P.heat_external = p->heat_external;
+    P.kernel_3d_legacy = p->kernel_3d_legacy;
+    for (int d = 0; d < 3; ++d) {
+        P.periodic[d] = p->periodic[d];
+        P.gravity[d] = R(p->gravity[d]);
+        P.heat_center[d] = R(p->heat_center[d]);
+        P.period_lo[d] = p->period_lo[d];
+        P.period_hi[d] = p->period_hi[d];
+    }
+    P.rho0 = R(p->rho0);
+    P.c0 = R(p->c0);
+    P.pmin = R(p->pmin);
+    P.eta = R(p->eta);
+    P.av_alpha = R(p->av_alpha);
+    P.av_beta = R(p->av_beta);
+    P.av_eta = R(p->av_eta);
+    P.ah_g1 = R(p->ah_g1);
+    P.ah_g2 = R(p->ah_g2);
+    P.ah_eta = R(p->ah_eta);
+    P.heat_q0 = R(p->heat_q0);
+    P.heat_sigma = R(p->heat_sigma);
+    P.heat_t_end = p->heat_t_end;
+    return P;
+}
+
+template <class R>
+ao::State<R> load_state(int dim, int64_t n, const R* x, const R* v, const R* m, const R* rho,
+                        const R* p, const R* u, const R* h, const int* itype, const R* dvdt,
+                        const R* dudt) {
+    ao::State<R> s;
+    s.n = n;
+    s.dim = dim;
+    s.x.assign(x, x + n * dim);
+    s.v.assign(v, v + n * dim);
+    s.m.assign(m, m + n);
+    s.rho.assign(rho, rho + n);
+    s.p.assign(p, p + n);
+    s.u.assign(u, u + n);
+    s.h.assign(h, h + n);
+    s.c.assign(n, R(0));
+    s.itype.assign(itype, itype + n);
+    if (dvdt) s.dvdt.assign(dvdt, dvdt + n * dim);
+    else s.dvdt.assign(n * dim, R(0));
+    if (dudt) s.dudt.assign(dudt, dudt + n);
+    else s.dudt.assign(n, R(0));
+    return s;
+}
+
+template <class R>
+void store_state(const ao::State<R>& s, R* x, R* v, R* rho, R* p, R* u, R* dvdt, R* dudt) {
+    std::memcpy(x, s.x.data(), sizeof(R) * s.n * s.dim);
+    std::memcpy(v, s.v.data(), sizeof(R) * s.n * s.dim);
+    std::memcpy(rho, s.rho.data(), sizeof(R) * s.n);
+    std::memcpy(p, s.p.data(), sizeof(R) * s.n);
+    std::memcpy(u, s.u.data(), sizeof(R) * s.n);
+    if (dvdt) std::memcpy(dvdt, s.dvdt.data(), sizeof(R) * s.n * s.dim);
+    if (dudt) std::memcpy(dudt, s.dudt.data(), sizeof(R) * s.n);
+}
+
+template <class Rc>
+int64_t link_list_impl(int64_t n, int dim, const Rc* x, const Rc* h, const int* periodic,
+                       const double* lo, const double* hi, int32_t* pi, int32_t* pj, int64_t cap,
+                       int64_t* cell_ids, double* grid_out, int use_direct) {
+    int per0[3] = {0, 0, 0};
+    const int* per = periodic ? periodic : per0;
+    double lo0[3] = {0, 0, 0}, hi0[3] = {0, 0, 0};
+    ao::PairList pl;
+    std::vector<int64_t> cid;
+    ao::Grid<Rc> g;
+    try {
+        g = ao::link_list<Rc>(n, dim, x, h, per, lo ? lo : lo0, hi ? hi : hi0, pl, &cid);
+        if (use_direct) ao::direct_find<Rc>(n, dim, x, h, per, g, pl);
+    } catch (const std::exception&) {
+        return -1;
+    }
+    if (cell_ids) std::memcpy(cell_ids, cid.data(), sizeof(int64_t) * n);
+    if (grid_out) {  // o[3], size[3], n[3], ncells
+        for (int d = 0; d < 3; ++d) {
+            grid_out[d] = (double)g.o[d];
+            grid_out[3 + d] = (double)g.size[d];
+            grid_out[6 + d] = (double)g.n[d];
+        }
+        grid_out[9] = (double)g.ncells;
+    }
+    int64_t np = (int64_t)pl.pi.size();
+    if (pi && pj && np <= cap) {
+        std::memcpy(pi, pl.pi.data(), sizeof(int32_t) * np);
+        std::memcpy(pj, pl.pj.data(), sizeof(int32_t) * np);
+    }
+    return np;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Neighbour pairs (i < j) by link_list (use_direct = 0) or direct_find (1), in
+// FP64 or FP32 coordinates. Returns the pair count (pairs copied only when it
+// fits in cap), -1 on error. grid_out: o[3], size[3], n[3], ncells.
+int64_t ao_link_list_f64(int64_t n, int dim, const double* x, const double* h, const int* periodic,
+                         const double* lo, const double* hi, int32_t* pi, int32_t* pj, int64_t cap,
+                         int64_t* cell_ids, double* grid_out, int use_direct) {
+    return link_list_impl<double>(n, dim, x, h, periodic, lo, hi, pi, pj, cap, cell_ids, grid_out,
+                                  use_direct);
+}
+int64_t ao_link_list_f32(int64_t n, int dim, const float* x, const float* h, const int* periodic,
+                         const double* lo, const double* hi, int32_t* pi, int32_t* pj, int64_t cap,
+                         int64_t* cell_ids, double* grid_out, int use_direct) {
+    return link_list_impl<float>(n, dim, x, h, periodic, lo, hi, pi, pj, cap, cell_ids, grid_out,
+                                 use_direct);
+}
+
+// Wendland W and dW/dr at (r, h) (armando.cu:137-191).
+void ao_kernel_f64(int dim, int legacy3d, int64_t n, const double* r, const double* h, double* w,
+                   double* dwdr) {
+    for (int64_t i = 0; i < n; ++i) {
+        w[i] = ao::kernel_w(r[i], h[i], dim, legacy3d);
+        dwdr[i] = ao::kernel_dwdr(r[i], h[i], dim, legacy3d);
+    }
+}
+
+// Tait pressure (eos.f90:255-283) of every rho, without the pmin clamp when
+// clamp == 0.
+void ao_tait_f64(int64_t n, const double* rho, double rho0, double c0, double pmin, int clamp,
+                 double* p) {
+    ao::Params<double> P;
+    P.rho0 = rho0;
+    P.c0 = c0;
+    P.pmin = clamp ? pmin : -INFINITY;
+    for (int64_t i = 0; i < n; ++i) {
+        double r = rho[i];
+        ao::eos_tait(r, p[i], P);
+    }
+}
+
+// int_force (+ art_visc when enabled) rates with the given rho and p (no
+// density summation, no EOS): dvdt[n*dim], dudt[n]. Pairs from link_list.
+int ao_forces_f64(const armando_params* prm, int64_t n, const double* x, const double* v,
+                  const double* m, const double* rho, const double* p, const double* u,
+                  const double* h, const int* itype, double* dvdt, double* dudt) {
+    ao::Params<double> P = to_params<double>(prm);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, nullptr, nullptr);
+    for (int64_t i = 0; i < n; ++i) s.c[i] = P.c0;
+    ao::PairList pl;
+    ao::Grid<double> g;
+    try {
+        g = ao::neighbour_search<double, double>(s, P, pl);
+    } catch (const std::exception&) {
+        return 1;
+    }
+    std::vector<double> dv, du, tds, avdv, avdu;
+    ao::int_force(s, g, P, pl, dv, du, tds);
+    if (P.visc_artificial) {
+        ao::art_visc(s, g, P, pl, avdv, avdu);
+        for (size_t k = 0; k < dv.size(); ++k) dv[k] += avdv[k];
+        for (size_t k = 0; k < du.size(); ++k) du[k] += avdu[k];
+    }
+    std::memcpy(dvdt, dv.data(), sizeof(double) * n * P.dim);
+    std::memcpy(dudt, du.data(), sizeof(double) * n);
+    return 0;
+}
+
+// One leapfrog iteration `its` (time_integration.f:131-218), pair-loop form.
+// nbr_fp32 = 1 runs the neighbour search in FP32 coordinates (GPU mirror).
+// extra (optional, n*2): per particle tdsdt, divv of the step.
+int ao_step_f64(const armando_params* prm, int64_t n, int its, double dt, double* x, double* v,
+                const double* m, double* rho, double* p, double* u, const double* h,
+                const int* itype, double* dvdt, double* dudt, int nbr_fp32, double* extra) {
+    ao::Params<double> P = to_params<double>(prm);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
+    ao::Rates<double> r;
+    try {
+        if (nbr_fp32) ao::leapfrog_step<double, float>(s, P, its, dt, &r);
+        else ao::leapfrog_step<double, double>(s, P, its, dt, &r);
+    } catch (const std::exception&) {
+        return 1;
+    }
+    store_state(s, x, v, rho, p, u, dvdt, dudt);
+    if (extra) {
+        for (int64_t i = 0; i < n; ++i) {
+            extra[2 * i] = r.tdsdt.empty() ? 0.0 : r.tdsdt[i];
+            extra[2 * i + 1] = r.divv.empty() ? 0.0 : r.divv[i];
+        }
+    }
+    return 0;
+}
+
+// Same iteration evaluated entirely in FP32 (the error floor of plain FP32
+// arithmetic on this algorithm).
+int ao_step_f32(const armando_params* prm, int64_t n, int its, double dt, float* x, float* v,
+                const float* m, float* rho, float* p, float* u, const float* h, const int* itype,
+                float* dvdt, float* dudt) {
+    ao::Params<float> P = to_params<float>(prm);
+    ao::State<float> s = load_state<float>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
+    try {
+        ao::leapfrog_step<float, float>(s, P, its, dt);
+    } catch (const std::exception&) {
+        return 1;
+    }
+    store_state(s, x, v, rho, p, u, dvdt, dudt);
+    return 0;
+}
+
+// `steps` iterations its0.. of the threaded gather form (FP64) on nthreads
+// host threads. The CPU baseline.
+int ao_integrate_gather_f64(const armando_params* prm, int64_t n, int its0, int steps, double dt,
+                            double* x, double* v, const double* m, double* rho, double* p,
+                            double* u, const double* h, const int* itype, double* dvdt,
+                            double* dudt, int nthreads) {
+    ao::Params<double> P = to_params<double>(prm);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
+    try {
+        for (int k = 0; k < steps; ++k) ao::leapfrog_step_gather(s, P, its0 + k, dt, nthreads);
+    } catch (const std::exception&) {
+        return 1;
+    }
+    store_state(s, x, v, rho, p, u, dvdt, dudt);
+    return 0;
+}
+
+int ao_hardware_threads(void) {
+    unsigned t = std::thread::hardware_concurrency();
+    return t ? (int)t : 1;
+}
+
+}  // extern "C"

@@ -1,0 +1,58 @@
+"""The oracle against golden outputs of the reference's own C host path
+(ArmandoThrust/acpu.c), recorded by tests/golden/make_golden.py."""
+import numpy as np
+
+from armando_gb300._abi import Params
+
+
+def test_wendland_matches_acpu(O, golden):
+    w, dw = O.kernel(golden["wendland_r"].astype(np.float64),
+                     golden["wendland_h"].astype(np.float64), 2)
+    assert np.abs(w - golden["wendland_w"]).max() <= 1e-6 * np.abs(w).max()
+    assert np.abs(dw - golden["wendland_dwdr"]).max() <= 1e-6 * np.abs(dw).max()
+
+
+def test_tait_matches_acpu(O, golden):
+    pr = golden["tait_props"]
+    p = O.tait(golden["tait_rho"], float(pr[0]), float(pr[1]))
+    # acpu.c evaluates powf(rho/rho0, 7) - 1 in FP32 (cancellation ~1e-6 of B).
+    assert np.abs(p - golden["tait_p"]).max() <= 2e-5 * np.abs(p).max()
+
+
+def test_cell_hash_matches_acpu_bit_exact(O, golden):
+    _, _, cid, g = O.link_list(golden["lattice_x"], golden["lattice_h"], 2, fp32=True)
+    gg = golden["lattice_grid"]
+    assert np.allclose([g["o"][0], g["o"][1], g["size"][0], g["n"][0], g["n"][1]], gg, rtol=0, atol=0)
+    assert np.array_equal(cid, golden["lattice_hash"].astype(np.int64))
+
+
+def test_neighbour_lists_match_acpu(O, golden):
+    n = golden["lattice_h"].size
+    pi, pj, _, _ = O.link_list(golden["lattice_x"], golden["lattice_h"], 2)
+    rows = [set() for _ in range(n)]
+    for a, b in zip(pi, pj):
+        rows[a].add(b)
+        rows[b].add(a)
+    offs, nbr = golden["list_offs"], golden["list_nbr"]
+    # acpu.c keeps at most MAXN = 21 entries (self included): no row may be truncated.
+    assert golden["list_count_with_self"].max() <= 21
+    for i in range(n):
+        assert set(nbr[offs[i]:offs[i + 1]].tolist()) == rows[i]
+
+
+def test_pressure_force_pa_sph0_matches_acpu(O, golden):
+    n = golden["lattice_h"].size
+    x = golden["lattice_x"]
+    P = Params.default(dim=2, pa_sph=0, rho0=1000.0, c0=20.0)
+    dv, _ = O.forces(P, x, np.zeros_like(x), golden["force_mass"], golden["force_rho"],
+                     golden["force_p"], np.zeros(n), golden["lattice_h"], np.ones(n, np.int32))
+    assert np.abs(dv - golden["force_acc"]).max() <= 2e-6 * np.abs(dv).max()
+
+
+def test_pressure_force_pa_sph1_matches_acpu_uniform_rho(O, golden):
+    n = golden["lattice_h"].size
+    x = golden["lattice_x"]
+    P = Params.default(dim=2, pa_sph=1, rho0=1000.0, c0=20.0)
+    dv, _ = O.forces(P, x, np.zeros_like(x), golden["force_mass"], np.full(n, 1000.0),
+                     golden["force_p"], np.zeros(n), golden["lattice_h"], np.ones(n, np.int32))
+    assert np.abs(dv - golden["force_acc_uniform_rho"]).max() <= 2e-6 * np.abs(dv).max()
