@@ -93,6 +93,7 @@ struct StateB {  // working set of one step (cell order)
     float4* tau;   // eta T_ab / rho^2 (or eta T_ab): {xx, yy, xy, zz}
     float4* tau2;  // {xz, yz, -, -}
     float* tds;    // T ds/dt
+    float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
 };
 
 template <int DIM>
@@ -500,14 +501,23 @@ __global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, 
     float u = A.u[j];
     const int it = A.itype[j];
     B.vmin[s] = make_float4(vm.x, vm.y, vm.z, u);
+    float ulo = 0.f;
     if (it > 0 && S.hdt != 0.f) {
         const float4 ap = A.ap[j];
         vm.x = fmaf(S.hdt, ap.x, vm.x);
         vm.y = fmaf(S.hdt, ap.y, vm.y);
         if (DIM == 3) vm.z = fmaf(S.hdt, ap.z, vm.z);
-        u = fmaf(S.hdt, ap.w, u);
-        if (u < 0.f) u = 0.f;
+        // u + dt/2 du kept as hi + lo: art_heat differences u_i - u_j of nearly
+        // equal energies would otherwise carry the rounding of u_half.
+        const sph::ff uh = sph::two_sum(u, __fmul_rn(S.hdt, ap.w));
+        u = uh.hi;
+        ulo = uh.lo;
+        if (u < 0.f) {
+            u = 0.f;
+            ulo = 0.f;
+        }
     }
+    if (B.ulo) B.ulo[s] = ulo;
     B.xh[s] = xh;
     B.vm[s] = vm;
     B.rp[s] = make_float4(A.rho[j], 0.f, u, 0.f);
@@ -595,6 +605,45 @@ __device__ __forceinline__ bool pair_delta(const float4& xi, const float4& xj, c
     return sph::within_support(dr2, xi.w, xj.w);
 }
 
+// Exact pair difference x_i - x_j = dh + dl per axis, minimum image applied
+// exactly on periodic axes (the wrap decision is the pair test's).
+template <int DIM>
+__device__ __forceinline__ void exact_delta(const float4& xi, const float4& xj, const DevGrid& g,
+                                            float* dh, float* dl) {
+    const float a[3] = {xi.x, xi.y, xi.z}, b[3] = {xj.x, xj.y, xj.z};
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        sph::ff s = sph::two_diff(a[k], b[k]);
+        if (g.periodic[k]) {
+            if (s.hi > g.half[k]) {
+                sph::ff u = sph::two_sum(s.hi, -g.L[k]);
+                s.hi = u.hi;
+                s.lo = __fadd_rn(s.lo, u.lo);
+            } else if (s.hi < -g.half[k]) {
+                sph::ff u = sph::two_sum(s.hi, g.L[k]);
+                s.hi = u.hi;
+                s.lo = __fadd_rn(s.lo, u.lo);
+            }
+        }
+        dh[k] = s.hi;
+        dl[k] = s.lo;
+    }
+}
+
+// On periodic axes the pair test's difference is rounded twice ((x_i - x_j)
+// then +- L); the force passes use the correctly rounded one instead.
+template <int DIM>
+__device__ __forceinline__ void refine_periodic(const float4& xi, const float4& xj,
+                                                const DevGrid& g, float* d, float& dr2) {
+    if (!(g.periodic[0] | g.periodic[1] | g.periodic[2])) return;
+    float dh[3], dl[3];
+    exact_delta<DIM>(xi, xj, g, dh, dl);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+        if (g.periodic[k]) d[k] = __fadd_rn(dh[k], dl[k]);
+    dr2 = sph::dist2_exact<DIM>(d);
+}
+
 template <int DIM>
 __device__ __forceinline__ sph::ff ff_pow_dim(sph::ff ih) {
     sph::ff a = sph::ff_sqr(ih);
@@ -654,9 +703,12 @@ __global__ void __launch_bounds__(kPassThreads)
                 ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
                 al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
             }
-            sph::ff_acc(S, sph::wendland_mw_ff<DIM>(d, ih, al, mj));
+            float dh[3], dl[3];
+            exact_delta<DIM>(xi, xj, g, dh, dl);
+            sph::ff_acc(S, sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj));
         }
         if (need_div) {
+            refine_periodic<DIM>(xi, xj, g, d, dr2);
             float ih = ihf, kgih = kgih_i;
             if (xj.w != xi.w) {
                 ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
@@ -711,6 +763,7 @@ __global__ void __launch_bounds__(kPassThreads)
         const float4 xj = __ldg(B.xh + k);
         float d[3], dr2;
         if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
+        refine_periodic<DIM>(xi, xj, g, d, dr2);
         const float4 vj = __ldg(B.vm + k);
         const float mj = mass_of<DIM>(xj, vj);
         const float rhoj = __ldg(&B.rp[k].x);
@@ -788,11 +841,13 @@ __global__ void __launch_bounds__(kPassThreads)
         if (DIM == 3) ti2 = B.tau2[s];
     }
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
+    const float ulo_i = P.heat_art ? B.ulo[s] : 0.f;
     for_candidates<DIM>(g, start, cc, [&](int k) {
         if (k == s) return;
         const float4 xj = __ldg(B.xh + k);
         float d[3], dr2;
         if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
+        refine_periodic<DIM>(xi, xj, g, d, dr2);
         const float4 vj = __ldg(B.vm + k);
         const float4 rpj = __ldg(B.rp + k);
         const float mj = mass_of<DIM>(xj, vj);
@@ -866,7 +921,8 @@ __global__ void __launch_bounds__(kPassThreads)
             float rdw = d[0] * w0 + d[1] * w1;
             if (DIM == 3) rdw += d[2] * w2;
             const float psi = (rpi.w + rpj.w) / (rho_bar * (dr2 + mh * mh * P.ah_eta2)) * rdw;
-            ah_du = fmaf(mj * psi, rpi.z - rpj.z, ah_du);
+            const float du_ij = (rpi.z - rpj.z) + (ulo_i - __ldg(B.ulo + k));
+            ah_du = fmaf(mj * psi, du_ij, ah_du);
         }
         (void)pi_i;
     });

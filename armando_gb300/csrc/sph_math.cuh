@@ -43,6 +43,13 @@ SPH_HD ff two_sum(float a, float b) {
     float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
     return {s, e};
 }
+// a - b == s + e exactly (TwoSum of a and -b).
+SPH_HD ff two_diff(float a, float b) {
+    float s = __fsub_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    float e = __fsub_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fadd_rn(b, bb));
+    return {s, e};
+}
 // Dekker Fast2Sum, requires |a| >= |b|.
 SPH_HD ff fast_two_sum(float a, float b) {
     float s = __fadd_rn(a, b);
@@ -106,23 +113,26 @@ SPH_HD float min_image(float dx, float L, float half) {
 }
 
 // ---- Wendland weight in float-float (density pass) ----
-// Returns m_j * W(r, h) with |relative error| ~1e-12 for exactly given dx,
-// h = (h_i + h_j)/2 passed as its reciprocal ih and the dim-dependent
-// prefactor alpha = K_dim * ih^dim (both float-float).
+// Returns m_j * W(r, h) with relative error ~1e-12 for the exact pair
+// difference x_i - x_j = dh + dl per axis (a float difference is not exact
+// when the coordinates differ by more than a factor 2, e.g. near the origin),
+// h = (h_i + h_j)/2 passed as its reciprocal ih and the prefactor
+// alpha = K_dim * ih^dim (both float-float).
 template <int DIM>
-SPH_HD ff wendland_mw_ff(const float* d, ff ih, ff alpha, float mj) {
-    // dr^2 exactly as hi + lo.
-    ff s = two_prod(d[0], d[0]);
-    ff t1 = two_prod(d[1], d[1]);
-    ff acc = two_sum(s.hi, t1.hi);
-    float lo = __fadd_rn(__fadd_rn(acc.lo, s.lo), t1.lo);
-    if (DIM == 3) {
-        ff t2 = two_prod(d[2], d[2]);
-        ff a2 = two_sum(acc.hi, t2.hi);
-        acc.hi = a2.hi;
-        lo = __fadd_rn(lo, __fadd_rn(a2.lo, t2.lo));
+SPH_HD ff wendland_mw_ff(const float* dh, const float* dl, ff ih, ff alpha, float mj) {
+    // dr^2 = sum (dh + dl)^2 as hi + lo (dl^2 is below the float-float unit).
+    ff s0 = two_prod(dh[0], dh[0]);
+    float hi = s0.hi;
+    float lo = fmaf(__fmul_rn(2.0f, dh[0]), dl[0], s0.lo);
+#pragma unroll
+    for (int a = 1; a < DIM; ++a) {
+        ff sa = two_prod(dh[a], dh[a]);
+        float la = fmaf(__fmul_rn(2.0f, dh[a]), dl[a], sa.lo);
+        ff t = two_sum(hi, sa.hi);
+        hi = t.hi;
+        lo = __fadd_rn(lo, __fadd_rn(t.lo, la));
     }
-    ff dr2 = fast_two_sum(acc.hi, lo);
+    ff dr2 = fast_two_sum(hi, lo);
     // r = sqrt(dr2) with one Newton correction.
     ff r;
     r.hi = __fsqrt_rn(dr2.hi);

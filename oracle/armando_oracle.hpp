@@ -68,6 +68,13 @@ struct Params {
 // alpha_2D = 7/(4 pi h^2) (acpu.c:162); alpha_3D = 21/(16 pi h^3) (acpu.c:159),
 // or 15/(16 pi h^3) with kernel_3d_legacy (armando.cu:150).
 // ---------------------------------------------------------------------------
+// Periodic box length, fixed as the FP32 difference of the FP32 bounds (the
+// library computes it the same way).
+template <class P>
+inline double period_length(const P& prm, int d) {
+    return (double)((float)prm.period_hi[d] - (float)prm.period_lo[d]);
+}
+
 template <class R>
 inline R kernel_alpha(const R& h, int dim, int legacy3d) {
     if (dim == 2) return R(7.0) / (R(4.0) * R(kPi) * h * h);
@@ -156,7 +163,7 @@ Grid<Rc> make_grid(int64_t nt, int dim, const Rc* x, const Rc* h, const int* per
     g.ncells = 1;
     for (int d = 0; d < dim; ++d) {
         if (periodic[d]) {
-            Rc L = Rc(hi[d]) - Rc(lo[d]);
+            Rc L = Rc((float)hi[d] - (float)lo[d]);
             int n = (int)(L / cell);
             if (n < 3) throw std::runtime_error("periodic axis shorter than 3 cells");
             g.o[d] = Rc(lo[d]);
@@ -323,7 +330,7 @@ inline void pair_geom(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, 
     for (int d = 0; d < dim; ++d) {
         R dx = s.x[(int64_t)i * dim + d] - s.x[(int64_t)j * dim + d];
         if (P.periodic[d]) {
-            R L = R(P.period_hi[d] - P.period_lo[d]);
+            R L = R(period_length(P, d));
             if (dx > R(0.5) * L) dx = dx - L;
             else if (dx < -R(0.5) * L) dx = dx + L;
         }
@@ -587,7 +594,7 @@ template <class R>
 inline void wrap_periodic(State<R>& s, const Params<R>& P, int64_t i) {
     for (int d = 0; d < s.dim; ++d) {
         if (!P.periodic[d]) continue;
-        R lo = R(P.period_lo[d]), hi = R(P.period_hi[d]), L = hi - lo;
+        R lo = R(P.period_lo[d]), hi = R(P.period_hi[d]), L = R(period_length(P, d));
         R& xv = s.x[i * s.dim + d];
         if (!(xv < hi)) xv = xv - L;
         else if (xv < lo) xv = xv + L;
