@@ -130,7 +130,7 @@ EXPORTED = [
     "armando_step", "armando_integrate", "armando_cell_ids",
     "armando_neighbours", "armando_sync", "armando_get_stats",
     "armando_last_error", "armando_destroy", "armando_abi_version",
-    "armando_get_stream", "armando_profile_phases",
+    "armando_get_stream", "armando_profile_phases", "armando_cell_ids_noalloc",
 ]
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
@@ -181,6 +181,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_get_stream.restype = C.c_int
     lib.armando_profile_phases.argtypes = [vp, C.c_int32, C.POINTER(C.c_float)]
     lib.armando_profile_phases.restype = C.c_int
+    lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
+    lib.armando_cell_ids_noalloc.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

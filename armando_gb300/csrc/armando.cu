@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -22,7 +23,14 @@ using namespace ag;
 
 namespace {
 
-thread_local std::string g_last_error = "no error";
+// Last error of context-less calls; a fixed buffer so that setting it never
+// allocates.
+thread_local char g_last_error[256] = "no error";
+
+void set_last_error(const char* msg) {
+    std::strncpy(g_last_error, msg, sizeof(g_last_error) - 1);
+    g_last_error[sizeof(g_last_error) - 1] = '\0';
+}
 
 struct GraphKey {
     float kdt, hdt, dt;
@@ -87,7 +95,7 @@ namespace {
 
 armando_status fail(armando_ctx* c, armando_status st, const std::string& msg) {
     if (c) c->err = msg;
-    g_last_error = msg;
+    set_last_error(msg.c_str());
     return st;
 }
 
@@ -520,9 +528,111 @@ armando_status check_step_args(armando_ctx* ctx, const void* x, const void* vx, 
     return ARMANDO_OK;
 }
 
+
+// ---- Allocation-free cell ids (armando_cell_ids_noalloc) -------------------
+// Scratch of the grid reduction in a file-scope device array instead of
+// cudaMalloc'd memory. It is held by every device that loads the library until
+// the process exits, and shared by every call (which is why overlapping calls
+// race on it).
+constexpr size_t kNoAllocScratchBytes = 32768;
+constexpr size_t kNoAllocPartOff = 0;  // kBBoxBlocks x 8 floats of bbox partials
+constexpr size_t kNoAllocGridOff = (size_t)kBBoxBlocks * 8 * sizeof(float);
+constexpr size_t kNoAllocFlagsOff = (kNoAllocGridOff + sizeof(DevGrid) + 255) & ~(size_t)255;
+constexpr int64_t kNoAllocMaxParticles = (int64_t)1 << 30;
+constexpr long long kNoAllocMaxCells = (long long)1 << 30;
+static_assert(kNoAllocFlagsOff + sizeof(unsigned) <= kNoAllocScratchBytes, "scratch too small");
+static_assert(kNoAllocGridOff % 16 == 0, "grid record alignment");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the host-side symbol is not a device address).
+armando_status noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error("armando_cell_ids_noalloc: cudaGetDevice failed");
+        return ARMANDO_ERR_NO_DEVICE;
+    }
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_last_error("armando_cell_ids_noalloc: device ordinal out of range");
+        return ARMANDO_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            set_last_error("armando_cell_ids_noalloc: cudaGetSymbolAddress of the scratch failed");
+            return ARMANDO_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return ARMANDO_OK;
+}
+
+armando_status noalloc_fail(armando_status st, const char* msg) {
+    set_last_error(msg);
+    return st;
+}
+
 }  // namespace
 
 extern "C" {
+
+armando_status armando_cell_ids_noalloc(const armando_params* params, const float* x,
+                                        const float* hsml, int64_t n, int32_t* cell,
+                                        void* stream) {
+    if (!params) return noalloc_fail(ARMANDO_ERR_INVALID_ARG, "armando_cell_ids_noalloc: params is NULL");
+    const int dim = params->dim;
+    if (dim != 2 && dim != 3) return noalloc_fail(ARMANDO_ERR_INVALID_ARG, "armando_cell_ids_noalloc: dim must be 2 or 3");
+    for (int d = 0; d < dim; ++d)
+        if (params->periodic[d] && !(params->period_hi[d] > params->period_lo[d]))
+            return noalloc_fail(ARMANDO_ERR_INVALID_ARG, "armando_cell_ids_noalloc: periodic axis needs period_hi > period_lo");
+    if (n < 0 || n > kNoAllocMaxParticles)
+        return noalloc_fail(ARMANDO_ERR_INVALID_ARG,
+                            "armando_cell_ids_noalloc: n must be in [0, 2^30] (limit of the static scratch's grid reduction)");
+    if (n == 0) return ARMANDO_OK;
+    if (!x || !hsml || !cell) return noalloc_fail(ARMANDO_ERR_INVALID_ARG, "armando_cell_ids_noalloc: NULL array");
+    unsigned char* base = nullptr;
+    armando_status st = noalloc_scratch(&base);
+    if (st != ARMANDO_OK) return st;
+    float* part = reinterpret_cast<float*>(base + kNoAllocPartOff);
+    DevGrid* grid = reinterpret_cast<DevGrid*>(base + kNoAllocGridOff);
+    unsigned* flags = reinterpret_cast<unsigned*>(base + kNoAllocFlagsOff);
+    const DevParams dp = make_dev_params(*params);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nn = (int)n;
+    // The status word keeps the previous call's value: clear it first.
+    if (cudaMemsetAsync(flags, 0, sizeof(unsigned), s) != cudaSuccess) {
+        cudaGetLastError();
+        return noalloc_fail(ARMANDO_ERR_CUDA, "armando_cell_ids_noalloc: cudaMemsetAsync failed");
+    }
+    if (dim == 2) k_bbox_partial_raw<2><<<kBBoxBlocks, 256, 0, s>>>(x, hsml, nn, part);
+    else k_bbox_partial_raw<3><<<kBBoxBlocks, 256, 0, s>>>(x, hsml, nn, part);
+    k_bbox_final<<<1, 256, 0, s>>>(part, kBBoxBlocks, dp, kNoAllocMaxCells, grid, flags);
+    if (dim == 2) k_keys_raw<2><<<blocks_for(nn, 256), 256, 0, s>>>(x, nn, grid, reinterpret_cast<int*>(cell));
+    else k_keys_raw<3><<<blocks_for(nn, 256), 256, 0, s>>>(x, nn, grid, reinterpret_cast<int*>(cell));
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(ARMANDO_ERR_CUDA, "armando_cell_ids_noalloc: kernel launch failed");
+    unsigned hflags = 0;
+    if (cudaMemcpyAsync(&hflags, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        cudaGetLastError();
+        return noalloc_fail(ARMANDO_ERR_CUDA, "armando_cell_ids_noalloc: stream synchronisation failed");
+    }
+    if (hflags & FLAG_PERIODIC_SMALL)
+        return noalloc_fail(ARMANDO_ERR_INVALID_ARG, "armando_cell_ids_noalloc: periodic box shorter than 3 cells of 2*max(h)");
+    if (hflags & FLAG_GRID_OVERFLOW)
+        return noalloc_fail(ARMANDO_ERR_GRID_OVERFLOW, "armando_cell_ids_noalloc: grid has more than 2^30 cells");
+    return ARMANDO_OK;
+}
 
 void armando_params_default(armando_params* p) {
     if (!p) return;
@@ -831,7 +941,7 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
 }
 
 const char* armando_last_error(const armando_ctx* ctx) {
-    return ctx ? ctx->err.c_str() : g_last_error.c_str();
+    return ctx ? ctx->err.c_str() : g_last_error;
 }
 
 armando_status armando_destroy(armando_ctx* ctx) {

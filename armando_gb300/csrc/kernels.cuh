@@ -286,6 +286,61 @@ __global__ void __launch_bounds__(kSortThreads)
     hist[threadIdx.x * num_tiles + blockIdx.x] = sh[threadIdx.x];
 }
 
+// Bbox partials straight from caller-layout arrays x[n*DIM], h[n].
+template <int DIM>
+__global__ void __launch_bounds__(256) k_bbox_partial_raw(const float* __restrict__ x,
+                                                          const float* __restrict__ h, int n,
+                                                          float* __restrict__ part) {
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mh = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+            const float v = x[(size_t)DIM * i + d];
+            mn[d] = fminf(mn[d], v);
+            mx[d] = fmaxf(mx[d], v);
+        }
+        mh = fmaxf(mh, h[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+        mh = fmaxf(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+    }
+    __shared__ float s[8][7];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        for (int d = 0; d < 3; ++d) {
+            s[warp][d] = mn[d];
+            s[warp][3 + d] = mx[d];
+        }
+        s[warp][6] = mh;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        int k = threadIdx.x;
+        float v = s[0][k];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+            v = (k < 3) ? fminf(v, s[w][k]) : fmaxf(v, s[w][k]);
+        part[blockIdx.x * 8 + k] = v;
+    }
+}
+
+// Cell keys straight from caller-layout positions x[n*DIM].
+template <int DIM>
+__global__ void k_keys_raw(const float* __restrict__ x, int n, const DevGrid* __restrict__ gp,
+                           int* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    DevGrid g = *gp;
+    const float4 a = make_float4(x[(size_t)DIM * i], x[(size_t)DIM * i + 1],
+                                 DIM == 3 ? x[(size_t)DIM * i + 2] : 0.f, 0.f);
+    out[i] = (int)cell_key<DIM>(a, g);
+}
+
 // Cell keys only (caller order), for the cell-id entry point.
 template <int DIM>
 __global__ void k_keys_only(const float4* __restrict__ xh, int n, const DevGrid* __restrict__ gp,

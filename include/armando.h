@@ -183,6 +183,30 @@ armando_status armando_get_stream(armando_ctx* ctx, void** stream);
  */
 armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms_per_phase);
 
+/*
+ * Allocation-free form of armando_cell_ids. It has no counterpart in the
+ * reference.
+ * For callers that must not allocate device memory: a host code that hands
+ * the GPU's memory to its own pool at start-up and treats any later cudaMalloc
+ * as an error, or a time loop that cannot afford the device-wide
+ * synchronisation a cudaMalloc/cudaFree implies. It needs no context. x[n*dim]
+ * and hsml[n] are device arrays (read), cell[n] a device array (written), all
+ * on the current device; stream is a cudaStream_t (NULL: legacy default stream).
+ * Its scratch (grid reduction partials, grid record, status word) is a fixed
+ * 32 KiB static device array, which every GPU that loads the library holds
+ * until the process exits. n is limited to 2^30 and the grid to 2^30 cells;
+ * larger sizes return ARMANDO_ERR_INVALID_ARG / ARMANDO_ERR_GRID_OVERFLOW. The
+ * first call on a device looks up the array's device address once
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture. All calls share the one array: calls that overlap
+ * on the GPU (other streams, other host threads) race on it. The call returns
+ * after the stream has finished the work; the last error is readable with
+ * armando_last_error(NULL).
+ */
+armando_status armando_cell_ids_noalloc(const armando_params* params, const float* x,
+                                        const float* hsml, int64_t n, int32_t* cell,
+                                        void* stream);
+
 /* Blocks until the context's stream is idle and returns its sticky status. */
 armando_status armando_sync(armando_ctx* ctx);
 armando_status armando_get_stats(const armando_ctx* ctx, armando_stats* out);
