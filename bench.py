@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="dambreak2d", choices=["dambreak2d", "channel3d"])
+    ap.add_argument("--dx", type=float, default=None,
+                    help="particle spacing override (smaller workloads for profiling)")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -66,12 +68,14 @@ def parse():
     return ap.parse_args()
 
 
-def make_case(name):
+def make_case(name, dx=None):
     from armando_gb300 import cases
 
     if name == "dambreak2d":
-        return cases.dam_break()
-    return cases.channel()
+        return cases.dam_break() if dx is None else cases.dam_break(dx=dx)
+    if dx is None:
+        return cases.channel()
+    return cases.channel(n_x=int(round(0.4 / dx)), n_yz=int(round(0.1 / dx)))
 
 
 def peaks():
@@ -169,7 +173,7 @@ def cpu_baseline(case, budget_s):
 def run_reference(args, rank):
     if rank != 0:
         return None
-    case = make_case(args.config)
+    case = make_case(args.config, args.dx)
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
 
@@ -214,7 +218,7 @@ def run_ours(args, rank, world, local_rank):
     import armando_gb300 as ag
 
     torch.cuda.set_device(local_rank)
-    case = make_case(args.config)
+    case = make_case(args.config, args.dx)
     dist = world > 1
     if dist:
         import torch.distributed as td
@@ -249,7 +253,9 @@ def run_ours(args, rank, world, local_rank):
         ms = float(t.item())
     value = world * case.n * args.steps / (ms * 1e-3)
     # Phase split (same kernels, direct launches with events between phases).
-    phases = ctx.profile_phases(args.profile_steps)
+    phases = ctx.profile_phases(args.profile_steps) if args.profile_steps > 0 else {
+        k: float("nan") for k in ("grid_hash", "radix_sort", "cells_reorder", "density",
+                                  "shear", "force")}
     st = ctx.stats()
     ctx.close()
 
@@ -281,7 +287,9 @@ def run_ours(args, rank, world, local_rank):
             "clocks": clk.summary(),
         }
     # e2e: armando_step with pinned host buffers, one call per step.
-    e2e_steps = args.e2e_steps or max(3, min(args.steps, 20))
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else max(3, min(args.steps, 20))
+    if e2e_steps <= 0:
+        return out
     pinned = {}
     for k, v in case.arrays().items():
         t = torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True)
@@ -315,7 +323,7 @@ def run_ours(args, rank, world, local_rank):
                       "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                       "steps": e2e_steps, "api": "armando_step, pinned host buffers"}
         if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(make_case(args.config), args.cpu_seconds)
+            out["cpu_baseline"] = cpu_baseline(make_case(args.config, args.dx), args.cpu_seconds)
     return out
 
 
