@@ -714,67 +714,208 @@ __device__ __forceinline__ float pow_grad(float ih) {
 }
 
 // ---------------------------------------------------------------------------
-// Pass 1: summation density (float-float), Tait EOS, div v for art_heat.
+// Candidate cursor and per-thread neighbour lists.
+//
+// A pass walks the candidate slots of its particle row by row (a "row" is the
+// contiguous slot range of the 3 x-adjacent cells at one (y, z), or a single
+// cell on a periodic x axis), tests them, and appends the neighbours to a list
+// in shared memory (slot-major [t][thread], conflict-free). The physics then
+// runs over the lists in a warp-converged loop, so lanes do not idle on
+// candidates that failed the pair test. Lists hold kListCap entries; a
+// particle with more neighbours takes several rounds.
+// ---------------------------------------------------------------------------
+constexpr int kListCap = 32;
+// Density pairs with q = r/h < kNearQ are evaluated in float-float, the others
+// (W below ~1% of W(0) each) in FP32.
+constexpr float kNearQ = 1.6f;
+
+struct Cursor {
+    int r, k, ke;
+};
+
+// Slot range [kb, ke) of candidate row r; false when r is past the last row.
+template <int DIM>
+__device__ __forceinline__ bool candidate_row(const DevGrid& g, const int* __restrict__ start,
+                                              const CellCoord& cc, int r, int& kb, int& ke) {
+    const int px = g.periodic[0];
+    const int R = (DIM == 3 ? 9 : 3) * (px ? 3 : 1);
+    if (r >= R) return false;
+    const int rest = px ? r / 3 : r;
+    int cy = cc.c[1] + rest % 3 - 1;
+    int cz = (DIM == 3) ? cc.c[2] + rest / 3 - 1 : 0;
+    kb = ke = 0;
+    if (DIM == 3) {
+        if (g.periodic[2]) cz = (cz + g.n[2]) % g.n[2];
+        else if (cz < 0 || cz >= g.n[2]) return true;
+    }
+    if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
+    else if (cy < 0 || cy >= g.n[1]) return true;
+    const int row = (cz * g.n[1] + cy) * g.n[0];
+    if (!px) {
+        const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
+        kb = __ldg(start + row + c0);
+        ke = __ldg(start + row + c1 + 1);
+    } else {
+        const int cx = (cc.c[0] + r % 3 - 1 + g.n[0]) % g.n[0];
+        kb = __ldg(start + row + cx);
+        ke = __ldg(start + row + cx + 1);
+    }
+    return true;
+}
+
+// Advances to the next non-empty row; false when the candidates are exhausted.
+template <int DIM>
+__device__ __forceinline__ bool cursor_next(const DevGrid& g, const int* __restrict__ start,
+                                            const CellCoord& cc, Cursor& cu) {
+    int kb, ke;
+    while (candidate_row<DIM>(g, start, cc, ++cu.r, kb, ke)) {
+        if (kb < ke) {
+            cu.k = kb;
+            cu.ke = ke;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Periodic wrap of a drifted coordinate (same branch order as the oracle).
+__device__ __forceinline__ float wrap_axis(float c, const DevParams& P, int d, bool& outside) {
+    if (!(c < P.period_hi[d])) c = __fsub_rn(c, P.period_L[d]);
+    else if (c < P.period_lo[d]) c = __fadd_rn(c, P.period_L[d]);
+    if (!(c >= P.period_lo[d] && c < P.period_hi[d])) outside = true;
+    return c;
+}
+
+__device__ __forceinline__ float fast_sqrt_pos(float x) {
+    return x > 0.f ? x * rsqrtf(x) : 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
 template <int DIM>
 __global__ void __launch_bounds__(kPassThreads)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+    __shared__ int s_near[kListCap][kPassThreads];
+    __shared__ int s_far[kListCap][kPassThreads];
+    const int tid = threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + tid;
+    const bool valid = s < n;
     const DevGrid g = *gp;
-    const float4 xi = B.xh[s];
-    const bool fluid = B.itype[s] > 0;
     const bool need_div = P.heat_art != 0;
-    float4 rp = B.rp[s];
-    float p = B.p[s];
-    if ((!fluid && !need_div) || !g.ok) {
-        rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
-        B.rp[s] = rp;
-        return;
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
+    float p = 0.f;
+    bool fluid = false;
+    if (valid) {
+        xi = B.xh[s];
+        rp = B.rp[s];
+        p = B.p[s];
+        fluid = B.itype[s] > 0;
+        if (DIM == 3 || need_div) vi = B.vm[s];
     }
-    const float4 vi = B.vm[s];
-    const float mi = mass_of<DIM>(xi, vi);
-    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    const bool work = valid && g.ok && (fluid || need_div);
+    CellCoord cc = {{0, 0, 0}};
+    if (work) cc = decode_key<DIM>(keys[s], g);
     const sph::ff kw = {P.kw_hi, P.kw_lo};
     const sph::ff ih_i = sph::ff_recip(xi.w);
     const sph::ff al_i = sph::ff_mul(kw, ff_pow_dim<DIM>(ih_i));
+    const float mi = mass_of<DIM>(xi, vi);
     // Self density m_i W(0, h_i) (density.f:39-42).
     sph::ff S = sph::ff_mul_f(al_i, mi);
     const float ihf = ih_i.hi;
     const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
+    const float kwf = P.kw_hi * (DIM == 2 ? ihf * ihf : ihf * ihf * ihf);
     float divs = 0.f;
-    for_candidates<DIM>(g, start, cc, [&](int k) {
-        if (k == s) return;
-        const float4 xj = __ldg(B.xh + k);
-        float d[3], dr2;
-        if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
-        float4 vj;
-        if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
-        const float mj = (DIM == 2) ? xj.z : vj.w;
-        if (fluid) {
+    Cursor cu = {-1, 0, 0};
+    bool done = !work;
+    while (__any_sync(0xffffffffu, !done)) {
+        int nn = 0, nf = 0;
+        // Test phase: fill the near / far lists.
+        while (!done) {
+            if (cu.k >= cu.ke) {
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
+                    done = true;
+                    break;
+                }
+                continue;
+            }
+            if (nn == kListCap || nf == kListCap) break;
+            const int k = cu.k++;
+            if (k == s) continue;
+            const float4 xj = __ldg(B.xh + k);
+            float d[3], dr2;
+            if (!pair_delta<DIM>(xi, xj, g, d, dr2)) continue;
+            const float hs = xi.w + xj.w;  // near: q < kNearQ with h = hs/2
+            if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k;
+            else s_far[nf++][tid] = k;
+        }
+        const int mn = __reduce_max_sync(0xffffffffu, nn);
+        const int mf = __reduce_max_sync(0xffffffffu, nf);
+        // Near pairs: float-float weights on the exact pair difference.
+        for (int t = 0; t < mn; ++t) {
+            if (t >= nn) continue;
+            const int k = s_near[t][tid];
+            const float4 xj = __ldg(B.xh + k);
+            float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
+            const float mj = mass_of<DIM>(xj, vj);
+            float dh[3], dl[3];
+            exact_delta<DIM>(xi, xj, g, dh, dl);
             sph::ff ih = ih_i, al = al_i;
             if (xj.w != xi.w) {
                 ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
                 al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
             }
-            float dh[3], dl[3];
-            exact_delta<DIM>(xi, xj, g, dh, dl);
-            sph::ff_acc(S, sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj));
-        }
-        if (need_div) {
-            refine_periodic<DIM>(xi, xj, g, d, dr2);
-            float ih = ihf, kgih = kgih_i;
-            if (xj.w != xi.w) {
-                ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
-                kgih = __fmul_rn(P.kg, pow_grad<DIM>(ih));
+            if (fluid) sph::ff_acc(S, sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj));
+            if (need_div) {
+                const float dr2 = sph::dist2_exact<DIM>(dh);
+                const float gw = sph::wendland_grad_factor<DIM>(
+                    fast_sqrt_pos(dr2), ih.hi, __fmul_rn(P.kg, pow_grad<DIM>(ih.hi)));
+                float vd = (vj.x - vi.x) * dh[0] + (vj.y - vi.y) * dh[1];
+                if (DIM == 3) vd += (vj.z - vi.z) * dh[2];
+                divs = fmaf(mj * gw, vd, divs);
             }
-            const float gw = sph::wendland_grad_factor<DIM>(__fsqrt_rn(dr2), ih, kgih);
-            float vd = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
-            if (DIM == 3) vd += (vj.z - vi.z) * d[2];
-            divs = fmaf(mj * gw, vd, divs);
         }
-    });
+        // Far pairs: FP32 weights (each below ~1% of the self term).
+        for (int t = 0; t < mf; ++t) {
+            if (t >= nf) continue;
+            const int k = s_far[t][tid];
+            const float4 xj = __ldg(B.xh + k);
+            float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
+            const float mj = mass_of<DIM>(xj, vj);
+            float d[3], dr2;
+            pair_delta<DIM>(xi, xj, g, d, dr2);
+            refine_periodic<DIM>(xi, xj, g, d, dr2);
+            float ih = ihf, kgih = kgih_i, kwh = kwf;
+            if (xj.w != xi.w) {
+                ih = __fdividef(2.0f, xi.w + xj.w);
+                kgih = P.kg * pow_grad<DIM>(ih);
+                kwh = P.kw_hi * (DIM == 2 ? ih * ih : ih * ih * ih);
+            }
+            const float q = fast_sqrt_pos(dr2) * ih;
+            if (fluid) {
+                float tt = fmaf(-0.5f, q, 1.0f);
+                tt = tt * tt;
+                tt = tt * tt;
+                sph::ff_acc(S, sph::ff{kwh * mj * tt * fmaf(2.0f, q, 1.0f), 0.f});
+            }
+            if (need_div) {
+                const float t3 = q - 2.0f;
+                const float gw = kgih * t3 * t3 * t3;
+                float vd = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
+                if (DIM == 3) vd += (vj.z - vi.z) * d[2];
+                divs = fmaf(mj * gw, vd, divs);
+            }
+        }
+    }
+    if (!valid) return;
+    if (!work) {  // wall without div v (or no grid): fixed rho and p
+        rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
+        B.rp[s] = rp;
+        return;
+    }
     float rho = rp.x;
     if (fluid) {
         float drho = __fadd_rn(__fsub_rn(S.hi, P.rho0), S.lo);
@@ -868,14 +1009,20 @@ __global__ void __launch_bounds__(kPassThreads)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
             int n) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
+    __shared__ int s_list[kListCap][kPassThreads];
+    const int tid = threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + tid;
+    const bool valid = s < n;
     const DevGrid g = *gp;
-    const float4 xi = B.xh[s];
-    const int it = B.itype[s];
-    const float4 vi = B.vm[s];
-    const float4 rpi = B.rp[s];
-    if (it <= 0 || !g.ok) {  // wall: fixed state, zero rates
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
+    int it = 0;
+    if (valid) {
+        xi = B.xh[s];
+        it = B.itype[s];
+        vi = B.vm[s];
+        rpi = B.rp[s];
+    }
+    if (valid && (it <= 0 || !g.ok)) {  // wall: fixed state, zero rates
         A.xh[s] = xi;
         A.vm[s] = vi;
         A.u[s] = B.vmin[s].w;
@@ -884,103 +1031,120 @@ __global__ void __launch_bounds__(kPassThreads)
         A.p[s] = B.p[s];
         A.itype[s] = it;
         A.id[s] = B.id[s];
-        return;
     }
-    const CellCoord cc = decode_key<DIM>(keys[s], g);
-    const float ihf = __frcp_rn(xi.w);
-    const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
-    const float pi_i = B.p[s];
+    const bool work = valid && it > 0 && g.ok;
+    CellCoord cc = {{0, 0, 0}};
+    if (work) cc = decode_key<DIM>(keys[s], g);
+    const float ihf = __fdividef(1.0f, xi.w);
+    const float kgih_i = P.kg * pow_grad<DIM>(ihf);
     float4 ti = make_float4(0.f, 0.f, 0.f, 0.f), ti2 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (P.visc) {
+    if (work && P.visc) {
         ti = B.tau[s];
         if (DIM == 3) ti2 = B.tau2[s];
     }
+    const float ulo_i = (work && P.heat_art) ? B.ulo[s] : 0.f;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
-    const float ulo_i = P.heat_art ? B.ulo[s] : 0.f;
-    for_candidates<DIM>(g, start, cc, [&](int k) {
-        if (k == s) return;
-        const float4 xj = __ldg(B.xh + k);
-        float d[3], dr2;
-        if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
-        refine_periodic<DIM>(xi, xj, g, d, dr2);
-        const float4 vj = __ldg(B.vm + k);
-        const float4 rpj = __ldg(B.rp + k);
-        const float mj = mass_of<DIM>(xj, vj);
-        float ih = ihf, kgih = kgih_i;
-        if (xj.w != xi.w) {
-            ih = __frcp_rn(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
-            kgih = __fmul_rn(P.kg, pow_grad<DIM>(ih));
+    Cursor cu = {-1, 0, 0};
+    bool done = !work;
+    while (__any_sync(0xffffffffu, !done)) {
+        int nl = 0;
+        while (!done) {
+            if (cu.k >= cu.ke) {
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
+                    done = true;
+                    break;
+                }
+                continue;
+            }
+            if (nl == kListCap) break;
+            const int k = cu.k++;
+            if (k == s) continue;
+            const float4 xj = __ldg(B.xh + k);
+            float d[3], dr2;
+            if (pair_delta<DIM>(xi, xj, g, d, dr2)) s_list[nl++][tid] = k;
         }
-        const float r = __fsqrt_rn(dr2);
-        const float gw = sph::wendland_grad_factor<DIM>(r, ih, kgih);
-        const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;
-        const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = (DIM == 3) ? vj.z - vi.z : 0.f;
-        // Pressure (internal_force.f:309-428 for pa_sph 1, 179-306 for pa_sph 0).
-        float fs;
-        float inv_rr = 1.f;
-        if (P.pa_sph == 1) {
-            fs = -(rpi.y + rpj.y);
-        } else {
-            fs = -(rpi.y + rpj.y);
-            inv_rr = __frcp_rn(rpi.x * rpj.x);
-        }
-        float h0 = fs * w0, h1 = fs * w1, h2 = fs * w2;
-        float he = vx * h0 + vy * h1;
-        if (DIM == 3) he += vz * h2;
-        if (P.visc) {
-            const float4 tj = __ldg(B.tau + k);
-            float4 tj2 = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (DIM == 3) tj2 = __ldg(B.tau2 + k);
-            const float sxx = ti.x + tj.x, syy = ti.y + tj.y, sxy = ti.z + tj.z;
-            if (DIM == 2) {
-                h0 += sxx * w0 + sxy * w1;
-                h1 += sxy * w0 + syy * w1;
-            } else {
-                const float szz = ti.w + tj.w, sxz = ti2.x + tj2.x, syz = ti2.y + tj2.y;
-                h0 += sxx * w0 + sxy * w1 + sxz * w2;
-                h1 += sxy * w0 + syy * w1 + syz * w2;
-                h2 += sxz * w0 + syz * w1 + szz * w2;
+        const int ml = __reduce_max_sync(0xffffffffu, nl);
+        for (int t = 0; t < ml; ++t) {
+            if (t >= nl) continue;
+            const int k = s_list[t][tid];
+            const float4 xj = __ldg(B.xh + k);
+            const float4 vj = __ldg(B.vm + k);
+            const float4 rpj = __ldg(B.rp + k);
+            float d[3], dr2;
+            pair_delta<DIM>(xi, xj, g, d, dr2);
+            refine_periodic<DIM>(xi, xj, g, d, dr2);
+            const float mj = mass_of<DIM>(xj, vj);
+            float ih = ihf, kgih = kgih_i;
+            if (xj.w != xi.w) {
+                ih = __fdividef(2.0f, xi.w + xj.w);
+                kgih = P.kg * pow_grad<DIM>(ih);
+            }
+            const float q = fast_sqrt_pos(dr2) * ih;
+            const float t3 = q - 2.0f;
+            const float gw = kgih * t3 * t3 * t3;
+            const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;
+            const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = (DIM == 3) ? vj.z - vi.z : 0.f;
+            // Pressure (internal_force.f:309-428 for pa_sph 1, 179-306 for pa_sph 0).
+            const float fs = -(rpi.y + rpj.y);
+            float h0 = fs * w0, h1 = fs * w1, h2 = fs * w2;
+            float he = vx * h0 + vy * h1;
+            if (DIM == 3) he += vz * h2;
+            if (P.visc) {
+                const float4 tj = __ldg(B.tau + k);
+                float4 tj2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (DIM == 3) tj2 = __ldg(B.tau2 + k);
+                const float sxx = ti.x + tj.x, syy = ti.y + tj.y, sxy = ti.z + tj.z;
+                if (DIM == 2) {
+                    h0 += sxx * w0 + sxy * w1;
+                    h1 += sxy * w0 + syy * w1;
+                } else {
+                    const float szz = ti.w + tj.w, sxz = ti2.x + tj2.x, syz = ti2.y + tj2.y;
+                    h0 += sxx * w0 + sxy * w1 + sxz * w2;
+                    h1 += sxy * w0 + syy * w1 + syz * w2;
+                    h2 += sxz * w0 + syz * w1 + szz * w2;
+                }
+            }
+            if (P.pa_sph != 1) {
+                const float inv_rr = __fdividef(1.0f, rpi.x * rpj.x);
+                h0 *= inv_rr;
+                h1 *= inv_rr;
+                h2 *= inv_rr;
+                he *= inv_rr;
+            }
+            a0 = fmaf(mj, h0, a0);
+            a1 = fmaf(mj, h1, a1);
+            if (DIM == 3) a2 = fmaf(mj, h2, a2);
+            he_sum = fmaf(mj, he, he_sum);
+            const float mh = 0.5f * (xi.w + xj.w);
+            const float rho_bar = 0.5f * (rpi.x + rpj.x);
+            // art_visc.f:71-100.
+            if (P.visc_art) {
+                float vr = vx * d[0] + vy * d[1];
+                if (DIM == 3) vr += vz * d[2];
+                if (vr > 0.f) {  // (v_i - v_j) . (x_i - x_j) = -vr < 0
+                    const float phi = __fdividef(-mh * vr, dr2 + mh * mh * P.av_eta2);
+                    const float piv = __fdividef((P.av_beta * phi - P.av_alpha * P.c0) * phi, rho_bar);
+                    const float mp = mj * piv;
+                    a0 = fmaf(-mp, w0, a0);
+                    a1 = fmaf(-mp, w1, a1);
+                    if (DIM == 3) a2 = fmaf(-mp, w2, a2);
+                    float vdw = vx * w0 + vy * w1;
+                    if (DIM == 3) vdw += vz * w2;
+                    av_du = fmaf(-0.5f * mp, vdw, av_du);
+                }
+            }
+            // art_heat.f:69-97.
+            if (P.heat_art) {
+                float rdw = d[0] * w0 + d[1] * w1;
+                if (DIM == 3) rdw += d[2] * w2;
+                const float psi =
+                    __fdividef(rpi.w + rpj.w, rho_bar * (dr2 + mh * mh * P.ah_eta2)) * rdw;
+                const float du_ij = (rpi.z - rpj.z) + (ulo_i - __ldg(B.ulo + k));
+                ah_du = fmaf(mj * psi, du_ij, ah_du);
             }
         }
-        if (P.pa_sph != 1) {
-            h0 *= inv_rr;
-            h1 *= inv_rr;
-            h2 *= inv_rr;
-            he *= inv_rr;
-        }
-        a0 = fmaf(mj, h0, a0);
-        a1 = fmaf(mj, h1, a1);
-        if (DIM == 3) a2 = fmaf(mj, h2, a2);
-        he_sum = fmaf(mj, he, he_sum);
-        const float mh = 0.5f * (xi.w + xj.w);
-        const float rho_bar = 0.5f * (rpi.x + rpj.x);
-        // art_visc.f:71-100.
-        if (P.visc_art) {
-            float vr = vx * d[0] + vy * d[1];
-            if (DIM == 3) vr += vz * d[2];
-            vr = -vr;  // (v_i - v_j) . (x_i - x_j)
-            if (vr < 0.f) {
-                const float phi = mh * vr / (dr2 + mh * mh * P.av_eta2);
-                const float piv = (P.av_beta * phi - P.av_alpha * P.c0) * phi / rho_bar;
-                const float mp = mj * piv;
-                a0 = fmaf(-mp, w0, a0);
-                a1 = fmaf(-mp, w1, a1);
-                if (DIM == 3) a2 = fmaf(-mp, w2, a2);
-                float vdw = vx * w0 + vy * w1;
-                if (DIM == 3) vdw += vz * w2;
-                av_du = fmaf(-0.5f * mp, vdw, av_du);
-            }
-        }
-        // art_heat.f:69-97.
-        if (P.heat_art) {
-            float rdw = d[0] * w0 + d[1] * w1;
-            if (DIM == 3) rdw += d[2] * w2;
-            const float psi = (rpi.w + rpj.w) / (rho_bar * (dr2 + mh * mh * P.ah_eta2)) * rdw;
-            const float du_ij = (rpi.z - rpj.z) + (ulo_i - __ldg(B.ulo + k));
-            ah_du = fmaf(mj * psi, du_ij, ah_du);
-        }
-        (void)pi_i;
-    });
+    }
+    if (!work) return;
     float du = 0.5f * he_sum + av_du + ah_du;  // internal_force.f:433-435
     if (P.visc) du += B.tds[s];
     if (S.heat_on) {
@@ -1007,15 +1171,11 @@ __global__ void __launch_bounds__(kPassThreads)
     xn.x = fmaf(S.dt, vn.x, xi.x);
     xn.y = fmaf(S.dt, vn.y, xi.y);
     if (DIM == 3) xn.z = fmaf(S.dt, vn.z, xi.z);
-    float* xv[3] = {&xn.x, &xn.y, &xn.z};
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-        if (!P.periodic[d]) continue;
-        float& c = *xv[d];
-        if (!(c < P.period_hi[d])) c = __fsub_rn(c, P.period_L[d]);
-        else if (c < P.period_lo[d]) c = __fadd_rn(c, P.period_L[d]);
-        if (!(c >= P.period_lo[d] && c < P.period_hi[d])) atomicOr(flags, (unsigned)FLAG_OUT_OF_GRID);
-    }
+    bool outside = false;
+    if (P.periodic[0]) xn.x = wrap_axis(xn.x, P, 0, outside);
+    if (P.periodic[1]) xn.y = wrap_axis(xn.y, P, 1, outside);
+    if (DIM == 3 && P.periodic[2]) xn.z = wrap_axis(xn.z, P, 2, outside);
+    if (outside) atomicOr(flags, (unsigned)FLAG_OUT_OF_GRID);
     const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + un + a0 + a1 + a2 + du;
     if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
     A.xh[s] = xn;
