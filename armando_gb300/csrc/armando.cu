@@ -353,6 +353,8 @@ armando_status alloc_state(armando_ctx* ctx) {
     F4(ctx->B.tau2);
     F1(ctx->B.tds, n);
     F1(ctx->B.ulo, n);
+    ctx->B.nmask = dalloc<uint4>(n, e);
+    ctx->owned.push_back(ctx->B.nmask);
     ctx->num_tiles = blocks_for(ctx->n, kSortTile);
     for (int k = 0; k < 2; ++k) {
         ctx->keys[k] = dalloc<unsigned>(n, e);

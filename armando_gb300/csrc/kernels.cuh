@@ -94,6 +94,7 @@ struct StateB {  // working set of one step (cell order)
     float4* tau2;  // {xz, yz, -, -}
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
+    uint4* nmask;  // 2D: neighbour bits over the first 128 candidates (all ones: more)
 };
 
 template <int DIM>
@@ -724,7 +725,9 @@ __device__ __forceinline__ float pow_grad(float ih) {
 // candidates that failed the pair test. Lists hold kListCap entries; a
 // particle with more neighbours takes several rounds.
 // ---------------------------------------------------------------------------
-constexpr int kListCap = 32;
+constexpr int kListCap = 32;      // force pass list
+constexpr int kListCapD = 24;     // density pass: near and far lists each
+constexpr int kTestBatch = 4;     // candidate loads issued together
 // Density pairs with q = r/h < kNearQ are evaluated in float-float, the others
 // (W below ~1% of W(0) each) in FP32.
 constexpr float kNearQ = 1.6f;
@@ -794,11 +797,11 @@ __device__ __forceinline__ float fast_sqrt_pos(float x) {
 // Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__global__ void __launch_bounds__(kPassThreads)
+__global__ void __launch_bounds__(kPassThreads, 8)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
-    __shared__ int s_near[kListCap][kPassThreads];
-    __shared__ int s_far[kListCap][kPassThreads];
+    __shared__ int s_near[kListCapD][kPassThreads];
+    __shared__ int s_far[kListCapD][kPassThreads];
     const int tid = threadIdx.x;
     const int s = blockIdx.x * blockDim.x + tid;
     const bool valid = s < n;
@@ -829,26 +832,45 @@ __global__ void __launch_bounds__(kPassThreads)
     float divs = 0.f;
     Cursor cu = {-1, 0, 0};
     bool done = !work;
+    int ord = 0;  // candidate ordinal (cursor order, self included)
+    unsigned long long mlo = 0ull, mhi = 0ull;  // neighbour bits of ordinals 0..127
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
-        // Test phase: fill the near / far lists.
+        // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
         while (!done) {
             if (cu.k >= cu.ke) {
                 if (!cursor_next<DIM>(g, start, cc, cu)) {
                     done = true;
                     break;
                 }
-                continue;
             }
-            if (nn == kListCap || nf == kListCap) break;
-            const int k = cu.k++;
-            if (k == s) continue;
-            const float4 xj = __ldg(B.xh + k);
-            float d[3], dr2;
-            if (!pair_delta<DIM>(xi, xj, g, d, dr2)) continue;
-            const float hs = xi.w + xj.w;  // near: q < kNearQ with h = hs/2
-            if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k;
-            else s_far[nf++][tid] = k;
+            if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
+            const int k0 = cu.k;
+            const int cnt = min(kTestBatch, cu.ke - k0);
+            float4 xb[kTestBatch];
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + min(k0 + u, cu.ke - 1));
+            cu.k += cnt;
+            unsigned pb = 0u;  // pass bits of this batch
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                float d[3], dr2;
+                if (u >= cnt || k0 + u == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
+                pb |= 1u << u;
+                const float hs = xi.w + xb[u].w;  // near: q < kNearQ with h = hs/2
+                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k0 + u;
+                else s_far[nf++][tid] = k0 + u;
+            }
+            if (DIM == 2 && pb != 0u && ord < 128) {
+                const unsigned long long b = pb;
+                if (ord < 64) {
+                    mlo |= b << ord;
+                    if (ord > 64 - kTestBatch) mhi |= b >> (64 - ord);
+                } else {
+                    mhi |= b << (ord - 64);
+                }
+            }
+            ord += cnt;
         }
         const int mn = __reduce_max_sync(0xffffffffu, nn);
         const int mf = __reduce_max_sync(0xffffffffu, nf);
@@ -911,6 +933,10 @@ __global__ void __launch_bounds__(kPassThreads)
         }
     }
     if (!valid) return;
+    if (DIM == 2 && fluid && work)
+        B.nmask[s] = (ord <= 128) ? make_uint4((unsigned)mlo, (unsigned)(mlo >> 32),
+                                               (unsigned)mhi, (unsigned)(mhi >> 32))
+                                  : make_uint4(~0u, ~0u, ~0u, ~0u);
     if (!work) {  // wall without div v (or no grid): fixed rho and p
         rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
         B.rp[s] = rp;
@@ -1005,7 +1031,7 @@ __global__ void __launch_bounds__(kPassThreads)
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__global__ void __launch_bounds__(kPassThreads)
+__global__ void __launch_bounds__(kPassThreads, 8)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
             int n) {
@@ -1046,22 +1072,63 @@ __global__ void __launch_bounds__(kPassThreads)
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
     Cursor cu = {-1, 0, 0};
     bool done = !work;
+    // 2D: the density pass left the neighbour bits of the first 128 candidates.
+    uint4 mk = make_uint4(0u, 0u, 0u, 0u);
+    bool from_mask = false;
+    if (DIM == 2 && work) {
+        mk = B.nmask[s];
+        from_mask = !(mk.x == ~0u && mk.y == ~0u && mk.z == ~0u && mk.w == ~0u);
+    }
+    int wi = 0, rbase = 0;  // mask word being decoded; ordinal of the cursor row's first slot
+    unsigned wbits = mk.x;
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
-        while (!done) {
+        while (!done && from_mask) {
+            if (nl == kListCap) break;
+            while (wbits == 0u && wi < 3) {
+                ++wi;
+                wbits = (wi == 1) ? mk.y : (wi == 2) ? mk.z : mk.w;
+            }
+            if (wbits == 0u) {
+                done = true;
+                break;
+            }
+            const int o = 32 * wi + __ffs(wbits) - 1;
+            wbits &= wbits - 1u;
+            bool in_rows = true;
+            while (o >= rbase + (cu.ke - cu.k)) {  // move to the row holding ordinal o
+                rbase += cu.ke - cu.k;
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
+                    in_rows = false;
+                    break;
+                }
+            }
+            if (!in_rows) {  // cannot happen for a mask of this step's candidates
+                done = true;
+                break;
+            }
+            s_list[nl++][tid] = cu.k + (o - rbase);
+        }
+        while (!done && !from_mask) {
             if (cu.k >= cu.ke) {
                 if (!cursor_next<DIM>(g, start, cc, cu)) {
                     done = true;
                     break;
                 }
-                continue;
             }
-            if (nl == kListCap) break;
-            const int k = cu.k++;
-            if (k == s) continue;
-            const float4 xj = __ldg(B.xh + k);
-            float d[3], dr2;
-            if (pair_delta<DIM>(xi, xj, g, d, dr2)) s_list[nl++][tid] = k;
+            if (nl > kListCap - kTestBatch) break;
+            const int k0 = cu.k;
+            const int cnt = min(kTestBatch, cu.ke - k0);
+            float4 xb[kTestBatch];
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + min(k0 + u, cu.ke - 1));
+            cu.k += cnt;
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                float d[3], dr2;
+                if (u < cnt && k0 + u != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
+                    s_list[nl++][tid] = k0 + u;
+            }
         }
         const int ml = __reduce_max_sync(0xffffffffu, nl);
         for (int t = 0; t < ml; ++t) {

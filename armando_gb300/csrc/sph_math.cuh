@@ -27,6 +27,7 @@ inline float __fsub_rn(float a, float b) { return a - b; }
 inline float __fdiv_rn(float a, float b) { return a / b; }
 inline float __frcp_rn(float a) { return 1.0f / a; }
 inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+inline float rsqrtf(float a) { return 1.0f / std::sqrt(a); }
 #endif
 
 namespace sph {
@@ -133,14 +134,14 @@ SPH_HD ff wendland_mw_ff(const float* dh, const float* dl, ff ih, ff alpha, floa
         lo = __fadd_rn(lo, __fadd_rn(t.lo, la));
     }
     ff dr2 = fast_two_sum(hi, lo);
-    // r = sqrt(dr2) with one Newton correction.
-    ff r;
-    r.hi = __fsqrt_rn(dr2.hi);
-    if (r.hi > 0.0f) {
-        float res = fmaf(-r.hi, r.hi, dr2.hi);
-        r.lo = __fmul_rn(__fadd_rn(res, dr2.lo), __fdiv_rn(0.5f, r.hi));
-    } else {
-        r.lo = 0.0f;
+    // r = sqrt(dr2): hardware reciprocal square root (a few ulp) and one exact
+    // Newton correction from the FMA residual dr2 - r0^2.
+    ff r = {0.0f, 0.0f};
+    if (dr2.hi > 0.0f) {
+        const float rs = rsqrtf(dr2.hi);
+        r.hi = __fmul_rn(dr2.hi, rs);
+        const float res = fmaf(-r.hi, r.hi, dr2.hi);
+        r.lo = __fmul_rn(__fadd_rn(res, dr2.lo), __fmul_rn(0.5f, rs));
     }
     ff q = ff_mul(r, ih);
     // t = 1 - q/2 (q < 2 so |1| >= |q/2|).
