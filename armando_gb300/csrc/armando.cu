@@ -221,7 +221,7 @@ int launch_grid_and_sort(armando_ctx* ctx) {
             ctx->hist, ctx->dtotal, ctx->num_tiles);
         L += 2;
     }
-    k_cell_start<<<blocks_for(n + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n, ctx->grid,
+    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n, ctx->grid,
                                                           ctx->start);
     return L + 1;
 }
@@ -283,7 +283,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     cudaEventRecord(ev[2], st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for(n + 1, 256), 256, 0, st>>>(skeys, n, ctx->grid, ctx->start);
+    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, ctx->grid, ctx->start);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
     cudaEventRecord(ev[3], st);
     k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,

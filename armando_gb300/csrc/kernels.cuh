@@ -466,16 +466,20 @@ __global__ void __launch_bounds__(kSortThreads)
     }
 }
 
-// start[c] = first sorted slot of cell c, for c in [0, ncells]; empty cells
-// get start[c] == start[c+1]. Slot s fills the cells (key[s-1], key[s]].
+// start[c] = first sorted slot of cell c (the number of keys below c), for c in
+// [0, ncells]; empty cells get start[c] == start[c+1]. One thread per cell, a
+// binary search over the sorted keys: no serial fill of long empty runs.
 __global__ void k_cell_start(const unsigned* __restrict__ keys, int n,
                              const DevGrid* __restrict__ gp, int* __restrict__ start) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s > n) return;
-    const int ncells = gp->ncells;
-    const int lo = (s == 0) ? 0 : (int)keys[s - 1] + 1;
-    const int hi = (s == n) ? ncells : (int)keys[s];
-    for (int c = lo; c <= hi; ++c) start[c] = s;
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > gp->ncells) return;
+    int lo = 0, hi = n;  // first slot with key >= c lies in [lo, hi]
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(keys + mid) < (unsigned)c) lo = mid + 1;
+        else hi = mid;
+    }
+    start[c] = lo;
 }
 
 // ---------------------------------------------------------------------------
