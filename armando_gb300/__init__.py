@@ -18,7 +18,7 @@ import numpy as np
 from ._abi import (ERR_UNSUPPORTED, EXPORTED, LIB_PATH, MEM_DEVICE, MEM_HOST, OK,  # noqa: F401
                    STATUS_NAMES, Params, Stats, load_library)
 
-__all__ = ["Context", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
+__all__ = ["Context", "Batch", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
            "MEM_DEVICE", "LIB_PATH", "EXPORTED"]
 
 
@@ -62,6 +62,12 @@ class Context:
         if st != OK:
             raise ArmandoError(st, self._lib.armando_last_error(None).decode())
         self._h = h
+
+    @classmethod
+    def _from_handle(cls, lib, h, params, dim, n, mem):
+        self = cls.__new__(cls)
+        self._lib, self._h, self.params, self.dim, self.n, self.mem = lib, h, params, dim, n, mem
+        return self
 
     # -- lifecycle ---------------------------------------------------------
     def close(self):
@@ -167,3 +173,40 @@ class Context:
 
     def sync(self):
         self._check(self._lib.armando_sync(self._h))
+
+
+class Batch(Context):
+    """Independent particle systems (a parameter sweep) in one context
+    (``armando_batch_create``): packed arrays, one time step per instance."""
+
+    def __init__(self, params_list, n_fluid, n_wall, mem: int = MEM_HOST):
+        lib = load_library()
+        k = len(params_list)
+        arr = (Params * k)(*[p.copy() for p in params_list])
+        nf = np.ascontiguousarray(n_fluid, np.int64)
+        nw = np.ascontiguousarray(n_wall, np.int64)
+        dim = int(params_list[0].dim)
+        h = C.c_void_p()
+        st = lib.armando_batch_create(C.byref(h), k, arr, dim, nf.ctypes.data_as(C.c_void_p),
+                                      nw.ctypes.data_as(C.c_void_p), mem)
+        if st != OK:
+            raise ArmandoError(st, lib.armando_last_error(None).decode())
+        self._lib, self._h, self.params, self.dim = lib, h, params_list[0].copy(), dim
+        self.n = int(nf.sum() + nw.sum())
+        self.mem = mem
+        self.n_instances = k
+        self.counts = nf + nw
+        self.offsets = np.concatenate([[0], np.cumsum(self.counts)])
+
+    def integrate_batch(self, s, dts, its0: int, steps: int):
+        """`steps` iterations of every instance, dts[k] the time step of instance k."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        d = np.ascontiguousarray(dts, np.float32)
+        if d.size != self.n_instances:
+            raise ValueError("one dt per instance")
+        self._check(self._lib.armando_batch_integrate(
+            self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+            _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
+            d.ctypes.data_as(C.c_void_p), int(its0), int(steps)))
+        return s

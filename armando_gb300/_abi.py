@@ -131,6 +131,7 @@ EXPORTED = [
     "armando_neighbours", "armando_sync", "armando_get_stats",
     "armando_last_error", "armando_destroy", "armando_abi_version",
     "armando_get_stream", "armando_profile_phases", "armando_cell_ids_noalloc",
+    "armando_batch_create", "armando_batch_integrate",
 ]
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
@@ -181,6 +182,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_get_stream.restype = C.c_int
     lib.armando_profile_phases.argtypes = [vp, C.c_int32, C.POINTER(C.c_float)]
     lib.armando_profile_phases.restype = C.c_int
+    lib.armando_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(Params),
+                                         C.c_int32, vp, vp, C.c_int32]
+    lib.armando_batch_create.restype = C.c_int
+    lib.armando_batch_integrate.argtypes = [vp] * 11 + [vp, C.c_int32, C.c_int32]
+    lib.armando_batch_integrate.restype = C.c_int
     lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
     lib.armando_cell_ids_noalloc.restype = C.c_int
     del fp, ip

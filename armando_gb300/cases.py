@@ -242,3 +242,65 @@ def perturbed(case: Case, seed: int, dv: float = 0.0, du: float = 0.0) -> Case:
     if du:
         c.u[fl] += (rng.standard_normal(int(fl.sum())) * du).astype(np.float32)
     return c
+
+
+FIELDS = ("x", "v", "mass", "rho", "p", "u", "h", "itype", "dvdt", "dudt")
+
+
+def pack(case_list):
+    """Concatenates instances into the packed layout of a batch context.
+    Returns (arrays dict, offsets[n_instances + 1])."""
+    arrays = {f: np.ascontiguousarray(np.concatenate([getattr(c, f) for c in case_list]))
+              for f in FIELDS}
+    counts = np.array([c.n for c in case_list], np.int64)
+    return arrays, np.concatenate([[0], np.cumsum(counts)])
+
+
+def unpack(arrays, offsets, case_list):
+    """Copies packed arrays back into per-instance Case objects (new copies)."""
+    out = []
+    for k, c in enumerate(case_list):
+        d = c.copy()
+        a, b = int(offsets[k]), int(offsets[k + 1])
+        for f in FIELDS:
+            src = arrays[f]
+            w = c.dim if f in ("x", "v", "dvdt") else 1
+            setattr(d, f, np.array(src[a * w:b * w]))
+        out.append(d)
+    return out
+
+
+def sweep(n_instances: int = 512, seed: int = 4, n_min: float = 2.0e3, n_max: float = 2.0e5,
+          steps: int = 500):
+    """Batched parameter sweep: alternating 2D dam breaks and lid-driven
+    cavities, particle counts log-uniform in [n_min, n_max], art. visc
+    alpha ~ U(0.005, 0.05), c0 ~ U(20, 80) m/s, dam column aspect ~ U(0.5, 3);
+    one seeded generator drives every draw. Returns a list of Case."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_instances):
+        n_k = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        alpha = float(rng.uniform(0.005, 0.05))
+        c0 = float(rng.uniform(20.0, 80.0))
+        aspect = float(rng.uniform(0.5, 3.0))
+        sub = int(rng.integers(1 << 30))
+        if k % 2 == 0:
+            dx = 1.0e-3
+            nx = max(4, int(round(np.sqrt(n_k / aspect))))
+            ny = max(4, int(round(aspect * nx)))
+            c = dam_break(dx=dx, col_w=nx * dx, col_h=ny * dx, tank_w=4 * nx * dx,
+                          tank_h=1.5 * ny * dx, seed=sub, steps=steps, alpha=alpha, c0=c0)
+        else:
+            side = max(4, int(round(np.sqrt(n_k))))
+            c = cavity(n_side=side, seed=sub, length=1.0, lid_u=1.0, steps=steps)
+            c.params.c0 = c0
+            c.params.visc = 0
+            c.params.visc_artificial = 1
+            c.params.av_alpha = alpha
+            c.params.av_beta = 0.0
+            h = float(c.h[0])
+            c.dt = 0.2 * h / c0
+        c.name = f"{c.name}#{k}"
+        c.meta.update(alpha=alpha, c0=c0, aspect=aspect, index=k)
+        out.append(c)
+    return out

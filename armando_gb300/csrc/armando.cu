@@ -89,6 +89,26 @@ struct armando_ctx {
     bool have_grid = false;
     float last_dt = 0.f;  // dt and next its of the state left on the device
     int next_its = 0;
+    // Batches of independent instances (n_inst > 1): packed state, one cell
+    // grid per instance, persistent passes over work items.
+    int n_inst = 1;
+    std::vector<int64_t> inst_n;            // particles per instance
+    std::vector<armando_params> prm_inst;   // parameters per instance
+    std::vector<float> inst_dt;             // time step per instance
+    int* d_inst0 = nullptr;                 // instance of each caller index
+    DevParams* d_params = nullptr;          // [n_inst]
+    DevGrid* d_grids = nullptr;             // [n_inst]
+    int* d_ncells_inst = nullptr;           // [n_inst]
+    int* d_inst_items = nullptr;            // [n_inst + 1] first work item per instance
+    WorkItem* d_items = nullptr;
+    int n_items = 0;
+    float* d_part_items = nullptr;          // [n_items * 8] bbox partials
+    int* d_total_cells = nullptr;
+    int* d_queue = nullptr;                 // [4] work-queue heads, reset every step
+    int* d_its = nullptr;
+    int any_visc = 0;
+    int grid_density = 0, grid_shear = 0, grid_force = 0;  // persistent CTAs
+    cudaGraphExec_t batch_graph = nullptr;
 };
 
 namespace {
@@ -192,6 +212,8 @@ StepArgs make_args(const armando_ctx* c, float dt, int its) {
 void free_graphs(armando_ctx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
+    if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
+    c->batch_graph = nullptr;
 }
 
 // ---- launch sequences -------------------------------------------------------
@@ -221,8 +243,8 @@ int launch_grid_and_sort(armando_ctx* ctx) {
             ctx->hist, ctx->dtotal, ctx->num_tiles);
         L += 2;
     }
-    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n, ctx->grid,
-                                                          ctx->start);
+    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n,
+                                                                   &ctx->grid->ncells, ctx->start);
     return L + 1;
 }
 
@@ -249,6 +271,85 @@ int launch_step(armando_ctx* ctx, const StepArgs& S) {
 
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
     return ctx->dim == 2 ? launch_step<2>(ctx, S) : launch_step<3>(ctx, S);
+}
+
+// Grid, hash and sort of a batch (one grid per instance, one shared table).
+template <int DIM>
+int launch_batch_grid_and_sort(armando_ctx* ctx, long long capacity) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    int L = 0;
+    k_bbox_items<<<ctx->n_items, kPassThreads, 0, st>>>(ctx->A.xh, ctx->d_items, DIM,
+                                                        ctx->d_part_items);
+    k_bbox_final_batch<<<ctx->n_inst, 256, 0, st>>>(ctx->d_part_items, ctx->d_inst_items,
+                                                    ctx->d_params, ctx->d_grids,
+                                                    ctx->d_ncells_inst, ctx->flags);
+    k_cell_offsets<<<1, 1024, 0, st>>>(ctx->d_ncells_inst, ctx->n_inst, capacity, ctx->d_grids,
+                                       ctx->d_total_cells, ctx->flags);
+    L += 3;
+    if (!ctx->start) return L;  // planning: grids only
+    k_hash_batch<DIM><<<ctx->num_tiles, kSortThreads, 0, st>>>(
+        ctx->A.xh, ctx->A.inst, n, ctx->d_grids, ctx->keys[0], ctx->hist, ctx->num_tiles);
+    ++L;
+    for (int p = 0; p < ctx->passes; ++p) {
+        const int shift = 8 * p;
+        const int a = p & 1, b = (p + 1) & 1;
+        if (p > 0) {
+            k_radix_hist<<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, shift,
+                                                                   ctx->hist, ctx->num_tiles);
+            ++L;
+        }
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal);
+        k_radix_scatter<<<ctx->num_tiles, kSortThreads, 0, st>>>(
+            ctx->keys[a], p == 0 ? nullptr : ctx->vals[a], ctx->keys[b], ctx->vals[b], n, shift,
+            ctx->hist, ctx->dtotal, ctx->num_tiles);
+        L += 2;
+    }
+    return L;
+}
+
+// One leapfrog step of every instance; ev (optional, ARMANDO_N_PHASES + 1
+// events) brackets the phases as in launch_step_phased.
+template <int DIM>
+int launch_batch_step(armando_ctx* ctx, cudaEvent_t* ev) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    if (ev) cudaEventRecord(ev[0], st);
+    cudaMemsetAsync(ctx->d_queue, 0, 4 * sizeof(int), st);
+    int L = launch_batch_grid_and_sort<DIM>(ctx, ctx->cell_cap);
+    if (ev) {  // grid + hash | sort are not split for batches
+        cudaEventRecord(ev[1], st);
+        cudaEventRecord(ev[2], st);
+    }
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, ctx->d_total_cells,
+                                                                   ctx->start);
+    k_reorder_batch<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, ctx->d_params,
+                                                             ctx->d_its, n);
+    if (ev) cudaEventRecord(ev[3], st);
+    k_density_batch<DIM><<<ctx->grid_density, kPassThreads, 0, st>>>(
+        ctx->B, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_items, ctx->n_items,
+        ctx->d_queue + 0);
+    if (ev) cudaEventRecord(ev[4], st);
+    L += 3;
+    if (ctx->any_visc) {
+        k_shear_batch<DIM><<<ctx->grid_shear, kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_items, ctx->n_items,
+            ctx->d_queue + 1);
+        ++L;
+    }
+    if (ev) cudaEventRecord(ev[5], st);
+    k_force_batch<DIM><<<ctx->grid_force, kPassThreads, 0, st>>>(
+        ctx->B, ctx->A, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_its, ctx->flags,
+        ctx->d_items, ctx->n_items, ctx->d_queue + 2);
+    k_advance_its<<<1, 1, 0, st>>>(ctx->d_its);
+    if (ev) cudaEventRecord(ev[6], st);
+    return L + 2;
+}
+
+int launch_batch_step_any(armando_ctx* ctx, cudaEvent_t* ev) {
+    return ctx->dim == 2 ? launch_batch_step<2>(ctx, ev) : launch_batch_step<3>(ctx, ev);
 }
 
 // The kernels of launch_step with an event recorded after each phase
@@ -283,7 +384,8 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     cudaEventRecord(ev[2], st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, ctx->grid, ctx->start);
+    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, &ctx->grid->ncells,
+                                                                   ctx->start);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
     cudaEventRecord(ev[3], st);
     k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,
@@ -302,7 +404,28 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     return L + 1;
 }
 
+armando_status run_batch_step(armando_ctx* ctx) {
+    if (!ctx->batch_graph) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        int L = launch_batch_step_any(ctx, nullptr);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&ctx->batch_graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        ctx->launches_per_step = L;
+    }
+    CK(cudaGraphLaunch(ctx->batch_graph, ctx->stream));
+    ctx->launches += ctx->launches_per_step;
+    ctx->steps_done += 1;
+    return ARMANDO_OK;
+}
+
 armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
+    if (ctx->n_inst > 1) return run_batch_step(ctx);
     GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
     auto itg = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
@@ -394,8 +517,37 @@ armando_status alloc_state(armando_ctx* ctx) {
 // Sizes the cell table from the grid of the current positions (A.xh): twice
 // the cells of that grid. A later grid larger than that ends a call with
 // ARMANDO_ERR_GRID_OVERFLOW (link_list.f:61-66 `stop`s in the same case).
+armando_status plan_grid_batch(armando_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const int L = ctx->dim == 2 ? launch_batch_grid_and_sort<2>(ctx, (long long)INT32_MAX)
+                                : launch_batch_grid_and_sort<3>(ctx, (long long)INT32_MAX);
+    ctx->launches += L;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    int total = 0;
+    unsigned fl = 0;
+    CK(cudaMemcpy(&total, ctx->d_total_cells, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&fl, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (fl & (FLAG_GRID_OVERFLOW | FLAG_PERIODIC_SMALL))
+        return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "an instance's neighbour grid is too large or its periodic box shorter than 3 cells");
+    long long cap = std::max<long long>(2LL * total, 4096);
+    if (cap > (1LL << 30)) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "the batch's neighbour grids need more than 2^30 cells");
+    int bits = 1;
+    while ((1LL << bits) < cap) ++bits;
+    ctx->passes = (bits + 7) / 8;
+    ctx->cell_cap = cap;
+    cudaError_t e = cudaSuccess;
+    ctx->start = dalloc<int>((size_t)cap + 1, e);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(cell table)");
+    ctx->owned.push_back(ctx->start);
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
 armando_status plan_grid(armando_ctx* ctx) {
     if (ctx->start) return ARMANDO_OK;
+    if (ctx->n_inst > 1) return plan_grid_batch(ctx);
     cudaStream_t st = ctx->stream;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, (int)ctx->n, ctx->dim, ctx->bbox_part);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, (long long)INT32_MAX,
@@ -423,7 +575,8 @@ armando_status plan_grid(armando_ctx* ctx) {
 
 armando_status check_flags(armando_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(ctx->h_grid, ctx->grid, sizeof(DevGrid), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_grid, ctx->n_inst > 1 ? ctx->d_grids : ctx->grid, sizeof(DevGrid),
+                       cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->last_grid = *ctx->h_grid;
     ctx->have_grid = true;
@@ -472,10 +625,10 @@ armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, co
     const int nn = (int)ctx->n;
     if (ctx->dim == 2)
         k_gather_in<2><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
-                                                            dvdt, dudt, ctx->A, nn);
+                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0);
     else
         k_gather_in<3><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
-                                                            dvdt, dudt, ctx->A, nn);
+                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0);
     ctx->launches += 1;
     CK(cudaGetLastError());
     return ARMANDO_OK;
@@ -516,6 +669,83 @@ armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, 
         CK(D2H(dudt, ctx->s_dudt, n * 4));
     }
     return ARMANDO_OK;
+}
+
+// Per-instance device parameters (the time step of each instance included).
+armando_status upload_batch_params(armando_ctx* ctx) {
+    std::vector<DevParams> hp(ctx->n_inst);
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        hp[k] = make_dev_params(ctx->prm_inst[k]);
+        hp[k].dt = ctx->inst_dt[k];
+        hp[k].heat_t_end = ctx->prm_inst[k].heat_t_end;
+    }
+    CK(cudaMemcpy(ctx->d_params, hp.data(), sizeof(DevParams) * ctx->n_inst, cudaMemcpyHostToDevice));
+    return ARMANDO_OK;
+}
+
+// Instance bookkeeping of a batch: instance ids, work items (<= kPassThreads
+// slots of one instance each), persistent grid sizes.
+armando_status alloc_batch(armando_ctx* ctx) {
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    const int ni = ctx->n_inst;
+    ctx->A.inst = dalloc<int>(n, e);
+    ctx->B.inst = dalloc<int>(n, e);
+    ctx->d_inst0 = dalloc<int>(n, e);
+    ctx->d_params = dalloc<DevParams>(ni, e);
+    ctx->d_grids = dalloc<DevGrid>(ni, e);
+    ctx->d_ncells_inst = dalloc<int>(ni, e);
+    ctx->d_inst_items = dalloc<int>(ni + 1, e);
+    ctx->d_total_cells = dalloc<int>(1, e);
+    ctx->d_queue = dalloc<int>(4, e);
+    ctx->d_its = dalloc<int>(1, e);
+    std::vector<int> inst0(n, 0), inst_items(ni + 1, 0);
+    std::vector<WorkItem> items;
+    int64_t s0 = 0;
+    for (int k = 0; k < ni; ++k) {
+        inst_items[k] = (int)items.size();
+        for (int64_t b = 0; b < ctx->inst_n[k]; b += kPassThreads) {
+            WorkItem w;
+            w.s0 = (int)(s0 + b);
+            w.s1 = (int)std::min<int64_t>(s0 + b + kPassThreads, s0 + ctx->inst_n[k]);
+            w.inst = k;
+            w.pad = 0;
+            items.push_back(w);
+        }
+        for (int64_t i = 0; i < ctx->inst_n[k]; ++i) inst0[s0 + i] = k;
+        s0 += ctx->inst_n[k];
+    }
+    inst_items[ni] = (int)items.size();
+    ctx->n_items = (int)items.size();
+    ctx->d_items = dalloc<WorkItem>(std::max(ctx->n_items, 1), e);
+    ctx->d_part_items = dalloc<float>((size_t)std::max(ctx->n_items, 1) * 8, e);
+    for (void* p : {(void*)ctx->A.inst, (void*)ctx->B.inst, (void*)ctx->d_inst0, (void*)ctx->d_params,
+                    (void*)ctx->d_grids, (void*)ctx->d_ncells_inst, (void*)ctx->d_inst_items,
+                    (void*)ctx->d_total_cells, (void*)ctx->d_queue, (void*)ctx->d_its,
+                    (void*)ctx->d_items, (void*)ctx->d_part_items})
+        ctx->owned.push_back(p);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(batch)");
+    CK(cudaMemcpy(ctx->d_inst0, inst0.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_inst_items, inst_items.data(), sizeof(int) * (ni + 1), cudaMemcpyHostToDevice));
+    if (ctx->n_items)
+        CK(cudaMemcpy(ctx->d_items, items.data(), sizeof(WorkItem) * ctx->n_items, cudaMemcpyHostToDevice));
+    int sms = 0, bd = 0, bs = 0, bf = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    if (ctx->dim == 2) {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, k_density_batch<2>, kPassThreads, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_shear_batch<2>, kPassThreads, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_force_batch<2>, kPassThreads, 0));
+    } else {
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, k_density_batch<3>, kPassThreads, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_shear_batch<3>, kPassThreads, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_force_batch<3>, kPassThreads, 0));
+    }
+    ctx->grid_density = std::max(1, std::min(sms * bd, ctx->n_items));
+    ctx->grid_shear = std::max(1, std::min(sms * bs, ctx->n_items));
+    ctx->grid_force = std::max(1, std::min(sms * bf, ctx->n_items));
+    ctx->any_visc = 0;
+    for (const auto& q : ctx->prm_inst) ctx->any_visc |= q.visc ? 1 : 0;
+    return upload_batch_params(ctx);
 }
 
 armando_status check_step_args(armando_ctx* ctx, const void* x, const void* vx, const void* mass,
@@ -656,16 +886,25 @@ void armando_params_default(armando_params* p) {
 
 int32_t armando_abi_version(void) { return ARMANDO_ABI_VERSION; }
 
-armando_status armando_create(armando_ctx** out, const armando_params* params, int32_t dim,
-                              int64_t n_fluid, int64_t n_wall, int32_t mem_kind) {
+static armando_status create_impl(armando_ctx** out, int32_t n_inst, const armando_params* params,
+                                  int32_t dim, const int64_t* n_fluid, const int64_t* n_wall,
+                                  int32_t mem_kind) {
     armando_ctx* ctx = nullptr;
     if (!out) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
-    std::string why;
-    armando_status vs = validate_params(params, dim, why);
-    if (vs != ARMANDO_OK) return fail(nullptr, vs, why);
-    if (n_fluid < 0 || n_wall < 0 || n_fluid + n_wall > (int64_t)INT32_MAX / 2)
-        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "particle counts out of range");
+    if (n_inst < 1 || !params || !n_fluid || !n_wall)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "need at least one instance with params and counts");
+    int64_t total = 0;
+    for (int k = 0; k < n_inst; ++k) {
+        std::string why;
+        armando_status vs = validate_params(params + k, dim, why);
+        if (vs != ARMANDO_OK) return fail(nullptr, vs, why);
+        if (n_fluid[k] < 0 || n_wall[k] < 0)
+            return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "particle counts out of range");
+        total += n_fluid[k] + n_wall[k];
+        if (total > (int64_t)INT32_MAX / 2)
+            return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "particle counts out of range");
+    }
     if (mem_kind != ARMANDO_MEM_HOST && mem_kind != ARMANDO_MEM_DEVICE)
         return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "mem_kind must be ARMANDO_MEM_HOST or ARMANDO_MEM_DEVICE");
     int dev = 0, ndev = 0;
@@ -682,12 +921,18 @@ armando_status armando_create(armando_ctx** out, const armando_params* params, i
                     std::string("library is built for sm_103a; device is ") + prop.name);
     ctx = new armando_ctx();
     ctx->device = dev;
-    ctx->prm = *params;
-    ctx->dp = make_dev_params(*params);
+    ctx->prm = params[0];
+    ctx->dp = make_dev_params(params[0]);
     ctx->dim = dim;
-    ctx->nf = n_fluid;
-    ctx->nw = n_wall;
-    ctx->n = n_fluid + n_wall;
+    ctx->n_inst = n_inst;
+    for (int k = 0; k < n_inst; ++k) {
+        ctx->nf += n_fluid[k];
+        ctx->nw += n_wall[k];
+        ctx->inst_n.push_back(n_fluid[k] + n_wall[k]);
+        ctx->prm_inst.push_back(params[k]);
+        ctx->inst_dt.push_back(0.f);
+    }
+    ctx->n = total;
     ctx->mem_kind = mem_kind;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -696,9 +941,11 @@ armando_status armando_create(armando_ctx** out, const armando_params* params, i
         return st;
     }
     armando_status st = alloc_state(ctx);
+    if (st == ARMANDO_OK && n_inst > 1) st = alloc_batch(ctx);
     if (st != ARMANDO_OK) {
+        std::string m = ctx->err;
         armando_destroy(ctx);
-        return st;
+        return fail(nullptr, st, m);
     }
     if (cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream) != cudaSuccess) {
         armando_destroy(ctx);
@@ -708,8 +955,21 @@ armando_status armando_create(armando_ctx** out, const armando_params* params, i
     return ARMANDO_OK;
 }
 
+armando_status armando_create(armando_ctx** out, const armando_params* params, int32_t dim,
+                              int64_t n_fluid, int64_t n_wall, int32_t mem_kind) {
+    return create_impl(out, 1, params, dim, &n_fluid, &n_wall, mem_kind);
+}
+
+armando_status armando_batch_create(armando_ctx** out, int32_t n_instances,
+                                    const armando_params* params, int32_t dim,
+                                    const int64_t* n_fluid, const int64_t* n_wall,
+                                    int32_t mem_kind) {
+    return create_impl(out, n_instances, params, dim, n_fluid, n_wall, mem_kind);
+}
+
 armando_status armando_set_params(armando_ctx* ctx, const armando_params* params) {
     if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batch contexts take their parameters at creation");
     std::string why;
     armando_status vs = validate_params(params, ctx->dim, why);
     if (vs != ARMANDO_OK) return fail(ctx, vs, why);
@@ -719,12 +979,58 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     return ARMANDO_OK;
 }
 
+armando_status armando_batch_integrate(armando_ctx* ctx, float* x, float* vx, const float* mass,
+                                       float* rho, float* p, float* u, const float* hsml,
+                                       const int32_t* itype, float* dvdt, float* dudt,
+                                       const float* dt, int32_t its0, int32_t steps) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!dt) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "dt is NULL");
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt[0], its0);
+    if (st != ARMANDO_OK) return st;
+    if (ctx->n_inst == 1) return armando_integrate(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt[0], its0, steps);
+    if (steps < 0) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps must be >= 0");
+    bool changed = false;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        if (!(dt[k] > 0.f) || !std::isfinite(dt[k]))
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "every dt must be finite and > 0");
+        changed |= dt[k] != ctx->inst_dt[k];
+    }
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->n == 0 || steps == 0) return ARMANDO_OK;
+    if (changed) {
+        for (int k = 0; k < ctx->n_inst; ++k) ctx->inst_dt[k] = dt[k];
+        st = upload_batch_params(ctx);
+        if (st != ARMANDO_OK) return st;
+    }
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+    if (st != ARMANDO_OK) return st;
+    st = plan_grid(ctx);
+    if (st != ARMANDO_OK) return st;
+    const int its = its0;
+    CK(cudaMemcpyAsync(ctx->d_its, &its, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    for (int k = 0; k < steps; ++k) {
+        st = run_batch_step(ctx);
+        if (st != ARMANDO_OK) return st;
+    }
+    ctx->last_dt = dt[0];
+    ctx->next_its = its0 + steps;
+    st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
+    if (st != ARMANDO_OK) return st;
+    return check_flags(ctx);
+}
+
 armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const float* mass,
                                  float* rho, float* p, float* u, const float* hsml,
                                  const int32_t* itype, float* dvdt, float* dudt, float dt,
                                  int32_t its0, int32_t steps) {
     armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
     if (st != ARMANDO_OK) return st;
+    if (ctx->n_inst > 1) {
+        std::vector<float> dts(ctx->n_inst, dt);
+        return armando_batch_integrate(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt,
+                                       dts.data(), its0, steps);
+    }
     if (steps < 0) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps must be >= 0");
     CK(cudaSetDevice(ctx->device));
     if (ctx->n == 0 || steps == 0) return ARMANDO_OK;
@@ -752,6 +1058,7 @@ armando_status armando_step(armando_ctx* ctx, float* x, float* vx, const float* 
 
 armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* hsml, int32_t* cell) {
     if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "cell ids of one particle system only");
     if (!x || !hsml || !cell) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL array");
     CK(cudaSetDevice(ctx->device));
     if (ctx->n == 0) return ARMANDO_OK;
@@ -792,6 +1099,7 @@ armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* h
 armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float* hsml,
                                   int64_t* offs, int32_t* nbr, int64_t cap, int64_t* total) {
     if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "neighbour lists of one particle system only");
     if (!x || !hsml || !offs || !total) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL array");
     CK(cudaSetDevice(ctx->device));
     const int nn = (int)ctx->n;
@@ -895,7 +1203,9 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
     armando_status st = ARMANDO_OK;
     for (int k = 0; k < steps && st == ARMANDO_OK; ++k) {
         const StepArgs S = make_args(ctx, ctx->last_dt, ctx->next_its);
-        int L = ctx->dim == 2 ? launch_step_phased<2>(ctx, S, ev) : launch_step_phased<3>(ctx, S, ev);
+        int L = ctx->n_inst > 1 ? launch_batch_step_any(ctx, ev)
+                : ctx->dim == 2 ? launch_step_phased<2>(ctx, S, ev)
+                                : launch_step_phased<3>(ctx, S, ev);
         ctx->launches += L;
         ctx->steps_done += 1;
         ctx->next_its += 1;

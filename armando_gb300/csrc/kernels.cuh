@@ -46,9 +46,15 @@ enum DevFlag : unsigned {
 struct DevGrid {
     float o[3], size[3], L[3], half[3];
     int n[3];
-    int ncells;  // cells in use (<= capacity)
-    int ok;      // 0 when the grid did not fit; passes then do nothing
+    int ncells;    // cells of this grid
+    int ok;        // 0 when the grid did not fit; passes then do nothing
     int periodic[3];
+    int cell_off;  // first cell of this grid in the shared cell table (batches)
+};
+
+// A unit of work of the persistent passes: slots [s0, s1) of one instance.
+struct WorkItem {
+    int s0, s1, inst, pad;
 };
 
 struct DevParams {
@@ -62,6 +68,8 @@ struct DevParams {
     float period_lo[3], period_hi[3], period_L[3], period_half[3];
     float kw_hi, kw_lo;  // K_dim as float-float
     float kg;            // K_dim * 5/8
+    float dt;            // time step of this instance (batches)
+    float heat_t_end;    // external heat gate its*dt <= heat_t_end
 };
 
 struct StepArgs {
@@ -80,6 +88,7 @@ struct StateA {  // integrated state (slot order of the last sort)
     float* p;
     int* itype;
     int* id;
+    int* inst;  // instance of each slot (batches; nullptr for one system)
 };
 
 struct StateB {  // working set of one step (cell order)
@@ -95,6 +104,7 @@ struct StateB {  // working set of one step (cell order)
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
     uint4* nmask;  // 2D: neighbour bits over the first 128 candidates (all ones: more)
+    int* inst;     // instance of each slot (batches; nullptr for one system)
 };
 
 template <int DIM>
@@ -181,6 +191,9 @@ __global__ void __launch_bounds__(256) k_bbox_partial(const float4* __restrict__
     }
 }
 
+__device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevParams& P,
+                                                  long long capacity, unsigned& fl);
+
 __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ part, int nparts,
                                                     DevParams P, long long capacity,
                                                     DevGrid* __restrict__ grid,
@@ -200,11 +213,21 @@ __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ pa
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
+    const float mm[7] = {s[0][0], s[1][0], s[2][0], s[3][0], s[4][0], s[5][0], s[6][0]};
+    unsigned fl = 0;
+    DevGrid g = grid_from_bbox(mm, P, capacity, fl);
+    *grid = g;
+    if (fl) atomicOr(flags, fl);
+}
+
+// The link_list grid (CERNsource/link_list.f:39-67) of a bbox mm = {min[3],
+// max[3], max h}, in FP32; periodic axes split their box into >= 3 cells.
+__device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevParams& P,
+                                                  long long capacity, unsigned& fl) {
     DevGrid g;
-    const float mh = s[6][0];
+    const float mh = mm[6];
     const float cell = __fmul_rn(2.0f, mh);  // scale_k * mh, scale_k = 2
     long long ncells = 1;
-    unsigned fl = 0;
     for (int d = 0; d < 3; ++d) {
         g.periodic[d] = P.periodic[d];
         g.o[d] = 0.f;
@@ -224,8 +247,8 @@ __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ pa
             g.half[d] = P.period_half[d];
             g.n[d] = nn;
         } else {
-            const float lo = __fsub_rn(s[d][0], mh);
-            const float hi = __fadd_rn(s[3 + d][0], mh);
+            const float lo = __fsub_rn(mm[d], mh);
+            const float hi = __fadd_rn(mm[3 + d], mh);
             float nf = __fdiv_rn(__fsub_rn(hi, lo), cell);
             g.o[d] = lo;
             g.size[d] = cell;
@@ -239,14 +262,14 @@ __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ pa
         ncells *= g.n[d];
     }
     g.ok = 1;
+    g.cell_off = 0;
     if (ncells > capacity || (fl & FLAG_GRID_OVERFLOW) || (fl & FLAG_PERIODIC_SMALL)) {
         fl |= (ncells > capacity) ? FLAG_GRID_OVERFLOW : 0u;
         g.ok = 0;
         ncells = capacity;
     }
     g.ncells = (int)ncells;
-    *grid = g;
-    if (fl) atomicOr(flags, fl);
+    return g;
 }
 
 template <int DIM>
@@ -260,7 +283,7 @@ __device__ __forceinline__ unsigned cell_key(const float4& a, const DevGrid& g) 
         key = key * (unsigned)g.n[d] + (unsigned)c;
     }
     if (!g.ok) key = 0;
-    return key;
+    return key + (unsigned)g.cell_off;
 }
 
 // Cell key of every slot + per-tile histogram of its low digit.
@@ -470,9 +493,9 @@ __global__ void __launch_bounds__(kSortThreads)
 // [0, ncells]; empty cells get start[c] == start[c+1]. One thread per cell, a
 // binary search over the sorted keys: no serial fill of long empty runs.
 __global__ void k_cell_start(const unsigned* __restrict__ keys, int n,
-                             const DevGrid* __restrict__ gp, int* __restrict__ start) {
+                             const int* __restrict__ ncells_total, int* __restrict__ start) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c > gp->ncells) return;
+    if (c > *ncells_total) return;
     int lo = 0, hi = n;  // first slot with key >= c lies in [lo, hi]
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -491,9 +514,10 @@ __global__ void k_gather_in(const float* __restrict__ x, const float* __restrict
                             const float* __restrict__ p, const float* __restrict__ u,
                             const float* __restrict__ h, const int* __restrict__ itype,
                             const float* __restrict__ dvdt, const float* __restrict__ dudt,
-                            StateA A, int n) {
+                            StateA A, int n, const int* __restrict__ inst0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (inst0) A.inst[i] = inst0[i];
     if (DIM == 2) {
         A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], m[i], h[i]);
         A.vm[i] = make_float4(v[2 * i], v[2 * i + 1], 0.f, 0.f);
@@ -596,6 +620,161 @@ __global__ void k_reorder_xh(StateA A, const int* __restrict__ perm, StateB B, i
 }
 
 // ---------------------------------------------------------------------------
+// Batched grid, hash and reorder (one cell grid per instance).
+// ---------------------------------------------------------------------------
+// Bbox partial {min[3], max[3], max h} of every work item.
+__global__ void __launch_bounds__(kPassThreads)
+    k_bbox_items(const float4* __restrict__ xh, const WorkItem* __restrict__ items, int dim,
+                 float* __restrict__ part) {
+    const WorkItem w = items[blockIdx.x];
+    const int s = w.s0 + threadIdx.x;
+    float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
+    if (s < w.s1) {
+        const float4 a = xh[s];
+        v[0] = v[3] = a.x;
+        v[1] = v[4] = a.y;
+        if (dim == 3) v[2] = v[5] = a.z;
+        v[6] = a.w;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < 7; ++k) {
+            const float t = __shfl_xor_sync(0xffffffffu, v[k], o);
+            v[k] = (k < 3) ? fminf(v[k], t) : fmaxf(v[k], t);
+        }
+    __shared__ float sw[kPassThreads / 32][7];
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 7; ++k) sw[threadIdx.x >> 5][k] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 7) {
+        const int k = threadIdx.x;
+        float r = sw[0][k];
+        for (int w2 = 1; w2 < kPassThreads / 32; ++w2) r = (k < 3) ? fminf(r, sw[w2][k]) : fmaxf(r, sw[w2][k]);
+        part[blockIdx.x * 8 + k] = r;
+    }
+}
+
+// Grid of instance blockIdx.x from the partials of its items.
+__global__ void __launch_bounds__(256)
+    k_bbox_final_batch(const float* __restrict__ part, const int* __restrict__ inst_items,
+                       const DevParams* __restrict__ params, DevGrid* __restrict__ grids,
+                       int* __restrict__ ncells_inst, unsigned* __restrict__ flags) {
+    __shared__ float sv[7][256];
+    const int k = blockIdx.x;
+    float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
+    for (int b = inst_items[k] + threadIdx.x; b < inst_items[k + 1]; b += blockDim.x)
+        for (int q = 0; q < 7; ++q)
+            v[q] = (q < 3) ? fminf(v[q], part[b * 8 + q]) : fmaxf(v[q], part[b * 8 + q]);
+    for (int q = 0; q < 7; ++q) sv[q][threadIdx.x] = v[q];
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int q = 0; q < 7; ++q)
+                sv[q][threadIdx.x] = (q < 3) ? fminf(sv[q][threadIdx.x], sv[q][threadIdx.x + st])
+                                             : fmaxf(sv[q][threadIdx.x], sv[q][threadIdx.x + st]);
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const float mm[7] = {sv[0][0], sv[1][0], sv[2][0], sv[3][0], sv[4][0], sv[5][0], sv[6][0]};
+    unsigned fl = 0;
+    DevGrid g = grid_from_bbox(mm, params[k], (long long)1 << 30, fl);
+    grids[k] = g;
+    ncells_inst[k] = g.ok ? g.ncells : 0;
+    if (fl) atomicOr(flags, fl);
+}
+
+// Cell offsets of the instances in the shared table (exclusive scan of their
+// cell counts); a total above the table's capacity disables every grid.
+__global__ void __launch_bounds__(1024)
+    k_cell_offsets(const int* __restrict__ ncells_inst, int n_inst, long long capacity,
+                   DevGrid* __restrict__ grids, int* __restrict__ total_cells,
+                   unsigned* __restrict__ flags) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned s_total;
+    const int per = (n_inst + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(b + per, n_inst);
+    unsigned sum = 0;
+    for (int k = b; k < e; ++k) sum += (unsigned)ncells_inst[k];
+    unsigned off = block_excl_scan<1024>(sum, s_warp, &s_total);
+    const bool over = (long long)s_total > capacity;
+    for (int k = b; k < e; ++k) {
+        grids[k].cell_off = over ? 0 : (int)off;
+        if (over) grids[k].ok = 0;
+        off += (unsigned)ncells_inst[k];
+    }
+    if (threadIdx.x == 0) {
+        *total_cells = over ? (int)capacity : (int)s_total;
+        if (over) atomicOr(flags, (unsigned)FLAG_GRID_OVERFLOW);
+    }
+}
+
+// Cell key of every slot under its instance's grid + digit-0 tile histogram.
+template <int DIM>
+__global__ void __launch_bounds__(kSortThreads)
+    k_hash_batch(const float4* __restrict__ xh, const int* __restrict__ inst, int n,
+                 const DevGrid* __restrict__ grids, unsigned* __restrict__ keys,
+                 unsigned* __restrict__ hist, int num_tiles) {
+    __shared__ unsigned sh[kRadix];
+    sh[threadIdx.x] = 0;
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        int i = base + k * kSortThreads + threadIdx.x;
+        if (i < n) {
+            const DevGrid g = grids[inst[i]];
+            unsigned key = cell_key<DIM>(xh[i], g);
+            keys[i] = key;
+            atomicAdd(&sh[key & 255u], 1u);
+        }
+    }
+    __syncthreads();
+    hist[threadIdx.x * num_tiles + blockIdx.x] = sh[threadIdx.x];
+}
+
+// Cell-ordered working set + leapfrog predictor, per-instance time step.
+template <int DIM>
+__global__ void k_reorder_batch(StateA A, const int* __restrict__ perm, StateB B,
+                                const DevParams* __restrict__ params, const int* __restrict__ its,
+                                int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int j = perm[s];
+    const int k = A.inst[j];
+    const float hdt = (*its == 1) ? 0.f : 0.5f * __ldg(&params[k].dt);
+    const float4 xh = A.xh[j];
+    float4 vm = A.vm[j];
+    float u = A.u[j];
+    const int it = A.itype[j];
+    B.vmin[s] = make_float4(vm.x, vm.y, vm.z, u);
+    float ulo = 0.f;
+    if (it > 0 && hdt != 0.f) {
+        const float4 ap = A.ap[j];
+        vm.x = fmaf(hdt, ap.x, vm.x);
+        vm.y = fmaf(hdt, ap.y, vm.y);
+        if (DIM == 3) vm.z = fmaf(hdt, ap.z, vm.z);
+        const sph::ff uh = sph::two_sum(u, __fmul_rn(hdt, ap.w));
+        u = uh.hi;
+        ulo = uh.lo;
+        if (u < 0.f) {
+            u = 0.f;
+            ulo = 0.f;
+        }
+    }
+    B.ulo[s] = ulo;
+    B.xh[s] = xh;
+    B.vm[s] = vm;
+    B.rp[s] = make_float4(A.rho[j], 0.f, u, 0.f);
+    B.p[s] = A.p[j];
+    B.itype[s] = it;
+    B.id[s] = A.id[j];
+    B.inst[s] = k;
+}
+
+__global__ void k_advance_its(int* its) { *its += 1; }
+
+// ---------------------------------------------------------------------------
 // Neighbour-cell iteration
 // ---------------------------------------------------------------------------
 struct CellCoord {
@@ -605,6 +784,7 @@ struct CellCoord {
 template <int DIM>
 __device__ __forceinline__ CellCoord decode_key(unsigned key, const DevGrid& g) {
     CellCoord cc;
+    key -= (unsigned)g.cell_off;
     cc.c[0] = (int)(key % (unsigned)g.n[0]);
     unsigned t = key / (unsigned)g.n[0];
     if (DIM == 2) {
@@ -634,7 +814,7 @@ __device__ __forceinline__ void for_candidates(const DevGrid& g, const int* __re
             int cy = cc.c[1] + dy;
             if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
             else if (cy < 0 || cy >= g.n[1]) continue;
-            const int row = (cz * g.n[1] + cy) * g.n[0];
+            const int row = g.cell_off + (cz * g.n[1] + cy) * g.n[0];
             if (!g.periodic[0]) {
                 const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
                 const int kb = __ldg(start + row + c0), ke = __ldg(start + row + c1 + 1);
@@ -757,7 +937,7 @@ __device__ __forceinline__ bool candidate_row(const DevGrid& g, const int* __res
     }
     if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
     else if (cy < 0 || cy >= g.n[1]) return true;
-    const int row = (cz * g.n[1] + cy) * g.n[0];
+    const int row = g.cell_off + (cz * g.n[1] + cy) * g.n[0];
     if (!px) {
         const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
         kb = __ldg(start + row + c0);
@@ -801,15 +981,12 @@ __device__ __forceinline__ float fast_sqrt_pos(float x) {
 // Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__global__ void __launch_bounds__(kPassThreads, 8)
-    k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
-              const DevGrid* __restrict__ gp, DevParams P, int n) {
-    __shared__ int s_near[kListCapD][kPassThreads];
-    __shared__ int s_far[kListCapD][kPassThreads];
+__device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
+                                             const int* __restrict__ start, const DevGrid& g,
+                                             const DevParams& P, const int s, const bool valid,
+                                             int (*s_near)[kPassThreads],
+                                             int (*s_far)[kPassThreads]) {
     const int tid = threadIdx.x;
-    const int s = blockIdx.x * blockDim.x + tid;
-    const bool valid = s < n;
-    const DevGrid g = *gp;
     const bool need_div = P.heat_art != 0;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
     float p = 0.f;
@@ -970,13 +1147,10 @@ __global__ void __launch_bounds__(kPassThreads, 8)
 // Pass 1b: shear tensor (physical viscosity), every particle.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__global__ void __launch_bounds__(kPassThreads)
-    k_shear(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
-            const DevGrid* __restrict__ gp, DevParams P, int n) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const DevGrid g = *gp;
-    if (!g.ok) return;
+__device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __restrict__ keys,
+                                           const int* __restrict__ start, const DevGrid& g,
+                                           const DevParams& P, const int s, const bool valid) {
+    if (!valid || !g.ok) return;
     const float4 xi = B.xh[s];
     const float4 vi = B.vm[s];
     const float rhoi = B.rp[s].x;
@@ -1035,15 +1209,13 @@ __global__ void __launch_bounds__(kPassThreads)
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
 template <int DIM>
-__global__ void __launch_bounds__(kPassThreads, 8)
-    k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
-            const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
-            int n) {
-    __shared__ int s_list[kListCap][kPassThreads];
+__device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
+                                           const unsigned* __restrict__ keys,
+                                           const int* __restrict__ start, const DevGrid& g,
+                                           const DevParams& P, const StepArgs& S,
+                                           unsigned* __restrict__ flags, const int s,
+                                           const bool valid, int (*s_list)[kPassThreads]) {
     const int tid = threadIdx.x;
-    const int s = blockIdx.x * blockDim.x + tid;
-    const bool valid = s < n;
-    const DevGrid g = *gp;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
     int it = 0;
     if (valid) {
@@ -1061,6 +1233,7 @@ __global__ void __launch_bounds__(kPassThreads, 8)
         A.p[s] = B.p[s];
         A.itype[s] = it;
         A.id[s] = B.id[s];
+        if (A.inst) A.inst[s] = B.inst[s];
     }
     const bool work = valid && it > 0 && g.ok;
     CellCoord cc = {{0, 0, 0}};
@@ -1257,6 +1430,138 @@ __global__ void __launch_bounds__(kPassThreads, 8)
     A.p[s] = B.p[s];
     A.itype[s] = it;
     A.id[s] = B.id[s];
+    if (A.inst) A.inst[s] = B.inst[s];
+}
+
+// ---------------------------------------------------------------------------
+// Pass kernels of one particle system: one CTA per 128 consecutive slots.
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads, 8)
+    k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+              const DevGrid* __restrict__ gp, DevParams P, int n) {
+    __shared__ int s_near[kListCapD][kPassThreads];
+    __shared__ int s_far[kListCapD][kPassThreads];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevGrid g = *gp;
+    density_body<DIM>(B, keys, start, g, P, s, s < n, s_near, s_far);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_shear(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+            const DevGrid* __restrict__ gp, DevParams P, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevGrid g = *gp;
+    shear_body<DIM>(B, keys, start, g, P, s, s < n);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads, 8)
+    k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
+            const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
+            int n) {
+    __shared__ int s_list[kListCap][kPassThreads];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const DevGrid g = *gp;
+    force_body<DIM>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
+}
+
+// ---------------------------------------------------------------------------
+// Batched (multi-instance) pass kernels: persistent CTAs pull work items
+// (one instance's slots [s0, s1), at most kPassThreads) from an atomic queue;
+// the item's instance parameters, grid and step arguments are staged in shared
+// memory for the CTA. Items are independent, so the order in which CTAs take
+// them does not change any result.
+// ---------------------------------------------------------------------------
+struct ItemCtx {
+    DevParams P;
+    DevGrid g;
+    StepArgs S;
+    WorkItem w;
+};
+
+template <class T>
+__device__ __forceinline__ void copy_to_shared(T* dst, const T* __restrict__ src) {
+    static_assert(sizeof(T) % 4 == 0, "word copy");
+    const int* a = reinterpret_cast<const int*>(src);
+    int* b = reinterpret_cast<int*>(dst);
+    for (int k = threadIdx.x; k < (int)(sizeof(T) / 4); k += blockDim.x) b[k] = __ldg(a + k);
+}
+
+// Takes the next item; false when the queue is empty. Ends with a barrier.
+// Step arguments of iteration `its` of an instance (time_integration.f:131-218).
+__device__ __forceinline__ StepArgs step_args_dev(const DevParams& P, int its) {
+    StepArgs S;
+    S.dt = P.dt;
+    S.kdt = (its == 1) ? 0.5f * P.dt : P.dt;
+    S.hdt = (its == 1) ? 0.f : 0.5f * P.dt;
+    S.heat_on = P.heat_ext && ((double)its * (double)P.dt <= (double)P.heat_t_end);
+    return S;
+}
+
+__device__ __forceinline__ bool next_item(ItemCtx& c, const WorkItem* __restrict__ items,
+                                          int n_items, int* __restrict__ queue,
+                                          const DevParams* __restrict__ params,
+                                          const DevGrid* __restrict__ grids,
+                                          const int* __restrict__ its) {
+    __shared__ int s_it;
+    __syncthreads();  // every thread is done with the previous item
+    if (threadIdx.x == 0) s_it = atomicAdd(queue, 1);
+    __syncthreads();
+    const int it = s_it;
+    if (it >= n_items) return false;
+    if (threadIdx.x == 0) {
+        c.w = items[it];
+        if (its) c.S = step_args_dev(params[c.w.inst], *its);
+    }
+    __syncthreads();
+    const int inst = c.w.inst;
+    copy_to_shared(&c.P, params + inst);
+    copy_to_shared(&c.g, grids + inst);
+    __syncthreads();
+    return true;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads, 8)
+    k_density_batch(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+                    const DevGrid* __restrict__ grids, const DevParams* __restrict__ params,
+                    const WorkItem* __restrict__ items, int n_items, int* __restrict__ queue) {
+    __shared__ int s_near[kListCapD][kPassThreads];
+    __shared__ int s_far[kListCapD][kPassThreads];
+    __shared__ ItemCtx c;
+    while (next_item(c, items, n_items, queue, params, grids, nullptr)) {
+        const int s = c.w.s0 + threadIdx.x;
+        density_body<DIM>(B, keys, start, c.g, c.P, s, s < c.w.s1, s_near, s_far);
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_shear_batch(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+                  const DevGrid* __restrict__ grids, const DevParams* __restrict__ params,
+                  const WorkItem* __restrict__ items, int n_items, int* __restrict__ queue) {
+    __shared__ ItemCtx c;
+    while (next_item(c, items, n_items, queue, params, grids, nullptr)) {
+        const int s = c.w.s0 + threadIdx.x;
+        if (c.P.visc) shear_body<DIM>(B, keys, start, c.g, c.P, s, s < c.w.s1);
+    }
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads, 8)
+    k_force_batch(StateB B, StateA A, const unsigned* __restrict__ keys,
+                  const int* __restrict__ start, const DevGrid* __restrict__ grids,
+                  const DevParams* __restrict__ params, const int* __restrict__ its,
+                  unsigned* __restrict__ flags, const WorkItem* __restrict__ items, int n_items,
+                  int* __restrict__ queue) {
+    __shared__ int s_list[kListCap][kPassThreads];
+    __shared__ ItemCtx c;
+    while (next_item(c, items, n_items, queue, params, grids, its)) {
+        const int s = c.w.s0 + threadIdx.x;
+        force_body<DIM>(B, A, keys, start, c.g, c.P, c.S, flags, s, s < c.w.s1, s_list);
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -111,7 +111,23 @@ armando_status armando_create(armando_ctx** ctx, const armando_params* params,
                               int32_t dim, int64_t n_fluid, int64_t n_wall,
                               int32_t mem_kind);
 
-/* Replaces the context's parameters (same dim). Takes effect at the next call. */
+/*
+ * Batched form: n_instances independent particle systems (a parameter sweep)
+ * in one context. The reference runs one domain per process (globals hRun,
+ * dMatProp in ArmandoThrust/armando.cu:117-134); here instance k has its own
+ * params[k], cell grid and time step, and all instances advance together in
+ * the same kernels (persistent passes over per-instance work items). Particle
+ * arrays are packed: instance k occupies particles [o_k, o_k + n_fluid[k] +
+ * n_wall[k]), o_k the sum of the earlier instances' counts. All instances share
+ * dim.
+ */
+armando_status armando_batch_create(armando_ctx** ctx, int32_t n_instances,
+                                    const armando_params* params, int32_t dim,
+                                    const int64_t* n_fluid, const int64_t* n_wall,
+                                    int32_t mem_kind);
+
+/* Replaces the context's parameters (same dim). Takes effect at the next call.
+ * Batch contexts: ARMANDO_ERR_UNSUPPORTED. */
 armando_status armando_set_params(armando_ctx* ctx, const armando_params* params);
 
 /*
@@ -144,6 +160,15 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx,
                                  const int32_t* itype, float* dvdt,
                                  float* dudt, float dt, int32_t its0,
                                  int32_t steps);
+
+/* armando_integrate on a batch context with a time step per instance, dt[k].
+ * armando_integrate / armando_step on a batch use the one dt for every instance. */
+armando_status armando_batch_integrate(armando_ctx* ctx, float* x, float* vx,
+                                       const float* mass, float* rho, float* p,
+                                       float* u, const float* hsml,
+                                       const int32_t* itype, float* dvdt,
+                                       float* dudt, const float* dt, int32_t its0,
+                                       int32_t steps);
 
 /* Cell id of every particle under the link_list.f grid of positions x (FP32
  * form of ArmandoThrust/acpu.c:2085-2105 / link_list.f:75-88), caller order.

@@ -1,0 +1,107 @@
+"""Batched multi-instance contexts (armando_batch_create / _integrate).
+
+A batch advances every instance with the kernels of one system plus per-instance
+grids and parameters, so each instance must come out bit-identical to the same
+instance run alone, and within the one-step tolerance of the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import armando_gb300 as ag
+from armando_gb300 import cases
+from helpers import FIELDS, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from armando_gb300 import build
+
+    build.build_library()
+    ag.load_library()
+
+
+def _instances_2d():
+    a = cases.perturbed(cases.dam_break(dx=0.03), seed=41, dv=0.05)
+    b = cases.cavity(n_side=24, length=1.0, lid_u=1.0)
+    b.params.c0, b.params.visc, b.params.visc_artificial = 30.0, 0, 1
+    b.params.av_alpha, b.params.av_beta = 0.02, 0.0
+    b.dt = 0.2 * float(b.h[0]) / 30.0
+    c = cases.dam_break(dx=0.04, col_w=0.6, col_h=1.5, tank_w=2.0, tank_h=2.0, seed=43,
+                        alpha=0.04, c0=40.0)
+    d = cases.cavity(n_side=12)  # physical viscosity instance
+    return [a, b, c, d]
+
+
+def _run_single(c, its0, steps):
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.integrate(got, c.dt, its0, steps)
+    return got
+
+
+def _run_batch(insts, its0, steps):
+    arrays, offs = cases.pack(insts)
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts]) as b:
+        b.integrate_batch(arrays, [c.dt for c in insts], its0, steps)
+        assert b.stats().gpu_launches > 0
+    return cases.unpack(arrays, offs, insts)
+
+
+def _packed_ok(insts):
+    # the batch assumes each instance's fluid/wall counts describe its slice
+    for c in insts:
+        assert c.n_fluid + c.n_wall == c.n
+
+
+@pytest.mark.parametrize("its0,steps", [(1, 1), (1, 6)])
+def test_batch_equals_instances_run_alone_2d(its0, steps):
+    insts = _instances_2d()
+    _packed_ok(insts)
+    got = _run_batch(insts, its0, steps)
+    for c, g in zip(insts, got):
+        ref = _run_single(c, its0, steps)
+        for f in FIELDS:
+            assert np.array_equal(getattr(g, f), getattr(ref, f)), (c.name, f)
+
+
+def test_batch_equals_instances_run_alone_3d_periodic():
+    insts = []
+    for k, (nx, nyz) in enumerate([(24, 8), (30, 10)]):
+        c = cases.perturbed(
+            cases.channel(n_x=nx, n_yz=nyz, length=nx * 7.9e-4, width=nyz * 7.9e-4, layers=3,
+                          jitter=0.01, seed=50 + k), seed=60 + k, dv=0.02, du=30.0)
+        insts.append(c)
+    got = _run_batch(insts, 1, 4)
+    for c, g in zip(insts, got):
+        ref = _run_single(c, 1, 4)
+        for f in FIELDS:
+            assert np.array_equal(getattr(g, f), getattr(ref, f)), (c.name, f)
+
+
+def test_sweep_instances_match_oracle(O):
+    insts = cases.sweep(n_instances=6, seed=44, n_min=400, n_max=3000)
+    arrays, offs = cases.pack(insts)
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts]) as b:
+        b.integrate_batch(arrays, [c.dt for c in insts], 1, 1)
+    got = cases.unpack(arrays, offs, insts)
+    for c, g in zip(insts, got):
+        ref = O.State(c)
+        O.step(ref, 1, c.dt)
+        for f in FIELDS:
+            e = rel_err(getattr(g, f), getattr(ref, f))
+            assert e <= TOL_STEP, (c.name, f, e)
+
+
+def test_batch_rejects_single_only_calls():
+    insts = _instances_2d()[:2]
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts]) as b:
+        with pytest.raises(ag.ArmandoError) as e:
+            b.cell_ids(insts[0].x, insts[0].h)
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
