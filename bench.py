@@ -65,6 +65,11 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 3D channel and batched-sweep workloads")
+    ap.add_argument("--extra-steps", type=int, default=20)
+    ap.add_argument("--sweep-instances", type=int, default=512)
+    ap.add_argument("--plain-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -204,6 +209,84 @@ def run_reference(args, rank):
     return line
 
 
+def timed_integrate(ctx, arrays, dts, its0, steps, batch=False):
+    """CUDA-event time (ms) of `steps` iterations on the context's stream."""
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    if batch:
+        ctx.integrate_batch(arrays, dts, its0, steps)
+    else:
+        ctx.integrate(arrays, dts, its0, steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_channel(args):
+    """3D heated channel, 504 x 126 x 126 fluid + 3 wall layers (8.0 M fluid)."""
+    import torch
+
+    import armando_gb300 as ag
+    from armando_gb300 import cases
+
+    c = cases.channel()
+    dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
+    with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+        ctx.integrate(dev, c.dt, 1, 3)
+        ms = timed_integrate(ctx, dev, c.dt, 4, args.extra_steps)
+        phases = ctx.profile_phases(2)
+    del dev
+    torch.cuda.empty_cache()
+    return {"workload": f"channel3d: {c.n_fluid} fluid + {c.n_wall} wall particles, periodic x, "
+                        f"art. visc + art. heat + Gaussian source",
+            "particles": c.n, "steps": args.extra_steps, "ms_per_step": ms / args.extra_steps,
+            "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC, "phases_ms": phases}
+
+
+def run_sweep(args):
+    """Batched sweep vs the plain step run instance by instance on the same GPU."""
+    import torch
+
+    import armando_gb300 as ag
+    from armando_gb300 import cases
+
+    insts = cases.sweep(n_instances=args.sweep_instances)
+    arrays, offs = cases.pack(insts)
+    dts = [c.dt for c in insts]
+    ntot = int(offs[-1])
+    dev = {k: torch.from_numpy(v).cuda() for k, v in arrays.items()}
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts], mem=ag.MEM_DEVICE) as b:
+        b.integrate_batch(dev, dts, 1, 3)
+        launches0 = b.stats().gpu_launches
+        ms_b = timed_integrate(b, dev, dts, 4, args.extra_steps, batch=True)
+        launches = b.stats().gpu_launches - launches0
+    del dev
+    torch.cuda.empty_cache()
+    batch_rate = ntot * args.extra_steps / (ms_b * 1e-3)
+    # Plain step, one instance after another (each its own context and graph).
+    ms_p = 0.0
+    for c in insts:
+        d = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
+        with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+            ctx.integrate(d, c.dt, 1, 3)
+            ms_p += timed_integrate(ctx, d, c.dt, 4, args.plain_steps)
+    plain_rate = ntot * args.plain_steps / (ms_p * 1e-3)
+    return {"workload": f"{len(insts)} instances (alternating 2D dam break / lid-driven cavity), "
+                        f"{ntot} particles, n_k log-uniform in [2e3, 2e5], alpha ~ U(0.005, 0.05), "
+                        f"c0 ~ U(20, 80), seed 4",
+            "particles": ntot, "instances": len(insts), "steps": args.extra_steps,
+            "value": batch_rate, "unit": METRIC, "ms_per_step": ms_b / args.extra_steps,
+            "gpu_launches_per_step": launches / args.extra_steps,
+            "plain_per_instance": {"value": plain_rate, "steps": args.plain_steps,
+                                   "ms_per_step_all_instances": ms_p / args.plain_steps},
+            "speedup_vs_plain": batch_rate / plain_rate}
+
+
 def config_dict(case, args):
     return {"workload": f"{case.name}: {case.n_fluid} fluid + {case.n_wall} wall particles, "
                         f"dim {case.dim}, dx {case.meta.get('dx'):.4g} m, dt {case.dt:.4g} s",
@@ -324,6 +407,8 @@ def run_ours(args, rank, world, local_rank):
                       "steps": e2e_steps, "api": "armando_step, pinned host buffers"}
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(make_case(args.config, args.dx), args.cpu_seconds)
+    if not args.no_extras and rank == 0 and world == 1:
+        out["workloads"] = {"channel3d": run_channel(args), "sweep": run_sweep(args)}
     return out
 
 
