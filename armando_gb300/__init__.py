@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from ._abi import (ERR_UNSUPPORTED, EXPORTED, LIB_PATH, MEM_DEVICE, MEM_HOST, OK,  # noqa: F401
-                   STATUS_NAMES, Params, Stats, load_library)
+                   STATUS_NAMES, ParamGrads, Params, Stats, load_library)
 
 __all__ = ["Context", "Batch", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
            "MEM_DEVICE", "LIB_PATH", "EXPORTED"]
@@ -127,6 +127,35 @@ class Context:
                                                 _ptr(a["dvdt"]), _ptr(a["dudt"]), float(dt),
                                                 int(its0), int(steps)))
         return s
+
+    # -- reverse mode -----------------------------------------------------------
+    def forward_checkpointed(self, s, dt: float, its0: int, steps: int, checkpoint_every: int):
+        """armando_integrate keeping a checkpoint every `checkpoint_every` iterations."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        self._check(self._lib.armando_forward_checkpointed(
+            self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+            _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
+            float(dt), int(its0), int(steps), int(checkpoint_every)))
+        return s
+
+    def backward(self, x_bar=None, v_bar=None, u_bar=None, p_bar=None, dvdt_bar=None,
+                 dudt_bar=None):
+        """Cotangents of the initial state and of the parameters for cotangents of the
+        final state of the last forward_checkpointed (host memory kind: numpy)."""
+        n, nd = self.n, self.n * self.dim
+        f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)  # noqa: E731
+        ins = [f32(a) for a in (x_bar, v_bar, u_bar, p_bar, dvdt_bar, dudt_bar)]
+        outs = {"x": np.zeros(nd, np.float32), "v": np.zeros(nd, np.float32),
+                "u": np.zeros(n, np.float32), "dvdt": np.zeros(nd, np.float32),
+                "dudt": np.zeros(n, np.float32)}
+        g = ParamGrads()
+        self._check(self._lib.armando_backward(
+            self._h, *[_ptr(a) for a in ins], _ptr(outs["x"]), _ptr(outs["v"]), _ptr(outs["u"]),
+            _ptr(outs["dvdt"]), _ptr(outs["dudt"]), C.byref(g)))
+        outs["params"] = {"av_alpha": g.av_alpha, "av_beta": g.av_beta, "c0": g.c0,
+                          "heat_q0": g.heat_q0}
+        return outs
 
     # -- diagnostics ---------------------------------------------------------
     def cell_ids(self, x, h):

@@ -108,6 +108,13 @@ class Params(C.Structure):
         return out
 
 
+class ParamGrads(C.Structure):
+    """``armando_param_grads``."""
+
+    _fields_ = [("av_alpha", C.c_double), ("av_beta", C.c_double), ("c0", C.c_double),
+                ("heat_q0", C.c_double)]
+
+
 class Stats(C.Structure):
     """``armando_stats``."""
 
@@ -132,6 +139,7 @@ EXPORTED = [
     "armando_last_error", "armando_destroy", "armando_abi_version",
     "armando_get_stream", "armando_profile_phases", "armando_cell_ids_noalloc",
     "armando_batch_create", "armando_batch_integrate",
+    "armando_forward_checkpointed", "armando_backward",
 ]
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
@@ -187,6 +195,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_batch_create.restype = C.c_int
     lib.armando_batch_integrate.argtypes = [vp] * 11 + [vp, C.c_int32, C.c_int32]
     lib.armando_batch_integrate.restype = C.c_int
+    lib.armando_forward_checkpointed.argtypes = step_args + [C.c_int32, C.c_int32]
+    lib.armando_forward_checkpointed.restype = C.c_int
+    lib.armando_backward.argtypes = [vp] * 12 + [C.POINTER(ParamGrads)]
+    lib.armando_backward.restype = C.c_int
     lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
     lib.armando_cell_ids_noalloc.restype = C.c_int
     del fp, ip

@@ -1,0 +1,456 @@
+// adjoint.cuh -- reverse mode of one leapfrog step (hand-written adjoint).
+//
+// The step is the forward of kernels.cuh: predictor, summation density, Tait
+// EOS, pressure force + Monaghan artificial viscosity + pressure work, external
+// heat, gravity, corrector (CERNsource time_integration.f:131-218 with
+// single_step.f, density.f, eos.f90:255-283, internal_force.f pa_sph = 1,
+// art_visc.f). Its reverse runs as three gathers over the step's neighbour
+// sets (the topology of the step is frozen), with no atomics:
+//   k_adj_out      cotangents of the corrector: a_bar, du_bar of every particle
+//   k_adj_force    pair adjoints of every (i, j) and (j, i) a particle takes
+//                  part in, then the EOS and external-heat adjoints of the
+//                  particle: x_bar, vh_bar (predicted velocity), rho_bar
+//   k_adj_density  adjoint of the summation density, assembly of the input
+//                  cotangents, scatter to the slot order of the step's input
+// Non-smooth points follow the value: art_visc acts while v_ij . r_ij < 0,
+// u = max(0, .) and the Tait clamp pass no gradient where they bind.
+// Supported: pa_sph = 1, no physical viscosity, no artificial heat.
+#pragma once
+#include "kernels.cuh"
+
+namespace ag {
+
+// Cotangents of the carried state (x, v, u, previous a, previous du), in one
+// slot order: xb {x_bar, -}, vb {v_bar, u_bar}, ab {a_bar, du_bar}.
+struct AdjState {
+    float4* xb;
+    float4* vb;
+    float4* ab;
+};
+
+enum AdjParam { ADJ_ALPHA = 0, ADJ_BETA = 1, ADJ_C0 = 2, ADJ_Q0 = 3, ADJ_NPARAM = 4 };
+
+// Caller-order cotangents -> slot order of the final state (A.id).
+template <int DIM>
+__global__ void k_adj_load(const int* __restrict__ id, const float* __restrict__ xbar,
+                           const float* __restrict__ vbar, const float* __restrict__ ubar,
+                           const float* __restrict__ abar, const float* __restrict__ dubar,
+                           const float* __restrict__ pbar, AdjState G, float* __restrict__ pbar_s,
+                           int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int i = id[s];
+    auto v3 = [&](const float* a) {
+        if (!a) return make_float4(0.f, 0.f, 0.f, 0.f);
+        return make_float4(a[DIM * i], a[DIM * i + 1], DIM == 3 ? a[DIM * i + 2] : 0.f, 0.f);
+    };
+    float4 xb = v3(xbar), vb = v3(vbar), ab = v3(abar);
+    vb.w = ubar ? ubar[i] : 0.f;
+    ab.w = dubar ? dubar[i] : 0.f;
+    G.xb[s] = xb;
+    G.vb[s] = vb;
+    G.ab[s] = ab;
+    pbar_s[s] = pbar ? pbar[i] : 0.f;
+}
+
+// Slot order (= caller order after the gather of the inputs) -> caller arrays.
+template <int DIM>
+__global__ void k_adj_store(AdjState G, int n, float* __restrict__ xbar, float* __restrict__ vbar,
+                            float* __restrict__ ubar, float* __restrict__ abar,
+                            float* __restrict__ dubar) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 xb = G.xb[i], vb = G.vb[i], ab = G.ab[i];
+    const float xs[3] = {xb.x, xb.y, xb.z}, vs[3] = {vb.x, vb.y, vb.z}, as[3] = {ab.x, ab.y, ab.z};
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        if (xbar) xbar[DIM * i + d] = xs[d];
+        if (vbar) vbar[DIM * i + d] = vs[d];
+        if (abar) abar[DIM * i + d] = as[d];
+    }
+    if (ubar) ubar[i] = vb.w;
+    if (dubar) dubar[i] = ab.w;
+}
+
+// Corrector reverse: x' = x + dt v', v' = v + kdt a, u' = max(0, u + kdt du),
+// outputs also carry a and du to the next predictor.
+__global__ void k_adj_out(StateB B, StateA A, AdjState G, StepArgs S, float4* __restrict__ abar,
+                          float4* __restrict__ xpart, float4* __restrict__ vpart, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (B.itype[s] <= 0) {
+        abar[s] = z;
+        xpart[s] = z;
+        vpart[s] = z;
+        return;
+    }
+    const float4 xb = G.xb[s], vb = G.vb[s], ab = G.ab[s];
+    const float4 vt = make_float4(fmaf(S.dt, xb.x, vb.x), fmaf(S.dt, xb.y, vb.y),
+                                  fmaf(S.dt, xb.z, vb.z), 0.f);
+    const float du = A.ap[s].w;
+    const bool clamped = fmaf(S.kdt, du, B.vmin[s].w) < 0.f;
+    const float ub = clamped ? 0.f : vb.w;
+    abar[s] = make_float4(fmaf(S.kdt, vt.x, ab.x), fmaf(S.kdt, vt.y, ab.y), fmaf(S.kdt, vt.z, ab.z),
+                          fmaf(S.kdt, ub, ab.w));
+    xpart[s] = make_float4(xb.x, xb.y, xb.z, 0.f);
+    vpart[s] = make_float4(vt.x, vt.y, vt.z, ub);
+}
+
+// Adjoint of the force and energy-rate terms of pair (i, j), i fluid:
+//   a_i  += -S d,   du_i += -S (w.d)/2,   S = m_j (P_i + P_j + Pi_ij) G(r),
+// d = x_i - x_j, w = vh_j - vh_i, Pi_ij the art_visc term (0 unless w.d > 0).
+// ab = {a_bar_i, du_bar_i}. Outputs cotangents on d and w, on P_i and P_j
+// (equal), on rho_i and rho_j (equal halves of rho_bar), and on alpha, beta, c0.
+struct PairAdj {
+    float db[3], wb[3];
+    float Pb, rb, al, be, c0;
+};
+
+template <int DIM>
+__device__ __forceinline__ void pair_adjoint(const float* d, const float* w, float dr2, float G,
+                                             float dGdr_r, float mh, float rho_bar, float Pi,
+                                             float Pj, float mj, const float4& ab,
+                                             const DevParams& P, PairAdj& o) {
+    float wd = w[0] * d[0] + w[1] * d[1];
+    float ad = ab.x * d[0] + ab.y * d[1];
+    if (DIM == 3) {
+        wd += w[2] * d[2];
+        ad += ab.z * d[2];
+    }
+    const float vr = -wd;  // (vh_i - vh_j) . (x_i - x_j)
+    float pv = 0.f, phi = 0.f, den = 1.f;
+    const bool av = P.visc_art && vr < 0.f;
+    if (av) {
+        den = dr2 + mh * mh * P.av_eta2;
+        phi = mh * vr / den;
+        pv = (P.av_beta * phi - P.av_alpha * P.c0) * phi / rho_bar;
+    }
+    const float T = Pi + Pj + pv;
+    const float Sv = mj * T * G;
+    const float Sb = -(ad + 0.5f * ab.w * wd);
+    const float abv[3] = {ab.x, ab.y, ab.z};
+    const float Gb = mj * T * Sb;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+        o.db[k] = -Sv * (abv[k] + 0.5f * ab.w * w[k]) + Gb * dGdr_r * d[k];
+        o.wb[k] = -0.5f * Sv * ab.w * d[k];
+    }
+    const float Tb = mj * G * Sb;
+    o.Pb = Tb;
+    o.rb = o.al = o.be = o.c0 = 0.f;
+    if (av) {
+        const float pb = Tb;
+        const float phib = pb * (2.f * P.av_beta * phi - P.av_alpha * P.c0) / rho_bar;
+        o.rb = -0.5f * pb * pv / rho_bar;
+        o.al = -pb * P.c0 * phi / rho_bar;
+        o.be = pb * phi * phi / rho_bar;
+        o.c0 = -pb * P.av_alpha * phi / rho_bar;
+        const float vrb = phib * mh / den;
+        const float r2b = -phib * phi / den;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+            o.wb[k] -= vrb * d[k];
+            o.db[k] += -vrb * w[k] + 2.f * r2b * d[k];
+        }
+    }
+}
+
+// Neighbours of a fluid particle in warp-converged rounds (same candidates and
+// pair test as the forward passes; 2D reuses the density pass's bit mask).
+template <int DIM>
+struct NbrStream {
+    Cursor cu;
+    bool done, from_mask;
+    uint4 mk;
+    int wi, rbase;
+    unsigned wbits;
+};
+
+template <int DIM>
+__device__ __forceinline__ void nbr_init(NbrStream<DIM>& ns, const StateB& B, int s, bool work) {
+    ns.cu = {-1, 0, 0};
+    ns.done = !work;
+    ns.mk = make_uint4(0u, 0u, 0u, 0u);
+    ns.from_mask = false;
+    if (DIM == 2 && work) {
+        ns.mk = B.nmask[s];
+        ns.from_mask = !(ns.mk.x == ~0u && ns.mk.y == ~0u && ns.mk.z == ~0u && ns.mk.w == ~0u);
+    }
+    ns.wi = 0;
+    ns.rbase = 0;
+    ns.wbits = ns.mk.x;
+}
+
+template <int DIM>
+__device__ __forceinline__ int nbr_fill(NbrStream<DIM>& ns, const StateB& B, const DevGrid& g,
+                                        const int* __restrict__ start, const CellCoord& cc,
+                                        const float4& xi, int s, int (*s_list)[kPassThreads]) {
+    const int tid = threadIdx.x;
+    int nl = 0;
+    while (!ns.done && ns.from_mask) {
+        if (nl == kListCap) break;
+        while (ns.wbits == 0u && ns.wi < 3) {
+            ++ns.wi;
+            ns.wbits = (ns.wi == 1) ? ns.mk.y : (ns.wi == 2) ? ns.mk.z : ns.mk.w;
+        }
+        if (ns.wbits == 0u) {
+            ns.done = true;
+            break;
+        }
+        const int o = 32 * ns.wi + __ffs(ns.wbits) - 1;
+        ns.wbits &= ns.wbits - 1u;
+        bool in_rows = true;
+        while (o >= ns.rbase + (ns.cu.ke - ns.cu.k)) {
+            ns.rbase += ns.cu.ke - ns.cu.k;
+            if (!cursor_next<DIM>(g, start, cc, ns.cu)) {
+                in_rows = false;
+                break;
+            }
+        }
+        if (!in_rows) {
+            ns.done = true;
+            break;
+        }
+        s_list[nl++][tid] = ns.cu.k + (o - ns.rbase);
+    }
+    while (!ns.done && !ns.from_mask) {
+        if (ns.cu.k >= ns.cu.ke) {
+            if (!cursor_next<DIM>(g, start, cc, ns.cu)) {
+                ns.done = true;
+                break;
+            }
+        }
+        if (nl == kListCap) break;
+        const int k = ns.cu.k++;
+        if (k == s) continue;
+        float d[3], dr2;
+        if (pair_delta<DIM>(xi, __ldg(B.xh + k), g, d, dr2)) s_list[nl++][tid] = k;
+    }
+    return nl;
+}
+
+// Forward pair geometry shared by the adjoint gathers.
+template <int DIM>
+struct PairGeo {
+    float d[3], dr2, G, dGdr_r, mh;
+};
+
+template <int DIM>
+__device__ __forceinline__ void pair_geo(const float4& xi, const float4& xj, const DevGrid& g,
+                                         const DevParams& P, PairGeo<DIM>& pg) {
+    pair_delta<DIM>(xi, xj, g, pg.d, pg.dr2);
+    refine_periodic<DIM>(xi, xj, g, pg.d, pg.dr2);
+    const float ih = (xj.w == xi.w) ? __fdividef(1.0f, xi.w) : __fdividef(2.0f, xi.w + xj.w);
+    const float kgih = P.kg * pow_grad<DIM>(ih);
+    const float r = fast_sqrt_pos(pg.dr2);
+    const float t = r * ih - 2.0f;
+    pg.G = kgih * t * t * t;
+    pg.dGdr_r = r > 0.f ? 3.0f * kgih * ih * t * t / r : 0.f;
+    pg.mh = 0.5f * (xi.w + xj.w);
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_adj_force(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+                const DevGrid* __restrict__ gp, DevParams P, StepArgs S,
+                const float4* __restrict__ abar, const float* __restrict__ pbar_loss,
+                float* __restrict__ rhobar, float4* __restrict__ xF, float4* __restrict__ vhb,
+                float* __restrict__ block_part, int n) {
+    __shared__ int s_list[kListCap][kPassThreads];
+    __shared__ float s_red[ADJ_NPARAM][kPassThreads / 32];
+    const int tid = threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + tid;
+    const bool valid = s < n;
+    const DevGrid g = *gp;
+    const bool work = valid && g.ok && B.itype[s] > 0;
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi, abi = xi;
+    float pi = 0.f;
+    if (work) {
+        xi = B.xh[s];
+        vi = B.vm[s];
+        rpi = B.rp[s];
+        pi = B.p[s];
+        abi = abar[s];
+    }
+    const float mi = mass_of<DIM>(xi, vi);
+    CellCoord cc = {{0, 0, 0}};
+    if (work) cc = decode_key<DIM>(keys[s], g);
+    float xb[3] = {0.f, 0.f, 0.f}, vb[3] = {0.f, 0.f, 0.f}, Pb = 0.f, rb = 0.f;
+    float pa[ADJ_NPARAM] = {0.f, 0.f, 0.f, 0.f};
+    NbrStream<DIM> ns;
+    nbr_init<DIM>(ns, B, s, work);
+    while (__any_sync(0xffffffffu, !ns.done)) {
+        const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
+        const int ml = __reduce_max_sync(0xffffffffu, nl);
+        for (int t = 0; t < ml; ++t) {
+            if (t >= nl) continue;
+            const int j = s_list[t][tid];
+            const float4 xj = __ldg(B.xh + j);
+            const float4 vj = __ldg(B.vm + j);
+            const float4 rpj = __ldg(B.rp + j);
+            const float4 abj = __ldg(abar + j);
+            const float mj = mass_of<DIM>(xj, vj);
+            PairGeo<DIM> pg;
+            pair_geo<DIM>(xi, xj, g, P, pg);
+            const float rho_bar = 0.5f * (rpi.x + rpj.x);
+            float w[3] = {vj.x - vi.x, vj.y - vi.y, DIM == 3 ? vj.z - vi.z : 0.f};
+            PairAdj o;
+            // Pair (s, j): the rates of s.
+            pair_adjoint<DIM>(pg.d, w, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpi.y, rpj.y, mj,
+                              abi, P, o);
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                xb[k] += o.db[k];
+                vb[k] -= o.wb[k];
+            }
+            Pb += o.Pb;
+            rb += o.rb;
+            pa[ADJ_ALPHA] += o.al;
+            pa[ADJ_BETA] += o.be;
+            pa[ADJ_C0] += o.c0;
+            // Pair (j, s): the rates of j (zero cotangents for walls).
+            if (abj.x != 0.f || abj.y != 0.f || abj.z != 0.f || abj.w != 0.f) {
+                float dn[3] = {-pg.d[0], -pg.d[1], -pg.d[2]};
+                float wn[3] = {-w[0], -w[1], -w[2]};
+                pair_adjoint<DIM>(dn, wn, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpj.y, rpi.y,
+                                  mi, abj, P, o);
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) {
+                    xb[k] -= o.db[k];
+                    vb[k] += o.wb[k];
+                }
+                Pb += o.Pb;
+                rb += o.rb;
+            }
+        }
+    }
+    if (work) {
+        const float rho = rpi.x;
+        if (S.heat_on) {  // du += q0 exp(-|x - xc|^2 k) / rho
+            const float e0 = xi.x - P.heat_center[0], e1 = xi.y - P.heat_center[1];
+            const float e2 = (DIM == 3) ? xi.z - P.heat_center[2] : 0.f;
+            const float ex = expf(-(e0 * e0 + e1 * e1 + e2 * e2) * P.heat_k);
+            const float dub = abi.w;
+            pa[ADJ_Q0] += dub * ex / rho;
+            rb -= dub * P.heat_q0 * ex / (rho * rho);
+            const float gx = -2.f * P.heat_k * dub * P.heat_q0 * ex / rho;
+            xb[0] += gx * e0;
+            xb[1] += gx * e1;
+            if (DIM == 3) xb[2] += gx * e2;
+        }
+        // Tait EOS and P = p/rho^2 (the clamp p < pmin sets constants: no gradient).
+        const bool clamped = (P.pmin > -FLT_MAX) && pi == 0.f && rho == P.rho0;
+        float rtot = 0.f;
+        if (!clamped) {
+            const float pb = Pb / (rho * rho) + pbar_loss[s];
+            const float ratio = rho * P.inv_rho0;
+            const float r3 = ratio * ratio * ratio;
+            rtot = rb - 2.f * Pb * pi / (rho * rho * rho) + pb * P.c0 * P.c0 * r3 * r3;
+            if (P.c0 > 0.f) pa[ADJ_C0] += pb * 2.f * pi / P.c0;
+        }
+        rhobar[s] = rtot;
+        xF[s] = make_float4(xb[0], xb[1], xb[2], 0.f);
+        vhb[s] = make_float4(vb[0], vb[1], vb[2], 0.f);
+    } else if (valid) {
+        rhobar[s] = 0.f;
+        xF[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        vhb[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    // Deterministic per-block partial sums of the parameter cotangents.
+#pragma unroll
+    for (int q = 0; q < ADJ_NPARAM; ++q) {
+        float v = pa[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) s_red[q][tid >> 5] = v;
+    }
+    __syncthreads();
+    if (tid < ADJ_NPARAM) {
+        float v = 0.f;
+        for (int w2 = 0; w2 < kPassThreads / 32; ++w2) v += s_red[tid][w2];
+        block_part[blockIdx.x * ADJ_NPARAM + tid] = v;
+    }
+}
+
+// Density reverse (rho_i = m_i W(0) + sum m_j W_ij), assembly, scatter to the
+// slot order of the step's input (perm: cell slot -> input slot).
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_adj_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+                  const DevGrid* __restrict__ gp, DevParams P, StepArgs S,
+                  const float* __restrict__ rhobar, const float4* __restrict__ xF,
+                  const float4* __restrict__ vhb, const float4* __restrict__ xpart,
+                  const float4* __restrict__ vpart, const int* __restrict__ perm, AdjState Gp,
+                  int n) {
+    __shared__ int s_list[kListCap][kPassThreads];
+    const int tid = threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + tid;
+    const bool valid = s < n;
+    const DevGrid g = *gp;
+    const bool work = valid && g.ok && B.itype[s] > 0;
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi;
+    float rbi = 0.f;
+    if (work) {
+        xi = B.xh[s];
+        vi = B.vm[s];
+        rbi = rhobar[s];
+    }
+    const float mi = mass_of<DIM>(xi, vi);
+    CellCoord cc = {{0, 0, 0}};
+    if (work) cc = decode_key<DIM>(keys[s], g);
+    float xb[3] = {0.f, 0.f, 0.f};
+    NbrStream<DIM> ns;
+    nbr_init<DIM>(ns, B, s, work);
+    while (__any_sync(0xffffffffu, !ns.done)) {
+        const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
+        const int ml = __reduce_max_sync(0xffffffffu, nl);
+        for (int t = 0; t < ml; ++t) {
+            if (t >= nl) continue;
+            const int j = s_list[t][tid];
+            const float4 xj = __ldg(B.xh + j);
+            float mj;
+            if (DIM == 2) mj = xj.z;
+            else mj = __ldg(&B.vm[j].w);
+            const float rbj = __ldg(rhobar + j);
+            PairGeo<DIM> pg;
+            pair_geo<DIM>(xi, xj, g, P, pg);
+            const float c = (rbi * mj + rbj * mi) * pg.G;
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) xb[k] = fmaf(c, pg.d[k], xb[k]);
+        }
+    }
+    if (!valid) return;
+    float4 gx = make_float4(0.f, 0.f, 0.f, 0.f), gv = gx, ga = gx;
+    if (work) {
+        const float4 xp = xpart[s], f = xF[s], vh = vhb[s], vp = vpart[s];
+        gx = make_float4(xp.x + f.x + xb[0], xp.y + f.y + xb[1], xp.z + f.z + xb[2], 0.f);
+        // predictor: vh = v + hdt a_prev (v_bar gets vh_bar; a_prev_bar = hdt vh_bar)
+        gv = make_float4(vp.x + vh.x, vp.y + vh.y, vp.z + vh.z, vp.w);
+        ga = make_float4(S.hdt * vh.x, S.hdt * vh.y, S.hdt * vh.z, 0.f);
+    }
+    const int j = perm[s];
+    Gp.xb[j] = gx;
+    Gp.vb[j] = gv;
+    Gp.ab[j] = ga;
+}
+
+// Adds the step's parameter cotangents (block partials, fixed order) to acc.
+__global__ void __launch_bounds__(256)
+    k_adj_params(const float* __restrict__ block_part, int nblocks, double* __restrict__ acc) {
+    __shared__ double s[ADJ_NPARAM][256];
+    for (int q = 0; q < ADJ_NPARAM; ++q) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += (double)block_part[b * ADJ_NPARAM + q];
+        s[q][threadIdx.x] = v;
+    }
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int q = 0; q < ADJ_NPARAM; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x < ADJ_NPARAM) acc[threadIdx.x] += s[threadIdx.x][0];
+}
+
+}  // namespace ag

@@ -18,6 +18,7 @@
 
 #include "../../include/armando.h"
 #include "kernels.cuh"
+#include "adjoint.cuh"
 
 using namespace ag;
 
@@ -109,6 +110,18 @@ struct armando_ctx {
     int any_visc = 0;
     int grid_density = 0, grid_shear = 0, grid_force = 0;  // persistent CTAs
     cudaGraphExec_t batch_graph = nullptr;
+    // Reverse mode (armando_forward_checkpointed / armando_backward).
+    std::vector<StateA> ckpts;           // state before iterations its0 + k*K
+    std::vector<StateA> seg;             // states of one segment during the reverse sweep
+    AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
+    float4 *adj_abar = nullptr, *adj_xpart = nullptr, *adj_vpart = nullptr, *adj_xF = nullptr,
+           *adj_vhb = nullptr;
+    float *adj_rhobar = nullptr, *adj_pbar = nullptr, *adj_blk = nullptr;
+    double* adj_pacc = nullptr;
+    std::map<GraphKey, cudaGraphExec_t> adj_graphs;
+    int adj_its0 = 0, adj_steps = 0, adj_K = 0;
+    float adj_dt = 0.f;
+    bool adj_ready = false;
 };
 
 namespace {
@@ -212,6 +225,8 @@ StepArgs make_args(const armando_ctx* c, float dt, int its) {
 void free_graphs(armando_ctx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
+    for (auto& kv : c->adj_graphs) cudaGraphExecDestroy(kv.second);
+    c->adj_graphs.clear();
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     c->batch_graph = nullptr;
 }
@@ -671,6 +686,127 @@ armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, 
     return ARMANDO_OK;
 }
 
+// ---- reverse mode ------------------------------------------------------------
+armando_status alloc_stateA(armando_ctx* ctx, StateA& a) {
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    a.xh = dalloc<float4>(n, e);
+    a.vm = dalloc<float4>(n, e);
+    a.u = dalloc<float>(n, e);
+    a.ap = dalloc<float4>(n, e);
+    a.rho = dalloc<float>(n, e);
+    a.p = dalloc<float>(n, e);
+    a.itype = dalloc<int>(n, e);
+    a.id = dalloc<int>(n, e);
+    a.inst = nullptr;
+    for (void* p : {(void*)a.xh, (void*)a.vm, (void*)a.u, (void*)a.ap, (void*)a.rho, (void*)a.p,
+                    (void*)a.itype, (void*)a.id})
+        ctx->owned.push_back(p);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(checkpoint)");
+    return ARMANDO_OK;
+}
+
+armando_status copy_stateA(armando_ctx* ctx, const StateA& dst, const StateA& src) {
+    const size_t n = (size_t)ctx->n;
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemcpyAsync(dst.xh, src.xh, n * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.vm, src.vm, n * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.u, src.u, n * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.ap, src.ap, n * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.rho, src.rho, n * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.p, src.p, n * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.itype, src.itype, n * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(dst.id, src.id, n * 4, cudaMemcpyDeviceToDevice, st));
+    return ARMANDO_OK;
+}
+
+armando_status alloc_adjoint(armando_ctx* ctx) {
+    if (ctx->adj_abar) return ARMANDO_OK;
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    for (AdjState* g : {&ctx->adjG, &ctx->adjGp}) {
+        g->xb = dalloc<float4>(n, e);
+        g->vb = dalloc<float4>(n, e);
+        g->ab = dalloc<float4>(n, e);
+        for (void* p : {(void*)g->xb, (void*)g->vb, (void*)g->ab}) ctx->owned.push_back(p);
+    }
+    ctx->adj_abar = dalloc<float4>(n, e);
+    ctx->adj_xpart = dalloc<float4>(n, e);
+    ctx->adj_vpart = dalloc<float4>(n, e);
+    ctx->adj_xF = dalloc<float4>(n, e);
+    ctx->adj_vhb = dalloc<float4>(n, e);
+    ctx->adj_rhobar = dalloc<float>(n, e);
+    ctx->adj_pbar = dalloc<float>(n, e);
+    ctx->adj_blk = dalloc<float>((size_t)blocks_for(ctx->n, kPassThreads) * ADJ_NPARAM + 4, e);
+    ctx->adj_pacc = dalloc<double>(ADJ_NPARAM, e);
+    for (void* p : {(void*)ctx->adj_abar, (void*)ctx->adj_xpart, (void*)ctx->adj_vpart,
+                    (void*)ctx->adj_xF, (void*)ctx->adj_vhb, (void*)ctx->adj_rhobar,
+                    (void*)ctx->adj_pbar, (void*)ctx->adj_blk, (void*)ctx->adj_pacc})
+        ctx->owned.push_back(p);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(adjoint)");
+    return ARMANDO_OK;
+}
+
+// Adjoint kernels of the step just recomputed (B holds its intermediates, A
+// its outputs): cotangents adjG (output order) -> adjGp (input order); then
+// adjG <- adjGp.
+template <int DIM>
+int launch_adjoint(armando_ctx* ctx, const StepArgs& S) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    const int nb = blocks_for(n, kPassThreads);
+    k_adj_out<<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, ctx->A, ctx->adjG, S, ctx->adj_abar,
+                                                  ctx->adj_xpart, ctx->adj_vpart, n);
+    k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, S,
+                                                 ctx->adj_abar, ctx->adj_pbar, ctx->adj_rhobar,
+                                                 ctx->adj_xF, ctx->adj_vhb, ctx->adj_blk, n);
+    k_adj_density<DIM><<<nb, kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, ctx->dp,
+                                                   S, ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb,
+                                                   ctx->adj_xpart, ctx->adj_vpart, perm,
+                                                   ctx->adjGp, n);
+    k_adj_params<<<1, 256, 0, st>>>(ctx->adj_blk, nb, ctx->adj_pacc);
+    cudaMemcpyAsync(ctx->adjG.xb, ctx->adjGp.xb, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(ctx->adjG.vb, ctx->adjGp.vb, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(ctx->adjG.ab, ctx->adjGp.ab, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
+    return 4;
+}
+
+armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S) {
+    GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
+    auto itg = ctx->adj_graphs.find(key);
+    cudaGraphExec_t exec = nullptr;
+    int per_step = 4;
+    if (itg == ctx->adj_graphs.end()) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        per_step = ctx->dim == 2 ? launch_adjoint<2>(ctx, S) : launch_adjoint<3>(ctx, S);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        if (le != cudaSuccess) return cuda_fail(ctx, le, "adjoint launch during capture");
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
+        ctx->adj_graphs[key] = exec;
+    } else {
+        exec = itg->second;
+    }
+    CK(cudaGraphLaunch(exec, ctx->stream));
+    ctx->launches += per_step;
+    return ARMANDO_OK;
+}
+
+armando_status check_adjoint_support(armando_ctx* ctx) {
+    if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
+    const armando_params& p = ctx->prm;
+    if (p.pa_sph != 1 || p.visc || p.heat_artificial)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
+                    "reverse mode supports pa_sph = 1 without physical viscosity and artificial heat");
+    return ARMANDO_OK;
+}
+
 // Per-instance device parameters (the time step of each instance included).
 armando_status upload_batch_params(armando_ctx* ctx) {
     std::vector<DevParams> hp(ctx->n_inst);
@@ -1026,6 +1162,7 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
                                  int32_t its0, int32_t steps) {
     armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
     if (st != ARMANDO_OK) return st;
+    ctx->adj_ready = false;
     if (ctx->n_inst > 1) {
         std::vector<float> dts(ctx->n_inst, dt);
         return armando_batch_integrate(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt,
@@ -1184,6 +1321,146 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float*
 #undef CKT
     cleanup();
     return check_flags(ctx);
+}
+
+armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* vx,
+                                           const float* mass, float* rho, float* p, float* u,
+                                           const float* hsml, const int32_t* itype, float* dvdt,
+                                           float* dudt, float dt, int32_t its0, int32_t steps,
+                                           int32_t checkpoint_every) {
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
+    if (st != ARMANDO_OK) return st;
+    if ((st = check_adjoint_support(ctx)) != ARMANDO_OK) return st;
+    if (steps < 1 || checkpoint_every < 1)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps and checkpoint_every must be >= 1");
+    CK(cudaSetDevice(ctx->device));
+    ctx->adj_ready = false;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if ((st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)) != ARMANDO_OK) return st;
+    if ((st = plan_grid(ctx)) != ARMANDO_OK) return st;
+    if ((st = alloc_adjoint(ctx)) != ARMANDO_OK) return st;
+    const int K = checkpoint_every;
+    const int nck = (steps + K - 1) / K;
+    while ((int)ctx->ckpts.size() < nck) {
+        StateA a{};
+        if ((st = alloc_stateA(ctx, a)) != ARMANDO_OK) return st;
+        ctx->ckpts.push_back(a);
+    }
+    const int nseg = std::min(K, steps);
+    while ((int)ctx->seg.size() < nseg) {
+        StateA a{};
+        if ((st = alloc_stateA(ctx, a)) != ARMANDO_OK) return st;
+        ctx->seg.push_back(a);
+    }
+    for (int k = 0; k < steps; ++k) {
+        if (k % K == 0 && (st = copy_stateA(ctx, ctx->ckpts[k / K], ctx->A)) != ARMANDO_OK) return st;
+        if ((st = run_step(ctx, make_args(ctx, dt, its0 + k))) != ARMANDO_OK) return st;
+    }
+    ctx->last_dt = dt;
+    ctx->next_its = its0 + steps;
+    ctx->adj_its0 = its0;
+    ctx->adj_steps = steps;
+    ctx->adj_K = K;
+    ctx->adj_dt = dt;
+    if ((st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt)) != ARMANDO_OK) return st;
+    if ((st = check_flags(ctx)) != ARMANDO_OK) return st;
+    ctx->adj_ready = true;
+    return ARMANDO_OK;
+}
+
+armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const float* v_bar,
+                                const float* u_bar, const float* p_bar, const float* dvdt_bar,
+                                const float* dudt_bar, float* x0_bar, float* v0_bar,
+                                float* u0_bar, float* dvdt0_bar, float* dudt0_bar,
+                                armando_param_grads* grads) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!ctx->adj_ready)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "call armando_forward_checkpointed first");
+    CK(cudaSetDevice(ctx->device));
+    armando_status st = ARMANDO_OK;
+    const int nn = (int)ctx->n;
+    const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
+    cudaStream_t sm = ctx->stream;
+    const bool host = ctx->mem_kind == ARMANDO_MEM_HOST;
+    // Output cotangents into the slot order of the final state (A after the forward).
+    const float* in[6] = {x_bar, v_bar, u_bar, p_bar, dvdt_bar, dudt_bar};
+    const size_t len[6] = {nd, nd, n, n, nd, n};
+    float* stage[6] = {ctx->s_x, ctx->s_v, ctx->s_u, ctx->s_p, ctx->s_dvdt, ctx->s_dudt};
+    const float* dev_in[6];
+    for (int k = 0; k < 6; ++k) {
+        dev_in[k] = in[k];
+        if (host && in[k]) {
+            CK(cudaMemcpyAsync(stage[k], in[k], len[k] * 4, cudaMemcpyHostToDevice, sm));
+            dev_in[k] = stage[k];
+        }
+    }
+    if (!host) CK(cudaDeviceSynchronize());
+    if (ctx->dim == 2)
+        k_adj_load<2><<<blocks_for(nn, 256), 256, 0, sm>>>(ctx->A.id, dev_in[0], dev_in[1], dev_in[2],
+                                                         dev_in[4], dev_in[5], dev_in[3], ctx->adjG,
+                                                         ctx->adj_pbar, nn);
+    else
+        k_adj_load<3><<<blocks_for(nn, 256), 256, 0, sm>>>(ctx->A.id, dev_in[0], dev_in[1], dev_in[2],
+                                                         dev_in[4], dev_in[5], dev_in[3], ctx->adjG,
+                                                         ctx->adj_pbar, nn);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(ctx->adj_pacc, 0, sizeof(double) * ADJ_NPARAM, sm));
+    const int K = ctx->adj_K, its0 = ctx->adj_its0, steps = ctx->adj_steps;
+    const float dt = ctx->adj_dt;
+    const int nck = (steps + K - 1) / K;
+    bool first = true;
+    for (int c = nck - 1; c >= 0; --c) {
+        const int a0 = c * K, len = std::min(K, steps - a0);
+        // Replay the segment, keeping the state before each iteration.
+        if ((st = copy_stateA(ctx, ctx->A, ctx->ckpts[c])) != ARMANDO_OK) return st;
+        for (int t = 0; t < len; ++t) {
+            if ((st = copy_stateA(ctx, ctx->seg[t], ctx->A)) != ARMANDO_OK) return st;
+            if (t + 1 < len && (st = run_step(ctx, make_args(ctx, dt, its0 + a0 + t))) != ARMANDO_OK)
+                return st;
+        }
+        for (int t = len - 1; t >= 0; --t) {
+            const StepArgs S = make_args(ctx, dt, its0 + a0 + t);
+            if ((st = copy_stateA(ctx, ctx->A, ctx->seg[t])) != ARMANDO_OK) return st;
+            if ((st = run_step(ctx, S)) != ARMANDO_OK) return st;  // intermediates of this iteration
+            if ((st = run_adjoint(ctx, S)) != ARMANDO_OK) return st;
+            if (first) {  // the pressure cotangent belongs to the last iteration only
+                CK(cudaMemsetAsync(ctx->adj_pbar, 0, n * 4, sm));
+                first = false;
+            }
+        }
+    }
+    // adjG is now in the slot order of the first input state = caller order.
+    const bool want[5] = {x0_bar != nullptr, v0_bar != nullptr, u0_bar != nullptr,
+                          dvdt0_bar != nullptr, dudt0_bar != nullptr};
+    float* dst[5] = {x0_bar, v0_bar, u0_bar, dvdt0_bar, dudt0_bar};
+    float* dstage[5] = {ctx->s_x, ctx->s_v, ctx->s_u, ctx->s_dvdt, ctx->s_dudt};
+    float* kout[5];
+    for (int k = 0; k < 5; ++k) kout[k] = want[k] ? (host ? dstage[k] : dst[k]) : nullptr;
+    if (ctx->dim == 2)
+        k_adj_store<2><<<blocks_for(nn, 256), 256, 0, sm>>>(ctx->adjG, nn, kout[0], kout[1], kout[2],
+                                                          kout[3], kout[4]);
+    else
+        k_adj_store<3><<<blocks_for(nn, 256), 256, 0, sm>>>(ctx->adjG, nn, kout[0], kout[1], kout[2],
+                                                          kout[3], kout[4]);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    const size_t olen[5] = {nd, nd, n, nd, n};
+    if (host)
+        for (int k = 0; k < 5; ++k)
+            if (want[k]) CK(cudaMemcpyAsync(dst[k], dstage[k], olen[k] * 4, cudaMemcpyDeviceToHost, sm));
+    double acc[ADJ_NPARAM];
+    CK(cudaMemcpyAsync(acc, ctx->adj_pacc, sizeof(acc), cudaMemcpyDeviceToHost, sm));
+    if ((st = check_flags(ctx)) != ARMANDO_OK) return st;
+    if (grads) {
+        grads->av_alpha = acc[ADJ_ALPHA];
+        grads->av_beta = acc[ADJ_BETA];
+        grads->c0 = acc[ADJ_C0];
+        grads->heat_q0 = acc[ADJ_Q0];
+    }
+    // The forward's final state is gone from A; a further backward needs a new forward.
+    ctx->adj_ready = false;
+    return ARMANDO_OK;
 }
 
 armando_status armando_get_stream(armando_ctx* ctx, void** stream) {

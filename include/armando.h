@@ -188,6 +188,43 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x,
                                   const float* hsml, int64_t* offs,
                                   int32_t* nbr, int64_t cap, int64_t* total);
 
+/* Gradients of a loss with respect to the parameters of the step. */
+typedef struct armando_param_grads {
+    double av_alpha;  /* art_visc alpha */
+    double av_beta;   /* art_visc beta  */
+    double c0;        /* Tait / art_visc sound speed */
+    double heat_q0;   /* external heat source amplitude */
+} armando_param_grads;
+
+/*
+ * Reverse mode, step 1: armando_integrate over `steps` iterations its0.., also
+ * keeping the state before every checkpoint_every-th iteration on the device
+ * for armando_backward. Outputs the final state like armando_integrate.
+ * Supports pa_sph = 1 without physical viscosity and without artificial heat
+ * (ARMANDO_ERR_UNSUPPORTED otherwise); one particle system (no batch).
+ */
+armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* vx,
+                                           const float* mass, float* rho, float* p, float* u,
+                                           const float* hsml, const int32_t* itype,
+                                           float* dvdt, float* dudt, float dt, int32_t its0,
+                                           int32_t steps, int32_t checkpoint_every);
+
+/*
+ * Reverse mode, step 2: the hand-written adjoint of the leapfrog steps of the
+ * last armando_forward_checkpointed, by recomputation from the checkpoints in
+ * reverse. In (caller order, NULL = zero): cotangents of the final x, vx, u, of
+ * the pressure p returned by the last iteration, and of the final dvdt, dudt.
+ * Out (caller order, NULL = not wanted): cotangents of the initial x, vx, u,
+ * dvdt, dudt, and in *grads those of alpha, beta, c0, q0. The neighbour
+ * topology of each iteration is that iteration's (frozen within it).
+ */
+armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const float* v_bar,
+                                const float* u_bar, const float* p_bar,
+                                const float* dvdt_bar, const float* dudt_bar,
+                                float* x0_bar, float* v0_bar, float* u0_bar,
+                                float* dvdt0_bar, float* dudt0_bar,
+                                armando_param_grads* grads);
+
 /* The CUDA stream (cudaStream_t) every call of the context is ordered on, so
  * a caller can bracket calls with its own CUDA events. */
 armando_status armando_get_stream(armando_ctx* ctx, void** stream);

@@ -25,6 +25,23 @@ REF_LIB_PATH = os.path.join(_HERE, "_ref", "libacpu.so")
 _lib = None
 
 
+class LossSpec(C.Structure):
+    """L = w_ke sum m|v|^2/2 + w_p sum w(x) p / w_ref + w_u sum w(x) u / w_ref on the
+    final state (p: pressure output of the last iteration), w(x) = (1 - |x - c|^2/R^2)^3
+    inside radius R, fluid particles only."""
+
+    _fields_ = [("w_ke", C.c_double), ("w_p", C.c_double), ("w_u", C.c_double),
+                ("c", C.c_double * 3), ("radius", C.c_double), ("w_ref", C.c_double)]
+
+    @classmethod
+    def make(cls, w_ke=1.0, w_p=0.0, w_u=0.0, c=(0, 0, 0), radius=1.0, w_ref=1.0):
+        l = cls()
+        l.w_ke, l.w_p, l.w_u, l.radius, l.w_ref = w_ke, w_p, w_u, radius, w_ref
+        for d in range(3):
+            l.c[d] = c[d] if d < len(c) else 0.0
+        return l
+
+
 def build(force: bool = False) -> str:
     """Compiles liboracle.so with the committed Makefile."""
     if force or not os.path.exists(LIB_PATH):
@@ -58,6 +75,12 @@ def lib() -> C.CDLL:
         L.ao_integrate_gather_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_int, C.c_double,
                                               vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.ao_integrate_gather_f64.restype = C.c_int
+        L.ao_loss_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_int, C.c_double] + \
+            [vp] * 10 + [C.POINTER(LossSpec)]
+        L.ao_loss_f64.restype = C.c_double
+        L.ao_tangent_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_int, C.c_double] + \
+            [vp] * 10 + [C.POINTER(LossSpec), vp, vp, vp, vp, vp]
+        L.ao_tangent_f64.restype = C.c_int
         L.ao_hardware_threads.argtypes = []
         L.ao_hardware_threads.restype = C.c_int
         _lib = L
@@ -188,3 +211,30 @@ def integrate_gather(state: State, its0: int, steps: int, dt: float, nthreads: i
 
 def hardware_threads() -> int:
     return lib().ao_hardware_threads()
+
+
+def _state_args(state):
+    return [_p(state.x), _p(state.v), _p(state.m), _p(state.rho), _p(state.p), _p(state.u),
+            _p(state.h), _p(state.itype), _p(state.dvdt), _p(state.dudt)]
+
+
+def loss(state: State, its0: int, steps: int, dt: float, spec: LossSpec, params=None) -> float:
+    """FP64 loss after `steps` iterations (state is not modified)."""
+    prm = params if params is not None else state.params
+    return lib().ao_loss_f64(C.byref(prm), state.n, its0, steps, dt, *_state_args(state),
+                             C.byref(spec))
+
+
+def tangent(state: State, its0: int, steps: int, dt: float, spec: LossSpec, dparam=None,
+            dx0=None, dv0=None, du0=None, params=None):
+    """FP64 tangent-linear (L, dL) along the seed (dparam = d alpha, d beta, d c0, d q0)."""
+    prm = params if params is not None else state.params
+    out = np.zeros(2)
+    dp = None if dparam is None else np.ascontiguousarray(dparam, np.float64)
+    keep = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (dx0, dv0, du0)]
+    rc = lib().ao_tangent_f64(C.byref(prm), state.n, its0, steps, dt, *_state_args(state),
+                              C.byref(spec), None if dp is None else _p(dp),
+                              *[None if a is None else _p(a) for a in keep], _p(out))
+    if rc:
+        raise RuntimeError("oracle tangent failed")
+    return float(out[0]), float(out[1])

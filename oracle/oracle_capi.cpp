@@ -7,6 +7,7 @@
 #include "../include/armando.h"
 #include "armando_oracle.hpp"
 #include "armando_oracle_gather.hpp"
+#include "armando_oracle_tangent.hpp"
 
 namespace {
 
@@ -235,6 +236,82 @@ int ao_integrate_gather_f64(const armando_params* prm, int64_t n, int its0, int 
         return 1;
     }
     store_state(s, x, v, rho, p, u, dvdt, dudt);
+    return 0;
+}
+
+// Loss specification shared with the Python wrapper (see armando_oracle_tangent.hpp).
+struct ao_loss_c {
+    double w_ke, w_p, w_u, c[3], radius, w_ref;
+};
+
+static ao::LossSpec to_loss(const ao_loss_c* l) {
+    ao::LossSpec L;
+    L.w_ke = l->w_ke;
+    L.w_p = l->w_p;
+    L.w_u = l->w_u;
+    for (int d = 0; d < 3; ++d) L.c[d] = l->c[d];
+    L.radius = l->radius;
+    L.w_ref = l->w_ref;
+    return L;
+}
+
+// FP64 loss after `steps` iterations its0.. (pair-loop oracle). NaN on error.
+double ao_loss_f64(const armando_params* prm, int64_t n, int its0, int steps, double dt,
+                   const double* x, const double* v, const double* m, const double* rho,
+                   const double* p, const double* u, const double* h, const int* itype,
+                   const double* dvdt, const double* dudt, const ao_loss_c* l) {
+    ao::Params<double> P = to_params<double>(prm);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
+    try {
+        return ao::run_loss<double>(s, P, its0, steps, dt, to_loss(l));
+    } catch (const std::exception&) {
+        return NAN;
+    }
+}
+
+// FP64 tangent-linear: out[0] = L, out[1] = dL along the seed (dparam[4] =
+// d alpha, d beta, d c0, d q0; dx0, dv0 [n*dim] and du0 [n], each nullable).
+int ao_tangent_f64(const armando_params* prm, int64_t n, int its0, int steps, double dt,
+                   const double* x, const double* v, const double* m, const double* rho,
+                   const double* p, const double* u, const double* h, const int* itype,
+                   const double* dvdt, const double* dudt, const ao_loss_c* l,
+                   const double* dparam, const double* dx0, const double* dv0,
+                   const double* du0, double* out) {
+    using ao::Dual;
+    ao::Params<Dual> P = to_params<Dual>(prm);
+    if (dparam) {
+        P.av_alpha.d = dparam[0];
+        P.av_beta.d = dparam[1];
+        P.c0.d = dparam[2];
+        P.heat_q0.d = dparam[3];
+    }
+    const int dim = P.dim;
+    ao::State<Dual> s;
+    s.n = n;
+    s.dim = dim;
+    auto lift = [](const double* a, int64_t k, const double* da) {
+        std::vector<Dual> r(k);
+        for (int64_t i = 0; i < k; ++i) r[i] = Dual(a[i], da ? da[i] : 0.0);
+        return r;
+    };
+    s.x = lift(x, n * dim, dx0);
+    s.v = lift(v, n * dim, dv0);
+    s.m = lift(m, n, nullptr);
+    s.rho = lift(rho, n, nullptr);
+    s.p = lift(p, n, nullptr);
+    s.u = lift(u, n, du0);
+    s.h = lift(h, n, nullptr);
+    s.c.assign(n, Dual(0.0));
+    s.itype.assign(itype, itype + n);
+    s.dvdt = dvdt ? lift(dvdt, n * dim, nullptr) : std::vector<Dual>(n * dim, Dual(0.0));
+    s.dudt = dudt ? lift(dudt, n, nullptr) : std::vector<Dual>(n, Dual(0.0));
+    try {
+        Dual L = ao::run_loss<Dual>(s, P, its0, steps, dt, to_loss(l));
+        out[0] = L.v;
+        out[1] = L.d;
+    } catch (const std::exception&) {
+        return 1;
+    }
     return 0;
 }
 

@@ -1,0 +1,205 @@
+"""Hand-written adjoint of the GPU step (armando_forward_checkpointed +
+armando_backward) against the FP64 tangent-linear of the oracle (dual numbers
+through the restated CERNsource step), on gradients of a loss
+(final kinetic energy + probe pressure + probe internal energy) with respect to
+alpha, beta, c0, q0 and directions of the initial x, v, u.
+
+Tolerances (relative, per gradient; the FP64 tangent-linear agrees with FP64
+central differences to ~1e-7, tests/test_oracle_tangent.py):
+  1 iteration    TOL_ONE  = 1e-5  (the adjoint itself; measured <= 8e-7)
+  5 iterations   TOL_GRAD = 1e-4
+  20 iterations  no better than the problem allows: at most the change of the
+                 FP64 gradient itself when the FP32 inputs move by one ulp (the
+                 dam break amplifies position errors through c0^2 in the EOS).
+"""
+import numpy as np
+import pytest
+
+import armando_gb300 as ag
+from armando_gb300 import cases
+from helpers import loss_and_cotangents
+
+pytestmark = pytest.mark.gpu
+
+TOL_ONE = 1e-5
+TOL_GRAD = 1e-4
+STEPS = 5
+LONG = 20
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from armando_gb300 import build
+
+    build.build_library()
+    ag.load_library()
+
+
+def adjoint_case():
+    c = cases.perturbed(cases.dam_break(dx=0.05), seed=71, dv=0.1)
+    c.params.av_beta = 0.3
+    c.params.heat_external = 1
+    c.params.heat_q0 = 1.0e6
+    c.params.heat_sigma = 0.3
+    c.params.set("heat_center", (0.5, 1.0, 0.0))
+    return c
+
+
+def spec_for(O):
+    return O.LossSpec.make(w_ke=1.0, w_p=1e-4, w_u=0.1, c=(0.9, 0.3), radius=0.4, w_ref=1.0)
+
+
+def gpu_gradients(c, spec, K, steps=STEPS):
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.forward_checkpointed(got, c.dt, 1, steps, K)
+        L, cot = loss_and_cotangents(got.arrays(), c.dim, c.mass, c.itype, spec)
+        g = ctx.backward(**cot)
+    return L, g
+
+
+@pytest.fixture(scope="module")
+def grads(O):
+    c = adjoint_case()
+    return c, gpu_gradients(c, spec_for(O), K=2)
+
+
+SEEDS = {"x": 1, "v": 2, "u": 3}
+
+
+def _direction(c, which):
+    rng = np.random.default_rng(SEEDS[which])
+    fl = c.itype > 0
+    if which == "u":
+        return rng.standard_normal(c.n) * fl
+    return rng.standard_normal(c.n * c.dim) * np.repeat(fl, c.dim)
+
+
+def _seed_kw(which, d):
+    return {"dx0": d} if which == "x" else {"dv0": d} if which == "v" else {"du0": d}
+
+
+def _tangent_all(O, c, steps):
+    """FP64 tangent-linear derivatives of every checked quantity."""
+    spec = spec_for(O)
+    out = {}
+    for k, name in enumerate(["av_alpha", "av_beta", "c0", "heat_q0"]):
+        dp = [0.0] * 4
+        dp[k] = 1.0
+        out[name] = O.tangent(O.State(c), 1, steps, c.dt, spec, dparam=dp)[1]
+    for which in ("x", "v", "u"):
+        out[which] = O.tangent(O.State(c), 1, steps, c.dt, spec,
+                               **_seed_kw(which, _direction(c, which)))[1]
+    return out
+
+
+def _gpu_all(c, g):
+    out = dict(g["params"])
+    for which in ("x", "v", "u"):
+        out[which] = float(np.dot(g[which].astype(np.float64), _direction(c, which)))
+    return out
+
+
+def test_one_iteration_adjoint_is_exact(O):
+    c = adjoint_case()
+    _, g = gpu_gradients(c, spec_for(O), K=1, steps=1)
+    got, ref = _gpu_all(c, g), _tangent_all(O, c, 1)
+    for k in ref:
+        assert abs(got[k] - ref[k]) <= TOL_ONE * abs(ref[k]), (k, got[k], ref[k])
+
+
+def test_long_horizon_gradients_within_conditioning(O):
+    """20 iterations: GPU gradient error vs the FP64 tangent-linear is no larger
+    than the FP64 gradient's own change under a one-ulp change of the inputs."""
+    c = adjoint_case()
+    _, g = gpu_gradients(c, spec_for(O), K=7, steps=LONG)
+    got, ref = _gpu_all(c, g), _tangent_all(O, c, LONG)
+    rng = np.random.default_rng(9)
+    c2 = c.copy()
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    c2.x = np.where(np.repeat(c.itype > 0, c.dim), np.nextafter(c.x, bump), c.x).astype(np.float32)
+    ref2 = _tangent_all(O, c2, LONG)
+    for k in ref:
+        err = abs(got[k] - ref[k]) / abs(ref[k])
+        cond = abs(ref2[k] - ref[k]) / abs(ref[k])
+        print(k, f"gpu {err:.1e} ulp-conditioning {cond:.1e}")
+        assert err <= max(TOL_GRAD, cond), (k, err, cond)
+
+
+def _rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-30)
+
+
+@pytest.mark.parametrize("k,name", [(0, "av_alpha"), (1, "av_beta"), (2, "c0"), (3, "heat_q0")])
+def test_parameter_gradients_match_tangent_linear(O, grads, k, name):
+    c, (L, g) = grads
+    dp = [0.0, 0.0, 0.0, 0.0]
+    dp[k] = 1.0
+    L64, dL = O.tangent(O.State(c), 1, STEPS, c.dt, spec_for(O), dparam=dp)
+    assert _rel(L, L64) < 1e-5
+    e = _rel(g["params"][name], dL)
+    print(name, g["params"][name], dL, f"{e:.2e}")
+    assert e <= TOL_GRAD, (name, g["params"][name], dL)
+
+
+@pytest.mark.parametrize("which", ["x", "v", "u"])
+def test_initial_state_directional_gradients(O, grads, which):
+    c, (L, g) = grads
+    d = _direction(c, which)
+    _, dL = O.tangent(O.State(c), 1, STEPS, c.dt, spec_for(O), **_seed_kw(which, d))
+    got = float(np.dot(g[which].astype(np.float64), d))
+    e = _rel(got, dL)
+    print(which, got, dL, f"{e:.2e}")
+    assert e <= TOL_GRAD, (which, got, dL)
+
+
+def test_checkpoint_interval_does_not_change_gradients(O):
+    c = adjoint_case()
+    spec = spec_for(O)
+    _, g1 = gpu_gradients(c, spec, K=1, steps=LONG)
+    _, g2 = gpu_gradients(c, spec, K=LONG, steps=LONG)
+    for f in ("x", "v", "u", "dvdt", "dudt"):
+        assert np.array_equal(g1[f], g2[f]), f
+    assert g1["params"] == g2["params"]
+
+
+def test_torch_autograd_wrapper(O):
+    """torch.autograd.Function over the C-ABI forward/backward (test driver only)."""
+    torch = pytest.importorskip("torch")
+    c = adjoint_case()
+    spec = spec_for(O)
+
+    class SPHRun(torch.autograd.Function):
+        @staticmethod
+        def forward(fctx, v0, alpha):
+            case = c.copy()
+            case.v = v0.detach().numpy().astype(np.float32).copy()
+            case.params.av_alpha = float(alpha)
+            sph = ag.Context(case.params, case.n_fluid, case.n_wall)
+            sph.forward_checkpointed(case, case.dt, 1, STEPS, 2)
+            fctx.sph = sph
+            return (torch.from_numpy(case.x.copy()), torch.from_numpy(case.v.copy()),
+                    torch.from_numpy(case.u.copy()), torch.from_numpy(case.p.copy()))
+
+        @staticmethod
+        def backward(fctx, xb, vb, ub, pb):
+            g = fctx.sph.backward(x_bar=xb.numpy(), v_bar=vb.numpy(), u_bar=ub.numpy(),
+                                  p_bar=pb.numpy())
+            fctx.sph.close()
+            return torch.from_numpy(g["v"]), torch.tensor(g["params"]["av_alpha"])
+
+    v0 = torch.from_numpy(c.v.copy()).requires_grad_(True)
+    alpha = torch.tensor(float(c.params.av_alpha), dtype=torch.float64, requires_grad=True)
+    x, v, u, p = SPHRun.apply(v0, alpha)
+    fl = torch.from_numpy(c.itype > 0)
+    m = torch.from_numpy(c.mass).double()
+    X = x.double().reshape(-1, 2)
+    e = X - torch.tensor(spec.c[:2], dtype=torch.float64)
+    t = 1.0 - (e * e).sum(1) / spec.radius ** 2
+    w = torch.where((t > 0) & fl, t ** 3, torch.zeros_like(t))
+    L = (spec.w_ke * 0.5 * (m[fl, None] * v.double().reshape(-1, 2)[fl] ** 2).sum()
+         + spec.w_p * (w * p.double()).sum() + spec.w_u * (w * u.double()).sum())
+    L.backward()
+    _, ref = gpu_gradients(c, spec, K=2)
+    assert np.array_equal(v0.grad.numpy(), ref["v"])
+    assert alpha.grad.item() == pytest.approx(ref["params"]["av_alpha"], rel=1e-6)
