@@ -196,8 +196,7 @@ def channel(n_x: int = 504, n_yz: int = 126, length: float = 0.4, width: float =
     T = 600 K + N(0, 1 K). Default 504 x 126 x 126 = 8.0 M fluid particles."""
     rng = np.random.default_rng(seed)
     dx = length / n_x
-    assert abs(width / dx - n_yz) < 1e-6 * n_yz or True
-    dyz = width / n_yz
+    dyz = width / n_yz  # 0.4 / 504 vs 0.1 / 126: near-cubic cells
     h = 1.3 * dx
     rho0, c0, cp = 10500.0, 20.0, 146.0
     ix = np.arange(n_x)
@@ -241,6 +240,16 @@ def perturbed(case: Case, seed: int, dv: float = 0.0, du: float = 0.0) -> Case:
         c.v = _f32(vv.ravel())
     if du:
         c.u[fl] += (rng.standard_normal(int(fl.sum())) * du).astype(np.float32)
+    return c
+
+
+def adjoint_dam_break(n_target: int = 250_000, seed: int = 5, v_std: float = 0.01) -> Case:
+    """Reverse-mode workload: the 2D dam break above (same geometry and physics)
+    with about `n_target` fluid particles (dx = sqrt(2 m^2 / n_target), 2.83 mm
+    for 250k) and seeded initial fluid velocities N(0, v_std)."""
+    dx = math.sqrt(2.0 / n_target)
+    c = perturbed(dam_break(dx=dx, seed=seed), seed + 100, dv=v_std)
+    c.name = "dambreak2d_adjoint"
     return c
 
 

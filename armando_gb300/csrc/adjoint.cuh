@@ -30,6 +30,55 @@ struct AdjState {
 
 enum AdjParam { ADJ_ALPHA = 0, ADJ_BETA = 1, ADJ_C0 = 2, ADJ_Q0 = 3, ADJ_NPARAM = 4 };
 
+// What the reverse of one iteration reads, saved when the iteration runs
+// forward: the cell-order working set, the neighbour structure (sorted keys,
+// cell table, grid, the cell slot -> input slot permutation) and the energy
+// rate the iteration output. About 116 B per particle in 2D.
+struct TapeSlot {
+    float4* xh;
+    float4* vm;
+    float4* vmin;
+    float4* rp;
+    float* p;
+    int* itype;
+    uint4* nmask;  // 2D only
+    unsigned* keys;
+    int* perm;
+    float* du;
+    int* start;
+    DevGrid* grid;
+};
+
+template <int DIM>
+__global__ void k_tape_save(StateB B, const unsigned* __restrict__ keys,
+                            const int* __restrict__ perm, const float4* __restrict__ ap,
+                            TapeSlot T, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    T.xh[s] = B.xh[s];
+    T.vm[s] = B.vm[s];
+    T.vmin[s] = B.vmin[s];
+    T.rp[s] = B.rp[s];
+    T.p[s] = B.p[s];
+    T.itype[s] = B.itype[s];
+    if (DIM == 2) T.nmask[s] = B.nmask[s];
+    T.keys[s] = keys[s];
+    T.perm[s] = perm[s];
+    T.du[s] = ap[s].w;
+}
+
+// The working set of a taped iteration as the pass kernels see it.
+inline StateB tape_view(StateB B, const TapeSlot& T) {
+    B.xh = T.xh;
+    B.vm = T.vm;
+    B.vmin = T.vmin;
+    B.rp = T.rp;
+    B.p = T.p;
+    B.itype = T.itype;
+    B.nmask = T.nmask;
+    return B;
+}
+
 // Caller-order cotangents -> slot order of the final state (A.id).
 template <int DIM>
 __global__ void k_adj_load(const int* __restrict__ id, const float* __restrict__ xbar,
@@ -74,8 +123,9 @@ __global__ void k_adj_store(AdjState G, int n, float* __restrict__ xbar, float* 
 
 // Corrector reverse: x' = x + dt v', v' = v + kdt a, u' = max(0, u + kdt du),
 // outputs also carry a and du to the next predictor.
-__global__ void k_adj_out(StateB B, StateA A, AdjState G, StepArgs S, float4* __restrict__ abar,
-                          float4* __restrict__ xpart, float4* __restrict__ vpart, int n) {
+__global__ void k_adj_out(StateB B, const float* __restrict__ du_out, AdjState G, StepArgs S,
+                          float4* __restrict__ abar, float4* __restrict__ xpart,
+                          float4* __restrict__ vpart, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -88,7 +138,7 @@ __global__ void k_adj_out(StateB B, StateA A, AdjState G, StepArgs S, float4* __
     const float4 xb = G.xb[s], vb = G.vb[s], ab = G.ab[s];
     const float4 vt = make_float4(fmaf(S.dt, xb.x, vb.x), fmaf(S.dt, xb.y, vb.y),
                                   fmaf(S.dt, xb.z, vb.z), 0.f);
-    const float du = A.ap[s].w;
+    const float du = du_out[s];
     const bool clamped = fmaf(S.kdt, du, B.vmin[s].w) < 0.f;
     const float ub = clamped ? 0.f : vb.w;
     abar[s] = make_float4(fmaf(S.kdt, vt.x, ab.x), fmaf(S.kdt, vt.y, ab.y), fmaf(S.kdt, vt.z, ab.z),

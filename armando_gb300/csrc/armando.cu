@@ -112,13 +112,13 @@ struct armando_ctx {
     cudaGraphExec_t batch_graph = nullptr;
     // Reverse mode (armando_forward_checkpointed / armando_backward).
     std::vector<StateA> ckpts;           // state before iterations its0 + k*K
-    std::vector<StateA> seg;             // states of one segment during the reverse sweep
+    std::vector<TapeSlot> tape;          // intermediates of each iteration of one segment
+    int tape_seg = -1;                   // the segment the tape holds (-1: none)
     AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
     float4 *adj_abar = nullptr, *adj_xpart = nullptr, *adj_vpart = nullptr, *adj_xF = nullptr,
            *adj_vhb = nullptr;
     float *adj_rhobar = nullptr, *adj_pbar = nullptr, *adj_blk = nullptr;
     double* adj_pacc = nullptr;
-    std::map<GraphKey, cudaGraphExec_t> adj_graphs;
     int adj_its0 = 0, adj_steps = 0, adj_K = 0;
     float adj_dt = 0.f;
     bool adj_ready = false;
@@ -225,8 +225,6 @@ StepArgs make_args(const armando_ctx* c, float dt, int its) {
 void free_graphs(armando_ctx* c) {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
-    for (auto& kv : c->adj_graphs) cudaGraphExecDestroy(kv.second);
-    c->adj_graphs.clear();
     if (c->batch_graph) cudaGraphExecDestroy(c->batch_graph);
     c->batch_graph = nullptr;
 }
@@ -747,54 +745,79 @@ armando_status alloc_adjoint(armando_ctx* ctx) {
     return ARMANDO_OK;
 }
 
-// Adjoint kernels of the step just recomputed (B holds its intermediates, A
-// its outputs): cotangents adjG (output order) -> adjGp (input order); then
-// adjG <- adjGp.
-template <int DIM>
-int launch_adjoint(armando_ctx* ctx, const StepArgs& S) {
-    cudaStream_t st = ctx->stream;
+armando_status alloc_tape(armando_ctx* ctx, int count) {
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    while ((int)ctx->tape.size() < count) {
+        TapeSlot T{};
+        T.xh = dalloc<float4>(n, e);
+        T.vm = dalloc<float4>(n, e);
+        T.vmin = dalloc<float4>(n, e);
+        T.rp = dalloc<float4>(n, e);
+        T.p = dalloc<float>(n, e);
+        T.itype = dalloc<int>(n, e);
+        T.nmask = dalloc<uint4>(ctx->dim == 2 ? n : 1, e);
+        T.keys = dalloc<unsigned>(n, e);
+        T.perm = dalloc<int>(n, e);
+        T.du = dalloc<float>(n, e);
+        T.start = dalloc<int>((size_t)ctx->cell_cap + 1, e);
+        T.grid = dalloc<DevGrid>(1, e);
+        for (void* p : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
+                        (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm, (void*)T.du,
+                        (void*)T.start, (void*)T.grid})
+            ctx->owned.push_back(p);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaMalloc(adjoint tape; a smaller checkpoint_every needs less)");
+        ctx->tape.push_back(T);
+    }
+    return ARMANDO_OK;
+}
+
+// Saves the intermediates of the iteration that just ran into tape slot t.
+armando_status save_tape(armando_ctx* ctx, int t) {
+    const TapeSlot& T = ctx->tape[t];
     const int n = (int)ctx->n;
+    cudaStream_t st = ctx->stream;
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
+    if (ctx->dim == 2)
+        k_tape_save<2><<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, skeys, perm, ctx->A.ap, T, n);
+    else
+        k_tape_save<3><<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, skeys, perm, ctx->A.ap, T, n);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(T.start, ctx->start, ((size_t)ctx->cell_cap + 1) * sizeof(int),
+                       cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(T.grid, ctx->grid, sizeof(DevGrid), cudaMemcpyDeviceToDevice, st));
+    return ARMANDO_OK;
+}
+
+// Reverse of the iteration held in tape slot t: cotangents adjG (its output
+// slot order) -> adjGp (its input slot order); then the two swap roles.
+template <int DIM>
+int launch_adjoint(armando_ctx* ctx, const StepArgs& S, const TapeSlot& T) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
     const int nb = blocks_for(n, kPassThreads);
-    k_adj_out<<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, ctx->A, ctx->adjG, S, ctx->adj_abar,
+    const StateB Bv = tape_view(ctx->B, T);
+    k_adj_out<<<blocks_for(n, 256), 256, 0, st>>>(Bv, T.du, ctx->adjG, S, ctx->adj_abar,
                                                   ctx->adj_xpart, ctx->adj_vpart, n);
-    k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, S,
+    k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
                                                  ctx->adj_abar, ctx->adj_pbar, ctx->adj_rhobar,
                                                  ctx->adj_xF, ctx->adj_vhb, ctx->adj_blk, n);
-    k_adj_density<DIM><<<nb, kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start, ctx->grid, ctx->dp,
-                                                   S, ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb,
-                                                   ctx->adj_xpart, ctx->adj_vpart, perm,
+    k_adj_density<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
+                                                   ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb,
+                                                   ctx->adj_xpart, ctx->adj_vpart, T.perm,
                                                    ctx->adjGp, n);
     k_adj_params<<<1, 256, 0, st>>>(ctx->adj_blk, nb, ctx->adj_pacc);
-    cudaMemcpyAsync(ctx->adjG.xb, ctx->adjGp.xb, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(ctx->adjG.vb, ctx->adjGp.vb, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(ctx->adjG.ab, ctx->adjGp.ab, (size_t)n * 16, cudaMemcpyDeviceToDevice, st);
     return 4;
 }
 
-armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S) {
-    GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
-    auto itg = ctx->adj_graphs.find(key);
-    cudaGraphExec_t exec = nullptr;
-    int per_step = 4;
-    if (itg == ctx->adj_graphs.end()) {
-        cudaGraph_t graph = nullptr;
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        per_step = ctx->dim == 2 ? launch_adjoint<2>(ctx, S) : launch_adjoint<3>(ctx, S);
-        cudaError_t le = cudaGetLastError();
-        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-        if (le != cudaSuccess) return cuda_fail(ctx, le, "adjoint launch during capture");
-        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
-        cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
-        ctx->adj_graphs[key] = exec;
-    } else {
-        exec = itg->second;
-    }
-    CK(cudaGraphLaunch(exec, ctx->stream));
-    ctx->launches += per_step;
+armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
+    const TapeSlot& T = ctx->tape[t];
+    ctx->launches += ctx->dim == 2 ? launch_adjoint<2>(ctx, S, T) : launch_adjoint<3>(ctx, S, T);
+    CK(cudaGetLastError());
+    std::swap(ctx->adjG, ctx->adjGp);
     return ARMANDO_OK;
 }
 
@@ -1346,16 +1369,17 @@ armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* v
         if ((st = alloc_stateA(ctx, a)) != ARMANDO_OK) return st;
         ctx->ckpts.push_back(a);
     }
-    const int nseg = std::min(K, steps);
-    while ((int)ctx->seg.size() < nseg) {
-        StateA a{};
-        if ((st = alloc_stateA(ctx, a)) != ARMANDO_OK) return st;
-        ctx->seg.push_back(a);
-    }
+    if ((st = alloc_tape(ctx, std::min(K, steps))) != ARMANDO_OK) return st;
+    // The last segment is taped as it runs: the backward sweep starts there
+    // without a replay.
+    const int last = (nck - 1) * K;
+    ctx->tape_seg = -1;
     for (int k = 0; k < steps; ++k) {
         if (k % K == 0 && (st = copy_stateA(ctx, ctx->ckpts[k / K], ctx->A)) != ARMANDO_OK) return st;
         if ((st = run_step(ctx, make_args(ctx, dt, its0 + k))) != ARMANDO_OK) return st;
+        if (k >= last && (st = save_tape(ctx, k - last)) != ARMANDO_OK) return st;
     }
+    ctx->tape_seg = nck - 1;
     ctx->last_dt = dt;
     ctx->next_its = its0 + steps;
     ctx->adj_its0 = its0;
@@ -1412,18 +1436,18 @@ armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const floa
     bool first = true;
     for (int c = nck - 1; c >= 0; --c) {
         const int a0 = c * K, len = std::min(K, steps - a0);
-        // Replay the segment, keeping the state before each iteration.
-        if ((st = copy_stateA(ctx, ctx->A, ctx->ckpts[c])) != ARMANDO_OK) return st;
-        for (int t = 0; t < len; ++t) {
-            if ((st = copy_stateA(ctx, ctx->seg[t], ctx->A)) != ARMANDO_OK) return st;
-            if (t + 1 < len && (st = run_step(ctx, make_args(ctx, dt, its0 + a0 + t))) != ARMANDO_OK)
-                return st;
+        if (ctx->tape_seg != c) {  // replay the segment from its checkpoint, taping it
+            ctx->tape_seg = -1;
+            if ((st = copy_stateA(ctx, ctx->A, ctx->ckpts[c])) != ARMANDO_OK) return st;
+            for (int t = 0; t < len; ++t) {
+                if ((st = run_step(ctx, make_args(ctx, dt, its0 + a0 + t))) != ARMANDO_OK) return st;
+                if ((st = save_tape(ctx, t)) != ARMANDO_OK) return st;
+            }
+            ctx->tape_seg = c;
         }
         for (int t = len - 1; t >= 0; --t) {
             const StepArgs S = make_args(ctx, dt, its0 + a0 + t);
-            if ((st = copy_stateA(ctx, ctx->A, ctx->seg[t])) != ARMANDO_OK) return st;
-            if ((st = run_step(ctx, S)) != ARMANDO_OK) return st;  // intermediates of this iteration
-            if ((st = run_adjoint(ctx, S)) != ARMANDO_OK) return st;
+            if ((st = run_adjoint(ctx, S, t)) != ARMANDO_OK) return st;
             if (first) {  // the pressure cotangent belongs to the last iteration only
                 CK(cudaMemsetAsync(ctx->adj_pbar, 0, n * 4, sm));
                 first = false;
@@ -1460,6 +1484,7 @@ armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const floa
     }
     // The forward's final state is gone from A; a further backward needs a new forward.
     ctx->adj_ready = false;
+    ctx->tape_seg = -1;
     return ARMANDO_OK;
 }
 

@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--checkpoint-every", type=int, default=50)
+    ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint"],
+                    help="run one extra workload alone and print its JSON")
     ap.add_argument("--config", default="dambreak2d", choices=["dambreak2d", "channel3d"])
     ap.add_argument("--dx", type=float, default=None,
                     help="particle spacing override (smaller workloads for profiling)")
@@ -287,6 +291,73 @@ def run_sweep(args):
             "speedup_vs_plain": batch_rate / plain_rate}
 
 
+def probe_cotangents(x, v, m, p, fl, dim, c, radius, w_ref):
+    """Cotangents of L = sum_fluid m|v|^2/2 + sum_fluid w(x) p / w_ref on the final
+    state, w(x) = (1 - |x - c|^2 / R^2)^3 inside R: (x_bar, v_bar, p_bar)."""
+    xx = x.reshape(-1, dim).astype(np.float64)
+    e = xx - np.asarray(c[:dim])
+    t = 1.0 - (e * e).sum(1) / radius ** 2
+    inside = (t > 0) & fl
+    w = np.where(inside, t ** 3, 0.0)
+    dw = np.where(inside, 3.0 * t ** 2, 0.0)[:, None] * (-2.0 * e / radius ** 2)
+    x_bar = (dw * (p.astype(np.float64) / w_ref)[:, None]).ravel()
+    v_bar = (v.reshape(-1, dim) * np.where(fl, m, 0.0)[:, None]).ravel()
+    return x_bar.astype(np.float32), v_bar.astype(np.float32), (w / w_ref).astype(np.float32)
+
+
+def run_adjoint(args):
+    """Reverse mode on a 250k-particle dam break: forward with a checkpoint every
+    K iterations, then the backward sweep, against the plain forward."""
+    import torch
+
+    import armando_gb300 as ag
+    from armando_gb300 import cases
+
+    c = cases.adjoint_dam_break()
+    steps, K = args.adjoint_steps, args.checkpoint_every
+    fl = c.itype > 0
+    centre, radius = (1.0, 0.05, 0.0), 0.05
+    xx = c.x.reshape(-1, 2)
+    t = 1.0 - ((xx - np.asarray(centre[:2])) ** 2).sum(1) / radius ** 2
+    w_ref = float(np.where((t > 0) & fl, t ** 3, 0.0).sum())
+    with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_HOST) as ctx:
+        warm = c.copy()
+        ctx.integrate(warm, c.dt, 1, 3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.integrate(c.copy(), c.dt, 1, steps)
+        t_plain = time.perf_counter() - t0
+        # Warm the checkpointed path (graphs of the adjoint) on a short run.
+        s = c.copy()
+        ctx.forward_checkpointed(s, c.dt, 1, 2 * K if steps > 2 * K else steps, K)
+        ctx.backward(v_bar=np.zeros_like(s.v))
+        s = c.copy()
+        t0 = time.perf_counter()
+        ctx.forward_checkpointed(s, c.dt, 1, steps, K)
+        t_fwd = time.perf_counter() - t0
+        xb, vb, pb = probe_cotangents(s.x, s.v, s.mass, s.p, fl, 2, centre, radius, w_ref)
+        l0 = ctx.stats().gpu_launches
+        t0 = time.perf_counter()
+        g = ctx.backward(x_bar=xb, v_bar=vb, p_bar=pb)
+        t_bwd = time.perf_counter() - t0
+        launches = ctx.stats().gpu_launches - l0
+    ms_plain = 1e3 * t_plain / steps
+    return {"workload": f"dambreak2d adjoint: {c.n_fluid} fluid + {c.n_wall} wall particles "
+                        f"(dx {c.meta['dx'] * 1e3:.2f} mm), initial v ~ N(0, 0.01 m/s) seed 5, "
+                        f"loss = final kinetic energy + mean p on a 5 cm probe at the column's "
+                        f"right face",
+            "particles": c.n, "steps": steps, "checkpoint_every": K,
+            "forward_plain_ms_per_step": ms_plain,
+            "forward_checkpointed_ms_per_step": 1e3 * t_fwd / steps,
+            "backward_ms_per_step": 1e3 * t_bwd / steps,
+            "backward_over_forward": t_bwd / t_plain,
+            "forward_plus_backward_over_forward": (t_fwd + t_bwd) / t_plain,
+            "gpu_launches_backward": int(launches),
+            "grads": {"av_alpha": g["params"]["av_alpha"], "c0": g["params"]["c0"],
+                      "v0_norm": float(np.linalg.norm(g["v"]))},
+            "timing": "host wall clock around each synchronous call (pinned-free host arrays)"}
+
+
 def config_dict(case, args):
     return {"workload": f"{case.name}: {case.n_fluid} fluid + {case.n_wall} wall particles, "
                         f"dim {case.dim}, dx {case.meta.get('dx'):.4g} m, dt {case.dt:.4g} s",
@@ -408,7 +479,8 @@ def run_ours(args, rank, world, local_rank):
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(make_case(args.config, args.dx), args.cpu_seconds)
     if not args.no_extras and rank == 0 and world == 1:
-        out["workloads"] = {"channel3d": run_channel(args), "sweep": run_sweep(args)}
+        out["workloads"] = {"channel3d": run_channel(args), "sweep": run_sweep(args),
+                            "adjoint": run_adjoint(args)}
     return out
 
 
@@ -417,6 +489,14 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.only is not None and args.impl == "ours":
+        import torch
+
+        torch.cuda.set_device(local_rank)
+        run = {"channel3d": run_channel, "sweep": run_sweep, "adjoint": run_adjoint}[args.only]
+        if rank == 0:
+            print(json.dumps({"workload_only": args.only, **run(args)}), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference(args, rank)
         if line is not None:
