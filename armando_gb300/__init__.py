@@ -16,7 +16,7 @@ import ctypes as C
 import numpy as np
 
 from ._abi import (ERR_UNSUPPORTED, EXPORTED, LIB_PATH, MEM_DEVICE, MEM_HOST, OK,  # noqa: F401
-                   STATUS_NAMES, ParamGrads, Params, Stats, load_library)
+                   N_TUNINGS, STATUS_NAMES, ParamGrads, Params, Stats, Tuning, load_library)
 
 __all__ = ["Context", "Batch", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
            "MEM_DEVICE", "LIB_PATH", "EXPORTED"]
@@ -199,6 +199,41 @@ class Context:
         out = (C.c_float * N_PHASES)()
         self._check(self._lib.armando_profile_phases(self._h, int(steps), out))
         return {PHASE_NAMES[k]: float(out[k]) for k in range(N_PHASES)}
+
+    # -- tuning ----------------------------------------------------------------
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self._check(self._lib.armando_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def set_tuning(self, reach: int = 1, threads_per_particle: int = 1, block: int = 128):
+        t = Tuning.make(reach, threads_per_particle, block)
+        self._check(self._lib.armando_set_tuning(self._h, C.byref(t)))
+
+    @staticmethod
+    def tuning_candidates() -> list:
+        lib = load_library()
+        out = []
+        for k in range(N_TUNINGS):
+            t = Tuning()
+            if lib.armando_tuning_candidate(k, C.byref(t)) != OK:
+                raise ArmandoError(1, "armando_tuning_candidate failed")
+            out.append(t.as_tuple())
+        return out
+
+    def autotune(self, s, dt: float, its0: int, steps_per_trial: int = 5):
+        """Times every candidate tuning on state `s` (not modified), keeps the
+        fastest; returns (best (reach, tpp, block), {candidate: ms per step})."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        best = Tuning()
+        ms = (C.c_float * N_TUNINGS)()
+        self._check(self._lib.armando_autotune(
+            self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+            _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
+            float(dt), int(its0), int(steps_per_trial), C.byref(best), ms))
+        cands = self.tuning_candidates()
+        return best.as_tuple(), {cands[k]: float(ms[k]) for k in range(N_TUNINGS)}
 
     def sync(self):
         self._check(self._lib.armando_sync(self._h))

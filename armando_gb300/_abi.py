@@ -115,6 +115,21 @@ class ParamGrads(C.Structure):
                 ("heat_q0", C.c_double)]
 
 
+class Tuning(C.Structure):
+    """``armando_tuning``: neighbour-grid reach (cells per support radius),
+    threads per particle and threads per CTA of the pair passes."""
+
+    _fields_ = [("reach", C.c_int32), ("threads_per_particle", C.c_int32), ("block", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    @classmethod
+    def make(cls, reach=1, threads_per_particle=1, block=128):
+        return cls(reach, threads_per_particle, block, 0)
+
+    def as_tuple(self):
+        return (self.reach, self.threads_per_particle, self.block)
+
+
 class Stats(C.Structure):
     """``armando_stats``."""
 
@@ -140,7 +155,9 @@ EXPORTED = [
     "armando_get_stream", "armando_profile_phases", "armando_cell_ids_noalloc",
     "armando_batch_create", "armando_batch_integrate",
     "armando_forward_checkpointed", "armando_backward",
+    "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
 ]
+N_TUNINGS = 18
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
 
@@ -199,6 +216,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_forward_checkpointed.restype = C.c_int
     lib.armando_backward.argtypes = [vp] * 12 + [C.POINTER(ParamGrads)]
     lib.armando_backward.restype = C.c_int
+    lib.armando_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    lib.armando_get_tuning.restype = C.c_int
+    lib.armando_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    lib.armando_set_tuning.restype = C.c_int
+    lib.armando_tuning_candidate.argtypes = [C.c_int32, C.POINTER(Tuning)]
+    lib.armando_tuning_candidate.restype = C.c_int
+    lib.armando_autotune.argtypes = [vp] * 11 + [C.c_float, C.c_int32, C.c_int32,
+                                                 C.POINTER(Tuning), C.POINTER(C.c_float)]
+    lib.armando_autotune.restype = C.c_int
     lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
     lib.armando_cell_ids_noalloc.restype = C.c_int
     del fp, ip

@@ -41,7 +41,7 @@ struct TapeSlot {
     float4* rp;
     float* p;
     int* itype;
-    uint4* nmask;  // 2D only
+    unsigned* nmask;  // mask_words<DIM>() words per slot, word-major
     unsigned* keys;
     int* perm;
     float* du;
@@ -61,14 +61,19 @@ __global__ void k_tape_save(StateB B, const unsigned* __restrict__ keys,
     T.rp[s] = B.rp[s];
     T.p[s] = B.p[s];
     T.itype[s] = B.itype[s];
-    if (DIM == 2) T.nmask[s] = B.nmask[s];
+    if (B.mtpp == 1) {  // chunks of 4 words, chunk-major (the lane is the slot)
+#pragma unroll
+        for (int c = 0; c < mask_words<DIM>() / 4; ++c)
+            reinterpret_cast<uint4*>(T.nmask)[(size_t)c * n + s] =
+                reinterpret_cast<const uint4*>(B.nmask)[(size_t)c * B.mstride + s];
+    }
     T.keys[s] = keys[s];
     T.perm[s] = perm[s];
     T.du[s] = ap[s].w;
 }
 
 // The working set of a taped iteration as the pass kernels see it.
-inline StateB tape_view(StateB B, const TapeSlot& T) {
+inline StateB tape_view(StateB B, const TapeSlot& T, int n) {
     B.xh = T.xh;
     B.vm = T.vm;
     B.vmin = T.vmin;
@@ -76,6 +81,7 @@ inline StateB tape_view(StateB B, const TapeSlot& T) {
     B.p = T.p;
     B.itype = T.itype;
     B.nmask = T.nmask;
+    B.mstride = n;
     return B;
 }
 
@@ -212,24 +218,27 @@ template <int DIM>
 struct NbrStream {
     Cursor cu;
     bool done, from_mask;
-    uint4 mk;
     int wi, rbase;
     unsigned wbits;
+    uint4 ch;
 };
 
 template <int DIM>
-__device__ __forceinline__ void nbr_init(NbrStream<DIM>& ns, const StateB& B, int s, bool work) {
-    ns.cu = {-1, 0, 0};
+__device__ __forceinline__ void nbr_init(NbrStream<DIM>& ns, const StateB& B, const DevGrid& g,
+                                         int s, bool work) {
+    ns.cu = cursor_begin<DIM>(g);
     ns.done = !work;
-    ns.mk = make_uint4(0u, 0u, 0u, 0u);
     ns.from_mask = false;
-    if (DIM == 2 && work) {
-        ns.mk = B.nmask[s];
-        ns.from_mask = !(ns.mk.x == ~0u && ns.mk.y == ~0u && ns.mk.z == ~0u && ns.mk.w == ~0u);
+    ns.wbits = 0u;
+    ns.ch = make_uint4(0u, 0u, 0u, 0u);
+    // masks of several lanes per particle are not in this layout: test instead
+    if (work && B.mtpp == 1) {
+        ns.ch = mask_load_chunk<mask_words<DIM>()>(B.nmask, B.mstride, s, 0);
+        ns.wbits = ns.ch.x;
+        ns.from_mask = !(ns.ch.x == ~0u && ns.ch.y == ~0u);
     }
     ns.wi = 0;
     ns.rbase = 0;
-    ns.wbits = ns.mk.x;
 }
 
 template <int DIM>
@@ -240,9 +249,11 @@ __device__ __forceinline__ int nbr_fill(NbrStream<DIM>& ns, const StateB& B, con
     int nl = 0;
     while (!ns.done && ns.from_mask) {
         if (nl == kListCap) break;
-        while (ns.wbits == 0u && ns.wi < 3) {
+        while (ns.wbits == 0u && ns.wi < mask_words<DIM>() - 1) {
             ++ns.wi;
-            ns.wbits = (ns.wi == 1) ? ns.mk.y : (ns.wi == 2) ? ns.mk.z : ns.mk.w;
+            if (ns.wi % 4 == 0)
+                ns.ch = mask_load_chunk<mask_words<DIM>()>(B.nmask, B.mstride, s, ns.wi / 4);
+            ns.wbits = chunk_word(ns.ch, ns.wi % 4);
         }
         if (ns.wbits == 0u) {
             ns.done = true;
@@ -329,7 +340,7 @@ __global__ void __launch_bounds__(kPassThreads)
     float xb[3] = {0.f, 0.f, 0.f}, vb[3] = {0.f, 0.f, 0.f}, Pb = 0.f, rb = 0.f;
     float pa[ADJ_NPARAM] = {0.f, 0.f, 0.f, 0.f};
     NbrStream<DIM> ns;
-    nbr_init<DIM>(ns, B, s, work);
+    nbr_init<DIM>(ns, B, g, s, work);
     while (__any_sync(0xffffffffu, !ns.done)) {
         const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
         const int ml = __reduce_max_sync(0xffffffffu, nl);
@@ -451,7 +462,7 @@ __global__ void __launch_bounds__(kPassThreads)
     if (work) cc = decode_key<DIM>(keys[s], g);
     float xb[3] = {0.f, 0.f, 0.f};
     NbrStream<DIM> ns;
-    nbr_init<DIM>(ns, B, s, work);
+    nbr_init<DIM>(ns, B, g, s, work);
     while (__any_sync(0xffffffffu, !ns.done)) {
         const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
         const int ml = __reduce_max_sync(0xffffffffu, nl);

@@ -14,6 +14,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/armando.h"
@@ -112,6 +113,7 @@ struct armando_ctx {
     cudaGraphExec_t batch_graph = nullptr;
     // Reverse mode (armando_forward_checkpointed / armando_backward).
     std::vector<StateA> ckpts;           // state before iterations its0 + k*K
+    armando_tuning tune{1, 1, 128, 0};   // neighbour-pass tuning (armando_set_tuning)
     std::vector<TapeSlot> tape;          // intermediates of each iteration of one segment
     int tape_seg = -1;                   // the segment the tape holds (-1: none)
     AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
@@ -173,8 +175,9 @@ armando_status validate_params(const armando_params* p, int dim, std::string& wh
     return ARMANDO_OK;
 }
 
-DevParams make_dev_params(const armando_params& p) {
+DevParams make_dev_params(const armando_params& p, int reach = 1) {
     DevParams d{};
+    d.reach = reach;
     d.dim = p.dim;
     d.pa_sph = p.pa_sph;
     d.visc = p.visc;
@@ -261,6 +264,48 @@ int launch_grid_and_sort(armando_ctx* ctx) {
     return L + 1;
 }
 
+// Calls f(tpp, block, periodic) with the context's tuning and whether any axis
+// is periodic as compile-time constants.
+template <class F>
+void with_tuning(const armando_tuning& t, bool per, F&& f) {
+    using std::integral_constant;
+    auto pick_per = [&](auto tpp, auto bs) {
+        if (per) f(tpp, bs, std::true_type{});
+        else f(tpp, bs, std::false_type{});
+    };
+    auto pick_tpp = [&](auto bs) {
+        if (t.threads_per_particle == 4) pick_per(integral_constant<int, 4>{}, bs);
+        else if (t.threads_per_particle == 2) pick_per(integral_constant<int, 2>{}, bs);
+        else pick_per(integral_constant<int, 1>{}, bs);
+    };
+    if (t.block == 256) pick_tpp(integral_constant<int, 256>{});
+    else pick_tpp(integral_constant<int, 128>{});
+}
+
+bool any_periodic(const DevParams& p) { return p.periodic[0] || p.periodic[1] || p.periodic[2]; }
+
+template <int DIM>
+void launch_density(armando_ctx* ctx, const unsigned* skeys) {
+    const int n = (int)ctx->n;
+    with_tuning(ctx->tune, any_periodic(ctx->dp), [&](auto tpp, auto bs, auto per) {
+        constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
+        constexpr bool PER = decltype(per)::value;
+        k_density<DIM, T, BSZ, PER><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
+    });
+}
+
+template <int DIM>
+void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
+    const int n = (int)ctx->n;
+    with_tuning(ctx->tune, any_periodic(ctx->dp), [&](auto tpp, auto bs, auto per) {
+        constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
+        constexpr bool PER = decltype(per)::value;
+        k_force<DIM, T, BSZ, PER><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+            ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+    });
+}
+
 template <int DIM>
 int launch_step(armando_ctx* ctx, const StepArgs& S) {
     cudaStream_t st = ctx->stream;
@@ -269,16 +314,14 @@ int launch_step(armando_ctx* ctx, const StepArgs& S) {
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
-    k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,
-                                                                         ctx->grid, ctx->dp, n);
+    launch_density<DIM>(ctx, skeys);
     L += 2;
     if (ctx->dp.visc) {
         k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
         ++L;
     }
-    k_force<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-        ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+    launch_force<DIM>(ctx, skeys, S);
     return L + 1;
 }
 
@@ -401,8 +444,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
                                                                    ctx->start);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
     cudaEventRecord(ev[3], st);
-    k_density<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(ctx->B, skeys, ctx->start,
-                                                                         ctx->grid, ctx->dp, n);
+    launch_density<DIM>(ctx, skeys);
     cudaEventRecord(ev[4], st);
     L += 3;
     if (ctx->dp.visc) {
@@ -411,8 +453,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
         ++L;
     }
     cudaEventRecord(ev[5], st);
-    k_force<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-        ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+    launch_force<DIM>(ctx, skeys, S);
     cudaEventRecord(ev[6], st);
     return L + 1;
 }
@@ -489,7 +530,9 @@ armando_status alloc_state(armando_ctx* ctx) {
     F4(ctx->B.tau2);
     F1(ctx->B.tds, n);
     F1(ctx->B.ulo, n);
-    ctx->B.nmask = dalloc<uint4>(n, e);
+    ctx->B.nmask = dalloc<unsigned>(n * (ctx->dim == 2 ? mask_words<2>() : mask_words<3>()), e);
+    ctx->B.mstride = (int)n;
+    ctx->B.mtpp = 1;
     ctx->owned.push_back(ctx->B.nmask);
     ctx->num_tiles = blocks_for(ctx->n, kSortTile);
     for (int k = 0; k < 2; ++k) {
@@ -756,7 +799,7 @@ armando_status alloc_tape(armando_ctx* ctx, int count) {
         T.rp = dalloc<float4>(n, e);
         T.p = dalloc<float>(n, e);
         T.itype = dalloc<int>(n, e);
-        T.nmask = dalloc<uint4>(ctx->dim == 2 ? n : 1, e);
+        T.nmask = dalloc<unsigned>(n * (ctx->dim == 2 ? mask_words<2>() : mask_words<3>()), e);
         T.keys = dalloc<unsigned>(n, e);
         T.perm = dalloc<int>(n, e);
         T.du = dalloc<float>(n, e);
@@ -799,7 +842,7 @@ int launch_adjoint(armando_ctx* ctx, const StepArgs& S, const TapeSlot& T) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n;
     const int nb = blocks_for(n, kPassThreads);
-    const StateB Bv = tape_view(ctx->B, T);
+    const StateB Bv = tape_view(ctx->B, T, n);
     k_adj_out<<<blocks_for(n, 256), 256, 0, st>>>(Bv, T.du, ctx->adjG, S, ctx->adj_abar,
                                                   ctx->adj_xpart, ctx->adj_vpart, n);
     k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
@@ -834,7 +877,7 @@ armando_status check_adjoint_support(armando_ctx* ctx) {
 armando_status upload_batch_params(armando_ctx* ctx) {
     std::vector<DevParams> hp(ctx->n_inst);
     for (int k = 0; k < ctx->n_inst; ++k) {
-        hp[k] = make_dev_params(ctx->prm_inst[k]);
+        hp[k] = make_dev_params(ctx->prm_inst[k], ctx->tune.reach);
         hp[k].dt = ctx->inst_dt[k];
         hp[k].heat_t_end = ctx->prm_inst[k].heat_t_end;
     }
@@ -1081,7 +1124,7 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
     ctx = new armando_ctx();
     ctx->device = dev;
     ctx->prm = params[0];
-    ctx->dp = make_dev_params(params[0]);
+    ctx->dp = make_dev_params(params[0], ctx->tune.reach);
     ctx->dim = dim;
     ctx->n_inst = n_inst;
     for (int k = 0; k < n_inst; ++k) {
@@ -1133,8 +1176,148 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     armando_status vs = validate_params(params, ctx->dim, why);
     if (vs != ARMANDO_OK) return fail(ctx, vs, why);
     ctx->prm = *params;
-    ctx->dp = make_dev_params(*params);
+    ctx->dp = make_dev_params(*params, ctx->tune.reach);
     free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+// ---- tuning and autotuner -------------------------------------------------------
+
+namespace {
+
+void release(armando_ctx* c, void* p) {
+    if (!p) return;
+    auto it = std::find(c->owned.begin(), c->owned.end(), p);
+    if (it != c->owned.end()) c->owned.erase(it);
+    cudaFree(p);
+}
+
+armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
+    if (t.reach < 1 || t.reach > 3) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "reach must be 1, 2 or 3");
+    if (t.threads_per_particle != 1 && t.threads_per_particle != 2 && t.threads_per_particle != 4)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "threads_per_particle must be 1, 2 or 4");
+    if (t.block != 128 && t.block != 256) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "block must be 128 or 256");
+    if (ctx->n_inst > 1 && t.threads_per_particle != 1)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches run one thread per particle");
+    return ARMANDO_OK;
+}
+
+// Applies a checked tuning. A new reach changes the cell count, so the cell
+// table (and the reverse-mode tape, which keeps copies of it) is re-planned on
+// the next iteration; any change ends a pending backward sweep.
+armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
+    const bool regrid = t.reach != ctx->tune.reach;
+    ctx->tune = t;
+    ctx->tune.reserved = 0;
+    ctx->B.mstride = (int)(ctx->n * t.threads_per_particle);
+    ctx->B.mtpp = t.threads_per_particle;
+    ctx->dp.reach = t.reach;
+    if (regrid) {
+        if (ctx->n_inst > 1) {
+            armando_status st = upload_batch_params(ctx);
+            if (st != ARMANDO_OK) return st;
+        }
+        CK(cudaStreamSynchronize(ctx->stream));
+        release(ctx, ctx->start);
+        ctx->start = nullptr;
+        for (const TapeSlot& T : ctx->tape)
+            for (void* q : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
+                            (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm,
+                            (void*)T.du, (void*)T.start, (void*)T.grid})
+                release(ctx, q);
+        ctx->tape.clear();
+    }
+    ctx->tape_seg = -1;
+    ctx->adj_ready = false;
+    ctx->next_its = 0;  // the device state no longer belongs to the last call
+    free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+}  // namespace
+
+armando_status armando_get_tuning(armando_ctx* ctx, armando_tuning* out) {
+    if (!ctx || !out) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    *out = ctx->tune;
+    return ARMANDO_OK;
+}
+
+armando_status armando_set_tuning(armando_ctx* ctx, const armando_tuning* t) {
+    if (!ctx || !t) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    armando_status st = check_tuning(ctx, *t);
+    if (st != ARMANDO_OK) return st;
+    CK(cudaSetDevice(ctx->device));
+    if (t->reach == ctx->tune.reach && t->threads_per_particle == ctx->tune.threads_per_particle &&
+        t->block == ctx->tune.block)
+        return ARMANDO_OK;
+    return apply_tuning(ctx, *t);
+}
+
+armando_status armando_tuning_candidate(int32_t k, armando_tuning* out) {
+    if (!out || k < 0 || k >= ARMANDO_N_TUNINGS)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "candidate index out of range");
+    static const int tpp[3] = {1, 2, 4};
+    out->reach = 1 + k / 6;
+    out->threads_per_particle = tpp[(k / 2) % 3];
+    out->block = (k % 2) ? 256 : 128;
+    out->reserved = 0;
+    return ARMANDO_OK;
+}
+
+armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* vx,
+                                const float* mass, const float* rho, const float* p,
+                                const float* u, const float* hsml, const int32_t* itype,
+                                const float* dvdt, const float* dudt, float dt, int32_t its0,
+                                int32_t steps_per_trial, armando_tuning* best,
+                                float* ms_per_step) {
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
+    if (st != ARMANDO_OK) return st;
+    if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "autotune one particle system at a time");
+    if (steps_per_trial < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps_per_trial must be >= 1");
+    CK(cudaSetDevice(ctx->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    armando_tuning win = ctx->tune;
+    float win_ms = -1.f;
+    for (int k = 0; k < ARMANDO_N_TUNINGS; ++k) {
+        armando_tuning t;
+        armando_tuning_candidate(k, &t);
+        float ms = -1.f;
+        if ((st = apply_tuning(ctx, t)) != ARMANDO_OK) break;
+        CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+        st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+        if (st == ARMANDO_OK) st = plan_grid(ctx);
+        // Two untimed iterations capture the graphs of the first and of the
+        // following iterations; then the timed ones.
+        for (int w = 0; w < 2 && st == ARMANDO_OK; ++w) st = run_step(ctx, make_args(ctx, dt, its0 + w));
+        if (st == ARMANDO_OK) {
+            CK(cudaEventRecord(e0, ctx->stream));
+            for (int q = 0; q < steps_per_trial && st == ARMANDO_OK; ++q)
+                st = run_step(ctx, make_args(ctx, dt, its0 + 2 + q));
+            CK(cudaEventRecord(e1, ctx->stream));
+        }
+        if (st == ARMANDO_OK) st = check_flags(ctx);
+        if (st == ARMANDO_OK) {
+            float el = 0.f;
+            CK(cudaEventElapsedTime(&el, e0, e1));
+            ms = el / (float)steps_per_trial;
+            if (win_ms < 0.f || ms < win_ms) {
+                win_ms = ms;
+                win = t;
+            }
+        } else if (st == ARMANDO_ERR_CUDA) {
+            break;  // a device error ends the search
+        }
+        st = ARMANDO_OK;  // a candidate that does not apply is skipped
+        if (ms_per_step) ms_per_step[k] = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != ARMANDO_OK) return st;
+    if (win_ms < 0.f) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "no candidate tuning runs on this state");
+    if ((st = apply_tuning(ctx, win)) != ARMANDO_OK) return st;
+    if (best) *best = win;
     return ARMANDO_OK;
 }
 
@@ -1244,8 +1427,10 @@ armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* h
     CK(cudaGetLastError());
     armando_status s = plan_grid(ctx);
     if (s != ARMANDO_OK) return s;
+    DevParams dp1 = ctx->dp;  // link_list's own grid, whatever the tuning
+    dp1.reach = 1;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, nn, ctx->dim, ctx->bbox_part);
-    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
+    k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, dp1, ctx->cell_cap, ctx->grid,
                                     ctx->flags);
     if (ctx->dim == 2) k_keys_only<2><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.xh, nn, ctx->grid, dcell);
     else k_keys_only<3><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.xh, nn, ctx->grid, dcell);

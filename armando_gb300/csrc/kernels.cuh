@@ -50,6 +50,8 @@ struct DevGrid {
     int ok;        // 0 when the grid did not fit; passes then do nothing
     int periodic[3];
     int cell_off;  // first cell of this grid in the shared cell table (batches)
+    int reach;     // stencil half-width in cells: cell size 2 max(h) / reach
+    int pad_;
 };
 
 // A unit of work of the persistent passes: slots [s0, s1) of one instance.
@@ -70,6 +72,8 @@ struct DevParams {
     float kg;            // K_dim * 5/8
     float dt;            // time step of this instance (batches)
     float heat_t_end;    // external heat gate its*dt <= heat_t_end
+    int reach;           // neighbour-grid cells per support radius (tuning; 1 = link_list)
+    int pad_;
 };
 
 struct StepArgs {
@@ -103,9 +107,53 @@ struct StateB {  // working set of one step (cell order)
     float4* tau2;  // {xz, yz, -, -}
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
-    uint4* nmask;  // 2D: neighbour bits over the first 128 candidates (all ones: more)
+    // Neighbour bits of each fluid slot over its first 32 * mask_words<DIM>()
+    // candidates (cursor order); words 0 and 1 all ones: more candidates than
+    // bits. With TPP lanes per particle, lane L = s * TPP + sub keeps
+    // mask_words / TPP words of its own candidates, in chunks of up to 4 words
+    // stored chunk-major (mask_word_index), so one vector load per warp reads
+    // a chunk of every lane.
+    unsigned* nmask;
     int* inst;     // instance of each slot (batches; nullptr for one system)
+    int mstride;   // lanes: n * TPP
+    int mtpp;      // the TPP the masks were written with
 };
+
+template <int DIM>
+__host__ __device__ constexpr int mask_words() {
+    return DIM == 2 ? 4 : 16;
+}
+
+// Words per chunk of a lane holding W mask words.
+template <int W>
+__host__ __device__ constexpr int mask_chunk() {
+    return W < 4 ? W : 4;
+}
+
+// Word w of lane L (nl lanes).
+template <int W>
+__device__ __forceinline__ size_t mask_word_index(int w, size_t nl, size_t L) {
+    constexpr int CW = mask_chunk<W>();
+    return ((size_t)(w / CW) * nl + L) * CW + (size_t)(w % CW);
+}
+
+// Chunk c of lane L as up to four words.
+template <int W>
+__device__ __forceinline__ uint4 mask_load_chunk(const unsigned* __restrict__ m, size_t nl,
+                                                 size_t L, int c) {
+    constexpr int CW = mask_chunk<W>();
+    const size_t at = (size_t)c * nl + L;
+    if (CW == 4) return __ldg(reinterpret_cast<const uint4*>(m) + at);
+    if (CW == 2) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(m) + at);
+        return make_uint4(v.x, v.y, 0u, 0u);
+    }
+    return make_uint4(__ldg(m + at), 0u, 0u, 0u);
+}
+
+__device__ __forceinline__ unsigned chunk_word(const uint4& ch, int j) {
+    return j == 0 ? ch.x : j == 1 ? ch.y : j == 2 ? ch.z : ch.w;
+}
 
 template <int DIM>
 __device__ __forceinline__ float mass_of(const float4& xh, const float4& vm) {
@@ -222,11 +270,25 @@ __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ pa
 
 // The link_list grid (CERNsource/link_list.f:39-67) of a bbox mm = {min[3],
 // max[3], max h}, in FP32; periodic axes split their box into >= 3 cells.
+// With P.reach = f > 1 the cells are 2 mh / f wide and the passes search
+// (2f + 1)^dim cells. Those cells are widened by a margin larger than the
+// rounding of a cell index ((x - o) / size: a few ulp of the index, i.e.
+// n * 2^-23 cells), so no pair the exact test accepts is outside the stencil;
+// f = 1 keeps link_list's cell exactly.
 __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevParams& P,
                                                   long long capacity, unsigned& fl) {
     DevGrid g;
     const float mh = mm[6];
-    const float cell = __fmul_rn(2.0f, mh);  // scale_k * mh, scale_k = 2
+    const int f = P.reach > 1 ? P.reach : 1;
+    float cell = __fmul_rn(2.0f, mh);  // scale_k * mh, scale_k = 2
+    if (f > 1) {
+        float span = 0.f;
+        for (int d = 0; d < P.dim; ++d)
+            span = fmaxf(span, P.periodic[d] ? P.period_L[d] : mm[3 + d] - mm[d] + 2.f * mh);
+        const float cf = cell / (float)f;
+        const float nmax = span / fmaxf(cf, FLT_MIN);
+        cell = cf * (1.0f + 0x1p-12f + fminf(nmax, 1.0e7f) * 0x1p-20f);
+    }
     long long ncells = 1;
     for (int d = 0; d < 3; ++d) {
         g.periodic[d] = P.periodic[d];
@@ -239,8 +301,9 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
         if (P.periodic[d]) {
             const float L = P.period_L[d];
             float nf = __fdiv_rn(L, cell);
-            int nn = (nf >= 3.0f && nf < 1.0e9f) ? (int)nf : 3;
-            if (!(nf >= 3.0f)) fl |= FLAG_PERIODIC_SMALL;
+            const float nmin = (float)(2 * f + 1);
+            int nn = (nf >= nmin && nf < 1.0e9f) ? (int)nf : 2 * f + 1;
+            if (!(nf >= nmin)) fl |= FLAG_PERIODIC_SMALL;
             g.o[d] = P.period_lo[d];
             g.size[d] = __fdiv_rn(L, (float)nn);
             g.L[d] = L;
@@ -263,6 +326,8 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
     }
     g.ok = 1;
     g.cell_off = 0;
+    g.reach = f;
+    g.pad_ = 0;
     if (ncells > capacity || (fl & FLAG_GRID_OVERFLOW) || (fl & FLAG_PERIODIC_SMALL)) {
         fl |= (ncells > capacity) ? FLAG_GRID_OVERFLOW : 0u;
         g.ok = 0;
@@ -797,40 +862,6 @@ __device__ __forceinline__ CellCoord decode_key(unsigned key, const DevGrid& g) 
     return cc;
 }
 
-// Calls f(k) for every sorted slot k in the 3^DIM cells around cc (k == self
-// included; callers skip it). Non-periodic x: one contiguous slot range per
-// (y, z) row.
-template <int DIM, class F>
-__device__ __forceinline__ void for_candidates(const DevGrid& g, const int* __restrict__ start,
-                                               const CellCoord& cc, F&& f) {
-    const int zlo = (DIM == 3) ? -1 : 0, zhi = (DIM == 3) ? 1 : 0;
-    for (int dz = zlo; dz <= zhi; ++dz) {
-        int cz = cc.c[2] + dz;
-        if (DIM == 3) {
-            if (g.periodic[2]) cz = (cz + g.n[2]) % g.n[2];
-            else if (cz < 0 || cz >= g.n[2]) continue;
-        }
-        for (int dy = -1; dy <= 1; ++dy) {
-            int cy = cc.c[1] + dy;
-            if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
-            else if (cy < 0 || cy >= g.n[1]) continue;
-            const int row = g.cell_off + (cz * g.n[1] + cy) * g.n[0];
-            if (!g.periodic[0]) {
-                const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
-                const int kb = __ldg(start + row + c0), ke = __ldg(start + row + c1 + 1);
-                for (int k = kb; k < ke; ++k) f(k);
-            } else {
-#pragma unroll
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const int cx = (cc.c[0] + dx + g.n[0]) % g.n[0];
-                    const int kb = __ldg(start + row + cx), ke = __ldg(start + row + cx + 1);
-                    for (int k = kb; k < ke; ++k) f(k);
-                }
-            }
-        }
-    }
-}
-
 // Difference x_i - x_j (minimum image) and the exact pair test.
 template <int DIM>
 __device__ __forceinline__ bool pair_delta(const float4& xi, const float4& xj, const DevGrid& g,
@@ -916,53 +947,97 @@ constexpr int kTestBatch = 4;     // candidate loads issued together
 // (W below ~1% of W(0) each) in FP32.
 constexpr float kNearQ = 1.6f;
 
+// Candidate rows: for each (dy, dz) in [-f, f]^(DIM-1) the cells cx-f..cx+f of
+// that row are consecutive keys, so one contiguous slot range. On a periodic x
+// axis the part past either end (at most one side, as n[0] >= 2f + 1) is a
+// second piece. Rows come in (dz, dy, piece) order, the same for every pass.
 struct Cursor {
-    int r, k, ke;
+    int k, ke;  // current slot range [k, ke)
+    int st;     // row state: dy + 8 (bits 0-3), dz + 8 (bits 4-7), piece (bit 8),
+                // piece 0 the in-range cells, 1 the wrapped ones
 };
 
-// Slot range [kb, ke) of candidate row r; false when r is past the last row.
 template <int DIM>
-__device__ __forceinline__ bool candidate_row(const DevGrid& g, const int* __restrict__ start,
-                                              const CellCoord& cc, int r, int& kb, int& ke) {
-    const int px = g.periodic[0];
-    const int R = (DIM == 3 ? 9 : 3) * (px ? 3 : 1);
-    if (r >= R) return false;
-    const int rest = px ? r / 3 : r;
-    int cy = cc.c[1] + rest % 3 - 1;
-    int cz = (DIM == 3) ? cc.c[2] + rest / 3 - 1 : 0;
-    kb = ke = 0;
-    if (DIM == 3) {
-        if (g.periodic[2]) cz = (cz + g.n[2]) % g.n[2];
-        else if (cz < 0 || cz >= g.n[2]) return true;
-    }
-    if (g.periodic[1]) cy = (cy + g.n[1]) % g.n[1];
-    else if (cy < 0 || cy >= g.n[1]) return true;
-    const int row = g.cell_off + (cz * g.n[1] + cy) * g.n[0];
-    if (!px) {
-        const int c0 = max(cc.c[0] - 1, 0), c1 = min(cc.c[0] + 1, g.n[0] - 1);
-        kb = __ldg(start + row + c0);
-        ke = __ldg(start + row + c1 + 1);
-    } else {
-        const int cx = (cc.c[0] + r % 3 - 1 + g.n[0]) % g.n[0];
-        kb = __ldg(start + row + cx);
-        ke = __ldg(start + row + cx + 1);
-    }
-    return true;
+__device__ __forceinline__ Cursor cursor_begin(const DevGrid& g) {
+    Cursor c;
+    c.k = c.ke = 0;
+    const int dy = -g.reach - 1, dz = (DIM == 3) ? -g.reach : 0;
+    c.st = (dy + 8) | ((dz + 8) << 4) | (1 << 8);
+    return c;
 }
 
-// Advances to the next non-empty row; false when the candidates are exhausted.
+// Advances to the next non-empty range; false when the candidates are
+// exhausted (and stays false).
 template <int DIM>
 __device__ __forceinline__ bool cursor_next(const DevGrid& g, const int* __restrict__ start,
                                             const CellCoord& cc, Cursor& cu) {
-    int kb, ke;
-    while (candidate_row<DIM>(g, start, cc, ++cu.r, kb, ke)) {
+    const int f = g.reach;
+    const bool px = g.periodic[0] != 0;
+    int dy = (cu.st & 15) - 8, dz = ((cu.st >> 4) & 15) - 8, pc = cu.st >> 8;
+    bool found = false;
+    for (;;) {
+        if (px && pc == 0) {
+            pc = 1;
+        } else {
+            pc = 0;
+            if (++dy > f) {
+                if (DIM == 2 || dz >= f) {
+                    dy = f + 1;
+                    cu.k = cu.ke = 0;
+                    break;
+                }
+                dy = -f;
+                ++dz;
+            }
+        }
+        int cy = cc.c[1] + dy;
+        if (cy < 0 || cy >= g.n[1]) {
+            if (!g.periodic[1]) continue;
+            cy += (cy < 0) ? g.n[1] : -g.n[1];
+        }
+        int cz = 0;
+        if (DIM == 3) {
+            cz = cc.c[2] + dz;
+            if (cz < 0 || cz >= g.n[2]) {
+                if (!g.periodic[2]) continue;
+                cz += (cz < 0) ? g.n[2] : -g.n[2];
+            }
+        }
+        const int row = g.cell_off + (cz * g.n[1] + cy) * g.n[0];
+        const int cx = cc.c[0];
+        int c0, c1;
+        if (pc == 0) {
+            c0 = max(cx - f, 0);
+            c1 = min(cx + f, g.n[0] - 1);
+        } else if (cx - f < 0) {
+            c0 = cx - f + g.n[0];
+            c1 = g.n[0] - 1;
+        } else if (cx + f >= g.n[0]) {
+            c0 = 0;
+            c1 = cx + f - g.n[0];
+        } else {
+            continue;
+        }
+        const int kb = __ldg(start + row + c0), ke = __ldg(start + row + c1 + 1);
         if (kb < ke) {
             cu.k = kb;
             cu.ke = ke;
-            return true;
+            found = true;
+            break;
         }
     }
-    return false;
+    cu.st = (dy + 8) | ((dz + 8) << 4) | (pc << 8);
+    return found;
+}
+
+// Calls fn(k) for every candidate slot k of the particle in cell cc (its own
+// slot included; callers skip it).
+template <int DIM, class F>
+__device__ __forceinline__ void for_candidates(const DevGrid& g, const int* __restrict__ start,
+                                               const CellCoord& cc, F&& fn) {
+    Cursor cu = cursor_begin<DIM>(g);
+    while (cursor_next<DIM>(g, start, cc, cu))
+        for (int k = cu.k; k < cu.ke; ++k) fn(k);
 }
 
 // Periodic wrap of a drifted coordinate (same branch order as the oracle).
@@ -977,16 +1052,39 @@ __device__ __forceinline__ float fast_sqrt_pos(float x) {
     return x > 0.f ? x * rsqrtf(x) : 0.f;
 }
 
+// Lanes of one particle: TPP consecutive threads split its candidates, lane
+// `sub` taking slots kb + sub, kb + sub + TPP, ... of every candidate range.
+template <int TPP>
+__device__ __forceinline__ unsigned group_mask() {
+    const unsigned lane = threadIdx.x & 31u;
+    return (TPP == 1) ? (1u << lane) : (((1u << TPP) - 1u) << (lane & ~(unsigned)(TPP - 1)));
+}
+
+// Sum over the lanes of one particle (xor butterfly; every lane gets the same
+// value, a + b being commutative).
+template <int TPP>
+__device__ __forceinline__ float group_sum(float v) {
+#pragma unroll
+    for (int o = 1; o < TPP; o <<= 1) v += __shfl_xor_sync(group_mask<TPP>(), v, o);
+    return v;
+}
+
+// The lane's candidates left in the cursor's current range.
+template <int TPP>
+__device__ __forceinline__ int lane_len(const Cursor& cu) {
+    return cu.k < cu.ke ? (cu.ke - cu.k + TPP - 1) / TPP : 0;
+}
+
 // ---------------------------------------------------------------------------
 // Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
-template <int DIM>
+template <int DIM, int TPP = 1, int BS = kPassThreads>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
-                                             int (*s_near)[kPassThreads],
-                                             int (*s_far)[kPassThreads]) {
+                                             int (*s_near)[BS], int (*s_far)[BS]) {
     const int tid = threadIdx.x;
+    const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     const bool need_div = P.heat_art != 0;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
     float p = 0.f;
@@ -1005,16 +1103,21 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     const sph::ff ih_i = sph::ff_recip(xi.w);
     const sph::ff al_i = sph::ff_mul(kw, ff_pow_dim<DIM>(ih_i));
     const float mi = mass_of<DIM>(xi, vi);
-    // Self density m_i W(0, h_i) (density.f:39-42).
+    // Self density m_i W(0, h_i) (density.f:39-42), on the particle's first lane.
     sph::ff S = sph::ff_mul_f(al_i, mi);
+    if (sub != 0) S = sph::ff{0.f, 0.f};
     const float ihf = ih_i.hi;
     const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
     const float kwf = P.kw_hi * (DIM == 2 ? ihf * ihf : ihf * ihf * ihf);
     float divs = 0.f;
-    Cursor cu = {-1, 0, 0};
+    constexpr int W = mask_words<DIM>() / TPP;  // mask words of this lane
+    const size_t mlane = (size_t)s * TPP + sub;
+    Cursor cu = cursor_begin<DIM>(g);
     bool done = !work;
+    const bool mask_on = work && fluid;
     int ord = 0;  // candidate ordinal (cursor order, self included)
-    unsigned long long mlo = 0ull, mhi = 0ull;  // neighbour bits of ordinals 0..127
+    int wb = 0;   // the accumulator holds the bits of ordinals 32 wb .. 32 wb + 63
+    unsigned long long cur = 0ull;
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
         // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
@@ -1024,33 +1127,36 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                     done = true;
                     break;
                 }
+                if (TPP > 1) {
+                    cu.k += sub;
+                    continue;
+                }
             }
             if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
             const int k0 = cu.k;
-            const int cnt = min(kTestBatch, cu.ke - k0);
+            const int cnt = min(kTestBatch, lane_len<TPP>(cu));
             float4 xb[kTestBatch];
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + min(k0 + u, cu.ke - 1));
-            cu.k += cnt;
+            for (int u = 0; u < kTestBatch; ++u)
+                xb[u] = __ldg(B.xh + min(k0 + u * TPP, cu.ke - 1));
+            cu.k += cnt * TPP;
             unsigned pb = 0u;  // pass bits of this batch
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 float d[3], dr2;
-                if (u >= cnt || k0 + u == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
+                const int k = k0 + u * TPP;
+                if (u >= cnt || k == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
                 pb |= 1u << u;
                 const float hs = xi.w + xb[u].w;  // near: q < kNearQ with h = hs/2
-                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k0 + u;
-                else s_far[nf++][tid] = k0 + u;
+                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k;
+                else s_far[nf++][tid] = k;
             }
-            if (DIM == 2 && pb != 0u && ord < 128) {
-                const unsigned long long b = pb;
-                if (ord < 64) {
-                    mlo |= b << ord;
-                    if (ord > 64 - kTestBatch) mhi |= b >> (64 - ord);
-                } else {
-                    mhi |= b << (ord - 64);
-                }
+            if (ord - 32 * wb >= 32) {  // word wb is complete
+                if (mask_on && wb < W) B.nmask[mask_word_index<W>(wb, B.mstride, mlane)] = (unsigned)cur;
+                cur >>= 32;
+                ++wb;
             }
+            cur |= (unsigned long long)pb << (ord - 32 * wb);
             ord += cnt;
         }
         const int mn = __reduce_max_sync(0xffffffffu, nn);
@@ -1113,11 +1219,28 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             }
         }
     }
+    if (TPP > 1) {  // the particle's lanes reach this point together
+        const unsigned gm = group_mask<TPP>();
+#pragma unroll
+        for (int o = 1; o < TPP; o <<= 1) {
+            const sph::ff t = {__shfl_xor_sync(gm, S.hi, o), __shfl_xor_sync(gm, S.lo, o)};
+            sph::ff_acc(S, t);
+        }
+        divs = group_sum<TPP>(divs);
+    }
     if (!valid) return;
-    if (DIM == 2 && fluid && work)
-        B.nmask[s] = (ord <= 128) ? make_uint4((unsigned)mlo, (unsigned)(mlo >> 32),
-                                               (unsigned)mhi, (unsigned)(mhi >> 32))
-                                  : make_uint4(~0u, ~0u, ~0u, ~0u);
+    if (mask_on) {
+        if (ord > 32 * W) {
+            B.nmask[mask_word_index<W>(0, B.mstride, mlane)] = ~0u;
+            if (W > 1) B.nmask[mask_word_index<W>(1, B.mstride, mlane)] = ~0u;
+        } else {
+            for (; wb < W; ++wb) {
+                B.nmask[mask_word_index<W>(wb, B.mstride, mlane)] = (unsigned)cur;
+                cur >>= 32;
+            }
+        }
+    }
+    if (sub != 0) return;
     if (!work) {  // wall without div v (or no grid): fixed rho and p
         rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
         B.rp[s] = rp;
@@ -1208,14 +1331,15 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // ---------------------------------------------------------------------------
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
-template <int DIM>
+template <int DIM, int TPP = 1, int BS = kPassThreads>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
                                            const DevParams& P, const StepArgs& S,
                                            unsigned* __restrict__ flags, const int s,
-                                           const bool valid, int (*s_list)[kPassThreads]) {
+                                           const bool valid, int (*s_list)[BS]) {
     const int tid = threadIdx.x;
+    const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
     int it = 0;
     if (valid) {
@@ -1224,7 +1348,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         vi = B.vm[s];
         rpi = B.rp[s];
     }
-    if (valid && (it <= 0 || !g.ok)) {  // wall: fixed state, zero rates
+    if (valid && (it <= 0 || !g.ok) && sub == 0) {  // wall: fixed state, zero rates
         A.xh[s] = xi;
         A.vm[s] = vi;
         A.u[s] = B.vmin[s].w;
@@ -1247,24 +1371,29 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     const float ulo_i = (work && P.heat_art) ? B.ulo[s] : 0.f;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
-    Cursor cu = {-1, 0, 0};
+    constexpr int W = mask_words<DIM>() / TPP;  // mask words of this lane
+    const size_t mlane = (size_t)s * TPP + sub;
+    Cursor cu = cursor_begin<DIM>(g);
     bool done = !work;
-    // 2D: the density pass left the neighbour bits of the first 128 candidates.
-    uint4 mk = make_uint4(0u, 0u, 0u, 0u);
+    // The density pass left the neighbour bits of the candidates (word-major).
+    constexpr int CW = mask_chunk<W>();
     bool from_mask = false;
-    if (DIM == 2 && work) {
-        mk = B.nmask[s];
-        from_mask = !(mk.x == ~0u && mk.y == ~0u && mk.z == ~0u && mk.w == ~0u);
+    uint4 ch = make_uint4(0u, 0u, 0u, 0u);  // mask chunk being decoded
+    unsigned wbits = 0u;                    // bits left of word wi
+    if (work) {
+        ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, 0);
+        wbits = ch.x;
+        from_mask = !(ch.x == ~0u && (W == 1 || ch.y == ~0u));
     }
-    int wi = 0, rbase = 0;  // mask word being decoded; ordinal of the cursor row's first slot
-    unsigned wbits = mk.x;
+    int wi = 0, rbase = 0;  // index of wbits; ordinal of the cursor row's first slot
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
         while (!done && from_mask) {
             if (nl == kListCap) break;
-            while (wbits == 0u && wi < 3) {
+            while (wbits == 0u && wi < W - 1) {
                 ++wi;
-                wbits = (wi == 1) ? mk.y : (wi == 2) ? mk.z : mk.w;
+                if (W > CW && wi % CW == 0) ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, wi / CW);
+                wbits = chunk_word(ch, wi % CW);
             }
             if (wbits == 0u) {
                 done = true;
@@ -1273,18 +1402,19 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             const int o = 32 * wi + __ffs(wbits) - 1;
             wbits &= wbits - 1u;
             bool in_rows = true;
-            while (o >= rbase + (cu.ke - cu.k)) {  // move to the row holding ordinal o
-                rbase += cu.ke - cu.k;
+            while (o >= rbase + lane_len<TPP>(cu)) {  // move to the range holding ordinal o
+                rbase += lane_len<TPP>(cu);
                 if (!cursor_next<DIM>(g, start, cc, cu)) {
                     in_rows = false;
                     break;
                 }
+                cu.k += sub;
             }
             if (!in_rows) {  // cannot happen for a mask of this step's candidates
                 done = true;
                 break;
             }
-            s_list[nl++][tid] = cu.k + (o - rbase);
+            s_list[nl++][tid] = cu.k + TPP * (o - rbase);
         }
         while (!done && !from_mask) {
             if (cu.k >= cu.ke) {
@@ -1292,19 +1422,24 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     done = true;
                     break;
                 }
+                if (TPP > 1) {
+                    cu.k += sub;
+                    continue;
+                }
             }
             if (nl > kListCap - kTestBatch) break;
             const int k0 = cu.k;
-            const int cnt = min(kTestBatch, cu.ke - k0);
+            const int cnt = min(kTestBatch, lane_len<TPP>(cu));
             float4 xb[kTestBatch];
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + min(k0 + u, cu.ke - 1));
-            cu.k += cnt;
+            for (int u = 0; u < kTestBatch; ++u)
+                xb[u] = __ldg(B.xh + min(k0 + u * TPP, cu.ke - 1));
+            cu.k += cnt * TPP;
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 float d[3], dr2;
-                if (u < cnt && k0 + u != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
-                    s_list[nl++][tid] = k0 + u;
+                const int k = k0 + u * TPP;
+                if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2)) s_list[nl++][tid] = k;
             }
         }
         const int ml = __reduce_max_sync(0xffffffffu, nl);
@@ -1388,7 +1523,15 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             }
         }
     }
-    if (!work) return;
+    if (TPP > 1) {  // the particle's lanes reach this point together
+        a0 = group_sum<TPP>(a0);
+        a1 = group_sum<TPP>(a1);
+        if (DIM == 3) a2 = group_sum<TPP>(a2);
+        he_sum = group_sum<TPP>(he_sum);
+        av_du = group_sum<TPP>(av_du);
+        ah_du = group_sum<TPP>(ah_du);
+    }
+    if (!work || sub != 0) return;
     float du = 0.5f * he_sum + av_du + ah_du;  // internal_force.f:433-435
     if (P.visc) du += B.tds[s];
     if (S.heat_on) {
@@ -1436,15 +1579,25 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
 // ---------------------------------------------------------------------------
 // Pass kernels of one particle system: one CTA per 128 consecutive slots.
 // ---------------------------------------------------------------------------
-template <int DIM>
-__global__ void __launch_bounds__(kPassThreads, 8)
+// The grid of a pass; PER = false (no periodic axis) makes the periodic flags
+// compile-time zeros, so the minimum-image code and its registers drop out.
+template <bool PER>
+__device__ __forceinline__ DevGrid load_grid(const DevGrid* __restrict__ gp) {
+    DevGrid g = *gp;
+    if (!PER) g.periodic[0] = g.periodic[1] = g.periodic[2] = 0;
+    return g;
+}
+
+// One CTA per BS / TPP consecutive slots.
+template <int DIM, int TPP, int BS, bool PER>
+__global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
-    __shared__ int s_near[kListCapD][kPassThreads];
-    __shared__ int s_far[kListCapD][kPassThreads];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const DevGrid g = *gp;
-    density_body<DIM>(B, keys, start, g, P, s, s < n, s_near, s_far);
+    __shared__ int s_near[kListCapD][BS];
+    __shared__ int s_far[kListCapD][BS];
+    const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
+    const DevGrid g = load_grid<PER>(gp);
+    density_body<DIM, TPP, BS>(B, keys, start, g, P, s, s < n, s_near, s_far);
 }
 
 template <int DIM>
@@ -1456,15 +1609,15 @@ __global__ void __launch_bounds__(kPassThreads)
     shear_body<DIM>(B, keys, start, g, P, s, s < n);
 }
 
-template <int DIM>
-__global__ void __launch_bounds__(kPassThreads, 8)
+template <int DIM, int TPP, int BS, bool PER>
+__global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
             int n) {
-    __shared__ int s_list[kListCap][kPassThreads];
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const DevGrid g = *gp;
-    force_body<DIM>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
+    __shared__ int s_list[kListCap][BS];
+    const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
+    const DevGrid g = load_grid<PER>(gp);
+    force_body<DIM, TPP, BS>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
 }
 
 // ---------------------------------------------------------------------------

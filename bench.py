@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip the autotuner (default tuning or --tuning)")
+    ap.add_argument("--tuning", default=None,
+                    help="reach,threads_per_particle,block instead of the autotuner")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--checkpoint-every", type=int, default=50)
     ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint"],
@@ -213,6 +217,22 @@ def run_reference(args, rank):
     return line
 
 
+def tune(ctx, args, arrays, dt):
+    """The tuning the timed region runs with: the autotuner's pick on this
+    workload's own state (untimed, state not modified), or a fixed one."""
+    if args.tuning:
+        r, t, b = (int(v) for v in args.tuning.split(","))
+        ctx.set_tuning(r, t, b)
+        return {"tuning": [r, t, b], "source": "fixed"}
+    if args.no_autotune:
+        return {"tuning": list(ctx.tuning().as_tuple()), "source": "default"}
+    t0 = time.perf_counter()
+    best, table = ctx.autotune(arrays, dt, 1, steps_per_trial=5)
+    return {"tuning": list(best), "source": "autotune",
+            "autotune_s": time.perf_counter() - t0,
+            "ms_per_step": {"%d,%d,%d" % k: round(v, 5) for k, v in table.items()}}
+
+
 def timed_integrate(ctx, arrays, dts, its0, steps, batch=False):
     """CUDA-event time (ms) of `steps` iterations on the context's stream."""
     import torch
@@ -240,6 +260,7 @@ def run_channel(args):
     c = cases.channel()
     dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
     with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+        tuned = tune(ctx, args, dev, c.dt)
         ctx.integrate(dev, c.dt, 1, 3)
         ms = timed_integrate(ctx, dev, c.dt, 4, args.extra_steps)
         phases = ctx.profile_phases(2)
@@ -248,7 +269,8 @@ def run_channel(args):
     return {"workload": f"channel3d: {c.n_fluid} fluid + {c.n_wall} wall particles, periodic x, "
                         f"art. visc + art. heat + Gaussian source",
             "particles": c.n, "steps": args.extra_steps, "ms_per_step": ms / args.extra_steps,
-            "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC, "phases_ms": phases}
+            "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC, "phases_ms": phases,
+            "tuning": tuned}
 
 
 def run_sweep(args):
@@ -321,6 +343,7 @@ def run_adjoint(args):
     t = 1.0 - ((xx - np.asarray(centre[:2])) ** 2).sum(1) / radius ** 2
     w_ref = float(np.where((t > 0) & fl, t ** 3, 0.0).sum())
     with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_HOST) as ctx:
+        tuned = tune(ctx, args, c, c.dt)
         warm = c.copy()
         ctx.integrate(warm, c.dt, 1, 3)
         torch.cuda.synchronize()
@@ -352,7 +375,7 @@ def run_adjoint(args):
             "backward_ms_per_step": 1e3 * t_bwd / steps,
             "backward_over_forward": t_bwd / t_plain,
             "forward_plus_backward_over_forward": (t_fwd + t_bwd) / t_plain,
-            "gpu_launches_backward": int(launches),
+            "gpu_launches_backward": int(launches), "tuning": tuned,
             "grads": {"av_alpha": g["params"]["av_alpha"], "c0": g["params"]["c0"],
                       "v0_norm": float(np.linalg.norm(g["v"]))},
             "timing": "host wall clock around each synchronous call (pinned-free host arrays)"}
@@ -385,6 +408,7 @@ def run_ours(args, rank, world, local_rank):
     dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in case.arrays().items()}
     ctx = ag.Context(case.params, case.n_fluid, case.n_wall, mem=ag.MEM_DEVICE)
     stream = torch.cuda.ExternalStream(ctx.stream_handle())
+    tuned = tune(ctx, args, dev, case.dt)
     # Warm-up: its = 1 .. W (graph capture, grid planning).
     ctx.integrate(dev, case.dt, 1, args.warmup)
     its = 1 + args.warmup
@@ -437,7 +461,7 @@ def run_ours(args, rank, world, local_rank):
             "step_roofline": {"alg_bytes_per_particle": b_step,
                               "achieved_gbs": b_step * case.n / step_s / 1e9,
                               "frac_of_measured_hbm": b_step * case.n / step_s / 1e9 / hbm},
-            "phases_ms": phases, "gpu_launches": int(launches),
+            "phases_ms": phases, "gpu_launches": int(launches), "tuning": tuned,
             "clocks": clk.summary(),
         }
     # e2e: armando_step with pinned host buffers, one call per step.
@@ -450,6 +474,7 @@ def run_ours(args, rank, world, local_rank):
         t.copy_(torch.from_numpy(v))
         pinned[k] = t.numpy()
     hctx = ag.Context(case.params, case.n_fluid, case.n_wall, mem=ag.MEM_HOST)
+    hctx.set_tuning(*tuned["tuning"])
     hs = torch.cuda.ExternalStream(hctx.stream_handle())
     hctx.step(pinned, case.dt, 1)
     barrier()

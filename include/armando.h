@@ -246,6 +246,55 @@ armando_status armando_get_stream(armando_ctx* ctx, void** stream);
 armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms_per_phase);
 
 /*
+ * Tuning of the neighbour passes. No reference counterpart: the reference
+ * fixes its cell at scale_k * max(h) = 2 max(h) (CERNsource/link_list.f:29-35)
+ * and gives each particle one thread (ArmandoThrust/armando.cu:2886-2926).
+ *   reach                the cells of the neighbour grid are 2 max(h) / reach
+ *                        wide and a particle's candidates are the
+ *                        (2 reach + 1)^dim cells around its own; 1 is
+ *                        link_list's grid. 1, 2 or 3.
+ *   threads_per_particle lanes that share one particle's candidates and
+ *                        reduce its sums: 1, 2 or 4 (batches: 1).
+ *   block                threads per CTA of the pair passes, i.e. the tile of
+ *                        consecutive cell-ordered particles whose candidate
+ *                        lists one CTA stages in shared memory: 128 or 256.
+ * The neighbour sets do not depend on the tuning; the sums differ only by
+ * their rounding (summation order). armando_cell_ids always uses reach 1.
+ */
+typedef struct armando_tuning {
+    int32_t reach;
+    int32_t threads_per_particle;
+    int32_t block;
+    int32_t reserved;
+} armando_tuning;
+
+armando_status armando_get_tuning(armando_ctx* ctx, armando_tuning* out);
+/* INVALID_ARG for a value outside the lists above; UNSUPPORTED for
+ * threads_per_particle > 1 on a batch context. */
+armando_status armando_set_tuning(armando_ctx* ctx, const armando_tuning* t);
+
+/* The autotuner's candidate tunings, k = 0 .. ARMANDO_N_TUNINGS - 1. */
+#define ARMANDO_N_TUNINGS 18
+armando_status armando_tuning_candidate(int32_t k, armando_tuning* out);
+
+/*
+ * Autotuner: for every candidate tuning, loads the given state (caller
+ * arrays in the context's memory kind, as for armando_step; none is
+ * modified), runs one untimed iteration its0 and then times steps_per_trial
+ * iterations its0 + 1 .. with CUDA events. Sets the fastest tuning on the
+ * context and writes it to *best (may be NULL); ms_per_step (may be NULL,
+ * else ARMANDO_N_TUNINGS floats) receives each candidate's mean time per
+ * iteration, or a negative value for a candidate that does not apply (e.g.
+ * a periodic box too short for its reach). One particle system only.
+ */
+armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* vx,
+                                const float* mass, const float* rho, const float* p,
+                                const float* u, const float* hsml, const int32_t* itype,
+                                const float* dvdt, const float* dudt, float dt, int32_t its0,
+                                int32_t steps_per_trial, armando_tuning* best,
+                                float* ms_per_step);
+
+/*
  * Allocation-free form of armando_cell_ids. It has no counterpart in the
  * reference.
  * For callers that must not allocate device memory: a host code that hands

@@ -99,3 +99,36 @@ def test_create_without_gpu_reports_status(lib):
     st = lib.armando_create(C.byref(h), C.byref(p), 2, 10, 0, 0)
     assert st == _abi.ERR_NO_DEVICE
     assert b"device" in lib.armando_last_error(None)
+
+
+def test_tuning_candidates_enumerate_every_tuning(lib):
+    got = []
+    for k in range(_abi.N_TUNINGS):
+        t = _abi.Tuning()
+        assert lib.armando_tuning_candidate(k, C.byref(t)) == _abi.OK
+        got.append(t.as_tuple())
+    assert sorted(got) == sorted((r, tp, b) for r in (1, 2, 3) for tp in (1, 2, 4)
+                                 for b in (128, 256))
+    assert got[0] == (1, 1, 128)  # link_list's grid, one thread per particle
+    t = _abi.Tuning()
+    assert lib.armando_tuning_candidate(_abi.N_TUNINGS, C.byref(t)) == _abi.ERR_INVALID_ARG
+    assert lib.armando_tuning_candidate(-1, C.byref(t)) == _abi.ERR_INVALID_ARG
+
+
+def test_tuning_struct_and_count_match_c():
+    code = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "armando.h"
+int main(void) {
+  printf("%zu %zu %d\n", sizeof(armando_tuning), offsetof(armando_tuning, block),
+         ARMANDO_N_TUNINGS);
+  return 0;
+}'''
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(src, "w").write(code)
+        subprocess.run(["gcc", "-I", os.path.join(REPO, "include"), src, "-o", exe], check=True)
+        got = list(map(int, subprocess.run([exe], capture_output=True, text=True).stdout.split()))
+    assert got == [C.sizeof(_abi.Tuning), _abi.Tuning.block.offset, _abi.N_TUNINGS]
