@@ -99,6 +99,70 @@ def peaks():
     return 6800.0, "fallback"
 
 
+_FP32 = {}
+
+
+def fp32_peak():
+    """FP32 roof in TFLOP/s: a cuBLAS fp32 GEMM (TF32 off) 8192^3, best of 5
+    (measured here, like the bf16 figure of the peaks file), and the nominal
+    SMs x 128 lanes x 2 x max SM clock beside it."""
+    if _FP32:
+        return _FP32
+    import torch
+
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+    c = a @ b
+    best = float("inf")
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    torch.backends.cuda.matmul.allow_tf32 = prev
+    del a, b, c
+    torch.cuda.empty_cache()
+    props = torch.cuda.get_device_properties(0)
+    mhz = 2070.0
+    pk = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        mhz = float(json.load(open(pk)).get("sm_max_mhz", mhz))
+    _FP32.update({"measured": 2.0 * n ** 3 / (best * 1e-3) / 1e12,
+                  "nominal": props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12,
+                  "how": "cuBLAS fp32 GEMM 8192^3, TF32 off, best of 5 (CUDA events)"})
+    return _FP32
+
+
+def two_roof(workload, n, ms_per_step, b_alg, hbm):
+    """T_roof = max(B_alg / HBM, F_alg / FP32) for the step, against the
+    measured step time. F_alg: the reference algorithm's FLOPs per particle
+    (profiles/flops.json, counted by the oracle)."""
+    p = os.path.join(REPO, "profiles", "flops.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p)).get(workload)
+    if not d:
+        return None
+    f_alg = float(d["flop_per_particle"])
+    pk = fp32_peak()
+    t_b = b_alg * n / (hbm * 1e9) * 1e3
+    t_f = f_alg * n / (pk["measured"] * 1e12) * 1e3
+    t_roof = max(t_b, t_f)
+    return {"bound": "fp32" if t_f >= t_b else "hbm", "t_roof_ms": t_roof,
+            "t_meas_ms": ms_per_step, "frac": t_roof / ms_per_step,
+            "f_alg_per_particle": f_alg, "b_alg_per_particle": b_alg,
+            "t_fp32_ms": t_f, "t_hbm_ms": t_b,
+            "fp32_tflops": pk["measured"], "fp32_tflops_nominal": pk["nominal"],
+            "fp32_how": pk["how"], "hbm_gbs": hbm,
+            "achieved_tflops_alg": f_alg * n / (ms_per_step * 1e-3) / 1e12}
+
+
 def traffic_per_particle(kernel, config):
     """DRAM bytes per particle of one launch, from the committed ncu summary."""
     p = os.path.join(REPO, "profiles", "traffic.json")
@@ -264,13 +328,16 @@ def run_channel(args):
         ctx.integrate(dev, c.dt, 1, 3)
         ms = timed_integrate(ctx, dev, c.dt, 4, args.extra_steps)
         phases = ctx.profile_phases(2)
+        cells_pp = ctx.stats().n_cells / c.n
     del dev
     torch.cuda.empty_cache()
     return {"workload": f"channel3d: {c.n_fluid} fluid + {c.n_wall} wall particles, periodic x, "
                         f"art. visc + art. heat + Gaussian source",
             "particles": c.n, "steps": args.extra_steps, "ms_per_step": ms / args.extra_steps,
             "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC, "phases_ms": phases,
-            "tuning": tuned}
+            "tuning": tuned,
+            "two_roof": two_roof("channel3d", c.n, ms / args.extra_steps,
+                                 step_bytes(3, cells_pp), peaks()[0])}
 
 
 def run_sweep(args):
@@ -461,6 +528,7 @@ def run_ours(args, rank, world, local_rank):
             "step_roofline": {"alg_bytes_per_particle": b_step,
                               "achieved_gbs": b_step * case.n / step_s / 1e9,
                               "frac_of_measured_hbm": b_step * case.n / step_s / 1e9 / hbm},
+            "two_roof": two_roof(args.config, case.n, ms / args.steps, b_step, hbm),
             "phases_ms": phases, "gpu_launches": int(launches), "tuning": tuned,
             "clocks": clk.summary(),
         }

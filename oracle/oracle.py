@@ -81,6 +81,8 @@ def lib() -> C.CDLL:
         L.ao_tangent_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_int, C.c_double] + \
             [vp] * 10 + [C.POINTER(LossSpec), vp, vp, vp, vp, vp]
         L.ao_tangent_f64.restype = C.c_int
+        L.ao_flops_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double] + [vp] * 11
+        L.ao_flops_f64.restype = C.c_int
         L.ao_hardware_threads.argtypes = []
         L.ao_hardware_threads.restype = C.c_int
         _lib = L
@@ -211,6 +213,16 @@ def integrate_gather(state: State, its0: int, steps: int, dt: float, nthreads: i
 
 def hardware_threads() -> int:
     return lib().ao_hardware_threads()
+
+
+def flops(state: State, its: int, dt: float):
+    """Operation count of iteration `its` of the reference algorithm on this
+    state (not modified): (whole iteration, its link_list neighbour search)."""
+    out = np.zeros(2)
+    rc = lib().ao_flops_f64(C.byref(state.params), state.n, its, dt, *_state_args(state), _p(out))
+    if rc:
+        raise RuntimeError("oracle flop count failed")
+    return float(out[0]), float(out[1])
 
 
 def _state_args(state):

@@ -7,6 +7,7 @@
 #include "../include/armando.h"
 #include "armando_oracle.hpp"
 #include "armando_oracle_gather.hpp"
+#include "armando_oracle_flops.hpp"
 #include "armando_oracle_tangent.hpp"
 
 namespace {
@@ -309,6 +310,50 @@ int ao_tangent_f64(const armando_params* prm, int64_t n, int its0, int steps, do
         Dual L = ao::run_loss<Dual>(s, P, its0, steps, dt, to_loss(l));
         out[0] = L.v;
         out[1] = L.d;
+    } catch (const std::exception&) {
+        return 1;
+    }
+    return 0;
+}
+
+// Operation count of iteration `its` of the reference algorithm on this state
+// (armando_oracle_flops.hpp): out[0] = the whole iteration, out[1] = its
+// neighbour search (link_list) alone. The state is not modified.
+int ao_flops_f64(const armando_params* prm, int64_t n, int its, double dt, const double* x,
+                 const double* v, const double* m, const double* rho, const double* p,
+                 const double* u, const double* h, const int* itype, const double* dvdt,
+                 const double* dudt, double* out) {
+    using ao::Flop;
+    ao::Params<Flop> P = to_params<Flop>(prm);
+    const int dim = P.dim;
+    ao::State<Flop> s;
+    s.n = n;
+    s.dim = dim;
+    auto lift = [](const double* a, int64_t k) {
+        std::vector<Flop> r(k);
+        for (int64_t i = 0; i < k; ++i) r[i] = Flop(a[i]);
+        return r;
+    };
+    s.x = lift(x, n * dim);
+    s.v = lift(v, n * dim);
+    s.m = lift(m, n);
+    s.rho = lift(rho, n);
+    s.p = lift(p, n);
+    s.u = lift(u, n);
+    s.h = lift(h, n);
+    s.c.assign(n, Flop(0.0));
+    s.itype.assign(itype, itype + n);
+    s.dvdt = dvdt ? lift(dvdt, n * dim) : std::vector<Flop>(n * dim, Flop(0.0));
+    s.dudt = dudt ? lift(dudt, n) : std::vector<Flop>(n, Flop(0.0));
+    try {
+        ao::PairList pl;
+        Flop::count = 0;
+        ao::neighbour_search<Flop, Flop>(s, P, pl);
+        const double search = (double)Flop::count;
+        Flop::count = 0;
+        ao::leapfrog_step<Flop, Flop>(s, P, its, dt);
+        out[0] = (double)Flop::count;
+        out[1] = search;
     } catch (const std::exception&) {
         return 1;
     }
