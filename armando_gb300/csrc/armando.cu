@@ -264,14 +264,20 @@ int launch_grid_and_sort(armando_ctx* ctx) {
     return L + 1;
 }
 
-// Calls f(tpp, block, periodic) with the context's tuning and whether any axis
-// is periodic as compile-time constants.
+// Calls f(tpp, block, periodic, lean) with the context's tuning, whether any
+// axis is periodic and whether the physics is lean (no physical viscosity, no
+// artificial heat) as compile-time constants. Lean variants exist for one
+// thread per particle.
 template <class F>
-void with_tuning(const armando_tuning& t, bool per, F&& f) {
+void with_tuning(const armando_tuning& t, bool per, bool lean, F&& f) {
     using std::integral_constant;
+    auto pick_lean = [&](auto tpp, auto bs, auto pr) {
+        if (decltype(tpp)::value == 1 && lean) f(tpp, bs, pr, std::true_type{});
+        else f(tpp, bs, pr, std::false_type{});
+    };
     auto pick_per = [&](auto tpp, auto bs) {
-        if (per) f(tpp, bs, std::true_type{});
-        else f(tpp, bs, std::false_type{});
+        if (per) pick_lean(tpp, bs, std::true_type{});
+        else pick_lean(tpp, bs, std::false_type{});
     };
     auto pick_tpp = [&](auto bs) {
         if (t.threads_per_particle == 4) pick_per(integral_constant<int, 4>{}, bs);
@@ -283,14 +289,16 @@ void with_tuning(const armando_tuning& t, bool per, F&& f) {
 }
 
 bool any_periodic(const DevParams& p) { return p.periodic[0] || p.periodic[1] || p.periodic[2]; }
+bool lean_physics(const DevParams& p) { return !p.visc && !p.heat_art; }
 
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
     const int n = (int)ctx->n;
-    with_tuning(ctx->tune, any_periodic(ctx->dp), [&](auto tpp, auto bs, auto per) {
+    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
+                [&](auto tpp, auto bs, auto per, auto lean) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
-        constexpr bool PER = decltype(per)::value;
-        k_density<DIM, T, BSZ, PER><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
+        k_density<DIM, T, BSZ, PER, LEAN><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
     });
 }
@@ -298,10 +306,11 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
 template <int DIM>
 void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     const int n = (int)ctx->n;
-    with_tuning(ctx->tune, any_periodic(ctx->dp), [&](auto tpp, auto bs, auto per) {
+    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
+                [&](auto tpp, auto bs, auto per, auto lean) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
-        constexpr bool PER = decltype(per)::value;
-        k_force<DIM, T, BSZ, PER><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
+        k_force<DIM, T, BSZ, PER, LEAN><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
     });
 }
@@ -530,6 +539,8 @@ armando_status alloc_state(armando_ctx* ctx) {
     F4(ctx->B.tau2);
     F1(ctx->B.tds, n);
     F1(ctx->B.ulo, n);
+    ctx->B.vr = dalloc<float4>(ctx->dim == 2 ? n : 1, e);
+    ctx->owned.push_back(ctx->B.vr);
     ctx->B.nmask = dalloc<unsigned>(n * (ctx->dim == 2 ? mask_words<2>() : mask_words<3>()), e);
     ctx->B.mstride = (int)n;
     ctx->B.mtpp = 1;

@@ -107,6 +107,7 @@ struct StateB {  // working set of one step (cell order)
     float4* tau2;  // {xz, yz, -, -}
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
+    float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
     // Neighbour bits of each fluid slot over its first 32 * mask_words<DIM>()
     // candidates (cursor order); words 0 and 1 all ones: more candidates than
     // bits. With TPP lanes per particle, lane L = s * TPP + sub keeps
@@ -1078,14 +1079,16 @@ __device__ __forceinline__ int lane_len(const Cursor& cu) {
 // ---------------------------------------------------------------------------
 // Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
-template <int DIM, int TPP = 1, int BS = kPassThreads>
+// LEAN: the parameters have no physical viscosity and no artificial heat, so
+// their operands and branches are compiled out.
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
                                              int (*s_near)[BS], int (*s_far)[BS]) {
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
-    const bool need_div = P.heat_art != 0;
+    const bool need_div = !LEAN && P.heat_art != 0;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
     float p = 0.f;
     bool fluid = false;
@@ -1094,7 +1097,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         rp = B.rp[s];
         p = B.p[s];
         fluid = B.itype[s] > 0;
-        if (DIM == 3 || need_div) vi = B.vm[s];
+        vi = B.vm[s];
     }
     const bool work = valid && g.ok && (fluid || need_div);
     CellCoord cc = {{0, 0, 0}};
@@ -1244,6 +1247,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     if (!work) {  // wall without div v (or no grid): fixed rho and p
         rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
         B.rp[s] = rp;
+        if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
         return;
     }
     float rho = rp.x;
@@ -1264,6 +1268,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         rp.w = P.ah_g1 * xi.w * P.c0 + P.ah_g2 * xi.w * xi.w * (fabsf(divv) - divv);
     }
     B.rp[s] = rp;
+    if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1331,7 +1336,7 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // ---------------------------------------------------------------------------
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
-template <int DIM, int TPP = 1, int BS = kPassThreads>
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
@@ -1365,11 +1370,12 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     const float ihf = __fdividef(1.0f, xi.w);
     const float kgih_i = P.kg * pow_grad<DIM>(ihf);
     float4 ti = make_float4(0.f, 0.f, 0.f, 0.f), ti2 = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (work && P.visc) {
+    const bool visc = !LEAN && P.visc, heat_art = !LEAN && P.heat_art;
+    if (work && visc) {
         ti = B.tau[s];
         if (DIM == 3) ti2 = B.tau2[s];
     }
-    const float ulo_i = (work && P.heat_art) ? B.ulo[s] : 0.f;
+    const float ulo_i = (work && heat_art) ? B.ulo[s] : 0.f;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
     constexpr int W = mask_words<DIM>() / TPP;  // mask words of this lane
     const size_t mlane = (size_t)s * TPP + sub;
@@ -1447,8 +1453,20 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             if (t >= nl) continue;
             const int k = s_list[t][tid];
             const float4 xj = __ldg(B.xh + k);
-            const float4 vj = __ldg(B.vm + k);
-            const float4 rpj = __ldg(B.rp + k);
+            float4 vj, rpj;
+            if (DIM == 2) {  // {vx, vy, rho, P}; u and psi only for art_heat
+                const float4 vr = __ldg(B.vr + k);
+                vj = make_float4(vr.x, vr.y, 0.f, 0.f);
+                rpj = make_float4(vr.z, vr.w, 0.f, 0.f);
+                if (heat_art) {
+                    const float4 r = __ldg(B.rp + k);
+                    rpj.z = r.z;
+                    rpj.w = r.w;
+                }
+            } else {
+                vj = __ldg(B.vm + k);
+                rpj = __ldg(B.rp + k);
+            }
             float d[3], dr2;
             pair_delta<DIM>(xi, xj, g, d, dr2);
             refine_periodic<DIM>(xi, xj, g, d, dr2);
@@ -1468,7 +1486,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             float h0 = fs * w0, h1 = fs * w1, h2 = fs * w2;
             float he = vx * h0 + vy * h1;
             if (DIM == 3) he += vz * h2;
-            if (P.visc) {
+            if (visc) {
                 const float4 tj = __ldg(B.tau + k);
                 float4 tj2 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (DIM == 3) tj2 = __ldg(B.tau2 + k);
@@ -1513,7 +1531,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 }
             }
             // art_heat.f:69-97.
-            if (P.heat_art) {
+            if (heat_art) {
                 float rdw = d[0] * w0 + d[1] * w1;
                 if (DIM == 3) rdw += d[2] * w2;
                 const float psi =
@@ -1533,7 +1551,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     if (!work || sub != 0) return;
     float du = 0.5f * he_sum + av_du + ah_du;  // internal_force.f:433-435
-    if (P.visc) du += B.tds[s];
+    if (visc) du += B.tds[s];
     if (S.heat_on) {
         float e0 = xi.x - P.heat_center[0], e1 = xi.y - P.heat_center[1];
         float dd = e0 * e0 + e1 * e1;
@@ -1589,7 +1607,7 @@ __device__ __forceinline__ DevGrid load_grid(const DevGrid* __restrict__ gp) {
 }
 
 // One CTA per BS / TPP consecutive slots.
-template <int DIM, int TPP, int BS, bool PER>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
@@ -1597,7 +1615,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_far[kListCapD][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    density_body<DIM, TPP, BS>(B, keys, start, g, P, s, s < n, s_near, s_far);
+    density_body<DIM, TPP, BS, LEAN>(B, keys, start, g, P, s, s < n, s_near, s_far);
 }
 
 template <int DIM>
@@ -1609,7 +1627,7 @@ __global__ void __launch_bounds__(kPassThreads)
     shear_body<DIM>(B, keys, start, g, P, s, s < n);
 }
 
-template <int DIM, int TPP, int BS, bool PER>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
@@ -1617,7 +1635,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_list[kListCap][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    force_body<DIM, TPP, BS>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
+    force_body<DIM, TPP, BS, LEAN>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
 }
 
 // ---------------------------------------------------------------------------
