@@ -83,6 +83,7 @@ struct armando_ctx {
           *s_u = nullptr, *s_h = nullptr, *s_dvdt = nullptr, *s_dudt = nullptr;
     int* s_itype = nullptr;
     std::vector<void*> owned;
+    int* inv = nullptr;  // caller index -> cell-order slot (outputs to mapped host memory)
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::string err = "no error";
     int64_t steps_done = 0, launches = 0;
@@ -259,8 +260,9 @@ int launch_grid_and_sort(armando_ctx* ctx) {
             ctx->hist, ctx->dtotal, ctx->num_tiles);
         L += 2;
     }
-    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n,
-                                                                   &ctx->grid->ncells, ctx->start);
+    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n,
+                                                                   &ctx->grid->ncells, (int)ctx->cell_cap,
+                                                                   ctx->start);
     return L + 1;
 }
 
@@ -388,8 +390,8 @@ int launch_batch_step(armando_ctx* ctx, cudaEvent_t* ev) {
     }
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, ctx->d_total_cells,
-                                                                   ctx->start);
+    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(skeys, n, ctx->d_total_cells,
+                                                                   (int)ctx->cell_cap, ctx->start);
     k_reorder_batch<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, ctx->d_params,
                                                              ctx->d_its, n);
     if (ev) cudaEventRecord(ev[3], st);
@@ -449,8 +451,8 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     cudaEventRecord(ev[2], st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for(ctx->cell_cap + 1, 256), 256, 0, st>>>(skeys, n, &ctx->grid->ncells,
-                                                                   ctx->start);
+    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(skeys, n, &ctx->grid->ncells,
+                                                                   (int)ctx->cell_cap, ctx->start);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
     cudaEventRecord(ev[3], st);
     launch_density<DIM>(ctx, skeys);
@@ -656,12 +658,42 @@ armando_status check_flags(armando_ctx* ctx) {
 }
 
 // Caller arrays -> A (caller order, id = index).
+// Device address of a page-locked host array the device maps, or nullptr: for
+// those, the copy kernels read and write the caller's memory across the host
+// link directly instead of staging through copies. Pageable memory (and any
+// pointer the runtime does not know) takes the staged copies.
+template <class T>
+T* mapped_host(T* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<T*>(a.devicePointer);
+}
+
 armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, const float* mass,
                            const float* rho, const float* p, const float* u, const float* hsml,
                            const int32_t* itype, const float* dvdt, const float* dudt) {
     const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
     cudaStream_t st = ctx->stream;
+    const float *mx = nullptr, *mv = nullptr, *mm = nullptr, *mrho = nullptr, *mp = nullptr,
+                *mu = nullptr, *mh = nullptr, *mdv = nullptr, *mdu = nullptr;
+    const int32_t* mit = nullptr;
+    bool zero_copy = false;
     if (ctx->mem_kind == ARMANDO_MEM_HOST) {
+        mx = mapped_host(x), mv = mapped_host(vx), mm = mapped_host(mass);
+        mrho = mapped_host(rho), mp = mapped_host(p), mu = mapped_host(u), mh = mapped_host(hsml);
+        mit = mapped_host(itype), mdv = mapped_host(dvdt), mdu = mapped_host(dudt);
+        zero_copy = mx && mv && mm && mrho && mp && mu && mh && mit && (!dvdt || mdv) &&
+                    (!dudt || mdu);
+    }
+    if (zero_copy) {
+        x = mx, vx = mv, mass = mm, rho = mrho, p = mp, u = mu, hsml = mh, itype = mit;
+        dvdt = mdv, dudt = mdu;
+    } else if (ctx->mem_kind == ARMANDO_MEM_HOST) {
         auto H2D = [&](void* dst, const void* src, size_t bytes) {
             return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
         };
@@ -707,6 +739,30 @@ armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, 
     const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
     cudaStream_t st = ctx->stream;
     const bool host = ctx->mem_kind == ARMANDO_MEM_HOST;
+    const int nn = (int)ctx->n;
+    if (host) {
+        float *mx = mapped_host(x), *mv = mapped_host(vx), *mrho = mapped_host(rho);
+        float *mp = mapped_host(p), *mu = mapped_host(u), *mdv = mapped_host(dvdt);
+        float* mdu = mapped_host(dudt);
+        if (mx && mv && mrho && mp && mu && mdv && mdu) {
+            if (!ctx->inv) {
+                cudaError_t e = cudaSuccess;
+                ctx->inv = dalloc<int>(n, e);
+                if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(inverse ids)");
+                ctx->owned.push_back(ctx->inv);
+            }
+            k_invert_ids<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.id, ctx->inv, nn);
+            if (ctx->dim == 2)
+                k_scatter_out_seq<2><<<blocks_for(nn, kScatterSeq), kScatterSeq, 0, st>>>(
+                    ctx->A, ctx->inv, nn, mx, mv, mrho, mp, mu, mdv, mdu);
+            else
+                k_scatter_out_seq<3><<<blocks_for(nn, kScatterSeq), kScatterSeq, 0, st>>>(
+                    ctx->A, ctx->inv, nn, mx, mv, mrho, mp, mu, mdv, mdu);
+            ctx->launches += 2;
+            CK(cudaGetLastError());
+            return ARMANDO_OK;
+        }
+    }
     float* dx = host ? ctx->s_x : x;
     float* dv = host ? ctx->s_v : vx;
     float* drho = host ? ctx->s_rho : rho;
@@ -714,7 +770,6 @@ armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, 
     float* du = host ? ctx->s_u : u;
     float* ddvdt = host ? ctx->s_dvdt : dvdt;
     float* ddudt = host ? ctx->s_dudt : dudt;
-    const int nn = (int)ctx->n;
     if (ctx->dim == 2)
         k_scatter_out<2><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, nn, dx, dv, drho, dp, du,
                                                               ddvdt, ddudt);

@@ -556,19 +556,36 @@ __global__ void __launch_bounds__(kSortThreads)
 }
 
 // start[c] = first sorted slot of cell c (the number of keys below c), for c in
-// [0, ncells]; empty cells get start[c] == start[c+1]. One thread per cell, a
-// binary search over the sorted keys: no serial fill of long empty runs.
-__global__ void k_cell_start(const unsigned* __restrict__ keys, int n,
-                             const int* __restrict__ ncells_total, int* __restrict__ start) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c > *ncells_total) return;
-    int lo = 0, hi = n;  // first slot with key >= c lies in [lo, hi]
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(keys + mid) < (unsigned)c) lo = mid + 1;
-        else hi = mid;
+// [0, ncells]; empty cells get start[c] == start[c+1]. One thread per slot
+// s in [0, n]: slot s is the first slot of every cell in (key[s-1], key[s]]
+// (slot n: of every cell after the last key, up to ncells), so each entry is
+// written exactly once. A lane whose run is longer than a warp hands it to the
+// whole warp (empty regions of the grid), which writes it 32 entries at a time.
+// Entries past `cap` (the table's last index) are never written.
+__global__ void __launch_bounds__(256)
+    k_cell_start(const unsigned* __restrict__ keys, int n, const int* __restrict__ ncells_total,
+                 int cap, int* __restrict__ start) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool valid = s <= n;
+    int lo = 0, hi = -1;  // cells [lo, hi] start at slot s
+    if (valid) {
+        const int nc = min(*ncells_total, cap);
+        lo = (s == 0) ? 0 : (int)__ldg(keys + s - 1) + 1;
+        hi = (s == n) ? nc : (int)__ldg(keys + s);
+        hi = min(hi, cap);
     }
-    start[c] = lo;
+    const bool big = hi - lo + 1 > 32;
+    if (!big)
+        for (int c = lo; c <= hi; ++c) start[c] = s;
+    unsigned m = __ballot_sync(0xffffffffu, big);
+    while (m) {
+        const int l = __ffs(m) - 1;
+        m &= m - 1u;
+        const int blo = __shfl_sync(0xffffffffu, lo, l), bhi = __shfl_sync(0xffffffffu, hi, l);
+        const int bs = __shfl_sync(0xffffffffu, s, l);
+        for (int c = blo + lane; c <= bhi; c += 32) start[c] = bs;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -611,6 +628,59 @@ __global__ void k_load_xh(const float* __restrict__ x, const float* __restrict__
     if (DIM == 2) A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], 0.f, h[i]);
     else A.xh[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], h[i]);
     A.id[i] = i;
+}
+
+// inv[id[s]] = s: the cell-order slot of each caller index.
+__global__ void k_invert_ids(const int* __restrict__ id, int* __restrict__ inv, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) inv[id[s]] = s;
+}
+
+// A -> caller arrays walking the caller order: the form for caller arrays in
+// host memory that the device maps, where every write crosses the host link.
+// The interleaved x, v, dv/dt of a block's kScatterSeq particles are staged in
+// shared memory and written as one contiguous run each (consecutive threads,
+// consecutive addresses: whole lines, no alignment needed); the reads of A are
+// the scattered side.
+constexpr int kScatterSeq = 256;
+
+template <int DIM>
+__global__ void __launch_bounds__(kScatterSeq)
+    k_scatter_out_seq(StateA A, const int* __restrict__ inv, int n, float* __restrict__ x,
+                      float* __restrict__ v, float* __restrict__ rho, float* __restrict__ p,
+                      float* __restrict__ u, float* __restrict__ dvdt,
+                      float* __restrict__ dudt) {
+    __shared__ float sx[DIM * kScatterSeq], sv[DIM * kScatterSeq], sa[DIM * kScatterSeq];
+    const int t = threadIdx.x;
+    const int i0 = blockIdx.x * kScatterSeq;
+    const int i = i0 + t;
+    if (i < n) {
+        const int s = inv[i];
+        const float4 a = A.xh[s], b = A.vm[s], r = A.ap[s];
+        sx[DIM * t] = a.x;
+        sx[DIM * t + 1] = a.y;
+        sv[DIM * t] = b.x;
+        sv[DIM * t + 1] = b.y;
+        sa[DIM * t] = r.x;
+        sa[DIM * t + 1] = r.y;
+        if (DIM == 3) {
+            sx[3 * t + 2] = a.z;
+            sv[3 * t + 2] = b.z;
+            sa[3 * t + 2] = r.z;
+        }
+        dudt[i] = r.w;
+        u[i] = A.u[s];
+        rho[i] = A.rho[s];
+        p[i] = A.p[s];
+    }
+    __syncthreads();
+    const int cnt = DIM * min(kScatterSeq, n - i0);
+    const size_t o = (size_t)DIM * i0;
+    for (int k = t; k < cnt; k += kScatterSeq) {
+        x[o + k] = sx[k];
+        v[o + k] = sv[k];
+        dvdt[o + k] = sa[k];
+    }
 }
 
 template <int DIM>
