@@ -206,8 +206,9 @@ class Context:
         self._check(self._lib.armando_get_tuning(self._h, C.byref(t)))
         return t
 
-    def set_tuning(self, reach: int = 1, threads_per_particle: int = 1, block: int = 128):
-        t = Tuning.make(reach, threads_per_particle, block)
+    def set_tuning(self, reach: int = 1, threads_per_particle: int = 1, block: int = 128,
+                   skin: int = 0):
+        t = Tuning.make(reach, threads_per_particle, block, skin)
         self._check(self._lib.armando_set_tuning(self._h, C.byref(t)))
 
     @staticmethod
@@ -223,7 +224,8 @@ class Context:
 
     def autotune(self, s, dt: float, its0: int, steps_per_trial: int = 5):
         """Times every candidate tuning on state `s` (not modified), keeps the
-        fastest; returns (best (reach, tpp, block), {candidate: ms per step})."""
+        fastest; returns (best (reach, tpp, block, skin), {tuning: ms per step}).
+        The skin candidates are keyed by the tuning they were timed with."""
         a = s.arrays() if hasattr(s, "arrays") else s
         self._validate(a)
         best = Tuning()
@@ -233,7 +235,12 @@ class Context:
             _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
             float(dt), int(its0), int(steps_per_trial), C.byref(best), ms))
         cands = self.tuning_candidates()
-        return best.as_tuple(), {cands[k]: float(ms[k]) for k in range(N_TUNINGS)}
+        first = min(range(18), key=lambda k: ms[k] if ms[k] > 0 else float("inf"))
+        table = {}
+        for k in range(N_TUNINGS):
+            key = cands[k] if k < 18 else cands[first][:3] + (cands[k][3],)
+            table[key] = float(ms[k])
+        return best.as_tuple(), table
 
     def sync(self):
         self._check(self._lib.armando_sync(self._h))

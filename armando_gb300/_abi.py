@@ -117,17 +117,18 @@ class ParamGrads(C.Structure):
 
 class Tuning(C.Structure):
     """``armando_tuning``: neighbour-grid reach (cells per support radius),
-    threads per particle and threads per CTA of the pair passes."""
+    threads per particle, threads per CTA of the pair passes and the sort skin
+    (percent of max h)."""
 
     _fields_ = [("reach", C.c_int32), ("threads_per_particle", C.c_int32), ("block", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("skin", C.c_int32)]
 
     @classmethod
-    def make(cls, reach=1, threads_per_particle=1, block=128):
-        return cls(reach, threads_per_particle, block, 0)
+    def make(cls, reach=1, threads_per_particle=1, block=128, skin=0):
+        return cls(reach, threads_per_particle, block, skin)
 
     def as_tuple(self):
-        return (self.reach, self.threads_per_particle, self.block)
+        return (self.reach, self.threads_per_particle, self.block, self.skin)
 
 
 class Stats(C.Structure):
@@ -143,6 +144,7 @@ class Stats(C.Structure):
         ("grid_origin", F3),
         ("grid_cell_size", F3),
         ("device_flags", C.c_uint32),
+        ("sorts_done", C.c_int64),
     ]
 
 
@@ -157,7 +159,7 @@ EXPORTED = [
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
 ]
-N_TUNINGS = 18
+N_TUNINGS = 21
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
 

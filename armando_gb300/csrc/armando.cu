@@ -53,6 +53,8 @@ T* dalloc(size_t count, cudaError_t& err) {
 
 inline int blocks_for(int64_t n, int t) { return (int)((n + t - 1) / t); }
 
+constexpr int kFlagWords = 4;
+
 }  // namespace
 
 struct armando_ctx {
@@ -115,6 +117,7 @@ struct armando_ctx {
     // Reverse mode (armando_forward_checkpointed / armando_backward).
     std::vector<StateA> ckpts;           // state before iterations its0 + k*K
     armando_tuning tune{1, 1, 128, 0};   // neighbour-pass tuning (armando_set_tuning)
+    int64_t sorts_done = 0;
     std::vector<TapeSlot> tape;          // intermediates of each iteration of one segment
     int tape_seg = -1;                   // the segment the tape holds (-1: none)
     AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
@@ -235,35 +238,54 @@ void free_graphs(armando_ctx* c) {
 
 // ---- launch sequences -------------------------------------------------------
 
+// The context's lazy-sort flags (see sort_skipped); nullptr: always sort.
+const int* resort_flags(armando_ctx* ctx) { return reinterpret_cast<const int*>(ctx->flags + 1); }
+
+// The next iteration rebuilds the grid and sorts (the state in A was loaded
+// or replaced since the last sort).
+armando_status force_sort(armando_ctx* ctx) {
+    CK(cudaMemsetAsync(ctx->flags + 1, 0x01, sizeof(unsigned), ctx->stream));
+    return ARMANDO_OK;
+}
+
 template <int DIM>
-int launch_grid_and_sort(armando_ctx* ctx) {
+int launch_grid_and_sort(armando_ctx* ctx, const int* rs) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n;
     int L = 0;
-    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part);
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
-                                    ctx->flags);
+                                    ctx->flags, rs);
     k_hash<DIM><<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->A.xh, n, ctx->grid, ctx->keys[0],
-                                                          ctx->hist, ctx->num_tiles);
+                                                          ctx->hist, ctx->num_tiles, rs);
     L += 3;
     for (int p = 0; p < ctx->passes; ++p) {
         const int shift = 8 * p;
         const int a = p & 1, b = (p + 1) & 1;
         if (p > 0) {
             k_radix_hist<<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, shift,
-                                                                   ctx->hist, ctx->num_tiles);
+                                                                   ctx->hist, ctx->num_tiles, rs);
             ++L;
         }
-        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal);
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal, rs);
         k_radix_scatter<<<ctx->num_tiles, kSortThreads, 0, st>>>(
             ctx->keys[a], p == 0 ? nullptr : ctx->vals[a], ctx->keys[b], ctx->vals[b], n, shift,
-            ctx->hist, ctx->dtotal, ctx->num_tiles);
+            ctx->hist, ctx->dtotal, ctx->num_tiles, rs);
         L += 2;
     }
     k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n,
                                                                    &ctx->grid->ncells, (int)ctx->cell_cap,
-                                                                   ctx->start);
+                                                                   ctx->start, rs);
     return L + 1;
+}
+
+// End of an iteration: the next one sorts if this one flagged it (always
+// without a skin); counts this iteration's sort.
+int launch_resort_advance(armando_ctx* ctx) {
+    k_resort_advance<<<1, 32, 0, ctx->stream>>>(reinterpret_cast<int*>(ctx->flags + 1),
+                                                ctx->tune.skin == 0 ? 1 : 0,
+                                                reinterpret_cast<int*>(ctx->flags + 3));
+    return 1;
 }
 
 // Calls f(tpp, block, periodic, lean) with the context's tuning, whether any
@@ -321,10 +343,11 @@ template <int DIM>
 int launch_step(armando_ctx* ctx, const StepArgs& S) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n;
-    int L = launch_grid_and_sort<DIM>(ctx);
+    const int* rs = resort_flags(ctx);
+    int L = launch_grid_and_sort<DIM>(ctx, rs);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     launch_density<DIM>(ctx, skeys);
     L += 2;
     if (ctx->dp.visc) {
@@ -333,7 +356,7 @@ int launch_step(armando_ctx* ctx, const StepArgs& S) {
         ++L;
     }
     launch_force<DIM>(ctx, skeys, S);
-    return L + 1;
+    return L + 1 + launch_resort_advance(ctx);
 }
 
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
@@ -427,11 +450,12 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     const int n = (int)ctx->n;
     int L = 0;
     cudaEventRecord(ev[0], st);
-    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part);
+    const int* rs = resort_flags(ctx);
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
-                                    ctx->flags);
+                                    ctx->flags, rs);
     k_hash<DIM><<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->A.xh, n, ctx->grid, ctx->keys[0],
-                                                          ctx->hist, ctx->num_tiles);
+                                                          ctx->hist, ctx->num_tiles, rs);
     L += 3;
     cudaEventRecord(ev[1], st);
     for (int p = 0; p < ctx->passes; ++p) {
@@ -439,21 +463,21 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
         const int a = p & 1, b = (p + 1) & 1;
         if (p > 0) {
             k_radix_hist<<<ctx->num_tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, shift,
-                                                                   ctx->hist, ctx->num_tiles);
+                                                                   ctx->hist, ctx->num_tiles, rs);
             ++L;
         }
-        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal);
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, ctx->num_tiles, ctx->dtotal, rs);
         k_radix_scatter<<<ctx->num_tiles, kSortThreads, 0, st>>>(
             ctx->keys[a], p == 0 ? nullptr : ctx->vals[a], ctx->keys[b], ctx->vals[b], n, shift,
-            ctx->hist, ctx->dtotal, ctx->num_tiles);
+            ctx->hist, ctx->dtotal, ctx->num_tiles, rs);
         L += 2;
     }
     cudaEventRecord(ev[2], st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
     k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(skeys, n, &ctx->grid->ncells,
-                                                                   (int)ctx->cell_cap, ctx->start);
-    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
+                                                                   (int)ctx->cell_cap, ctx->start, rs);
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     cudaEventRecord(ev[3], st);
     launch_density<DIM>(ctx, skeys);
     cudaEventRecord(ev[4], st);
@@ -465,6 +489,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     }
     cudaEventRecord(ev[5], st);
     launch_force<DIM>(ctx, skeys, S);
+    L += launch_resort_advance(ctx);
     cudaEventRecord(ev[6], st);
     return L + 1;
 }
@@ -543,6 +568,8 @@ armando_status alloc_state(armando_ctx* ctx) {
     F1(ctx->B.ulo, n);
     ctx->B.vr = dalloc<float4>(ctx->dim == 2 ? n : 1, e);
     ctx->owned.push_back(ctx->B.vr);
+    ctx->B.xsort = dalloc<float4>(n, e);
+    ctx->owned.push_back(ctx->B.xsort);
     ctx->B.nmask = dalloc<unsigned>(n * (ctx->dim == 2 ? mask_words<2>() : mask_words<3>()), e);
     ctx->B.mstride = (int)n;
     ctx->B.mtpp = 1;
@@ -558,7 +585,8 @@ armando_status alloc_state(armando_ctx* ctx) {
     ctx->dtotal = dalloc<unsigned>(kRadix, e);
     ctx->bbox_part = dalloc<float>(kBBoxBlocks * 8, e);
     ctx->grid = dalloc<DevGrid>(1, e);
-    ctx->flags = dalloc<unsigned>(1, e);
+    // [0] status bits, [1] this iteration sorts, [2] the next one must, [3] sorts done
+    ctx->flags = dalloc<unsigned>(kFlagWords, e);
     for (void* p : {(void*)ctx->hist, (void*)ctx->dtotal, (void*)ctx->bbox_part, (void*)ctx->grid,
                     (void*)ctx->flags})
         ctx->owned.push_back(p);
@@ -576,7 +604,8 @@ armando_status alloc_state(armando_ctx* ctx) {
         I1(ctx->s_itype);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc");
-    cudaError_t he = cudaMallocHost((void**)&ctx->h_flags, sizeof(unsigned));
+    CK(cudaMemset(ctx->flags, 0, kFlagWords * sizeof(unsigned)));
+    cudaError_t he = cudaMallocHost((void**)&ctx->h_flags, kFlagWords * sizeof(unsigned));
     if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
     he = cudaMallocHost((void**)&ctx->h_grid, sizeof(DevGrid));
     if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
@@ -643,12 +672,14 @@ armando_status plan_grid(armando_ctx* ctx) {
 }
 
 armando_status check_flags(armando_ctx* ctx) {
-    CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, kFlagWords * sizeof(unsigned),
+                       cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_grid, ctx->n_inst > 1 ? ctx->d_grids : ctx->grid, sizeof(DevGrid),
                        cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->last_grid = *ctx->h_grid;
     ctx->have_grid = true;
+    ctx->sorts_done = ctx->h_flags[3];
     const unsigned f = *ctx->h_flags;
     if (f & FLAG_PERIODIC_SMALL) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "periodic box shorter than 3 cells of 2*max(h)");
     if (f & FLAG_GRID_OVERFLOW) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "neighbour grid exceeded the context's cell capacity");
@@ -730,7 +761,7 @@ armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, co
                                                             dvdt, dudt, ctx->A, nn, ctx->d_inst0);
     ctx->launches += 1;
     CK(cudaGetLastError());
-    return ARMANDO_OK;
+    return force_sort(ctx);  // A is in caller order now
 }
 
 // A -> caller arrays.
@@ -1263,8 +1294,11 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
     if (t.threads_per_particle != 1 && t.threads_per_particle != 2 && t.threads_per_particle != 4)
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "threads_per_particle must be 1, 2 or 4");
     if (t.block != 128 && t.block != 256) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "block must be 128 or 256");
+    if (t.skin < 0 || t.skin > 100) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "skin must be 0-100 (percent of max h)");
     if (ctx->n_inst > 1 && t.threads_per_particle != 1)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches run one thread per particle");
+    if (ctx->n_inst > 1 && t.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches sort every iteration (skin 0)");
     return ARMANDO_OK;
 }
 
@@ -1272,12 +1306,12 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
 // table (and the reverse-mode tape, which keeps copies of it) is re-planned on
 // the next iteration; any change ends a pending backward sweep.
 armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
-    const bool regrid = t.reach != ctx->tune.reach;
+    const bool regrid = t.reach != ctx->tune.reach || t.skin != ctx->tune.skin;
     ctx->tune = t;
-    ctx->tune.reserved = 0;
     ctx->B.mstride = (int)(ctx->n * t.threads_per_particle);
     ctx->B.mtpp = t.threads_per_particle;
     ctx->dp.reach = t.reach;
+    ctx->dp.skin = 0.01f * (float)t.skin;
     if (regrid) {
         if (ctx->n_inst > 1) {
             armando_status st = upload_batch_params(ctx);
@@ -1314,7 +1348,7 @@ armando_status armando_set_tuning(armando_ctx* ctx, const armando_tuning* t) {
     if (st != ARMANDO_OK) return st;
     CK(cudaSetDevice(ctx->device));
     if (t->reach == ctx->tune.reach && t->threads_per_particle == ctx->tune.threads_per_particle &&
-        t->block == ctx->tune.block)
+        t->block == ctx->tune.block && t->skin == ctx->tune.skin)
         return ARMANDO_OK;
     return apply_tuning(ctx, *t);
 }
@@ -1323,10 +1357,15 @@ armando_status armando_tuning_candidate(int32_t k, armando_tuning* out) {
     if (!out || k < 0 || k >= ARMANDO_N_TUNINGS)
         return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "candidate index out of range");
     static const int tpp[3] = {1, 2, 4};
+    static const int skin[3] = {10, 20, 40};
+    if (k >= 18) {  // a skin for the fastest of the first 18
+        *out = armando_tuning{0, 0, 0, skin[k - 18]};
+        return ARMANDO_OK;
+    }
     out->reach = 1 + k / 6;
     out->threads_per_particle = tpp[(k / 2) % 3];
     out->block = (k % 2) ? 256 : 128;
-    out->reserved = 0;
+    out->skin = 0;
     return ARMANDO_OK;
 }
 
@@ -1349,6 +1388,11 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
     for (int k = 0; k < ARMANDO_N_TUNINGS; ++k) {
         armando_tuning t;
         armando_tuning_candidate(k, &t);
+        if (k >= 18) {  // second stage: the winner so far with a sort skin
+            const int skin = t.skin;
+            t = win;
+            t.skin = skin;
+        }
         float ms = -1.f;
         if ((st = apply_tuning(ctx, t)) != ARMANDO_OK) break;
         CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
@@ -1553,7 +1597,8 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float*
         cleanup();
         return s;
     }
-    int L = ctx->dim == 2 ? launch_grid_and_sort<2>(ctx) : launch_grid_and_sort<3>(ctx);
+    int L = ctx->dim == 2 ? launch_grid_and_sort<2>(ctx, nullptr) : launch_grid_and_sort<3>(ctx, nullptr);
+    ctx->next_its = 0;  // A now holds these positions, not a step's state
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
     k_reorder_xh<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, nn);
@@ -1627,6 +1672,9 @@ armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* v
     ctx->tape_seg = -1;
     for (int k = 0; k < steps; ++k) {
         if (k % K == 0 && (st = copy_stateA(ctx, ctx->ckpts[k / K], ctx->A)) != ARMANDO_OK) return st;
+        // Reverse mode sorts every iteration, so a replay from a checkpoint
+        // repeats the forward bit for bit.
+        if ((st = force_sort(ctx)) != ARMANDO_OK) return st;
         if ((st = run_step(ctx, make_args(ctx, dt, its0 + k))) != ARMANDO_OK) return st;
         if (k >= last && (st = save_tape(ctx, k - last)) != ARMANDO_OK) return st;
     }
@@ -1691,6 +1739,7 @@ armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const floa
             ctx->tape_seg = -1;
             if ((st = copy_stateA(ctx, ctx->A, ctx->ckpts[c])) != ARMANDO_OK) return st;
             for (int t = 0; t < len; ++t) {
+                if ((st = force_sort(ctx)) != ARMANDO_OK) return st;
                 if ((st = run_step(ctx, make_args(ctx, dt, its0 + a0 + t))) != ARMANDO_OK) return st;
                 if ((st = save_tape(ctx, t)) != ARMANDO_OK) return st;
             }
@@ -1802,6 +1851,7 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
         }
     }
     out->device_flags = cctx->h_flags ? *cctx->h_flags : 0u;
+    out->sorts_done = cctx->sorts_done;
     return ARMANDO_OK;
 }
 

@@ -50,8 +50,8 @@ struct DevGrid {
     int ok;        // 0 when the grid did not fit; passes then do nothing
     int periodic[3];
     int cell_off;  // first cell of this grid in the shared cell table (batches)
-    int reach;     // stencil half-width in cells: cell size 2 max(h) / reach
-    int pad_;
+    int reach;       // stencil half-width in cells: cell size (2 max(h) + skin) / reach
+    float half_skin2;  // (skin / 2)^2: a particle this far from its binned position forces a sort
 };
 
 // A unit of work of the persistent passes: slots [s0, s1) of one instance.
@@ -73,7 +73,7 @@ struct DevParams {
     float dt;            // time step of this instance (batches)
     float heat_t_end;    // external heat gate its*dt <= heat_t_end
     int reach;           // neighbour-grid cells per support radius (tuning; 1 = link_list)
-    int pad_;
+    float skin;          // sort skin as a fraction of max h (tuning; 0 = sort every step)
 };
 
 struct StepArgs {
@@ -108,6 +108,7 @@ struct StateB {  // working set of one step (cell order)
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
+    float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour bits of each fluid slot over its first 32 * mask_words<DIM>()
     // candidates (cursor order); words 0 and 1 all ones: more candidates than
     // bits. With TPP lanes per particle, lane L = s * TPP + sub keeps
@@ -161,6 +162,25 @@ __device__ __forceinline__ float mass_of(const float4& xh, const float4& vm) {
     return DIM == 2 ? xh.z : vm.w;
 }
 
+// Lazy sorting (sort skin). resort[0] != 0: this iteration sorts; the force
+// pass sets resort[1] when a particle has moved more than half the skin from
+// where it was binned; k_resort_advance moves it to resort[0] for the next
+// iteration. The grid, hash, sort and cell-table kernels return at once on an
+// iteration that does not sort (their outputs from the last sort stay valid:
+// cells of 2 max(h) + skin hold every pair within 2 max(h) while no particle
+// is farther than skin / 2 from its binned position). resort == nullptr:
+// always sort.
+__device__ __forceinline__ bool sort_skipped(const int* resort) {
+    return resort != nullptr && *(volatile const int*)resort == 0;
+}
+
+__global__ void k_resort_advance(int* __restrict__ resort, int always, int* __restrict__ sorts) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (resort[0] != 0) ++sorts[0];
+    resort[0] = always ? 1 : resort[1];
+    resort[1] = 0;
+}
+
 // ---------------------------------------------------------------------------
 // Small block-level helpers
 // ---------------------------------------------------------------------------
@@ -198,7 +218,9 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* s_warp
 // Grid: bbox of all particles and the link_list grid in FP32.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_bbox_partial(const float4* __restrict__ xh, int n, int dim,
-                                                      float* __restrict__ part) {
+                                                      float* __restrict__ part,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX}, mh = 0.f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         float4 a = xh[i];
@@ -246,7 +268,9 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
 __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ part, int nparts,
                                                     DevParams P, long long capacity,
                                                     DevGrid* __restrict__ grid,
-                                                    unsigned* __restrict__ flags) {
+                                                    unsigned* __restrict__ flags,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     __shared__ float s[7][256];
     float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
     for (int b = threadIdx.x; b < nparts; b += blockDim.x)
@@ -271,22 +295,24 @@ __global__ void __launch_bounds__(256) k_bbox_final(const float* __restrict__ pa
 
 // The link_list grid (CERNsource/link_list.f:39-67) of a bbox mm = {min[3],
 // max[3], max h}, in FP32; periodic axes split their box into >= 3 cells.
-// With P.reach = f > 1 the cells are 2 mh / f wide and the passes search
-// (2f + 1)^dim cells. Those cells are widened by a margin larger than the
-// rounding of a cell index ((x - o) / size: a few ulp of the index, i.e.
-// n * 2^-23 cells), so no pair the exact test accepts is outside the stencil;
-// f = 1 keeps link_list's cell exactly.
+// With P.reach = f the cells are (2 mh + skin) / f wide, skin = P.skin * mh,
+// and the passes search (2f + 1)^dim cells. Unless f = 1 and skin = 0 (which
+// keep link_list's cell exactly) the cells are widened by a margin larger
+// than the rounding of a cell index ((x - o) / size: a few ulp of the index,
+// i.e. n * 2^-23 cells), so no pair the exact test accepts is outside the
+// stencil.
 __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevParams& P,
                                                   long long capacity, unsigned& fl) {
     DevGrid g;
     const float mh = mm[6];
     const int f = P.reach > 1 ? P.reach : 1;
+    const float skin = P.skin > 0.f ? P.skin * mh : 0.f;
     float cell = __fmul_rn(2.0f, mh);  // scale_k * mh, scale_k = 2
-    if (f > 1) {
+    if (f > 1 || skin > 0.f) {
         float span = 0.f;
         for (int d = 0; d < P.dim; ++d)
             span = fmaxf(span, P.periodic[d] ? P.period_L[d] : mm[3 + d] - mm[d] + 2.f * mh);
-        const float cf = cell / (float)f;
+        const float cf = (cell + skin) / (float)f;
         const float nmax = span / fmaxf(cf, FLT_MIN);
         cell = cf * (1.0f + 0x1p-12f + fminf(nmax, 1.0e7f) * 0x1p-20f);
     }
@@ -328,7 +354,7 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
     g.ok = 1;
     g.cell_off = 0;
     g.reach = f;
-    g.pad_ = 0;
+    g.half_skin2 = 0.25f * skin * skin;
     if (ncells > capacity || (fl & FLAG_GRID_OVERFLOW) || (fl & FLAG_PERIODIC_SMALL)) {
         fl |= (ncells > capacity) ? FLAG_GRID_OVERFLOW : 0u;
         g.ok = 0;
@@ -356,7 +382,9 @@ __device__ __forceinline__ unsigned cell_key(const float4& a, const DevGrid& g) 
 template <int DIM>
 __global__ void __launch_bounds__(kSortThreads)
     k_hash(const float4* __restrict__ xh, int n, const DevGrid* __restrict__ gp,
-           unsigned* __restrict__ keys, unsigned* __restrict__ hist, int num_tiles) {
+           unsigned* __restrict__ keys, unsigned* __restrict__ hist, int num_tiles,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     __shared__ unsigned sh[kRadix];
     __shared__ DevGrid g;
     if (threadIdx.x == 0) g = *gp;
@@ -446,7 +474,9 @@ __global__ void k_keys_only(const float4* __restrict__ xh, int n, const DevGrid*
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kSortThreads)
     k_radix_hist(const unsigned* __restrict__ keys, int n, int shift, unsigned* __restrict__ hist,
-                 int num_tiles) {
+                 int num_tiles,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     __shared__ unsigned sh[kRadix];
     sh[threadIdx.x] = 0;
     __syncthreads();
@@ -462,7 +492,9 @@ __global__ void __launch_bounds__(kSortThreads)
 
 // Block d: exclusive scan of the tile counts of digit d; total per digit.
 __global__ void __launch_bounds__(256)
-    k_radix_scan(unsigned* __restrict__ hist, int num_tiles, unsigned* __restrict__ dtotal) {
+    k_radix_scan(unsigned* __restrict__ hist, int num_tiles, unsigned* __restrict__ dtotal,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     __shared__ unsigned s_warp[32];
     __shared__ unsigned s_total;
     unsigned* row = hist + (size_t)blockIdx.x * num_tiles;
@@ -486,7 +518,9 @@ __global__ void __launch_bounds__(kSortThreads)
     k_radix_scatter(const unsigned* __restrict__ keys_in, const int* __restrict__ vals_in,
                     unsigned* __restrict__ keys_out, int* __restrict__ vals_out, int n, int shift,
                     const unsigned* __restrict__ hist, const unsigned* __restrict__ dtotal,
-                    int num_tiles) {
+                    int num_tiles,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     __shared__ unsigned s_warp[32];
     __shared__ unsigned s_base[kRadix];
     __shared__ unsigned s_tstart[kRadix];
@@ -564,7 +598,9 @@ __global__ void __launch_bounds__(kSortThreads)
 // Entries past `cap` (the table's last index) are never written.
 __global__ void __launch_bounds__(256)
     k_cell_start(const unsigned* __restrict__ keys, int n, const int* __restrict__ ncells_total,
-                 int cap, int* __restrict__ start) {
+                 int cap, int* __restrict__ start,
+    const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool valid = s <= n;
@@ -711,12 +747,15 @@ __global__ void k_scatter_out(StateA A, int n, float* __restrict__ x, float* __r
 
 // Cell-ordered working set + leapfrog predictor (time_integration.f:136-154).
 template <int DIM>
+// An iteration that does not sort keeps the slot order (perm = identity).
 __global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, StepArgs S,
-                              int n) {
+                              int n, const int* __restrict__ resort = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const int j = perm[s];
+    const bool sorted = !sort_skipped(resort);
+    const int j = sorted ? perm[s] : s;
     const float4 xh = A.xh[j];
+    if (sorted && B.xsort) B.xsort[s] = xh;
     float4 vm = A.vm[j];
     float u = A.u[j];
     const int it = A.itype[j];
@@ -1651,6 +1690,12 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     if (P.periodic[1]) xn.y = wrap_axis(xn.y, P, 1, outside);
     if (DIM == 3 && P.periodic[2]) xn.z = wrap_axis(xn.z, P, 2, outside);
     if (outside) atomicOr(flags, (unsigned)FLAG_OUT_OF_GRID);
+    if (g.half_skin2 > 0.f && B.xsort) {  // moved more than half the skin since the sort: sort next
+        const float4 x0 = B.xsort[s];
+        const float e0 = xn.x - x0.x, e1 = xn.y - x0.y, e2 = (DIM == 3) ? xn.z - x0.z : 0.f;
+        if (e0 * e0 + e1 * e1 + e2 * e2 > g.half_skin2 && *(volatile unsigned*)(flags + 2) == 0u)
+            atomicExch(flags + 2, 1u);
+    }
     const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + un + a0 + a1 + a2 + du;
     if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
     A.xh[s] = xn;

@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="skip the autotuner (default tuning or --tuning)")
     ap.add_argument("--tuning", default=None,
-                    help="reach,threads_per_particle,block instead of the autotuner")
+                    help="reach,threads_per_particle,block[,skin] instead of the autotuner")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--checkpoint-every", type=int, default=50)
     ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint"],
@@ -285,16 +285,16 @@ def tune(ctx, args, arrays, dt):
     """The tuning the timed region runs with: the autotuner's pick on this
     workload's own state (untimed, state not modified), or a fixed one."""
     if args.tuning:
-        r, t, b = (int(v) for v in args.tuning.split(","))
-        ctx.set_tuning(r, t, b)
-        return {"tuning": [r, t, b], "source": "fixed"}
+        v = [int(x) for x in args.tuning.split(",")]
+        ctx.set_tuning(*v)
+        return {"tuning": list(ctx.tuning().as_tuple()), "source": "fixed"}
     if args.no_autotune:
         return {"tuning": list(ctx.tuning().as_tuple()), "source": "default"}
     t0 = time.perf_counter()
     best, table = ctx.autotune(arrays, dt, 1, steps_per_trial=5)
     return {"tuning": list(best), "source": "autotune",
             "autotune_s": time.perf_counter() - t0,
-            "ms_per_step": {"%d,%d,%d" % k: round(v, 5) for k, v in table.items()}}
+            "ms_per_step": {",".join(map(str, k)): round(v, 5) for k, v in table.items()}}
 
 
 def timed_integrate(ctx, arrays, dts, its0, steps, batch=False):
@@ -326,7 +326,9 @@ def run_channel(args):
     with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
         tuned = tune(ctx, args, dev, c.dt)
         ctx.integrate(dev, c.dt, 1, 3)
+        sorts0 = ctx.stats().sorts_done
         ms = timed_integrate(ctx, dev, c.dt, 4, args.extra_steps)
+        sorts = ctx.stats().sorts_done - sorts0
         phases = ctx.profile_phases(2)
         cells_pp = ctx.stats().n_cells / c.n
     del dev
@@ -335,7 +337,7 @@ def run_channel(args):
                         f"art. visc + art. heat + Gaussian source",
             "particles": c.n, "steps": args.extra_steps, "ms_per_step": ms / args.extra_steps,
             "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC, "phases_ms": phases,
-            "tuning": tuned,
+            "tuning": tuned, "sorts_in_timed_region": int(sorts),
             "two_roof": two_roof("channel3d", c.n, ms / args.extra_steps,
                                  step_bytes(3, cells_pp), peaks()[0])}
 
@@ -411,6 +413,10 @@ def run_adjoint(args):
     w_ref = float(np.where((t > 0) & fl, t ** 3, 0.0).sum())
     with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_HOST) as ctx:
         tuned = tune(ctx, args, c, c.dt)
+        # Reverse mode sorts every iteration; the forward it is set against does too.
+        t = tuned["tuning"]
+        ctx.set_tuning(t[0], t[1], t[2], 0)
+        tuned["tuning"] = list(ctx.tuning().as_tuple())
         warm = c.copy()
         ctx.integrate(warm, c.dt, 1, 3)
         torch.cuda.synchronize()
@@ -480,6 +486,7 @@ def run_ours(args, rank, world, local_rank):
     ctx.integrate(dev, case.dt, 1, args.warmup)
     its = 1 + args.warmup
     launches0 = ctx.stats().gpu_launches
+    sorts0 = ctx.stats().sorts_done
     barrier()
     with ClockSampler(local_rank) as clk:
         e0 = torch.cuda.Event(enable_timing=True)
@@ -492,6 +499,7 @@ def run_ours(args, rank, world, local_rank):
     ms = e0.elapsed_time(e1)
     its += args.steps
     launches = ctx.stats().gpu_launches - launches0
+    sorts = ctx.stats().sorts_done - sorts0
     if dist:
         t = torch.tensor([ms], device="cuda")
         td.all_reduce(t, op=td.ReduceOp.MAX)
@@ -530,6 +538,7 @@ def run_ours(args, rank, world, local_rank):
                               "frac_of_measured_hbm": b_step * case.n / step_s / 1e9 / hbm},
             "two_roof": two_roof(args.config, case.n, ms / args.steps, b_step, hbm),
             "phases_ms": phases, "gpu_launches": int(launches), "tuning": tuned,
+            "sorts_in_timed_region": int(sorts),
             "clocks": clk.summary(),
         }
     # e2e: armando_step with pinned host buffers, one call per step.

@@ -93,6 +93,8 @@ typedef struct armando_stats {
     float grid_origin[3];     /* grid origin (link_list.f:53-57: bbox min - max h) */
     float grid_cell_size[3];  /* cell edge per axis (2 * max h when not periodic) */
     uint32_t device_flags;    /* raw device status word of the last check        */
+    int64_t sorts_done;       /* iterations that rebuilt the grid and sorted (all
+                                 of them unless the tuning has a sort skin)       */
 } armando_stats;
 
 typedef struct armando_ctx armando_ctx;
@@ -258,6 +260,13 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
  *   block                threads per CTA of the pair passes, i.e. the tile of
  *                        consecutive cell-ordered particles whose candidate
  *                        lists one CTA stages in shared memory: 128 or 256.
+ *   skin                 sort skin in percent of max(h), 0-100: the cells grow
+ *                        by skin and armando_integrate rebuilds the grid and
+ *                        sorts only on iterations where some particle has
+ *                        moved more than half the skin since the last sort
+ *                        (0: every iteration; one-particle-system contexts
+ *                        only; armando_step, which takes fresh arrays, and
+ *                        the reverse mode always sort).
  * The neighbour sets do not depend on the tuning; the sums differ only by
  * their rounding (summation order). armando_cell_ids always uses reach 1.
  */
@@ -265,16 +274,19 @@ typedef struct armando_tuning {
     int32_t reach;
     int32_t threads_per_particle;
     int32_t block;
-    int32_t reserved;
+    int32_t skin;
 } armando_tuning;
 
 armando_status armando_get_tuning(armando_ctx* ctx, armando_tuning* out);
 /* INVALID_ARG for a value outside the lists above; UNSUPPORTED for
- * threads_per_particle > 1 on a batch context. */
+ * threads_per_particle > 1 or skin > 0 on a batch context. */
 armando_status armando_set_tuning(armando_ctx* ctx, const armando_tuning* t);
 
-/* The autotuner's candidate tunings, k = 0 .. ARMANDO_N_TUNINGS - 1. */
-#define ARMANDO_N_TUNINGS 18
+/* The autotuner's candidate tunings, k = 0 .. ARMANDO_N_TUNINGS - 1: k < 18
+ * every (reach, threads_per_particle, block) with skin 0; k >= 18 a skin
+ * (10, 20, 40 percent) applied to the fastest of the first 18, returned here
+ * with reach = threads_per_particle = block = 0. */
+#define ARMANDO_N_TUNINGS 21
 armando_status armando_tuning_candidate(int32_t k, armando_tuning* out);
 
 /*

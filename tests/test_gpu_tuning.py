@@ -15,7 +15,7 @@ from helpers import FIELDS, history_state, step_errors
 pytestmark = pytest.mark.gpu
 
 TOL_STEP = 1e-5
-CANDIDATES = [(r, t, b) for r in (1, 2, 3) for t in (1, 2, 4) for b in (128, 256)]
+CANDIDATES = [(r, t, b, 0) for r in (1, 2, 3) for t in (1, 2, 4) for b in (128, 256)]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -86,7 +86,7 @@ def test_neighbour_sets_every_reach(O, name, reach):
     assert np.array_equal(cid.astype(np.int64), ref_cid)
 
 
-@pytest.mark.parametrize("tuning", CANDIDATES, ids=lambda t: "r%d_t%d_b%d" % t)
+@pytest.mark.parametrize("tuning", CANDIDATES, ids=lambda t: "r%d_t%d_b%d_s%d" % t)
 @pytest.mark.parametrize("name", ["dambreak", "channel3d", "dambreak_wide_h"])
 def test_one_step_parity_every_tuning(refs, name, tuning):
     inp, ref = refs[name]
@@ -115,13 +115,14 @@ def test_tunings_agree_over_many_steps(O):
     O.integrate_gather(ref, 1, 50, c.dt)
     O.integrate_gather(pert, 1, 50, c.dt)
     runs = {}
-    for t in [(1, 1, 128), (2, 2, 128), (3, 4, 256), (2, 1, 256)]:
+    for t in [(1, 1, 128, 0), (2, 2, 128, 0), (3, 4, 256, 0), (2, 1, 256, 0), (1, 1, 128, 20),
+              (2, 1, 128, 40)]:
         s = c.copy()
         with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
             ctx.set_tuning(*t)
             ctx.integrate(s, c.dt, 1, 50)
         runs[t] = s
-    base = runs[(1, 1, 128)]
+    base = runs[(1, 1, 128, 0)]
     for t, s in runs.items():
         for f in FIELDS:
             b = np.asarray(getattr(ref, f), np.float64)
@@ -139,8 +140,9 @@ def test_autotune_picks_a_candidate_and_leaves_inputs(O):
         best, table = ctx.autotune(c, c.dt, 1, steps_per_trial=3)
         for f in FIELDS + ("mass", "h", "itype"):
             assert np.array_equal(getattr(c, f), getattr(before, f)), f
-        assert best in CANDIDATES and ctx.tuning().as_tuple() == best
-        assert set(table) == set(CANDIDATES)
+        assert ctx.tuning().as_tuple() == best
+        assert best[:3] + (0,) in CANDIDATES and best[3] in (0, 10, 20, 40)
+        assert set(CANDIDATES) <= set(table) and len(table) == 21
         assert all(v > 0 for v in table.values())
         assert table[best] == min(table.values())
         errs, _, _ = step_errors(O, ctx, c, its=1)
@@ -151,17 +153,21 @@ def test_autotune_picks_a_candidate_and_leaves_inputs(O):
 def test_set_tuning_rejects_bad_values():
     c = cases.dam_break(dx=0.05)
     with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
-        for bad in [(0, 1, 128), (4, 1, 128), (1, 3, 128), (1, 1, 96)]:
+        for bad in [(0, 1, 128), (4, 1, 128), (1, 3, 128), (1, 1, 96), (1, 1, 128, -1),
+                    (1, 1, 128, 101)]:
             with pytest.raises(ag.ArmandoError) as e:
                 ctx.set_tuning(*bad)
             assert e.value.status == ag._abi.ERR_INVALID_ARG
-        assert ctx.tuning().as_tuple() == (1, 1, 128)
+        assert ctx.tuning().as_tuple() == (1, 1, 128, 0)
     insts = [cases.dam_break(dx=0.05), cases.cavity(n_side=12)]
     with ag.Batch([k.params for k in insts], [k.n_fluid for k in insts],
                   [k.n_wall for k in insts]) as b:
         b.set_tuning(reach=2)
         with pytest.raises(ag.ArmandoError) as e:
             b.set_tuning(reach=1, threads_per_particle=2)
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
+        with pytest.raises(ag.ArmandoError) as e:
+            b.set_tuning(reach=1, skin=20)
         assert e.value.status == ag._abi.ERR_UNSUPPORTED
 
 
