@@ -117,7 +117,11 @@ struct armando_ctx {
     // Reverse mode (armando_forward_checkpointed / armando_backward).
     std::vector<StateA> ckpts;           // state before iterations its0 + k*K
     armando_tuning tune{1, 1, 128, 0};   // neighbour-pass tuning (armando_set_tuning)
-    int64_t sorts_done = 0;
+    int64_t sorts_done = 0;              // lazily sorting iterations that sorted (device count)
+    int64_t sorts_host = 0;              // iterations that always sort
+    cudaStream_t stream2 = nullptr;      // captures the conditional sort body
+    bool no_conditional = false;         // conditional graphs failed to build here
+    float4* xsort_buf = nullptr;
     std::vector<TapeSlot> tape;          // intermediates of each iteration of one segment
     int tape_seg = -1;                   // the segment the tape holds (-1: none)
     AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
@@ -249,8 +253,7 @@ armando_status force_sort(armando_ctx* ctx) {
 }
 
 template <int DIM>
-int launch_grid_and_sort(armando_ctx* ctx, const int* rs) {
-    cudaStream_t st = ctx->stream;
+int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st) {
     const int n = (int)ctx->n;
     int L = 0;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
@@ -279,11 +282,13 @@ int launch_grid_and_sort(armando_ctx* ctx, const int* rs) {
     return L + 1;
 }
 
-// End of an iteration: the next one sorts if this one flagged it (always
-// without a skin); counts this iteration's sort.
+// Whether the context sorts lazily (a sort skin; one particle system).
+bool lazy(const armando_ctx* ctx) { return ctx->tune.skin > 0 && ctx->n_inst == 1; }
+
+// End of a lazily sorting iteration: the next one sorts if this one flagged
+// it; counts this iteration's sort.
 int launch_resort_advance(armando_ctx* ctx) {
     k_resort_advance<<<1, 32, 0, ctx->stream>>>(reinterpret_cast<int*>(ctx->flags + 1),
-                                                ctx->tune.skin == 0 ? 1 : 0,
                                                 reinterpret_cast<int*>(ctx->flags + 3));
     return 1;
 }
@@ -339,24 +344,105 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     });
 }
 
+// Reorder/predictor, the pair passes and (lazy sorting) the flag advance.
 template <int DIM>
-int launch_step(armando_ctx* ctx, const StepArgs& S) {
+int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n;
-    const int* rs = resort_flags(ctx);
-    int L = launch_grid_and_sort<DIM>(ctx, rs);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     launch_density<DIM>(ctx, skeys);
-    L += 2;
+    int L = 2;
     if (ctx->dp.visc) {
         k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
         ++L;
     }
     launch_force<DIM>(ctx, skeys, S);
-    return L + 1 + launch_resort_advance(ctx);
+    ++L;
+    if (rs) L += launch_resort_advance(ctx);
+    return L;
+}
+
+// One iteration as a plain launch sequence (lazy sorting: the grid and sort
+// kernels test the flag and return at once when the iteration does not sort).
+template <int DIM>
+int launch_step(armando_ctx* ctx, const StepArgs& S) {
+    const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
+    const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream);
+    return L + launch_passes<DIM>(ctx, S, rs);
+}
+
+// One lazily sorting iteration as a graph whose grid and sort kernels sit in
+// the body of a conditional (IF) node: a one-thread kernel sets the condition
+// from the flag, so iterations that do not sort launch none of them. The body
+// is captured from a second stream into the node's child graph.
+template <int DIM>
+armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphExec_t* out,
+                                int* launches) {
+    cudaError_t e = cudaSuccess;
+    if (!ctx->stream2 && (e = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaStreamCreate");
+    cudaGraph_t graph = nullptr;
+    if ((e = cudaGraphCreate(&graph, 0)) != cudaSuccess) return cuda_fail(ctx, e, "cudaGraphCreate");
+    bool main_cap = false, body_cap = false;
+    auto fail_graph = [&](cudaError_t err, const char* where) {
+        cudaGraph_t g = nullptr;
+        if (body_cap) cudaStreamEndCapture(ctx->stream2, &g);
+        if (main_cap && cudaStreamEndCapture(ctx->stream, &g) == cudaSuccess && g && g != graph)
+            cudaGraphDestroy(g);
+        cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return cuda_fail(ctx, err, where);
+    };
+    cudaGraphConditionalHandle h;
+    if ((e = cudaGraphConditionalHandleCreate(&h, graph, 0, 0)) != cudaSuccess)
+        return fail_graph(e, "cudaGraphConditionalHandleCreate");
+    if ((e = cudaStreamBeginCaptureToGraph(ctx->stream, graph, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return fail_graph(e, "cudaStreamBeginCaptureToGraph");
+    main_cap = true;
+    k_resort_cond<<<1, 32, 0, ctx->stream>>>(h, resort_flags(ctx));
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if ((e = cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, nullptr, &deps, nullptr, &nd)) != cudaSuccess)
+        return fail_graph(e, "cudaStreamGetCaptureInfo");
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if ((e = cudaGraphAddNode(&cnode, graph, deps, nullptr, nd, &p)) != cudaSuccess)
+        return fail_graph(e, "cudaGraphAddNode(conditional)");
+    if ((e = cudaStreamUpdateCaptureDependencies(ctx->stream, &cnode, nullptr, 1,
+                                                 cudaStreamSetCaptureDependencies)) != cudaSuccess)
+        return fail_graph(e, "cudaStreamUpdateCaptureDependencies");
+    if ((e = cudaStreamBeginCaptureToGraph(ctx->stream2, p.conditional.phGraph_out[0], nullptr,
+                                           nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return fail_graph(e, "cudaStreamBeginCaptureToGraph(body)");
+    body_cap = true;
+    int L = 1 + launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2);
+    cudaGraph_t body_out = nullptr;
+    e = cudaStreamEndCapture(ctx->stream2, &body_out);
+    body_cap = false;
+    if (e != cudaSuccess) return fail_graph(e, "cudaStreamEndCapture(body)");
+    L += launch_passes<DIM>(ctx, S, resort_flags(ctx));
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_graph(e, "kernel launch during capture");
+    cudaGraph_t g_out = nullptr;
+    e = cudaStreamEndCapture(ctx->stream, &g_out);
+    main_cap = false;
+    if (e != cudaSuccess) return fail_graph(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return cuda_fail(ctx, e, "cudaGraphInstantiate(conditional)");
+    }
+    *launches = L;
+    return ARMANDO_OK;
 }
 
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
@@ -450,7 +536,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     const int n = (int)ctx->n;
     int L = 0;
     cudaEventRecord(ev[0], st);
-    const int* rs = resort_flags(ctx);
+    const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
                                     ctx->flags, rs);
@@ -489,7 +575,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     }
     cudaEventRecord(ev[5], st);
     launch_force<DIM>(ctx, skeys, S);
-    L += launch_resort_advance(ctx);
+    if (rs) L += launch_resort_advance(ctx);
     cudaEventRecord(ev[6], st);
     return L + 1;
 }
@@ -519,6 +605,19 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
     auto itg = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
+    if (itg == ctx->graphs.end() && lazy(ctx) && !ctx->no_conditional) {
+        int L = 0;
+        armando_status gs = ctx->dim == 2 ? build_lazy_graph<2>(ctx, S, &exec, &L)
+                                          : build_lazy_graph<3>(ctx, S, &exec, &L);
+        if (gs == ARMANDO_OK) {
+            ctx->graphs[key] = exec;
+            ctx->launches_per_step = L;
+            itg = ctx->graphs.find(key);
+        } else {
+            ctx->no_conditional = true;  // the plain sequence below instead
+            exec = nullptr;
+        }
+    }
     if (itg == ctx->graphs.end()) {
         cudaGraph_t graph = nullptr;
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -538,6 +637,7 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     CK(cudaGraphLaunch(exec, ctx->stream));
     ctx->launches += ctx->launches_per_step;
     ctx->steps_done += 1;
+    if (!lazy(ctx)) ctx->sorts_host += 1;
     return ARMANDO_OK;
 }
 
@@ -568,8 +668,8 @@ armando_status alloc_state(armando_ctx* ctx) {
     F1(ctx->B.ulo, n);
     ctx->B.vr = dalloc<float4>(ctx->dim == 2 ? n : 1, e);
     ctx->owned.push_back(ctx->B.vr);
-    ctx->B.xsort = dalloc<float4>(n, e);
-    ctx->owned.push_back(ctx->B.xsort);
+    ctx->xsort_buf = dalloc<float4>(n, e);  // B.xsort points here while sorting lazily
+    ctx->owned.push_back(ctx->xsort_buf);
     ctx->B.nmask = dalloc<unsigned>(n * (ctx->dim == 2 ? mask_words<2>() : mask_words<3>()), e);
     ctx->B.mstride = (int)n;
     ctx->B.mtpp = 1;
@@ -1312,6 +1412,7 @@ armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
     ctx->B.mtpp = t.threads_per_particle;
     ctx->dp.reach = t.reach;
     ctx->dp.skin = 0.01f * (float)t.skin;
+    ctx->B.xsort = lazy(ctx) ? ctx->xsort_buf : nullptr;
     if (regrid) {
         if (ctx->n_inst > 1) {
             armando_status st = upload_batch_params(ctx);
@@ -1597,7 +1698,8 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float*
         cleanup();
         return s;
     }
-    int L = ctx->dim == 2 ? launch_grid_and_sort<2>(ctx, nullptr) : launch_grid_and_sort<3>(ctx, nullptr);
+    int L = ctx->dim == 2 ? launch_grid_and_sort<2>(ctx, nullptr, st)
+                          : launch_grid_and_sort<3>(ctx, nullptr, st);
     ctx->next_its = 0;  // A now holds these positions, not a step's state
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
@@ -1851,7 +1953,7 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
         }
     }
     out->device_flags = cctx->h_flags ? *cctx->h_flags : 0u;
-    out->sorts_done = cctx->sorts_done;
+    out->sorts_done = cctx->sorts_done + cctx->sorts_host;
     return ARMANDO_OK;
 }
 
@@ -1868,6 +1970,7 @@ armando_status armando_destroy(armando_ctx* ctx) {
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_grid) cudaFreeHost(ctx->h_grid);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     delete ctx;
     return ARMANDO_OK;
 }

@@ -174,11 +174,17 @@ __device__ __forceinline__ bool sort_skipped(const int* resort) {
     return resort != nullptr && *(volatile const int*)resort == 0;
 }
 
-__global__ void k_resort_advance(int* __restrict__ resort, int always, int* __restrict__ sorts) {
+__global__ void k_resort_advance(int* __restrict__ resort, int* __restrict__ sorts) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (resort[0] != 0) ++sorts[0];
-    resort[0] = always ? 1 : resort[1];
+    resort[0] = resort[1];
     resort[1] = 0;
+}
+
+// Head of a lazily sorting step graph: the IF node after it runs the grid,
+// hash, sort and cell-table kernels only when this iteration sorts.
+__global__ void k_resort_cond(cudaGraphConditionalHandle handle, const int* __restrict__ resort) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(handle, resort[0] != 0 ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------
