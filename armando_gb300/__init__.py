@@ -235,10 +235,15 @@ class Context:
             _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
             float(dt), int(its0), int(steps_per_trial), C.byref(best), ms))
         cands = self.tuning_candidates()
-        first = min(range(18), key=lambda k: ms[k] if ms[k] > 0 else float("inf"))
         table = {}
         for k in range(N_TUNINGS):
-            key = cands[k] if k < 18 else cands[first][:3] + (cands[k][3],)
+            key = cands[k]
+            if k >= 18:  # the skin on its reach's fastest skin-0 tuning
+                same = [j for j in range(18) if cands[j][0] == key[0] and ms[j] > 0]
+                if not same:
+                    continue
+                j = min(same, key=lambda j: ms[j])
+                key = cands[j][:3] + (key[3],)
             table[key] = float(ms[k])
         return best.as_tuple(), table
 

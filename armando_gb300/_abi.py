@@ -159,7 +159,7 @@ EXPORTED = [
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
 ]
-N_TUNINGS = 21
+N_TUNINGS = 27
 N_PHASES = 6
 PHASE_NAMES = ["grid_hash", "radix_sort", "cells_reorder", "density", "shear", "force"]
 

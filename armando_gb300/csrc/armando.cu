@@ -1459,8 +1459,8 @@ armando_status armando_tuning_candidate(int32_t k, armando_tuning* out) {
         return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "candidate index out of range");
     static const int tpp[3] = {1, 2, 4};
     static const int skin[3] = {10, 20, 40};
-    if (k >= 18) {  // a skin for the fastest of the first 18
-        *out = armando_tuning{0, 0, 0, skin[k - 18]};
+    if (k >= 18) {  // a skin for the fastest of the first 18 with this reach
+        *out = armando_tuning{1 + (k - 18) / 3, 0, 0, skin[(k - 18) % 3]};
         return ARMANDO_OK;
     }
     out->reach = 1 + k / 6;
@@ -1486,12 +1486,18 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
     CK(cudaEventCreate(&e1));
     armando_tuning win = ctx->tune;
     float win_ms = -1.f;
+    armando_tuning reach_win[4] = {};  // fastest of the first 18 per reach
+    float reach_ms[4] = {-1.f, -1.f, -1.f, -1.f};
     for (int k = 0; k < ARMANDO_N_TUNINGS; ++k) {
         armando_tuning t;
         armando_tuning_candidate(k, &t);
-        if (k >= 18) {  // second stage: the winner so far with a sort skin
+        if (k >= 18) {  // second stage: a sort skin on that reach's fastest tuning
+            if (reach_ms[t.reach] < 0.f) {
+                if (ms_per_step) ms_per_step[k] = -1.f;
+                continue;
+            }
             const int skin = t.skin;
-            t = win;
+            t = reach_win[t.reach];
             t.skin = skin;
         }
         float ms = -1.f;
@@ -1516,6 +1522,10 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
             if (win_ms < 0.f || ms < win_ms) {
                 win_ms = ms;
                 win = t;
+            }
+            if (k < 18 && (reach_ms[t.reach] < 0.f || ms < reach_ms[t.reach])) {
+                reach_ms[t.reach] = ms;
+                reach_win[t.reach] = t;
             }
         } else if (st == ARMANDO_ERR_CUDA) {
             break;  // a device error ends the search

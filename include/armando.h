@@ -284,9 +284,9 @@ armando_status armando_set_tuning(armando_ctx* ctx, const armando_tuning* t);
 
 /* The autotuner's candidate tunings, k = 0 .. ARMANDO_N_TUNINGS - 1: k < 18
  * every (reach, threads_per_particle, block) with skin 0; k >= 18 a skin
- * (10, 20, 40 percent) applied to the fastest of the first 18, returned here
- * with reach = threads_per_particle = block = 0. */
-#define ARMANDO_N_TUNINGS 21
+ * (10, 20, 40 percent) applied to the fastest of the first 18 with the same
+ * reach, returned here with threads_per_particle = block = 0. */
+#define ARMANDO_N_TUNINGS 27
 armando_status armando_tuning_candidate(int32_t k, armando_tuning* out);
 
 /*

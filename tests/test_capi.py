@@ -110,7 +110,7 @@ def test_tuning_candidates_enumerate_every_tuning(lib):
     assert sorted(got[:18]) == sorted((r, tp, b, 0) for r in (1, 2, 3) for tp in (1, 2, 4)
                                       for b in (128, 256))
     assert got[0] == (1, 1, 128, 0)  # link_list's grid, one thread per particle, no skin
-    assert got[18:] == [(0, 0, 0, 10), (0, 0, 0, 20), (0, 0, 0, 40)]
+    assert got[18:] == [(r, 0, 0, sk) for r in (1, 2, 3) for sk in (10, 20, 40)]
     t = _abi.Tuning()
     assert lib.armando_tuning_candidate(_abi.N_TUNINGS, C.byref(t)) == _abi.ERR_INVALID_ARG
     assert lib.armando_tuning_candidate(-1, C.byref(t)) == _abi.ERR_INVALID_ARG

@@ -142,7 +142,7 @@ def test_autotune_picks_a_candidate_and_leaves_inputs(O):
             assert np.array_equal(getattr(c, f), getattr(before, f)), f
         assert ctx.tuning().as_tuple() == best
         assert best[:3] + (0,) in CANDIDATES and best[3] in (0, 10, 20, 40)
-        assert set(CANDIDATES) <= set(table) and len(table) == 21
+        assert set(CANDIDATES) <= set(table) and len(table) == 27
         assert all(v > 0 for v in table.values())
         assert table[best] == min(table.values())
         errs, _, _ = step_errors(O, ctx, c, its=1)
