@@ -276,7 +276,7 @@ int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st) {
             ctx->hist, ctx->dtotal, ctx->num_tiles, rs);
         L += 2;
     }
-    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(ctx->keys[ctx->passes & 1], n,
+    k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(ctx->keys[ctx->passes & 1], n,
                                                                    &ctx->grid->ncells, (int)ctx->cell_cap,
                                                                    ctx->start, rs);
     return L + 1;
@@ -499,7 +499,7 @@ int launch_batch_step(armando_ctx* ctx, cudaEvent_t* ev) {
     }
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(skeys, n, ctx->d_total_cells,
+    k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(skeys, n, ctx->d_total_cells,
                                                                    (int)ctx->cell_cap, ctx->start);
     k_reorder_batch<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, ctx->d_params,
                                                              ctx->d_its, n);
@@ -561,7 +561,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     cudaEventRecord(ev[2], st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_cell_start<<<blocks_for((int64_t)n + 1, 256), 256, 0, st>>>(skeys, n, &ctx->grid->ncells,
+    k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(skeys, n, &ctx->grid->ncells,
                                                                    (int)ctx->cell_cap, ctx->start, rs);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     cudaEventRecord(ev[3], st);

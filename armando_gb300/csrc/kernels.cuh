@@ -599,16 +599,22 @@ __global__ void __launch_bounds__(kSortThreads)
 // [0, ncells]; empty cells get start[c] == start[c+1]. One thread per slot
 // s in [0, n]: slot s is the first slot of every cell in (key[s-1], key[s]]
 // (slot n: of every cell after the last key, up to ncells), so each entry is
-// written exactly once. A lane whose run is longer than a warp hands it to the
-// whole warp (empty regions of the grid), which writes it 32 entries at a time.
-// Entries past `cap` (the table's last index) are never written.
-__global__ void __launch_bounds__(256)
+// written exactly once. Runs longer than a warp (empty regions of the grid;
+// neighbouring slots often own one each, e.g. the empty rows between two walls)
+// are queued in shared memory and written by the whole block, 256 entries at a
+// time. Entries past `cap` (the table's last index) are never written.
+constexpr int kCellStartThreads = 256;
+
+__global__ void __launch_bounds__(kCellStartThreads)
     k_cell_start(const unsigned* __restrict__ keys, int n, const int* __restrict__ ncells_total,
                  int cap, int* __restrict__ start,
     const int* __restrict__ resort = nullptr) {
     if (sort_skipped(resort)) return;
+    __shared__ int q_lo[kCellStartThreads], q_hi[kCellStartThreads], q_s[kCellStartThreads];
+    __shared__ int q_n;
+    if (threadIdx.x == 0) q_n = 0;
+    __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
     const bool valid = s <= n;
     int lo = 0, hi = -1;  // cells [lo, hi] start at slot s
     if (valid) {
@@ -617,16 +623,19 @@ __global__ void __launch_bounds__(256)
         hi = (s == n) ? nc : (int)__ldg(keys + s);
         hi = min(hi, cap);
     }
-    const bool big = hi - lo + 1 > 32;
-    if (!big)
+    if (hi - lo + 1 <= 32) {
         for (int c = lo; c <= hi; ++c) start[c] = s;
-    unsigned m = __ballot_sync(0xffffffffu, big);
-    while (m) {
-        const int l = __ffs(m) - 1;
-        m &= m - 1u;
-        const int blo = __shfl_sync(0xffffffffu, lo, l), bhi = __shfl_sync(0xffffffffu, hi, l);
-        const int bs = __shfl_sync(0xffffffffu, s, l);
-        for (int c = blo + lane; c <= bhi; c += 32) start[c] = bs;
+    } else {
+        const int k = atomicAdd(&q_n, 1);  // at most one entry per thread
+        q_lo[k] = lo;
+        q_hi[k] = hi;
+        q_s[k] = s;
+    }
+    __syncthreads();
+    const int nq = q_n;
+    for (int q = 0; q < nq; ++q) {
+        const int bs = q_s[q], bhi = q_hi[q];
+        for (int c = q_lo[q] + (int)threadIdx.x; c <= bhi; c += kCellStartThreads) start[c] = bs;
     }
 }
 
@@ -1299,8 +1308,8 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 const float dr2 = sph::dist2_exact<DIM>(dh);
                 const float gw = sph::wendland_grad_factor<DIM>(
                     fast_sqrt_pos(dr2), ih.hi, __fmul_rn(P.kg, pow_grad<DIM>(ih.hi)));
-                float vd = (vj.x - vi.x) * dh[0] + (vj.y - vi.y) * dh[1];
-                if (DIM == 3) vd += (vj.z - vi.z) * dh[2];
+                float vd = fmaf(vj.y - vi.y, dh[1], __fmul_rn(vj.x - vi.x, dh[0]));
+                if (DIM == 3) vd = fmaf(vj.z - vi.z, dh[2], vd);
                 divs = fmaf(mj * gw, vd, divs);
             }
         }
@@ -1321,7 +1330,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 kgih = P.kg * pow_grad<DIM>(ih);
                 kwh = P.kw_hi * (DIM == 2 ? ih * ih : ih * ih * ih);
             }
-            const float q = fast_sqrt_pos(dr2) * ih;
+            const float q = __fmul_rn(fast_sqrt_pos(dr2), ih);
             if (fluid) {
                 float tt = fmaf(-0.5f, q, 1.0f);
                 tt = tt * tt;
@@ -1331,8 +1340,8 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             if (need_div) {
                 const float t3 = q - 2.0f;
                 const float gw = kgih * t3 * t3 * t3;
-                float vd = (vj.x - vi.x) * d[0] + (vj.y - vi.y) * d[1];
-                if (DIM == 3) vd += (vj.z - vi.z) * d[2];
+                float vd = fmaf(vj.y - vi.y, d[1], __fmul_rn(vj.x - vi.x, d[0]));
+                if (DIM == 3) vd = fmaf(vj.z - vi.z, d[2], vd);
                 divs = fmaf(mj * gw, vd, divs);
             }
         }
@@ -1380,7 +1389,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rho, rho)) : p;
     if (need_div) {
         const float divv = __fdiv_rn(divs, rho);
-        rp.w = P.ah_g1 * xi.w * P.c0 + P.ah_g2 * xi.w * xi.w * (fabsf(divv) - divv);
+        rp.w = fmaf(P.ah_g2 * xi.w * xi.w, fabsf(divv) - divv, __fmul_rn(P.ah_g1 * xi.w, P.c0));
     }
     B.rp[s] = rp;
     if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
@@ -1591,29 +1600,31 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 ih = __fdividef(2.0f, xi.w + xj.w);
                 kgih = P.kg * pow_grad<DIM>(ih);
             }
-            const float q = fast_sqrt_pos(dr2) * ih;
+            const float q = __fmul_rn(fast_sqrt_pos(dr2), ih);
             const float t3 = q - 2.0f;
             const float gw = kgih * t3 * t3 * t3;
             const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;
             const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = (DIM == 3) ? vj.z - vi.z : 0.f;
             // Pressure (internal_force.f:309-428 for pa_sph 1, 179-306 for pa_sph 0).
             const float fs = -(rpi.y + rpj.y);
+            // Products that feed a sum are written out (fmaf / __fmul_rn) so that
+            // every instantiation of this body rounds alike (no free contraction).
             float h0 = fs * w0, h1 = fs * w1, h2 = fs * w2;
-            float he = vx * h0 + vy * h1;
-            if (DIM == 3) he += vz * h2;
+            float he = fmaf(vy, h1, __fmul_rn(vx, h0));
+            if (DIM == 3) he = fmaf(vz, h2, he);
             if (visc) {
                 const float4 tj = __ldg(B.tau + k);
                 float4 tj2 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (DIM == 3) tj2 = __ldg(B.tau2 + k);
                 const float sxx = ti.x + tj.x, syy = ti.y + tj.y, sxy = ti.z + tj.z;
                 if (DIM == 2) {
-                    h0 += sxx * w0 + sxy * w1;
-                    h1 += sxy * w0 + syy * w1;
+                    h0 = fmaf(sxy, w1, fmaf(sxx, w0, h0));
+                    h1 = fmaf(syy, w1, fmaf(sxy, w0, h1));
                 } else {
                     const float szz = ti.w + tj.w, sxz = ti2.x + tj2.x, syz = ti2.y + tj2.y;
-                    h0 += sxx * w0 + sxy * w1 + sxz * w2;
-                    h1 += sxy * w0 + syy * w1 + syz * w2;
-                    h2 += sxz * w0 + syz * w1 + szz * w2;
+                    h0 = fmaf(sxz, w2, fmaf(sxy, w1, fmaf(sxx, w0, h0)));
+                    h1 = fmaf(syz, w2, fmaf(syy, w1, fmaf(sxy, w0, h1)));
+                    h2 = fmaf(szz, w2, fmaf(syz, w1, fmaf(sxz, w0, h2)));
                 }
             }
             if (P.pa_sph != 1) {
@@ -1631,26 +1642,27 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             const float rho_bar = 0.5f * (rpi.x + rpj.x);
             // art_visc.f:71-100.
             if (P.visc_art) {
-                float vr = vx * d[0] + vy * d[1];
-                if (DIM == 3) vr += vz * d[2];
+                float vr = fmaf(vy, d[1], __fmul_rn(vx, d[0]));
+                if (DIM == 3) vr = fmaf(vz, d[2], vr);
                 if (vr > 0.f) {  // (v_i - v_j) . (x_i - x_j) = -vr < 0
-                    const float phi = __fdividef(-mh * vr, dr2 + mh * mh * P.av_eta2);
-                    const float piv = __fdividef((P.av_beta * phi - P.av_alpha * P.c0) * phi, rho_bar);
+                    const float phi = __fdividef(-mh * vr, fmaf(__fmul_rn(mh, mh), P.av_eta2, dr2));
+                    const float piv = __fdividef(
+                        fmaf(P.av_beta, phi, -__fmul_rn(P.av_alpha, P.c0)) * phi, rho_bar);
                     const float mp = mj * piv;
                     a0 = fmaf(-mp, w0, a0);
                     a1 = fmaf(-mp, w1, a1);
                     if (DIM == 3) a2 = fmaf(-mp, w2, a2);
-                    float vdw = vx * w0 + vy * w1;
-                    if (DIM == 3) vdw += vz * w2;
+                    float vdw = fmaf(vy, w1, __fmul_rn(vx, w0));
+                    if (DIM == 3) vdw = fmaf(vz, w2, vdw);
                     av_du = fmaf(-0.5f * mp, vdw, av_du);
                 }
             }
             // art_heat.f:69-97.
             if (heat_art) {
-                float rdw = d[0] * w0 + d[1] * w1;
-                if (DIM == 3) rdw += d[2] * w2;
-                const float psi =
-                    __fdividef(rpi.w + rpj.w, rho_bar * (dr2 + mh * mh * P.ah_eta2)) * rdw;
+                float rdw = fmaf(d[1], w1, __fmul_rn(d[0], w0));
+                if (DIM == 3) rdw = fmaf(d[2], w2, rdw);
+                const float psi = __fdividef(
+                    rpi.w + rpj.w, rho_bar * fmaf(__fmul_rn(mh, mh), P.ah_eta2, dr2)) * rdw;
                 const float du_ij = (rpi.z - rpj.z) + (ulo_i - __ldg(B.ulo + k));
                 ah_du = fmaf(mj * psi, du_ij, ah_du);
             }
@@ -1665,14 +1677,14 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         ah_du = group_sum<TPP>(ah_du);
     }
     if (!work || sub != 0) return;
-    float du = 0.5f * he_sum + av_du + ah_du;  // internal_force.f:433-435
+    float du = __fadd_rn(fmaf(0.5f, he_sum, av_du), ah_du);  // internal_force.f:433-435
     if (visc) du += B.tds[s];
     if (S.heat_on) {
         float e0 = xi.x - P.heat_center[0], e1 = xi.y - P.heat_center[1];
-        float dd = e0 * e0 + e1 * e1;
+        float dd = fmaf(e1, e1, __fmul_rn(e0, e0));
         if (DIM == 3) {
             float e2 = xi.z - P.heat_center[2];
-            dd += e2 * e2;
+            dd = fmaf(e2, e2, dd);
         }
         du += P.heat_q0 * expf(-dd * P.heat_k) / rpi.x;
     }
