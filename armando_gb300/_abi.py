@@ -67,6 +67,7 @@ class Params(C.Structure):
         ("heat_t_end", C.c_float),
         ("period_lo", F3),
         ("period_hi", F3),
+        ("wall_model", C.c_int32),
     ]
 
     @classmethod

@@ -180,12 +180,17 @@ armando_status validate_params(const armando_params* p, int dim, std::string& wh
             why = "periodic axis needs period_hi > period_lo";
             return ARMANDO_ERR_INVALID_ARG;
         }
+    if (p->wall_model < 0 || p->wall_model > 2) {
+        why = "wall_model must be 0, 1 or 2";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
     return ARMANDO_OK;
 }
 
 DevParams make_dev_params(const armando_params& p, int reach = 1) {
     DevParams d{};
     d.reach = reach;
+    d.wall_model = p.wall_model;
     d.dim = p.dim;
     d.pa_sph = p.pa_sph;
     d.visc = p.visc;
@@ -318,7 +323,7 @@ void with_tuning(const armando_tuning& t, bool per, bool lean, F&& f) {
 }
 
 bool any_periodic(const DevParams& p) { return p.periodic[0] || p.periodic[1] || p.periodic[2]; }
-bool lean_physics(const DevParams& p) { return !p.visc && !p.heat_art; }
+bool lean_physics(const DevParams& p) { return !p.visc && !p.heat_art && p.wall_model == 0; }
 
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
@@ -1064,9 +1069,10 @@ armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
 armando_status check_adjoint_support(armando_ctx* ctx) {
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
     const armando_params& p = ctx->prm;
-    if (p.pa_sph != 1 || p.visc || p.heat_artificial)
+    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
-                    "reverse mode supports pa_sph = 1 without physical viscosity and artificial heat");
+                    "reverse mode supports pa_sph = 1, wall_model 0, without physical viscosity "
+                    "and artificial heat");
     return ARMANDO_OK;
 }
 

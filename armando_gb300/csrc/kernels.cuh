@@ -74,6 +74,8 @@ struct DevParams {
     float heat_t_end;    // external heat gate its*dt <= heat_t_end
     int reach;           // neighbour-grid cells per support radius (tuning; 1 = link_list)
     float skin;          // sort skin as a fraction of max h (tuning; 0 = sort every step)
+    int wall_model;      // pairs of different itype: 0 like any pair, 1 push only, 2 both
+    int pad_;
 };
 
 struct StepArgs {
@@ -1215,12 +1217,14 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     const bool need_div = !LEAN && P.heat_art != 0;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
     float p = 0.f;
+    int it_i = 0;
     bool fluid = false;
     if (valid) {
         xi = B.xh[s];
         rp = B.rp[s];
         p = B.p[s];
-        fluid = B.itype[s] > 0;
+        it_i = B.itype[s];
+        fluid = it_i > 0;
         vi = B.vm[s];
     }
     const bool work = valid && g.ok && (fluid || need_div);
@@ -1292,6 +1296,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         for (int t = 0; t < mn; ++t) {
             if (t >= nn) continue;
             const int k = s_near[t][tid];
+            if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;  // push only
             const float4 xj = __ldg(B.xh + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
             if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
@@ -1317,6 +1322,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         for (int t = 0; t < mf; ++t) {
             if (t >= nf) continue;
             const int k = s_far[t][tid];
+            if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;
             const float4 xj = __ldg(B.xh + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
             if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
@@ -1601,6 +1607,30 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 kgih = P.kg * pow_grad<DIM>(ih);
             }
             const float q = __fmul_rn(fast_sqrt_pos(dr2), ih);
+            if (!LEAN && P.wall_model != 0 && __ldg(B.itype + k) != it) {
+                // Push between particles of different type (ArmandoThrust/armando.cu:507-513
+                // for wall_model 1, acpu.c:424-429 for 2) along (x_i - x_j)/r, c = c0.
+                const float r = fast_sqrt_pos(dr2);
+                if (r > 0.f) {
+                    float tt = fmaf(-0.5f, q, 1.0f);
+                    tt = tt * tt;
+                    tt = tt * tt;
+                    tt *= fmaf(2.0f, q, 1.0f);  // W / W(0)
+                    const float c2 = P.c0 * P.c0;
+                    float f;
+                    if (P.wall_model == 1) {
+                        const float alpha = P.kw_hi * (DIM == 2 ? ih * ih : ih * ih * ih);
+                        f = 0.5f * alpha * tt * mj / (rpj.x * xj.w) * c2;
+                    } else {
+                        f = 0.02f * tt * c2 / r * mj / (mass_of<DIM>(xi, vi) + mj);
+                    }
+                    f /= r;
+                    a0 = fmaf(f, d[0], a0);
+                    a1 = fmaf(f, d[1], a1);
+                    if (DIM == 3) a2 = fmaf(f, d[2], a2);
+                }
+                if (P.wall_model == 1) continue;  // no other interaction
+            }
             const float t3 = q - 2.0f;
             const float gw = kgih * t3 * t3 * t3;
             const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;

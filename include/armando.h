@@ -80,6 +80,16 @@ typedef struct armando_params {
     float heat_t_end;         /* source active while its*dt <= heat_t_end (fluka_heat gate) */
     float period_lo[3];       /* periodic box lower bound per axis                          */
     float period_hi[3];       /* periodic box upper bound per axis                          */
+    int32_t wall_model;       /* how particles of different itype interact:
+                                 0 = CERN virtual particles: like any pair (density.f,
+                                     internal_force.f);
+                                 1 = GPU-C device kernel (ArmandoThrust/armando.cu:472-513):
+                                     no density, pressure or viscosity between them; i is
+                                     pushed from j by 0.5 W m_j/(rho_j h_j) c_j^2;
+                                 2 = GPU-C host path (ArmandoThrust/acpu.c:390-429): like
+                                     any pair, plus a push 0.02 (W/W(0)) c_i c_j
+                                     m_j/((m_i + m_j) r). Pushes act along (x_i - x_j)/r on
+                                     momentum only; c = c0; W at h = (h_i + h_j)/2.     */
 } armando_params;
 
 /* Per-step statistics of the last completed call. */

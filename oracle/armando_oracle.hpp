@@ -58,6 +58,7 @@ struct Params {
     R heat_q0 = R(0), heat_sigma = R(1), heat_center[3] = {R(0), R(0), R(0)};
     double heat_t_end = INFINITY;
     double period_lo[3] = {0, 0, 0}, period_hi[3] = {0, 0, 0};
+    int wall_model = 0;  // pairs of different itype: 0 like any pair, 1 push only, 2 both
 };
 
 // ---------------------------------------------------------------------------
@@ -538,6 +539,58 @@ void art_heat(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const Pa
     }
 }
 
+// Pairs of equal and of different itype. Returns the pairs the density, force
+// and heat sums run over: all of them, except for wall_model 1, where pairs of
+// different itype take part in none of those sums (ArmandoThrust/armando.cu:
+// 472-506 acts on same-material pairs only) and only push (wall_repulsion).
+template <class R>
+const PairList& split_by_itype(const State<R>& s, const Params<R>& P, const PairList& pl,
+                               PairList& same, PairList& other) {
+    if (P.wall_model == 0) return pl;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        PairList& dst = (s.itype[pl.pi[k]] == s.itype[pl.pj[k]]) ? same : other;
+        dst.pi.push_back(pl.pi[k]);
+        dst.pj.push_back(pl.pj[k]);
+    }
+    return (P.wall_model == 1) ? same : pl;
+}
+
+// Push between particles of different itype (the GPU-C codes' boundary
+// repulsion, momentum only, along (x_i - x_j)/r, c = c0, W at h = (h_i+h_j)/2):
+//   wall_model 1, ArmandoThrust/armando.cu:507-513:  f = 0.5 W m_j / (rho_j h_j) c_j^2
+//   wall_model 2, ArmandoThrust/acpu.c:424-429:      f = 0.02 (W / W(0)) c_i c_j / r
+//                                                        * m_j / (m_i + m_j)
+// (the reference evaluates W with h_i; identical for uniform h). A coincident
+// pair has no direction and pushes nothing. Walls are not integrated, so only
+// fluid particles keep their rate.
+template <class R, class Rc>
+void wall_repulsion(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+                    std::vector<R>& dvdt) {
+    const int dim = s.dim;
+    dvdt.assign(s.n * dim, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        if (!(pg.r > R(0))) continue;
+        const R w_rel = pg.w / kernel_w(R(0), pg.mh, dim, P.kernel_3d_legacy);
+        R fi, fj;  // push on i (from j) and on j (from i), per unit (x_i - x_j)/r
+        if (P.wall_model == 1) {
+            fi = R(0.5) * pg.w * s.m[j] / (s.rho[j] * s.h[j]) * s.c[j] * s.c[j];
+            fj = R(0.5) * pg.w * s.m[i] / (s.rho[i] * s.h[i]) * s.c[i] * s.c[i];
+        } else {
+            const R base = R(0.02) * w_rel * s.c[i] * s.c[j] / pg.r;
+            fi = base * s.m[j] / (s.m[i] + s.m[j]);
+            fj = base * s.m[i] / (s.m[i] + s.m[j]);
+        }
+        for (int d = 0; d < dim; ++d) {
+            const R e = pg.dx[d] / pg.r;
+            if (s.fluid(i)) dvdt[(int64_t)i * dim + d] = dvdt[(int64_t)i * dim + d] + fi * e;
+            if (s.fluid(j)) dvdt[(int64_t)j * dim + d] = dvdt[(int64_t)j * dim + d] - fj * e;
+        }
+    }
+}
+
 // External volumetric heat, du_i += q(x_i)/rho_i (fluka_heat.f:337-338), with
 // q(x) = q0 exp(-|x - xc|^2 / (2 sigma^2)).
 template <class R>
@@ -563,15 +616,18 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
                  double dt, Rates<R>& out) {
     const int dim = s.dim;
     const int64_t n = s.n;
-    sum_density(s, g, P, pl);
+    PairList same, other;
+    const PairList& body = split_by_itype(s, P, pl, same, other);
+    sum_density(s, g, P, body);
     for (int64_t i = 0; i < n; ++i) {
         s.c[i] = P.c0;
         if (s.fluid(i)) eos_tait(s.rho[i], s.p[i], P);
     }
-    std::vector<R> indvdt, indudt, avdvdt, avdudt, ahdudt, exdudt;
-    int_force(s, g, P, pl, indvdt, indudt, out.tdsdt);
-    if (P.visc_artificial) art_visc(s, g, P, pl, avdvdt, avdudt);
-    if (P.heat_artificial) art_heat(s, g, P, pl, ahdudt, out.divv);
+    std::vector<R> indvdt, indudt, avdvdt, avdudt, ahdudt, exdudt, rpdvdt;
+    int_force(s, g, P, body, indvdt, indudt, out.tdsdt);
+    if (P.visc_artificial) art_visc(s, g, P, body, avdvdt, avdudt);
+    if (P.heat_artificial) art_heat(s, g, P, body, ahdudt, out.divv);
+    if (P.wall_model != 0) wall_repulsion(s, g, P, other, rpdvdt);
     if (P.heat_external && (double(its) * dt <= P.heat_t_end)) ext_heat(s, P, exdudt);
     out.dv.assign(n * dim, R(0));
     out.du.assign(n, R(0));
@@ -580,6 +636,7 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
         for (int d = 0; d < dim; ++d) {
             R a = indvdt[i * dim + d] + P.gravity[d];
             if (P.visc_artificial) a = a + avdvdt[i * dim + d];
+            if (P.wall_model != 0) a = a + rpdvdt[i * dim + d];
             out.dv[i * dim + d] = a;
         }
         R du = indudt[i];

@@ -42,6 +42,7 @@ ao::Params<R> to_params(const armando_params* p) {
     P.heat_q0 = R(p->heat_q0);
     P.heat_sigma = R(p->heat_sigma);
     P.heat_t_end = p->heat_t_end;
+    P.wall_model = p->wall_model;
     return P;
 }
 
@@ -170,12 +171,18 @@ int ao_forces_f64(const armando_params* prm, int64_t n, const double* x, const d
     } catch (const std::exception&) {
         return 1;
     }
-    std::vector<double> dv, du, tds, avdv, avdu;
-    ao::int_force(s, g, P, pl, dv, du, tds);
+    std::vector<double> dv, du, tds, avdv, avdu, rpdv;
+    ao::PairList same, other;
+    const ao::PairList& body = ao::split_by_itype(s, P, pl, same, other);
+    ao::int_force(s, g, P, body, dv, du, tds);
     if (P.visc_artificial) {
-        ao::art_visc(s, g, P, pl, avdv, avdu);
+        ao::art_visc(s, g, P, body, avdv, avdu);
         for (size_t k = 0; k < dv.size(); ++k) dv[k] += avdv[k];
         for (size_t k = 0; k < du.size(); ++k) du[k] += avdu[k];
+    }
+    if (P.wall_model != 0) {
+        ao::wall_repulsion(s, g, P, other, rpdv);
+        for (size_t k = 0; k < dv.size(); ++k) dv[k] += rpdv[k];
     }
     std::memcpy(dvdt, dv.data(), sizeof(double) * n * P.dim);
     std::memcpy(dudt, du.data(), sizeof(double) * n);
@@ -230,6 +237,7 @@ int ao_integrate_gather_f64(const armando_params* prm, int64_t n, int its0, int 
                             double* u, const double* h, const int* itype, double* dvdt,
                             double* dudt, int nthreads) {
     ao::Params<double> P = to_params<double>(prm);
+    if (P.wall_model != 0) return 2;  // the gather form restates wall_model 0 only
     ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
     try {
         for (int k = 0; k < steps; ++k) ao::leapfrog_step_gather(s, P, its0 + k, dt, nthreads);

@@ -8,7 +8,9 @@ oracle/_ref/libacpu.so from ArmandoThrust/acpu.c (oracle/Makefile, target
   updateHashHost                            acpu.c:2085-2105
   updateSetsHost + updateListHost           acpu.c:2135-2243 (MAXN = 21)
   balanceMassMomentumHost (v = 0, one material: only the pressure action
-                           -(P_i + P_j)/(rho_i rho_j) dW/dr (x_i - x_j)/r acts)
+                           -(P_i + P_j)/(rho_i rho_j) dW/dr (x_i - x_j)/r acts;
+                           two materials: plus the boundary repulsion of
+                           different-material pairs, acpu.c:424-429)
                                             acpu.c:346-437
 The cell tables are padded with empty guard cells because updateListHost
 visits cell ids ic +- nX*nY without bounds checks in 2D.
@@ -159,6 +161,19 @@ def main(ref_dir="/root/reference"):
     acc_u[order, 0] = vdx
     acc_u[order, 1] = vdy
     out["force_acc_uniform_rho"] = acc_u.ravel()
+    # Two materials: the lowest rows of the lattice are material 2.
+    y_cut = np.quantile(x[:, 1], 0.25)
+    mat2 = np.where(x[:, 1] < y_cut, 2, 1).astype(np.int32)
+    msort[:] = mat2[order]
+    dsort[:] = dens[order]
+    for a in (ddot, vdx, vdy, vdz):
+        a[:] = 0.0
+    L.balanceMassMomentumHost(n, *args)
+    acc_m = np.zeros((n, 2), np.float32)
+    acc_m[order, 0] = vdx
+    acc_m[order, 1] = vdy
+    out["force_mat"] = mat2
+    out["force_acc_two_materials"] = acc_m.ravel()
     path = os.path.join(HERE, "acpu_pins.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, {k: v.shape for k, v in out.items()})

@@ -61,9 +61,10 @@ def test_struct_layout_matches_c():
 #include <stddef.h>
 #include "armando.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu\n", sizeof(armando_params), offsetof(armando_params, rho0),
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(armando_params), offsetof(armando_params, rho0),
          offsetof(armando_params, gravity), offsetof(armando_params, period_hi),
-         sizeof(armando_stats), offsetof(armando_stats, device_flags));
+         sizeof(armando_stats), offsetof(armando_stats, device_flags),
+         offsetof(armando_params, wall_model));
   return 0;
 }'''
     with tempfile.TemporaryDirectory() as d:
@@ -74,7 +75,7 @@ int main(void) {
         got = list(map(int, subprocess.run([exe], capture_output=True, text=True).stdout.split()))
     P, S = _abi.Params, _abi.Stats
     assert got == [C.sizeof(P), P.rho0.offset, P.gravity.offset, P.period_hi.offset,
-                   C.sizeof(S), S.device_flags.offset]
+                   C.sizeof(S), S.device_flags.offset, P.wall_model.offset]
 
 
 def test_params_default_matches_python(lib):

@@ -105,3 +105,16 @@ def test_batch_rejects_single_only_calls():
         with pytest.raises(ag.ArmandoError) as e:
             b.cell_ids(insts[0].x, insts[0].h)
         assert e.value.status == ag._abi.ERR_UNSUPPORTED
+
+
+def test_batch_of_boundary_models_matches_instances_alone():
+    """Instances with different wall models (0, 1, 2) in one batch."""
+    insts = _instances_2d()[:3]
+    insts[1].params.wall_model = 1
+    insts[2].params.wall_model = 2
+    _packed_ok(insts)
+    outs = _run_batch(insts, 1, 4)
+    for k, c in enumerate(insts):
+        alone = _run_single(c, 1, 4)
+        for f in FIELDS:
+            assert np.array_equal(getattr(outs[k], f), getattr(alone, f)), (k, f)

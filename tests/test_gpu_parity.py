@@ -51,6 +51,10 @@ def small_cases():
 
 
 def _case(name):
+    if name.endswith(("_w1", "_w2")):  # the GPU-C boundary models
+        c = small_cases()[name[:-3]]
+        c.params.wall_model = int(name[-1])
+        return c
     c = small_cases()[name]
     if name == "dambreak_pa0":
         c.params.pa_sph = 0
@@ -88,7 +92,8 @@ def test_neighbour_sets_bit_exact(O, name):
     assert len(qi) == len(pi)
 
 
-@pytest.mark.parametrize("name", ["cavity", "dambreak", "dambreak_pa0", "channel3d"])
+@pytest.mark.parametrize("name", ["cavity", "dambreak", "dambreak_pa0", "channel3d",
+                                  "dambreak_w1", "dambreak_w2", "channel3d_w2", "cavity_w1"])
 def test_one_step_parity(O, name):
     c = history_state(O, _case(name), steps=2)
     with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:

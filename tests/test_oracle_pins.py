@@ -56,3 +56,20 @@ def test_pressure_force_pa_sph1_matches_acpu_uniform_rho(O, golden):
     dv, _ = O.forces(P, x, np.zeros_like(x), golden["force_mass"], np.full(n, 1000.0),
                      golden["force_p"], np.zeros(n), golden["lattice_h"], np.ones(n, np.int32))
     assert np.abs(dv - golden["force_acc_uniform_rho"]).max() <= 2e-6 * np.abs(dv).max()
+
+
+def test_boundary_repulsion_matches_acpu_two_materials(O, golden):
+    """wall_model 2 (acpu.c:424-429): pressure action of every pair plus the
+    repulsion 0.02 (W/W0) c_i c_j m_j / ((m_i + m_j) r) between particles of
+    different material, against the reference's own compiled host path."""
+    n = golden["lattice_h"].size
+    x = golden["lattice_x"]
+    mat = golden["force_mat"].astype(np.int32)
+    P = Params.default(dim=2, pa_sph=0, rho0=1000.0, c0=20.0)
+    P.wall_model = 2
+    dv, _ = O.forces(P, x, np.zeros_like(x), golden["force_mass"], golden["force_rho"],
+                     golden["force_p"], np.zeros(n), golden["lattice_h"], mat)
+    ref = golden["force_acc_two_materials"]
+    assert np.abs(dv - ref).max() <= 2e-6 * np.abs(dv).max()
+    # the repulsion is a visible part of the result, not rounding
+    assert np.abs(ref - golden["force_acc"]).max() > 1e-2 * np.abs(ref).max()
