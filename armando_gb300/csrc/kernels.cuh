@@ -1416,8 +1416,10 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
     const float ihf = __frcp_rn(xi.w);
     const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
     float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // xx yy zz xy xz yz
+    const int it_i = B.itype[s];
     for_candidates<DIM>(g, start, cc, [&](int k) {
         if (k == s) return;
+        if (P.wall_model == 1 && __ldg(B.itype + k) != it_i) return;  // push only
         const float4 xj = __ldg(B.xh + k);
         float d[3], dr2;
         if (!pair_delta<DIM>(xi, xj, g, d, dr2)) return;
@@ -1434,17 +1436,20 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
         const float w0 = gw * d[0], w1 = gw * d[1], w2 = gw * d[2];
         const float dv0 = vj.x - vi.x, dv1 = vj.y - vi.y, dv2 = (DIM == 3) ? vj.z - vi.z : 0.f;
         float hxx, hyy, hzz = 0.f, hxy, hxz = 0.f, hyz = 0.f;
+        // explicit fused / unfused products: every instantiation rounds alike
+        const float e00 = __fmul_rn(dv0, w0), e11 = __fmul_rn(dv1, w1);
         if (DIM == 2) {
-            hxx = 2.f * dv0 * w0 - dv1 * w1;
-            hyy = 2.f * dv1 * w1 - dv0 * w0;
-            hxy = dv0 * w1 + dv1 * w0;
+            hxx = fmaf(2.f, e00, -e11);
+            hyy = fmaf(2.f, e11, -e00);
+            hxy = fmaf(dv1, w0, __fmul_rn(dv0, w1));
         } else {
-            hxx = 2.f * dv0 * w0 - dv1 * w1 - dv2 * w2;
-            hyy = 2.f * dv1 * w1 - dv0 * w0 - dv2 * w2;
-            hzz = 2.f * dv2 * w2 - dv0 * w0 - dv1 * w1;
-            hyz = dv1 * w2 + dv2 * w1;
-            hxz = dv0 * w2 + dv2 * w0;
-            hxy = dv0 * w1 + dv1 * w0;
+            const float e22 = __fmul_rn(dv2, w2);
+            hxx = fmaf(2.f, e00, -e11) - e22;
+            hyy = fmaf(2.f, e11, -e00) - e22;
+            hzz = fmaf(2.f, e22, -e00) - e11;
+            hyz = fmaf(dv2, w1, __fmul_rn(dv1, w2));
+            hxz = fmaf(dv2, w0, __fmul_rn(dv0, w2));
+            hxy = fmaf(dv1, w0, __fmul_rn(dv0, w1));
         }
         const float c = mj / rhoj;
         const float c23 = c * (2.f / 3.f);
@@ -1455,8 +1460,8 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
         t[4] = fmaf(c, hxz, t[4]);
         t[5] = fmaf(c, hyz, t[5]);
     });
-    float q = t[0] * t[0] + t[1] * t[1] + 2.f * t[3] * t[3];
-    if (DIM == 3) q += t[2] * t[2] + 2.f * t[5] * t[5] + 2.f * t[4] * t[4];
+    float q = fmaf(2.f * t[3], t[3], fmaf(t[1], t[1], __fmul_rn(t[0], t[0])));
+    if (DIM == 3) q = fmaf(2.f * t[4], t[4], fmaf(2.f * t[5], t[5], fmaf(t[2], t[2], q)));
     B.tds[s] = 0.5f * P.eta / rhoi * q;
     const float sc = (P.pa_sph == 1) ? P.eta / (rhoi * rhoi) : P.eta;
     B.tau[s] = make_float4(sc * t[0], sc * t[1], sc * t[3], sc * t[2]);
