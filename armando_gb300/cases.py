@@ -313,3 +313,15 @@ def sweep(n_instances: int = 512, seed: int = 4, n_min: float = 2.0e3, n_max: fl
         c.meta.update(alpha=alpha, c0=c0, aspect=aspect, index=k)
         out.append(c)
     return out
+
+
+def sweep_subset(case_list, smallest: int = 64, strata: int = 16):
+    """Indices of the instances a CPU check of a sweep covers: the `smallest`
+    instances by particle count, plus one instance from the middle of each of
+    `strata` equal slices of the others in size order. Sorted ascending."""
+    order = sorted(range(len(case_list)), key=lambda k: (case_list[k].n, k))
+    pick = set(order[:smallest])
+    rest = order[smallest:]
+    for q in range(min(strata, len(rest))):
+        pick.add(rest[int((q + 0.5) * len(rest) / strata)])
+    return sorted(pick)

@@ -88,6 +88,8 @@ def parse():
     ap.add_argument("--profile-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-suite", action="store_true",
+                    help="time only the FP64 oracle over every benchmark workload (host cores)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 3D channel and batched-sweep workloads")
     ap.add_argument("--extra-steps", type=int, default=20)
@@ -242,33 +244,85 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(case, budget_s):
-    """FP64 oracle (threaded gather form) on all host threads, bounded steps."""
+def _oracle():
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O  # the checker's CPU restatement
 
+    return O
+
+
+def _time_oracle(O, st, its0, dt, threads, budget_s, max_steps):
+    """Gather-form FP64 oracle steps from iteration its0 on `threads` threads
+    until budget_s has elapsed (at least one step). Returns (steps, seconds)."""
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        O.integrate_gather(st, its0 + steps, 1, dt, threads)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= max_steps:
+            return steps, el
+
+
+def cpu_baseline(case, budget_s):
+    """FP64 oracle (threaded gather form) on all host threads, bounded steps,
+    then on one thread for a third of the budget."""
+    O = _oracle()
     threads = O.hardware_threads()
     st = O.State(case)
     O.integrate_gather(st, 1, 1, case.dt, threads)  # its = 1 (untimed)
-    steps, t0 = 0, time.perf_counter()
-    while True:
-        O.integrate_gather(st, 2 + steps, 1, case.dt, threads)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or steps >= 200:
-            break
+    steps, el = _time_oracle(O, st, 2, case.dt, threads, budget_s, 200)
+    steps1, el1 = _time_oracle(O, st, 2 + steps, case.dt, 1, budget_s / 3.0, 50)
     return {"value": case.n * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": f"{case.name}, {case.n} particles, steps its=2..{steps + 1} "
-                      f"({el:.1f} s), FP64"}
+                      f"({el:.1f} s), FP64",
+            "single_core": {"value": case.n * steps1 / el1, "unit": METRIC, "cores": 1,
+                            "sample": f"steps its={steps + 2}..{steps + steps1 + 1} "
+                                      f"({el1:.1f} s), FP64"}}
+
+
+def cpu_suite(args):
+    """The FP64 oracle on this host over the benchmark workloads, all hardware
+    threads and one thread: cavity over its full 3000 steps, dam break and 3D
+    channel over 10 steps (one thread: 3 and 1), the sweep's checked subset
+    (smallest 64 + 16 size-stratified instances) over 10 steps. Rates are
+    particle-steps/s of the timed steps; the untimed first iteration (its = 1)
+    precedes each timing."""
+    from armando_gb300 import cases
+
+    O = _oracle()
+    threads = O.hardware_threads()
+    rows = []
+
+    def timed(name, insts, steps_all, steps_one):
+        for th, k in ((threads, steps_all), (1, steps_one)):
+            states = [O.State(c) for c in insts]
+            for c, st in zip(insts, states):
+                O.integrate_gather(st, 1, 1, c.dt, threads)
+            t0 = time.perf_counter()
+            for c, st in zip(insts, states):
+                O.integrate_gather(st, 2, k, c.dt, th)
+            el = time.perf_counter() - t0
+            n = sum(c.n for c in insts)
+            rows.append({"workload": name, "particles": n, "instances": len(insts),
+                         "steps": k, "threads": th, "seconds": el,
+                         "particle_steps_per_s": n * k / el})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+
+    timed("cavity 2D (3000 steps)", [cases.cavity()], 2999, 2999)
+    timed("dam break 2D", [cases.dam_break()], 10, 3)
+    timed("channel 3D", [cases.channel()], 10, 1)
+    sw = cases.sweep()
+    timed("sweep subset (64 smallest + 16 stratified of 512)",
+          [sw[k] for k in cases.sweep_subset(sw)], 10, 10)
+    return {"cpu_suite": rows, "host_threads": threads, "kind": "port", "dtype": "f64",
+            "oracle": "gather form of the CERN-F77 leapfrog, FP64"}
 
 
 def run_reference(args, rank):
     if rank != 0:
         return None
     case = make_case(args.config, args.dx)
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import oracle as O
-
+    O = _oracle()
     threads = O.hardware_threads()
     st = O.State(case)
     w = max(1, min(args.warmup, 2))
@@ -612,6 +666,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.cpu_suite:
+        if rank == 0:
+            print(json.dumps(cpu_suite(args)), flush=True)
+        return
     if args.only is not None and args.impl == "ours":
         import torch
 

@@ -98,6 +98,33 @@ def test_sweep_instances_match_oracle(O):
             assert e <= TOL_STEP, (c.name, f, e)
 
 
+def test_full_sweep_subset_matches_oracle(O):
+    """The 512-instance benchmark sweep (22.9 M particles) in one batch: after
+    one batched iteration, a second from those FP32 states; the smallest 64
+    instances and 16 size-stratified others each within TOL_STEP of the FP64
+    oracle's iteration from the same inputs, on every output."""
+    insts = cases.sweep()
+    subset = cases.sweep_subset(insts)
+    assert len(subset) == 80
+    arrays, offs = cases.pack(insts)
+    dts = [c.dt for c in insts]
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts]) as b:
+        b.integrate_batch(arrays, dts, 1, 1)
+        first = cases.unpack({k: v.copy() for k, v in arrays.items()}, offs, insts)
+        b.integrate_batch(arrays, dts, 2, 1)
+    got = cases.unpack(arrays, offs, insts)
+    worst = 0.0
+    for k in subset:
+        ref = O.State(first[k])
+        O.step(ref, 2, insts[k].dt)
+        for f in FIELDS:
+            e = rel_err(getattr(got[k], f), getattr(ref, f))
+            worst = max(worst, e)
+            assert e <= TOL_STEP, (insts[k].name, insts[k].n, f, e)
+    print(f"sweep subset ({len(subset)} of {len(insts)} instances): worst {worst:.2e}")
+
+
 def test_batch_rejects_single_only_calls():
     insts = _instances_2d()[:2]
     with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],

@@ -17,13 +17,17 @@ from helpers import FIELDS, history_state, rel_err, step_errors
 pytestmark = pytest.mark.gpu
 
 TOL_STEP = 1e-5
-REPORT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out",
-                      "parity_report.json")
+# Error report of the parity runs (per case and field; drift curves), written
+# as parity_report.json into $ARMANDO_REPORT_DIR when that is set.
+REPORT_DIR = os.environ.get("ARMANDO_REPORT_DIR")
 
 
 def _record(name, errs):
+    if not REPORT_DIR:
+        return
+    REPORT = os.path.join(REPORT_DIR, "parity_report.json")
     try:
-        os.makedirs(os.path.dirname(REPORT), exist_ok=True)
+        os.makedirs(REPORT_DIR, exist_ok=True)
         data = json.load(open(REPORT)) if os.path.exists(REPORT) else {}
         data[name] = errs
         json.dump(data, open(REPORT, "w"), indent=1)
@@ -132,7 +136,34 @@ def test_integrate_equals_repeated_steps_and_is_deterministic():
         assert np.array_equal(getattr(a, f), getattr(d, f)), f
 
 
-DRIFT_CHECKPOINTS = (1, 10, 100, 1000)
+def one_ulp_twin(c, seed):
+    """Copy of `c` whose fluid positions move by one FP32 ulp, randomly up or down."""
+    rng = np.random.default_rng(seed)
+    c2 = c.copy()
+    fl = np.repeat(c.itype > 0, c.dim)
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    c2.x = np.where(fl, np.nextafter(c.x, bump), c.x).astype(np.float32)
+    return c2
+
+
+def drift_curve(O, c, checkpoints, seed):
+    """GPU and FP64 oracle trajectories from the same FP32 state, plus the
+    oracle from the one-ulp twin: {checkpoint: {field: (gpu err, twin err)}}."""
+    ref, pert = O.State(c), O.State(one_ulp_twin(c, seed))
+    got = c.copy()
+    curve = {}
+    done = 0
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        for cp in checkpoints:
+            ctx.integrate(got, c.dt, done + 1, cp - done)
+            O.integrate_gather(ref, done + 1, cp - done, c.dt)
+            O.integrate_gather(pert, done + 1, cp - done, c.dt)
+            done = cp
+            curve[cp] = {f: (rel_err(getattr(got, f), getattr(ref, f)),
+                             rel_err(getattr(pert, f), getattr(ref, f))) for f in FIELDS}
+    for cp, e in curve.items():
+        print("drift", cp, {f: f"{g:.1e}/{i:.1e}" for f, (g, i) in e.items()})
+    return curve
 
 
 def test_multi_step_drift_is_bounded(O):
@@ -140,28 +171,22 @@ def test_multi_step_drift_is_bounded(O):
     oracle's own divergence when its FP32 inputs are perturbed by one ulp (the
     conditioning of the trajectory). Bound: GPU error <= 20x that, or 1e-5."""
     c = cases.perturbed(cases.dam_break(dx=0.03), seed=31, dv=0.05)
-    rng = np.random.default_rng(32)
-    c2 = c.copy()
-    fl = np.repeat(c.itype > 0, c.dim)
-    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
-    c2.x = np.where(fl, np.nextafter(c.x, bump), c.x).astype(np.float32)
-    ref, pert = O.State(c), O.State(c2)
-    got = c.copy()
-    curve = {}
-    done = 0
-    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
-        for cp in DRIFT_CHECKPOINTS:
-            ctx.integrate(got, c.dt, done + 1, cp - done)
-            O.integrate_gather(ref, done + 1, cp - done, c.dt)
-            O.integrate_gather(pert, done + 1, cp - done, c.dt)
-            done = cp
-            curve[cp] = {f: (rel_err(getattr(got, f), getattr(ref, f)),
-                             rel_err(getattr(pert, f), getattr(ref, f))) for f in FIELDS}
+    curve = drift_curve(O, c, (1, 10, 100, 1000), seed=32)
     _record("drift/dambreak", {str(k): v for k, v in curve.items()})
-    for cp, e in curve.items():
-        print("drift", cp, {f: f"{g:.1e}/{i:.1e}" for f, (g, i) in e.items()})
-    for f, (g, i) in curve[DRIFT_CHECKPOINTS[-1]].items():
+    for f, (g, i) in curve[1000].items():
         assert np.isfinite(g) and g <= max(20.0 * i, 1e-5), (f, g, i)
+
+
+def test_cavity_full_length_drift_is_bounded(O):
+    """The 2D cavity benchmark over its full 3000 steps (1600 fluid + 320 wall
+    particles, lid 1e-3 m/s, shear viscosity): the same bound as the dam break
+    at every checkpoint."""
+    c = cases.cavity()
+    curve = drift_curve(O, c, (1, 10, 100, 300, 1000, 3000), seed=33)
+    _record("drift/cavity", {str(k): v for k, v in curve.items()})
+    for cp, e in curve.items():
+        for f, (g, i) in e.items():
+            assert np.isfinite(g) and g <= max(20.0 * i, 1e-5), (cp, f, g, i)
 
 
 def test_device_memory_path_matches_host():
