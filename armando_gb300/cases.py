@@ -228,6 +228,34 @@ def channel(n_x: int = 504, n_yz: int = 126, length: float = 0.4, width: float =
                 dt=0.2 * h / c0, steps=steps, meta=dict(dx=dx, seed=seed, cp=cp))
 
 
+def with_mirror_ghosts(case: Case, lo, hi) -> Case:
+    """Copy of `case` for the mirror-ghost wall model (wall_model 3): every wall
+    particle's velocity entry becomes its inward unit normal, as the CERN
+    virtual-particle files carry it (CERNsource/input.f:256-314). The fluid
+    region is lo[d] <= x_d <= hi[d] per axis (None: open); a wall particle
+    outside it on several axes (a corner) takes the normalised sum of the
+    inward axis directions."""
+    c = case.copy()
+    dim = c.dim
+    x = c.x.reshape(-1, dim).astype(np.float64)
+    nrm = np.zeros_like(x)
+    for d in range(dim):
+        if lo[d] is not None:
+            nrm[:, d] += x[:, d] < lo[d]
+        if hi[d] is not None:
+            nrm[:, d] -= x[:, d] > hi[d]
+    wall = c.itype <= 0
+    length = np.linalg.norm(nrm, axis=1)
+    if np.any(wall & (length == 0)):
+        raise ValueError("a wall particle lies inside the fluid region")
+    v = c.v.reshape(-1, dim).copy()
+    v[wall] = nrm[wall] / length[wall, None]
+    c.v = _f32(v.ravel())
+    c.params.wall_model = 3
+    c.name = c.name + "_ghosts"
+    return c
+
+
 def perturbed(case: Case, seed: int, dv: float = 0.0, du: float = 0.0) -> Case:
     """Copy of `case` with seeded random fluid velocities (std dv) and energy (std du),
     used to give single-step parity tests non-trivial art_visc / art_heat terms."""

@@ -58,8 +58,17 @@ struct Params {
     R heat_q0 = R(0), heat_sigma = R(1), heat_center[3] = {R(0), R(0), R(0)};
     double heat_t_end = INFINITY;
     double period_lo[3] = {0, 0, 0}, period_hi[3] = {0, 0, 0};
-    int wall_model = 0;  // pairs of different itype: 0 like any pair, 1 push only, 2 both
+    // Wall treatment: 0 virtual particles (every pair alike), 1 and 2 the GPU-C
+    // pushes between different itype (1 push only, 2 push and every sum),
+    // 3 virtual particles plus mirror ghosts (ghost_particles).
+    int wall_model = 0;
 };
+
+// Whether pairs of different itype push (wall_model 1 and 2).
+template <class R>
+inline bool repulsive_walls(const Params<R>& P) {
+    return P.wall_model == 1 || P.wall_model == 2;
+}
 
 // ---------------------------------------------------------------------------
 // Wendland C2 kernel, support 2h (armando.cu:137-191).
@@ -546,7 +555,7 @@ void art_heat(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const Pa
 template <class R>
 const PairList& split_by_itype(const State<R>& s, const Params<R>& P, const PairList& pl,
                                PairList& same, PairList& other) {
-    if (P.wall_model == 0) return pl;
+    if (!repulsive_walls(P)) return pl;
     for (size_t k = 0; k < pl.pi.size(); ++k) {
         PairList& dst = (s.itype[pl.pi[k]] == s.itype[pl.pj[k]]) ? same : other;
         dst.pi.push_back(pl.pi[k]);
@@ -609,11 +618,131 @@ void ext_heat(const State<R>& s, const Params<R>& P, std::vector<R>& dudt) {
     }
 }
 
+// Mirror ghost particles (wall_model 3): CERNsource/ghost.f:1-86, rebuilt
+// every iteration after the predictor (time_integration.f:156-161). A fluid
+// particle i whose pairs include wall particles (itype <= 0) takes the
+// nearest one, w, whose velocity entry holds its inward unit normal n (the
+// Fortran's virtual-particle files carry normals there, input.f:256-314), and
+// gains the ghost
+//   x_g = x_i - 2 n ((x_i - x_w) . n),   v_g = v_i - 2 n (v_i . n)
+// (ghost.f:67-75) with m and h of i; rho, p and u of i are copied to it after
+// the density and EOS of the iteration (single_step.f:188-196). Ghosts follow
+// the real particles, in the order of their owners (ghost.f:60-84).
+// Departures, each without effect on a defined result:
+//   * candidates are the pairs at the current positions; the Fortran reuses
+//     the previous iteration's pair list. The two differ only where the
+//     nearest wall particle sits at the edge of the support, and such a ghost
+//     lies beyond the reach of every fluid particle.
+//   * the nearest is chosen on the squared distance in coordinate precision
+//     Rc (that of the pair test), ties to the lower index; the Fortran compares
+//     in FP64 and keeps the first in pair order.
+//   * ghosts have c = c0 and itype 0; the Fortran leaves both unset.
+// The ghosts' neighbour-search coordinates are computed in Rc from the Rc
+// coordinates, in the library's operation order (xc).
+template <class R, class Rc>
+struct Ghosts {
+    int64_t n_real = 0;
+    std::vector<int64_t> owner, wall;  // of ghost k = particle n_real + k
+    std::vector<Rc> xc;                // [k * dim + d]
+};
+
+template <class R, class Rc>
+void ghost_particles(State<R>& s, const Params<R>& P, Ghosts<R, Rc>& G) {
+    const int dim = s.dim;
+    const int64_t n = s.n;
+    for (int d = 0; d < dim; ++d)
+        if (P.periodic[d]) throw std::runtime_error("mirror ghosts need a system without periodic axes");
+    G.n_real = n;
+    G.owner.clear();
+    G.wall.clear();
+    G.xc.clear();
+    std::vector<Rc> xc(n * dim), hc(n);
+    for (int64_t i = 0; i < n * dim; ++i) xc[i] = Rc(s.x[i]);
+    for (int64_t i = 0; i < n; ++i) hc[i] = Rc(s.h[i]);
+    PairList pl;
+    link_list<Rc>(n, dim, xc.data(), hc.data(), P.periodic, P.period_lo, P.period_hi, pl);
+    std::vector<int64_t> best(n, -1);
+    std::vector<Rc> bestd(n, Rc(0));
+    auto offer = [&](int64_t a, int64_t w) {
+        Rc dd = Rc(0);
+        for (int d = 0; d < dim; ++d) {  // ghost.f:49-52, (x_w - x_i)^2 summed over axes
+            Rc t = Rc(xc[w * dim + d] - xc[a * dim + d]);
+            Rc sq = t * t;
+            dd = (d == 0) ? sq : Rc(dd + sq);
+        }
+        if (best[a] < 0 || dd < bestd[a] || (dd == bestd[a] && w < best[a])) {
+            best[a] = w;
+            bestd[a] = dd;
+        }
+    };
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        const int64_t a = pl.pi[k], b = pl.pj[k];
+        if (s.fluid(a) && !s.fluid(b)) offer(a, b);
+        else if (s.fluid(b) && !s.fluid(a)) offer(b, a);
+    }
+    for (int64_t a = 0; a < n; ++a)
+        if (best[a] >= 0) {
+            G.owner.push_back(a);
+            G.wall.push_back(best[a]);
+        }
+    const int64_t ng = (int64_t)G.owner.size(), nt = n + ng;
+    s.x.resize(nt * dim);
+    s.v.resize(nt * dim);
+    for (auto* a : {&s.m, &s.rho, &s.p, &s.u, &s.h, &s.c}) a->resize(nt);
+    s.itype.resize(nt);
+    s.dvdt.resize(nt * dim, R(0));
+    s.dudt.resize(nt, R(0));
+    G.xc.resize(ng * dim);
+    for (int64_t k = 0; k < ng; ++k) {
+        const int64_t a = G.owner[k], w = G.wall[k], g = n + k;
+        R dd1 = R(0), dd2 = R(0);
+        Rc e = Rc(0);
+        for (int d = 0; d < dim; ++d) {  // ghost.f:66-70
+            const R nd = s.v[w * dim + d];
+            const R t1 = (s.x[a * dim + d] - s.x[w * dim + d]) * nd;
+            const R t2 = s.v[a * dim + d] * nd;
+            dd1 = (d == 0) ? t1 : R(dd1 + t1);
+            dd2 = (d == 0) ? t2 : R(dd2 + t2);
+            const Rc tc = Rc(Rc(xc[a * dim + d] - xc[w * dim + d]) * Rc(nd));
+            e = (d == 0) ? tc : Rc(e + tc);
+        }
+        for (int d = 0; d < dim; ++d) {  // ghost.f:72-75
+            const R nd = s.v[w * dim + d];
+            s.x[g * dim + d] = s.x[a * dim + d] - R(2) * nd * dd1;
+            s.v[g * dim + d] = s.v[a * dim + d] - R(2) * nd * dd2;
+            G.xc[k * dim + d] = Rc(xc[a * dim + d] - Rc(Rc(Rc(2) * Rc(nd)) * e));
+            s.dvdt[g * dim + d] = R(0);
+        }
+        s.m[g] = s.m[a];  // ghost.f:77-80
+        s.h[g] = s.h[a];
+        s.rho[g] = s.rho[a];
+        s.p[g] = s.p[a];
+        s.u[g] = s.u[a];
+        s.c[g] = P.c0;
+        s.itype[g] = 0;
+        s.dudt[g] = R(0);
+    }
+    s.n = nt;
+}
+
+// Drops the ghosts again after the iteration (time_integration.f:190-205
+// advances particles 1..np only).
+template <class R, class Rc>
+void drop_ghosts(State<R>& s, const Ghosts<R, Rc>& G) {
+    const int64_t n = G.n_real;
+    const int dim = s.dim;
+    s.x.resize(n * dim);
+    s.v.resize(n * dim);
+    for (auto* a : {&s.m, &s.rho, &s.p, &s.u, &s.h, &s.c}) a->resize(n);
+    s.itype.resize(n);
+    s.n = n;
+}
+
 // single_step.f:92-234 for summation density and the Tait family:
 // fills s.rho, s.p (fluid), s.c, and rates dv, du (zero for walls).
 template <class R, class Rc>
 void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl, int its,
-                 double dt, Rates<R>& out) {
+                 double dt, Rates<R>& out, const Ghosts<R, Rc>* ghosts = nullptr) {
     const int dim = s.dim;
     const int64_t n = s.n;
     PairList same, other;
@@ -623,11 +752,18 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
         s.c[i] = P.c0;
         if (s.fluid(i)) eos_tait(s.rho[i], s.p[i], P);
     }
+    if (ghosts)  // single_step.f:188-196
+        for (size_t k = 0; k < ghosts->owner.size(); ++k) {
+            const int64_t gi = ghosts->n_real + (int64_t)k, o = ghosts->owner[k];
+            s.rho[gi] = s.rho[o];
+            s.p[gi] = s.p[o];
+            s.u[gi] = s.u[o];
+        }
     std::vector<R> indvdt, indudt, avdvdt, avdudt, ahdudt, exdudt, rpdvdt;
     int_force(s, g, P, body, indvdt, indudt, out.tdsdt);
     if (P.visc_artificial) art_visc(s, g, P, body, avdvdt, avdudt);
     if (P.heat_artificial) art_heat(s, g, P, body, ahdudt, out.divv);
-    if (P.wall_model != 0) wall_repulsion(s, g, P, other, rpdvdt);
+    if (repulsive_walls(P)) wall_repulsion(s, g, P, other, rpdvdt);
     if (P.heat_external && (double(its) * dt <= P.heat_t_end)) ext_heat(s, P, exdudt);
     out.dv.assign(n * dim, R(0));
     out.du.assign(n, R(0));
@@ -636,7 +772,7 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
         for (int d = 0; d < dim; ++d) {
             R a = indvdt[i * dim + d] + P.gravity[d];
             if (P.visc_artificial) a = a + avdvdt[i * dim + d];
-            if (P.wall_model != 0) a = a + rpdvdt[i * dim + d];
+            if (repulsive_walls(P)) a = a + rpdvdt[i * dim + d];
             out.dv[i * dim + d] = a;
         }
         R du = indudt[i];
@@ -661,10 +797,13 @@ inline void wrap_periodic(State<R>& s, const Params<R>& P, int64_t i) {
 // Neighbour search for the physics: link_list in coordinate precision Rc on
 // the current positions.
 template <class R, class Rc>
-Grid<Rc> neighbour_search(const State<R>& s, const Params<R>& P, PairList& pl) {
+Grid<Rc> neighbour_search(const State<R>& s, const Params<R>& P, PairList& pl,
+                          const Ghosts<R, Rc>* ghosts = nullptr) {
     std::vector<Rc> xc(s.n * s.dim), hc(s.n);
     for (int64_t i = 0; i < s.n * s.dim; ++i) xc[i] = Rc(s.x[i]);
     for (int64_t i = 0; i < s.n; ++i) hc[i] = Rc(s.h[i]);
+    if (ghosts)
+        for (size_t k = 0; k < ghosts->xc.size(); ++k) xc[ghosts->n_real * s.dim + (int64_t)k] = ghosts->xc[k];
     return link_list<Rc>(s.n, s.dim, xc.data(), hc.data(), P.periodic, P.period_lo, P.period_hi,
                          pl);
 }
@@ -688,10 +827,18 @@ void leapfrog_step(State<R>& s, const Params<R>& P, int its, double dt, Rates<R>
             for (int d = 0; d < dim; ++d) s.v[i * dim + d] = s.v[i * dim + d] + hdt * s.dvdt[i * dim + d];
         }
     }
+    Ghosts<R, Rc> G;
+    const bool ghosts = P.wall_model == 3;
+    if (ghosts) ghost_particles(s, P, G);
     PairList pl;
-    Grid<Rc> g = neighbour_search<R, Rc>(s, P, pl);
+    Grid<Rc> g = neighbour_search<R, Rc>(s, P, pl, ghosts ? &G : nullptr);
     Rates<R> r;
-    single_step(s, g, P, pl, its, dt, r);
+    single_step(s, g, P, pl, its, dt, r, ghosts ? &G : nullptr);
+    if (ghosts) {
+        drop_ghosts(s, G);
+        r.dv.resize(n * dim);
+        r.du.resize(n);
+    }
     for (int64_t i = 0; i < n; ++i) {
         if (!s.fluid(i)) continue;
         if (its != 1) {

@@ -83,6 +83,8 @@ def lib() -> C.CDLL:
         L.ao_tangent_f64.restype = C.c_int
         L.ao_flops_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double] + [vp] * 11
         L.ao_flops_f64.restype = C.c_int
+        L.ao_ghosts_f64.argtypes = [C.POINTER(Params), i64, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp]
+        L.ao_ghosts_f64.restype = i64
         L.ao_hardware_threads.argtypes = []
         L.ao_hardware_threads.restype = C.c_int
         _lib = L
@@ -209,6 +211,24 @@ def integrate_gather(state: State, its0: int, steps: int, dt: float, nthreads: i
     if rc:
         raise RuntimeError("oracle gather integrate failed")
     return state
+
+
+def ghosts(params: Params, x, v, h, itype, fp32=True):
+    """Mirror ghosts (wall_model 3) of the given positions and velocities:
+    (owner, wall, x_ghost [ng, dim], v_ghost [ng, dim])."""
+    d = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    x, v, h = d(x), d(v), d(h)
+    itype = np.ascontiguousarray(itype, np.int32)
+    n, dim = h.shape[0], params.dim
+    owner = np.zeros(n, np.int64)
+    wall = np.zeros(n, np.int64)
+    xg = np.zeros(n * dim)
+    vg = np.zeros(n * dim)
+    ng = lib().ao_ghosts_f64(C.byref(params), n, _p(x), _p(v), _p(h), _p(itype), int(fp32),
+                             _p(owner), _p(wall), _p(xg), _p(vg))
+    if ng < 0:
+        raise RuntimeError("oracle ghosts failed")
+    return owner[:ng], wall[:ng], xg[:ng * dim].reshape(ng, dim), vg[:ng * dim].reshape(ng, dim)
 
 
 def hardware_threads() -> int:

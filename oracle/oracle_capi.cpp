@@ -180,7 +180,7 @@ int ao_forces_f64(const armando_params* prm, int64_t n, const double* x, const d
         for (size_t k = 0; k < dv.size(); ++k) dv[k] += avdv[k];
         for (size_t k = 0; k < du.size(); ++k) du[k] += avdu[k];
     }
-    if (P.wall_model != 0) {
+    if (ao::repulsive_walls(P)) {
         ao::wall_repulsion(s, g, P, other, rpdv);
         for (size_t k = 0; k < dv.size(); ++k) dv[k] += rpdv[k];
     }
@@ -366,6 +366,44 @@ int ao_flops_f64(const armando_params* prm, int64_t n, int its, double dt, const
         return 1;
     }
     return 0;
+}
+
+// Mirror ghosts (wall_model 3, ghost.f) of a state at its current positions,
+// velocities as given (no predictor): returns the ghost count (-1 on error)
+// and fills owner[ng], wall[ng], xg[ng*dim], vg[ng*dim] (capacity n each).
+// fp32 = 1: candidates and the nearest wall in FP32 coordinates.
+int64_t ao_ghosts_f64(const armando_params* prm, int64_t n, const double* x, const double* v,
+                      const double* h, const int* itype, int fp32, int64_t* owner, int64_t* wall,
+                      double* xg, double* vg) {
+    ao::Params<double> P = to_params<double>(prm);
+    const int dim = P.dim;
+    std::vector<double> zero(n, 0.0);
+    ao::State<double> s = load_state<double>(dim, n, x, v, zero.data(), zero.data(), zero.data(),
+                                             zero.data(), h, itype, nullptr, nullptr);
+    auto emit = [&](const auto& G) {
+        const int64_t ng = (int64_t)G.owner.size();
+        for (int64_t k = 0; k < ng; ++k) {
+            owner[k] = G.owner[k];
+            wall[k] = G.wall[k];
+            for (int d = 0; d < dim; ++d) {
+                xg[k * dim + d] = s.x[(n + k) * dim + d];
+                vg[k * dim + d] = s.v[(n + k) * dim + d];
+            }
+        }
+        return ng;
+    };
+    try {
+        if (fp32) {
+            ao::Ghosts<double, float> G;
+            ao::ghost_particles(s, P, G);
+            return emit(G);
+        }
+        ao::Ghosts<double, double> G;
+        ao::ghost_particles(s, P, G);
+        return emit(G);
+    } catch (const std::exception&) {
+        return -1;
+    }
 }
 
 int ao_hardware_threads(void) {
