@@ -146,6 +146,7 @@ class Stats(C.Structure):
         ("grid_cell_size", F3),
         ("device_flags", C.c_uint32),
         ("sorts_done", C.c_int64),
+        ("ghosts", C.c_int64),
     ]
 
 

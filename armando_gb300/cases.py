@@ -232,18 +232,18 @@ def with_mirror_ghosts(case: Case, lo, hi) -> Case:
     """Copy of `case` for the mirror-ghost wall model (wall_model 3): every wall
     particle's velocity entry becomes its inward unit normal, as the CERN
     virtual-particle files carry it (CERNsource/input.f:256-314). The fluid
-    region is lo[d] <= x_d <= hi[d] per axis (None: open); a wall particle
-    outside it on several axes (a corner) takes the normalised sum of the
-    inward axis directions."""
+    region is lo[d] < x_d < hi[d] per axis (None: open); a wall particle on or
+    beyond a bound takes the inward direction of that axis, on several axes (a
+    corner) their normalised sum."""
     c = case.copy()
     dim = c.dim
     x = c.x.reshape(-1, dim).astype(np.float64)
     nrm = np.zeros_like(x)
     for d in range(dim):
         if lo[d] is not None:
-            nrm[:, d] += x[:, d] < lo[d]
+            nrm[:, d] += x[:, d] <= lo[d]
         if hi[d] is not None:
-            nrm[:, d] -= x[:, d] > hi[d]
+            nrm[:, d] -= x[:, d] >= hi[d]
     wall = c.itype <= 0
     length = np.linalg.norm(nrm, axis=1)
     if np.any(wall & (length == 0)):

@@ -20,6 +20,7 @@
 #include "../../include/armando.h"
 #include "kernels.cuh"
 #include "adjoint.cuh"
+#include "ghosts.cuh"
 
 using namespace ag;
 
@@ -64,6 +65,10 @@ struct armando_ctx {
     DevParams dp{};
     int dim = 2;
     int64_t n = 0, nf = 0, nw = 0;
+    // Particle slots of the step arrays: n, plus one mirror ghost per fluid
+    // particle for contexts created with wall_model 3. n_work: particles of
+    // the iteration being launched (n + its ghosts).
+    int64_t cap = 0, n_work = 0;
     int mem_kind = ARMANDO_MEM_HOST;
     StateA A{};
     StateB B{};
@@ -132,6 +137,19 @@ struct armando_ctx {
     int adj_its0 = 0, adj_steps = 0, adj_K = 0;
     float adj_dt = 0.f;
     bool adj_ready = false;
+    // Mirror ghosts (wall_model 3): the wall grid of the call, the walls in
+    // cell order, and per iteration the nearest wall of each particle and the
+    // ghosts' owners.
+    WallGrid* wgrid = nullptr;
+    WallGrid* h_wgrid = nullptr;  // pinned
+    int* wstart = nullptr;
+    long long wstart_cap = 0;
+    int wall_cells = 0;
+    float4 *wall_xh = nullptr, *wall_n = nullptr;
+    int *wall_id = nullptr, *g_best = nullptr, *g_owner = nullptr, *g_slot = nullptr,
+        *d_ng = nullptr, *h_ng = nullptr;
+    unsigned *g_tile_count = nullptr, *g_tile_off = nullptr;
+    int64_t ghosts_last = 0;
 };
 
 namespace {
@@ -180,10 +198,16 @@ armando_status validate_params(const armando_params* p, int dim, std::string& wh
             why = "periodic axis needs period_hi > period_lo";
             return ARMANDO_ERR_INVALID_ARG;
         }
-    if (p->wall_model < 0 || p->wall_model > 2) {
-        why = "wall_model must be 0, 1 or 2";
+    if (p->wall_model < 0 || p->wall_model > 3) {
+        why = "wall_model must be 0, 1, 2 or 3";
         return ARMANDO_ERR_INVALID_ARG;
     }
+    if (p->wall_model == 3)
+        for (int d = 0; d < dim; ++d)
+            if (p->periodic[d]) {
+                why = "mirror ghosts (wall_model 3) need a system without periodic axes";
+                return ARMANDO_ERR_INVALID_ARG;
+            }
     return ARMANDO_OK;
 }
 
@@ -259,7 +283,7 @@ armando_status force_sort(armando_ctx* ctx) {
 
 template <int DIM>
 int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st) {
-    const int n = (int)ctx->n;
+    const int n = (int)ctx->n_work;
     int L = 0;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
@@ -327,7 +351,7 @@ bool lean_physics(const DevParams& p) { return !p.visc && !p.heat_art && p.wall_
 
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
-    const int n = (int)ctx->n;
+    const int n = (int)ctx->n_work;
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
                 [&](auto tpp, auto bs, auto per, auto lean) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
@@ -339,7 +363,7 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
 
 template <int DIM>
 void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
-    const int n = (int)ctx->n;
+    const int n = (int)ctx->n_work;
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
                 [&](auto tpp, auto bs, auto per, auto lean) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
@@ -353,12 +377,18 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
 template <int DIM>
 int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     cudaStream_t st = ctx->stream;
-    const int n = (int)ctx->n;
+    const int n = (int)ctx->n_work;
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     launch_density<DIM>(ctx, skeys);
     int L = 2;
+    if (n > ctx->n) {  // mirror ghosts take their owners' density, pressure, energy
+        k_invert_ids<<<blocks_for(n, 256), 256, 0, st>>>(ctx->B.id, ctx->g_slot, n);
+        k_ghost_sync<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, ctx->g_slot, ctx->g_owner,
+                                                               ctx->dp, n);
+        L += 2;
+    }
     if (ctx->dp.visc) {
         k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
@@ -605,8 +635,50 @@ armando_status run_batch_step(armando_ctx* ctx) {
     return ARMANDO_OK;
 }
 
+// One iteration with mirror ghosts (wall_model 3), as direct launches: the
+// nearest-wall search and the ghost write, one read-back of the ghost count,
+// then the step over the real particles and their ghosts.
+template <int DIM>
+armando_status run_ghost_step(armando_ctx* ctx, const StepArgs& S) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    int ng = 0, L = 0;
+    if (ctx->wall_cells > 0 && n > 0) {
+        const int tiles = blocks_for(n, kGhostTile);
+        k_ghost_select<DIM><<<tiles, kGhostThreads, 0, st>>>(ctx->A, n, ctx->wgrid, ctx->wstart,
+                                                             ctx->wall_xh, ctx->wall_id,
+                                                             ctx->g_best, ctx->g_tile_count);
+        k_ghost_scan<<<1, 1024, 0, st>>>(ctx->g_tile_count, tiles, ctx->g_tile_off, ctx->d_ng);
+        k_ghost_write<DIM><<<tiles, kGhostThreads, 0, st>>>(ctx->A, n, ctx->g_best, ctx->wall_xh,
+                                                            ctx->wall_n, ctx->g_tile_off,
+                                                            ctx->g_owner, S);
+        L += 3;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(ctx->h_ng, ctx->d_ng, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        ng = *ctx->h_ng;
+        if (ng < 0 || (int64_t)ng > ctx->nf)
+            return fail(ctx, ARMANDO_ERR_CUDA, "mirror ghost count out of range");
+    }
+    ctx->n_work = (int64_t)n + ng;
+    ctx->num_tiles = blocks_for(ctx->n_work, kSortTile);
+    L += launch_grid_and_sort<DIM>(ctx, nullptr, st);
+    L += launch_passes<DIM>(ctx, S, nullptr);
+    ctx->n_work = n;
+    ctx->num_tiles = blocks_for(n, kSortTile);
+    CK(cudaGetLastError());
+    ctx->ghosts_last = ng;
+    ctx->launches += L;
+    ctx->launches_per_step = L;
+    ctx->steps_done += 1;
+    ctx->sorts_host += 1;
+    return ARMANDO_OK;
+}
+
 armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     if (ctx->n_inst > 1) return run_batch_step(ctx);
+    if (ctx->prm.wall_model == 3)
+        return ctx->dim == 2 ? run_ghost_step<2>(ctx, S) : run_ghost_step<3>(ctx, S);
     GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
     auto itg = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
@@ -648,7 +720,7 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
 
 armando_status alloc_state(armando_ctx* ctx) {
     cudaError_t e = cudaSuccess;
-    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    const size_t n = (size_t)std::max<int64_t>(ctx->cap, 1);  // step slots (ghosts included)
     auto F4 = [&](float4*& p) { p = dalloc<float4>(n, e); ctx->owned.push_back(p); };
     auto F1 = [&](float*& p, size_t k) { p = dalloc<float>(k, e); ctx->owned.push_back(p); };
     auto I1 = [&](int*& p) { p = dalloc<int>(n, e); ctx->owned.push_back(p); };
@@ -679,7 +751,7 @@ armando_status alloc_state(armando_ctx* ctx) {
     ctx->B.mstride = (int)n;
     ctx->B.mtpp = 1;
     ctx->owned.push_back(ctx->B.nmask);
-    ctx->num_tiles = blocks_for(ctx->n, kSortTile);
+    ctx->num_tiles = blocks_for(ctx->cap, kSortTile);  // sizes the histogram; set per sort below
     for (int k = 0; k < 2; ++k) {
         ctx->keys[k] = dalloc<unsigned>(n, e);
         ctx->vals[k] = dalloc<int>(n, e);
@@ -687,6 +759,7 @@ armando_status alloc_state(armando_ctx* ctx) {
         ctx->owned.push_back(ctx->vals[k]);
     }
     ctx->hist = dalloc<unsigned>((size_t)kRadix * std::max(ctx->num_tiles, 1), e);
+    ctx->num_tiles = blocks_for(ctx->n, kSortTile);
     ctx->dtotal = dalloc<unsigned>(kRadix, e);
     ctx->bbox_part = dalloc<float>(kBBoxBlocks * 8, e);
     ctx->grid = dalloc<DevGrid>(1, e);
@@ -696,17 +769,37 @@ armando_status alloc_state(armando_ctx* ctx) {
                     (void*)ctx->flags})
         ctx->owned.push_back(p);
     if (ctx->mem_kind == ARMANDO_MEM_HOST) {
-        const size_t nd = n * ctx->dim;
+        const size_t nc = (size_t)std::max<int64_t>(ctx->n, 1), nd = nc * ctx->dim;
         F1(ctx->s_x, nd);
         F1(ctx->s_v, nd);
         F1(ctx->s_dvdt, nd);
-        F1(ctx->s_m, n);
-        F1(ctx->s_rho, n);
-        F1(ctx->s_p, n);
-        F1(ctx->s_u, n);
-        F1(ctx->s_h, n);
-        F1(ctx->s_dudt, n);
-        I1(ctx->s_itype);
+        F1(ctx->s_m, nc);
+        F1(ctx->s_rho, nc);
+        F1(ctx->s_p, nc);
+        F1(ctx->s_u, nc);
+        F1(ctx->s_h, nc);
+        F1(ctx->s_dudt, nc);
+        ctx->s_itype = dalloc<int>(nc, e);
+        ctx->owned.push_back(ctx->s_itype);
+    }
+    if (ctx->prm.wall_model == 3) {  // mirror ghosts
+        const size_t nr = (size_t)std::max<int64_t>(ctx->n, 1);
+        const size_t tiles = (size_t)std::max(blocks_for(ctx->n, kGhostTile), 1);
+        ctx->wgrid = dalloc<WallGrid>(1, e);
+        ctx->wall_xh = dalloc<float4>(nr, e);
+        ctx->wall_n = dalloc<float4>(nr, e);
+        ctx->wall_id = dalloc<int>(nr, e);
+        ctx->g_best = dalloc<int>(nr, e);
+        ctx->g_owner = dalloc<int>((size_t)std::max<int64_t>(ctx->nf, 1), e);
+        ctx->g_slot = dalloc<int>(n, e);
+        ctx->d_ng = dalloc<int>(1, e);
+        ctx->g_tile_count = dalloc<unsigned>(tiles, e);
+        ctx->g_tile_off = dalloc<unsigned>(tiles, e);
+        for (void* q : {(void*)ctx->wgrid, (void*)ctx->wall_xh, (void*)ctx->wall_n,
+                        (void*)ctx->wall_id, (void*)ctx->g_best, (void*)ctx->g_owner,
+                        (void*)ctx->g_slot, (void*)ctx->d_ng, (void*)ctx->g_tile_count,
+                        (void*)ctx->g_tile_off})
+            ctx->owned.push_back(q);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc");
     CK(cudaMemset(ctx->flags, 0, kFlagWords * sizeof(unsigned)));
@@ -714,6 +807,11 @@ armando_status alloc_state(armando_ctx* ctx) {
     if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
     he = cudaMallocHost((void**)&ctx->h_grid, sizeof(DevGrid));
     if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
+    if (ctx->prm.wall_model == 3) {
+        he = cudaMallocHost((void**)&ctx->h_wgrid, sizeof(WallGrid));
+        if (he == cudaSuccess) he = cudaMallocHost((void**)&ctx->h_ng, sizeof(int));
+        if (he != cudaSuccess) return cuda_fail(ctx, he, "cudaMallocHost");
+    }
     return ARMANDO_OK;
 }
 
@@ -774,6 +872,68 @@ armando_status plan_grid(armando_ctx* ctx) {
     CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
     free_graphs(ctx);
     return ARMANDO_OK;
+}
+
+// The wall grid of a call with mirror ghosts: the walls do not move within
+// the call, so their grid, cell order and copies serve every iteration.
+template <int DIM>
+armando_status build_wall_grid_dim(armando_ctx* ctx) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    k_wall_grid<DIM><<<1, kWallGridThreads, 0, st>>>(ctx->A, n, 1LL << 28, ctx->wgrid);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_wgrid, ctx->wgrid, sizeof(WallGrid), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const WallGrid g = *ctx->h_wgrid;
+    ctx->launches += 1;
+    if (g.ncells < 0) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "wall grid of the mirror ghosts needs more than 2^28 cells");
+    ctx->wall_cells = g.ncells;
+    if (g.ncells == 0) return ARMANDO_OK;
+    if ((long long)g.ncells + 1 > ctx->wstart_cap) {
+        cudaError_t e = cudaSuccess;
+        if (ctx->wstart) {
+            auto it = std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->wstart);
+            if (it != ctx->owned.end()) ctx->owned.erase(it);
+            cudaFree(ctx->wstart);
+        }
+        ctx->wstart_cap = 2LL * g.ncells + 1;
+        ctx->wstart = dalloc<int>((size_t)ctx->wstart_cap, e);
+        if (e != cudaSuccess) {
+            ctx->wstart = nullptr;
+            ctx->wstart_cap = 0;
+            return cuda_fail(ctx, e, "cudaMalloc(wall cell table)");
+        }
+        ctx->owned.push_back(ctx->wstart);
+    }
+    // Sort the walls by cell (fluid keys = ncells sort after them).
+    int bits = 1;
+    while ((1LL << bits) <= (long long)g.ncells) ++bits;
+    const int passes = (bits + 7) / 8;
+    const int tiles = blocks_for(n, kSortTile);
+    k_wall_keys<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, n, ctx->wgrid, ctx->keys[0]);
+    int L = 1;
+    for (int p = 0; p < passes; ++p) {
+        const int a = p & 1, b = (p + 1) & 1;
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ctx->keys[a], n, 8 * p, ctx->hist, tiles);
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, tiles, ctx->dtotal);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ctx->keys[a], p == 0 ? nullptr : ctx->vals[a],
+                                                        ctx->keys[b], ctx->vals[b], n, 8 * p,
+                                                        ctx->hist, ctx->dtotal, tiles);
+        L += 3;
+    }
+    k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(
+        ctx->keys[passes & 1], n, &ctx->wgrid->ncells, g.ncells, ctx->wstart);
+    k_wall_gather<<<blocks_for(n, 256), 256, 0, st>>>(ctx->vals[passes & 1], ctx->wstart, ctx->wgrid,
+                                                      ctx->A, n, ctx->wall_xh, ctx->wall_n,
+                                                      ctx->wall_id);
+    ctx->launches += L + 2;
+    CK(cudaGetLastError());
+    return ARMANDO_OK;
+}
+
+armando_status build_wall_grid(armando_ctx* ctx) {
+    if (ctx->prm.wall_model != 3) return ARMANDO_OK;
+    return ctx->dim == 2 ? build_wall_grid_dim<2>(ctx) : build_wall_grid_dim<3>(ctx);
 }
 
 armando_status check_flags(armando_ctx* ctx) {
@@ -1338,7 +1498,16 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
         ctx->inst_dt.push_back(0.f);
     }
     ctx->n = total;
+    ctx->n_work = total;
+    ctx->cap = total + (params[0].wall_model == 3 ? ctx->nf : 0);
+    ctx->dp.n_real = (int)total;
     ctx->mem_kind = mem_kind;
+    if (n_inst > 1)
+        for (int k = 0; k < n_inst; ++k)
+            if (params[k].wall_model == 3) {
+                delete ctx;
+                return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) are not available in batches");
+            }
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         armando_status st = cuda_fail(ctx, e, "cudaStreamCreate");
@@ -1378,8 +1547,14 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     std::string why;
     armando_status vs = validate_params(params, ctx->dim, why);
     if (vs != ARMANDO_OK) return fail(ctx, vs, why);
+    if (params->wall_model == 3 && ctx->cap < ctx->n + ctx->nf)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) need a context created with wall_model 3");
+    if (params->wall_model == 3 && ctx->tune.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) sort every iteration: set a tuning with skin 0 first");
     ctx->prm = *params;
     ctx->dp = make_dev_params(*params, ctx->tune.reach);
+    ctx->dp.n_real = (int)ctx->n;
+    ctx->dp.skin = 0.01f * (float)ctx->tune.skin;
     free_graphs(ctx);
     return ARMANDO_OK;
 }
@@ -1405,6 +1580,8 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches run one thread per particle");
     if (ctx->n_inst > 1 && t.skin != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches sort every iteration (skin 0)");
+    if (ctx->prm.wall_model == 3 && t.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) sort every iteration (skin 0)");
     return ARMANDO_OK;
 }
 
@@ -1414,7 +1591,7 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
 armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
     const bool regrid = t.reach != ctx->tune.reach || t.skin != ctx->tune.skin;
     ctx->tune = t;
-    ctx->B.mstride = (int)(ctx->n * t.threads_per_particle);
+    ctx->B.mstride = (int)(ctx->cap * t.threads_per_particle);
     ctx->B.mtpp = t.threads_per_particle;
     ctx->dp.reach = t.reach;
     ctx->dp.skin = 0.01f * (float)t.skin;
@@ -1507,10 +1684,15 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
             t.skin = skin;
         }
         float ms = -1.f;
+        if (t.skin != 0 && ctx->prm.wall_model == 3) {  // mirror ghosts sort every iteration
+            if (ms_per_step) ms_per_step[k] = -1.f;
+            continue;
+        }
         if ((st = apply_tuning(ctx, t)) != ARMANDO_OK) break;
         CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
         st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
         if (st == ARMANDO_OK) st = plan_grid(ctx);
+        if (st == ARMANDO_OK) st = build_wall_grid(ctx);
         // Two untimed iterations capture the graphs of the first and of the
         // following iterations; then the timed ones.
         for (int w = 0; w < 2 && st == ARMANDO_OK; ++w) st = run_step(ctx, make_args(ctx, dt, its0 + w));
@@ -1608,6 +1790,8 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
     if (st != ARMANDO_OK) return st;
     st = plan_grid(ctx);
+    if (st != ARMANDO_OK) return st;
+    st = build_wall_grid(ctx);
     if (st != ARMANDO_OK) return st;
     for (int k = 0; k < steps; ++k) {
         st = run_step(ctx, make_args(ctx, dt, its0 + k));
@@ -1916,6 +2100,8 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
     if (!ctx || !ms_per_phase || steps < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "bad argument");
     if (!ctx->start || ctx->next_its < 2 || !(ctx->last_dt > 0.f))
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "no device state: call armando_integrate first");
+    if (ctx->prm.wall_model == 3)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "phase timing does not cover mirror ghosts (wall_model 3)");
     CK(cudaSetDevice(ctx->device));
     cudaEvent_t ev[ARMANDO_N_PHASES + 1];
     for (auto& e : ev) CK(cudaEventCreate(&e));
@@ -1970,6 +2156,7 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
     }
     out->device_flags = cctx->h_flags ? *cctx->h_flags : 0u;
     out->sorts_done = cctx->sorts_done + cctx->sorts_host;
+    out->ghosts = cctx->ghosts_last;
     return ARMANDO_OK;
 }
 
@@ -1985,6 +2172,8 @@ armando_status armando_destroy(armando_ctx* ctx) {
     for (void* p : ctx->owned) cudaFree(p);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     if (ctx->h_grid) cudaFreeHost(ctx->h_grid);
+    if (ctx->h_wgrid) cudaFreeHost(ctx->h_wgrid);
+    if (ctx->h_ng) cudaFreeHost(ctx->h_ng);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     delete ctx;

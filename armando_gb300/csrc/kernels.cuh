@@ -74,9 +74,15 @@ struct DevParams {
     float heat_t_end;    // external heat gate its*dt <= heat_t_end
     int reach;           // neighbour-grid cells per support radius (tuning; 1 = link_list)
     float skin;          // sort skin as a fraction of max h (tuning; 0 = sort every step)
-    int wall_model;      // pairs of different itype: 0 like any pair, 1 push only, 2 both
-    int pad_;
+    // Wall treatment: 0 like any pair, 1 push only, 2 push and every sum between
+    // different itype; 3 like 0 plus mirror ghosts (particles with id >= n_real).
+    int wall_model;
+    int n_real;          // real particles; ids from n_real on are mirror ghosts
 };
+
+__host__ __device__ inline bool repulsive_walls(const DevParams& P) {
+    return P.wall_model == 1 || P.wall_model == 2;
+}
 
 struct StepArgs {
     float kdt;    // corrector step: dt (its > 1) or dt/2 (its == 1)
@@ -1394,6 +1400,8 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     rp.x = rho;
     rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rho, rho)) : p;
     if (need_div) {
+        // a mirror ghost's psi waits for its owner's density (k_ghost_sync)
+        if (P.wall_model == 3 && !fluid) B.tds[s] = divs;
         const float divv = __fdiv_rn(divs, rho);
         rp.w = fmaf(P.ah_g2 * xi.w * xi.w, fabsf(divv) - divv, __fmul_rn(P.ah_g1 * xi.w, P.c0));
     }
@@ -1488,16 +1496,23 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         vi = B.vm[s];
         rpi = B.rp[s];
     }
+    // The next state goes to the slot of this sort, or with mirror ghosts
+    // (wall_model 3) to the particle's own index, the ghosts being dropped.
+    const bool ghosts = !LEAN && P.wall_model == 3;
     if (valid && (it <= 0 || !g.ok) && sub == 0) {  // wall: fixed state, zero rates
-        A.xh[s] = xi;
-        A.vm[s] = vi;
-        A.u[s] = B.vmin[s].w;
-        A.ap[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-        A.rho[s] = rpi.x;
-        A.p[s] = B.p[s];
-        A.itype[s] = it;
-        A.id[s] = B.id[s];
-        if (A.inst) A.inst[s] = B.inst[s];
+        const int id = B.id[s];
+        if (!ghosts || id < P.n_real) {
+            const int o = ghosts ? id : s;
+            A.xh[o] = xi;
+            A.vm[o] = vi;
+            A.u[o] = B.vmin[s].w;
+            A.ap[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+            A.rho[o] = rpi.x;
+            A.p[o] = B.p[s];
+            A.itype[o] = it;
+            A.id[o] = id;
+            if (A.inst) A.inst[o] = B.inst[s];
+        }
     }
     const bool work = valid && it > 0 && g.ok;
     CellCoord cc = {{0, 0, 0}};
@@ -1612,7 +1627,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 kgih = P.kg * pow_grad<DIM>(ih);
             }
             const float q = __fmul_rn(fast_sqrt_pos(dr2), ih);
-            if (!LEAN && P.wall_model != 0 && __ldg(B.itype + k) != it) {
+            if (!LEAN && repulsive_walls(P) && __ldg(B.itype + k) != it) {
                 // Push between particles of different type (ArmandoThrust/armando.cu:507-513
                 // for wall_model 1, acpu.c:424-429 for 2) along (x_i - x_j)/r, c = c0.
                 const float r = fast_sqrt_pos(dr2);
@@ -1751,15 +1766,17 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + un + a0 + a1 + a2 + du;
     if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
-    A.xh[s] = xn;
-    A.vm[s] = vn;
-    A.u[s] = un;
-    A.ap[s] = make_float4(a0, a1, a2, du);
-    A.rho[s] = rpi.x;
-    A.p[s] = B.p[s];
-    A.itype[s] = it;
-    A.id[s] = B.id[s];
-    if (A.inst) A.inst[s] = B.inst[s];
+    const int id = B.id[s];
+    const int o = ghosts ? id : s;
+    A.xh[o] = xn;
+    A.vm[o] = vn;
+    A.u[o] = un;
+    A.ap[o] = make_float4(a0, a1, a2, du);
+    A.rho[o] = rpi.x;
+    A.p[o] = B.p[s];
+    A.itype[o] = it;
+    A.id[o] = id;
+    if (A.inst) A.inst[o] = B.inst[s];
 }
 
 // ---------------------------------------------------------------------------

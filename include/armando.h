@@ -89,7 +89,16 @@ typedef struct armando_params {
                                  2 = GPU-C host path (ArmandoThrust/acpu.c:390-429): like
                                      any pair, plus a push 0.02 (W/W(0)) c_i c_j
                                      m_j/((m_i + m_j) r). Pushes act along (x_i - x_j)/r on
-                                     momentum only; c = c0; W at h = (h_i + h_j)/2.     */
+                                     momentum only; c = c0; W at h = (h_i + h_j)/2;
+                                 3 = CERN virtual particles plus mirror ghosts
+                                     (CERNsource/ghost.f, single_step.f:188-196): every
+                                     iteration, each fluid particle with a wall particle
+                                     in reach is mirrored across the nearest one's plane;
+                                     a wall particle's vx holds its inward unit normal
+                                     (and, as in the Fortran, enters the pair sums as its
+                                     velocity). Needs a context created with wall_model 3,
+                                     no periodic axis, no sort skin; not in batches or
+                                     the reverse mode.                                    */
 } armando_params;
 
 /* Per-step statistics of the last completed call. */
@@ -105,6 +114,7 @@ typedef struct armando_stats {
     uint32_t device_flags;    /* raw device status word of the last check        */
     int64_t sorts_done;       /* iterations that rebuilt the grid and sorted (all
                                  of them unless the tuning has a sort skin)       */
+    int64_t ghosts;           /* mirror ghosts of the last iteration (wall_model 3) */
 } armando_stats;
 
 typedef struct armando_ctx armando_ctx;
