@@ -19,7 +19,7 @@ from ._abi import (ERR_UNSUPPORTED, EXPORTED, LIB_PATH, MEM_DEVICE, MEM_HOST, OK
                    N_TUNINGS, STATUS_NAMES, ParamGrads, Params, Stats, Tuning, load_library)
 
 __all__ = ["Context", "Batch", "Params", "Stats", "ArmandoError", "load_library", "MEM_HOST",
-           "MEM_DEVICE", "LIB_PATH", "EXPORTED"]
+           "MEM_DEVICE", "LIB_PATH", "EXPORTED", "read_deck", "write_deck", "write_vtk"]
 
 
 class ArmandoError(RuntimeError):
@@ -286,3 +286,54 @@ class Batch(Context):
             _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
             d.ctypes.data_as(C.c_void_p), int(its0), int(steps)))
         return s
+
+
+# ---- particle decks and snapshots (host only) ------------------------------------
+
+DECK_FIELDS = ("x", "v", "mass", "rho", "p", "u", "h", "itype")
+
+
+def _io_check(lib, st):
+    if st != OK:
+        raise ArmandoError(st, lib.armando_last_error(None).decode())
+
+
+def read_deck(directory: str, dim: int) -> dict:
+    """CERN-F77 particle deck (f_*.dat, and v_*.dat when present) as step
+    arrays: x, v, mass, rho, p, u, h (float32), itype (int32), the real
+    particles first, plus the counts n_real and n_virtual."""
+    lib = load_library()
+    nr, nv = C.c_int64(), C.c_int64()
+    d = str(directory).encode()
+    _io_check(lib, lib.armando_deck_count(d, C.byref(nr), C.byref(nv)))
+    n = nr.value + nv.value
+    a = {f: np.zeros(n * dim if f in ("x", "v") else n, np.int32 if f == "itype" else np.float32)
+         for f in DECK_FIELDS}
+    _io_check(lib, lib.armando_deck_read(d, dim, nr.value, nv.value,
+                                         *[_ptr(a[f]) for f in DECK_FIELDS]))
+    a["n_real"], a["n_virtual"] = nr.value, nv.value
+    return a
+
+
+def write_deck(directory: str, dim: int, n_real: int, arrays) -> None:
+    """Writes the arrays (real particles first, n_real of them) as a CERN-F77
+    deck: f_*.dat for the real particles, v_*.dat for the rest."""
+    lib = load_library()
+    a = arrays.arrays() if hasattr(arrays, "arrays") else arrays
+    n = int(np.asarray(a["mass"]).size)
+    if not 0 <= n_real <= n:
+        raise ValueError("n_real out of range")
+    arrs = [np.ascontiguousarray(a[f], np.int32 if f == "itype" else np.float32)
+            for f in DECK_FIELDS]
+    _io_check(lib, lib.armando_deck_write(str(directory).encode(), dim, n_real, n - n_real,
+                                          *[_ptr(q) for q in arrs]))
+
+
+def write_vtk(path: str, dim: int, arrays) -> None:
+    """Legacy ASCII VTK snapshot (the GPU-C code's outputVTK format)."""
+    lib = load_library()
+    a = arrays.arrays() if hasattr(arrays, "arrays") else arrays
+    n = int(np.asarray(a["mass"]).size)
+    arrs = [np.ascontiguousarray(a[f], np.int32 if f == "itype" else np.float32)
+            for f in ("x", "v", "rho", "p", "u", "itype")]
+    _io_check(lib, lib.armando_write_vtk(str(path).encode(), dim, n, *[_ptr(q) for q in arrs]))

@@ -23,12 +23,13 @@ ERR_TIMEOUT = 6
 ERR_CUDA = 7
 ERR_NO_DEVICE = 8
 ERR_UNSUPPORTED = 9
+ERR_IO = 10
 
 STATUS_NAMES = {
     OK: "OK", ERR_INVALID_ARG: "INVALID_ARG", ERR_OOM: "OOM",
     ERR_GRID_OVERFLOW: "GRID_OVERFLOW", ERR_NONFINITE: "NONFINITE",
     ERR_OUT_OF_GRID: "OUT_OF_GRID", ERR_TIMEOUT: "TIMEOUT", ERR_CUDA: "CUDA",
-    ERR_NO_DEVICE: "NO_DEVICE", ERR_UNSUPPORTED: "UNSUPPORTED",
+    ERR_NO_DEVICE: "NO_DEVICE", ERR_UNSUPPORTED: "UNSUPPORTED", ERR_IO: "IO",
 }
 
 MEM_HOST = 0
@@ -160,6 +161,7 @@ EXPORTED = [
     "armando_batch_create", "armando_batch_integrate",
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
+    "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
 ]
 N_TUNINGS = 27
 N_PHASES = 6
@@ -231,6 +233,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_autotune.restype = C.c_int
     lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
     lib.armando_cell_ids_noalloc.restype = C.c_int
+    cp = C.c_char_p
+    lib.armando_deck_count.argtypes = [cp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    lib.armando_deck_count.restype = C.c_int
+    lib.armando_deck_read.argtypes = [cp, C.c_int32, C.c_int64, C.c_int64] + [vp] * 8
+    lib.armando_deck_read.restype = C.c_int
+    lib.armando_deck_write.argtypes = [cp, C.c_int32, C.c_int64, C.c_int64] + [vp] * 8
+    lib.armando_deck_write.restype = C.c_int
+    lib.armando_write_vtk.argtypes = [cp, C.c_int32, C.c_int64] + [vp] * 6
+    lib.armando_write_vtk.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

@@ -21,6 +21,7 @@
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ghosts.cuh"
+#include "deck_io.h"
 
 using namespace ag;
 
@@ -2162,6 +2163,62 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
 
 const char* armando_last_error(const armando_ctx* ctx) {
     return ctx ? ctx->err.c_str() : g_last_error;
+}
+
+armando_status armando_deck_count(const char* dir, int64_t* n_real, int64_t* n_virtual) {
+    if (!dir || !n_real || !n_virtual) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    std::string err;
+    const long long nr = deck::count(dir, "f", err);
+    if (nr < 0)
+        return fail(nullptr, ARMANDO_ERR_IO, err.empty() ? std::string("cannot open ") + dir + "/f_xv.dat" : err);
+    const long long nv = deck::count(dir, "v", err);
+    if (nv == -2) return fail(nullptr, ARMANDO_ERR_IO, err);
+    *n_real = nr;
+    *n_virtual = nv < 0 ? 0 : nv;
+    return ARMANDO_OK;
+}
+
+armando_status armando_deck_read(const char* dir, int32_t dim, int64_t n_real, int64_t n_virtual,
+                                 float* x, float* vx, float* mass, float* rho, float* p,
+                                 float* u, float* hsml, int32_t* itype) {
+    if (!dir || !x || !vx || !mass || !rho || !p || !u || !hsml || !itype)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if ((dim != 2 && dim != 3) || n_real < 0 || n_virtual < 0)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "dim must be 2 or 3, counts >= 0");
+    const deck::Arrays a{x, vx, mass, rho, p, u, hsml, itype};
+    std::string err;
+    if (!deck::read_set(dir, "f", dim, 0, n_real, a, err)) return fail(nullptr, ARMANDO_ERR_IO, err);
+    if (n_virtual > 0 && !deck::read_set(dir, "v", dim, n_real, n_virtual, a, err))
+        return fail(nullptr, ARMANDO_ERR_IO, err);
+    return ARMANDO_OK;
+}
+
+armando_status armando_deck_write(const char* dir, int32_t dim, int64_t n_real,
+                                  int64_t n_virtual, const float* x, const float* vx,
+                                  const float* mass, const float* rho, const float* p,
+                                  const float* u, const float* hsml, const int32_t* itype) {
+    if (!dir || !x || !vx || !mass || !rho || !p || !u || !hsml || !itype)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if ((dim != 2 && dim != 3) || n_real < 0 || n_virtual < 0)
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "dim must be 2 or 3, counts >= 0");
+    const deck::Arrays a{const_cast<float*>(x), const_cast<float*>(vx), const_cast<float*>(mass),
+                         const_cast<float*>(rho), const_cast<float*>(p), const_cast<float*>(u),
+                         const_cast<float*>(hsml), const_cast<int32_t*>(itype)};
+    std::string err;
+    if (!deck::write_set(dir, "f", dim, 0, n_real, a, err)) return fail(nullptr, ARMANDO_ERR_IO, err);
+    if (!deck::write_set(dir, "v", dim, n_real, n_virtual, a, err)) return fail(nullptr, ARMANDO_ERR_IO, err);
+    return ARMANDO_OK;
+}
+
+armando_status armando_write_vtk(const char* path, int32_t dim, int64_t n, const float* x,
+                                 const float* vx, const float* rho, const float* p,
+                                 const float* u, const int32_t* itype) {
+    if (!path || (n > 0 && (!x || !vx || !rho || !p || !u || !itype)))
+        return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if ((dim != 2 && dim != 3) || n < 0) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "dim must be 2 or 3, n >= 0");
+    std::string err;
+    if (!deck::write_vtk(path, dim, n, x, vx, rho, p, u, itype, err)) return fail(nullptr, ARMANDO_ERR_IO, err);
+    return ARMANDO_OK;
 }
 
 armando_status armando_destroy(armando_ctx* ctx) {

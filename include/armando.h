@@ -40,7 +40,9 @@ typedef enum armando_status {
     ARMANDO_ERR_TIMEOUT = 6,       /* a bounded device-side wait gave up            */
     ARMANDO_ERR_CUDA = 7,          /* a CUDA runtime call failed                    */
     ARMANDO_ERR_NO_DEVICE = 8,     /* no sm_103 device visible                      */
-    ARMANDO_ERR_UNSUPPORTED = 9    /* option the GPU step does not implement        */
+    ARMANDO_ERR_UNSUPPORTED = 9,   /* option the GPU step does not implement        */
+    ARMANDO_ERR_IO = 10            /* a deck or output file failed to open, parse or
+                                      write (armando_deck_*, armando_write_vtk)      */
 } armando_status;
 
 typedef enum armando_mem_kind {
@@ -357,6 +359,32 @@ armando_status armando_get_stats(const armando_ctx* ctx, armando_stats* out);
 const char* armando_last_error(const armando_ctx* ctx);
 armando_status armando_destroy(armando_ctx* ctx);
 int32_t armando_abi_version(void);
+
+/* ---- particle decks and snapshots (host only; no context, no GPU) --------------
+ * Decks of the CERN-F77 code, in directory dir: real particles in f_xv.dat,
+ * f_state.dat, f_other.dat (read by CERNsource/input.f:197-255, written by
+ * output.f:31-54), virtual (wall) particles in v_xv.dat, v_state.dat,
+ * v_other.dat (input.f:256-314, output.f:56-73). Arrays hold the n_real real
+ * particles first, then the n_virtual virtual ones, in the step's layout
+ * (x[i*dim + d]); itype is the deck's material number (<= 0: wall). Reading
+ * is list-directed like the Fortran's; writing reproduces its formats
+ * (1x,I6,6(2x,e14.8)), (1x,I6,7(2x,e14.8)), (1x,I6,2x,I4,2x,e14.8). A deck
+ * without v_ files has n_virtual = 0. Errors: ARMANDO_ERR_IO (message in
+ * armando_last_error(NULL)). */
+armando_status armando_deck_count(const char* dir, int64_t* n_real, int64_t* n_virtual);
+armando_status armando_deck_read(const char* dir, int32_t dim, int64_t n_real, int64_t n_virtual,
+                                 float* x, float* vx, float* mass, float* rho, float* p,
+                                 float* u, float* hsml, int32_t* itype);
+armando_status armando_deck_write(const char* dir, int32_t dim, int64_t n_real,
+                                  int64_t n_virtual, const float* x, const float* vx,
+                                  const float* mass, const float* rho, const float* p,
+                                  const float* u, const float* hsml, const int32_t* itype);
+/* Legacy ASCII VTK snapshot of n particles in the format of the GPU-C code's
+ * outputVTK (ArmandoThrust/armando.cu:1596-1670): points (z = 0 in 2D), one
+ * vertex cell each, material, density, pressure, energy, velocity. */
+armando_status armando_write_vtk(const char* path, int32_t dim, int64_t n, const float* x,
+                                 const float* vx, const float* rho, const float* p,
+                                 const float* u, const int32_t* itype);
 
 #ifdef __cplusplus
 }
