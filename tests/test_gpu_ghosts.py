@@ -173,3 +173,28 @@ def test_refusals():
     with pytest.raises(ag.ArmandoError) as e:
         ag.Context(per.params, per.n_fluid, per.n_wall)
     assert e.value.status == ag._abi.ERR_INVALID_ARG
+
+
+def test_deck_to_step(O, tmp_path):
+    """The Fortran virtual_part workflow: a deck with the walls' normals in the
+    v_ files, read back and stepped with mirror ghosts."""
+    c = ghost_cases()["dambreak"]
+    order = np.argsort(c.itype <= 0, kind="stable")
+    arrs = {f: (getattr(c, f).reshape(c.n, -1)[order].ravel() if f in ("x", "v")
+                else getattr(c, f)[order]) for f in ag.DECK_FIELDS}
+    ag.write_deck(tmp_path, 2, c.n_fluid, arrs)
+    d = ag.read_deck(tmp_path, 2)
+    assert d["n_real"] == c.n_fluid and d["n_virtual"] == c.n_wall
+    inp = c.copy()
+    for f in ag.DECK_FIELDS:
+        setattr(inp, f, d[f])
+    inp.dvdt = np.zeros_like(inp.x)
+    inp.dudt = np.zeros_like(inp.u)
+    ref = O.State(inp)
+    O.step(ref, 1, inp.dt, nbr_fp32=True)
+    got = inp.copy()
+    with ag.Context(inp.params, inp.n_fluid, inp.n_wall) as ctx:
+        ctx.step(got, inp.dt, 1)
+        assert ctx.stats().ghosts > 0
+    for f in FIELDS:
+        assert rel_err(getattr(got, f), getattr(ref, f)) <= TOL_STEP, f
