@@ -247,6 +247,15 @@ class Context:
             table[key] = float(ms[k])
         return best.as_tuple(), table
 
+    def set_materials(self, materials):
+        """Material table of the GPU-C schemes: a list of _abi.Material (or
+        (eos, props) pairs), entry k for the particles with |itype| = k."""
+        from ._abi import Material
+
+        ms = [m if isinstance(m, Material) else Material.make(*m) for m in materials]
+        tab = (Material * len(ms))(*ms)
+        self._check(self._lib.armando_set_materials(self._h, len(ms), tab))
+
     def sync(self):
         self._check(self._lib.armando_sync(self._h))
 

@@ -69,6 +69,7 @@ class Params(C.Structure):
         ("period_lo", F3),
         ("period_hi", F3),
         ("wall_model", C.c_int32),
+        ("scheme", C.c_int32),
     ]
 
     @classmethod
@@ -108,6 +109,25 @@ class Params(C.Structure):
             v = getattr(self, name)
             out[name] = list(v) if hasattr(v, "__len__") else v
         return out
+
+
+class Material(C.Structure):
+    """``armando_material``: EOS type and properties of one material of the
+    GPU-C schemes (0 boundary, 1 ideal gas, 2 polynomial, 3 shock, 4 Tait, 5 ESS)."""
+
+    _fields_ = [("eos", C.c_int32), ("prop", C.c_float * 10)]
+
+    @classmethod
+    def make(cls, eos, prop=()):
+        m = cls()
+        m.eos = eos
+        for k, v in enumerate(prop):
+            m.prop[k] = v
+        return m
+
+
+EOS_BOUNDARY, EOS_GAS, EOS_POLY, EOS_SHOCK, EOS_TAIT, EOS_ESS = range(6)
+MAX_MATERIALS = 64
 
 
 class ParamGrads(C.Structure):
@@ -162,6 +182,7 @@ EXPORTED = [
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
     "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
+    "armando_set_materials",
 ]
 N_TUNINGS = 27
 N_PHASES = 6
@@ -242,6 +263,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_deck_write.restype = C.c_int
     lib.armando_write_vtk.argtypes = [cp, C.c_int32, C.c_int64] + [vp] * 6
     lib.armando_write_vtk.restype = C.c_int
+    lib.armando_set_materials.argtypes = [vp, C.c_int32, C.POINTER(Material)]
+    lib.armando_set_materials.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

@@ -353,3 +353,40 @@ def sweep_subset(case_list, smallest: int = 64, strata: int = 16):
     for q in range(min(strata, len(rest))):
         pick.add(rest[int((q + 0.5) * len(rest) / strata)])
     return sorted(pick)
+
+
+def gpuc_dam_break(scale: int = 1, fluid=(100, 50), tank=(269, 80), dr1: float = 0.02,
+                   rho0: float = 1000.0, c0: float = 50.0, scheme: int = 1) -> Case:
+    """The GPU-C codes' 2D dam break (the geometry of ArmandoThrust/acpu.c:
+    1784-1902, the published Tab.1 cases): dr = dr1 / scale; a lattice of
+    (fluid[0] scale + 1) x (fluid[1] scale + 1) water particles at
+    ((i + 1/2) dr, (j + 1/2) dr); three rows of wall particles at integer
+    lattice points under the tank (x from -3 dr to (tank[0] scale + 2) dr) and
+    three columns on each side (left at -3..-1 dr, right from tank[0] scale dr,
+    y from 0 to tank[1] scale dr). h = 1.2 dr, m = rho0 dr^2, rho = rho0, p = u
+    = 0; water itype 1, walls -1 (both Tait rho0, c0 in the default material
+    table); gravity -9.81; dt = 4e-4 s / scale. Scales 1, 2, 4 give the
+    published 6,462 / 22,899 / 85,773 particles."""
+    dr = dr1 / scale
+    nfx, nfy = fluid[0] * scale + 1, fluid[1] * scale + 1
+    i, j = np.meshgrid(np.arange(nfx), np.arange(nfy), indexing="ij")
+    xf = np.stack([(i.ravel() + 0.5) * dr, (j.ravel() + 0.5) * dr], axis=1)
+    ntx, nty = tank[0] * scale, tank[1] * scale
+    walls = []
+    bi = np.arange(-3, ntx + 3)
+    for row in (-3, -2, -1):
+        walls.append(np.stack([bi * dr, np.full(bi.shape, row * dr)], 1))
+    sj = np.arange(0, nty + 1)
+    for col in list(range(-3, 0)) + list(range(ntx, ntx + 3)):
+        walls.append(np.stack([np.full(sj.shape, col * dr), sj * dr], 1))
+    xw = np.concatenate(walls)
+    x = np.concatenate([xf, xw])
+    nf, n = len(xf), len(xf) + len(xw)
+    h = 1.2 * dr
+    P = Params.default(dim=2, rho0=rho0, c0=c0, gravity=(0.0, -G, 0.0))
+    P.scheme = scheme
+    return Case(f"gpuc_dambreak_x{scale}", P, 2, _f32(x.ravel()), _f32(np.zeros(2 * n)),
+                _f32(np.full(n, rho0 * dr * dr)), _f32(np.full(n, rho0)), _f32(np.zeros(n)),
+                _f32(np.zeros(n)), _f32(np.full(n, h)),
+                np.concatenate([np.ones(nf), -np.ones(n - nf)]).astype(np.int32),
+                dt=4.0e-4 / scale, steps=10000 * scale, meta=dict(dx=dr, scale=scale))

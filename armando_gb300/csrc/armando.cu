@@ -21,6 +21,7 @@
 #include "kernels.cuh"
 #include "adjoint.cuh"
 #include "ghosts.cuh"
+#include "gpuc.cuh"
 #include "deck_io.h"
 
 using namespace ag;
@@ -151,6 +152,12 @@ struct armando_ctx {
         *d_ng = nullptr, *h_ng = nullptr;
     unsigned *g_tile_count = nullptr, *g_tile_off = nullptr;
     int64_t ghosts_last = 0;
+    // GPU-C schemes (scheme 1, 2): the RK3 working state in cell order and the
+    // material table (default: Tait with rho0, c0 for every |itype|).
+    GpucState gs{};
+    bool gs_ready = false;
+    DevMaterial* d_mat = nullptr;
+    std::vector<armando_material> materials;  // set by armando_set_materials
 };
 
 namespace {
@@ -209,6 +216,21 @@ armando_status validate_params(const armando_params* p, int dim, std::string& wh
                 why = "mirror ghosts (wall_model 3) need a system without periodic axes";
                 return ARMANDO_ERR_INVALID_ARG;
             }
+    if (p->scheme < 0 || p->scheme > 2) {
+        why = "scheme must be 0, 1 or 2";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
+    if (p->scheme != 0) {
+        if (p->wall_model != 0) {
+            why = "the GPU-C schemes carry their own wall treatment: wall_model must be 0";
+            return ARMANDO_ERR_INVALID_ARG;
+        }
+        for (int d = 0; d < dim; ++d)
+            if (p->periodic[d]) {
+                why = "the GPU-C schemes have no periodic axes";
+                return ARMANDO_ERR_INVALID_ARG;
+            }
+    }
     return ARMANDO_OK;
 }
 
@@ -481,7 +503,38 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
     return ARMANDO_OK;
 }
 
+// One GPU-C RK3 step: grid and sort on the step's start positions, the cell
+// order state, three stages ping-ponging between the working copies, the
+// result back to A.
+template <int DIM>
+int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S) {
+    cudaStream_t st = ctx->stream;
+    const int n = (int)ctx->n;
+    const int nm = ctx->materials.empty() ? ARMANDO_MAX_MATERIALS : (int)ctx->materials.size();
+    int L = launch_grid_and_sort<DIM>(ctx, nullptr, st);
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_gpuc_gather<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->gs, ctx->d_mat, nm,
+                                                           ctx->flags, n);
+    static const float alphas[3] = {1.0f, 0.25f, 2.0f / 3.0f};
+    for (int q = 0; q < 3; ++q) {
+        const int cur = q & 1;
+        if (ctx->prm.scheme == 1)
+            k_gpuc_stage<DIM, 1><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+                ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->flags,
+                alphas[q], S.dt, n);
+        else
+            k_gpuc_stage<DIM, 2><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+                ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->flags,
+                alphas[q], S.dt, n);
+    }
+    k_gpuc_scatter<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->gs, 1, ctx->A, n);
+    return L + 5;
+}
+
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
+    if (ctx->prm.scheme != 0)
+        return ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S) : launch_gpuc_step<3>(ctx, S);
     return ctx->dim == 2 ? launch_step<2>(ctx, S) : launch_step<3>(ctx, S);
 }
 
@@ -937,6 +990,50 @@ armando_status build_wall_grid(armando_ctx* ctx) {
     return ctx->dim == 2 ? build_wall_grid_dim<2>(ctx) : build_wall_grid_dim<3>(ctx);
 }
 
+// GPU-C schemes: the working state (first use) and the material table of
+// this call.
+armando_status prepare_gpuc(armando_ctx* ctx) {
+    if (ctx->prm.scheme == 0) return ARMANDO_OK;
+    cudaError_t e = cudaSuccess;
+    if (!ctx->gs_ready) {
+        const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+        GpucState& g = ctx->gs;
+        g.x0 = dalloc<float4>(n, e);
+        g.v0 = dalloc<float4>(n, e);
+        g.q0 = dalloc<float2>(n, e);
+        for (int k = 0; k < 2; ++k) {
+            g.xw[k] = dalloc<float4>(n, e);
+            g.vw[k] = dalloc<float4>(n, e);
+            g.sw[k] = dalloc<float4>(n, e);
+        }
+        g.rates = dalloc<float4>(n, e);
+        g.itype = dalloc<int>(n, e);
+        g.id = dalloc<int>(n, e);
+        ctx->d_mat = dalloc<DevMaterial>(ARMANDO_MAX_MATERIALS, e);
+        for (void* q : {(void*)g.x0, (void*)g.v0, (void*)g.q0, (void*)g.xw[0], (void*)g.xw[1],
+                        (void*)g.vw[0], (void*)g.vw[1], (void*)g.sw[0], (void*)g.sw[1],
+                        (void*)g.rates, (void*)g.itype, (void*)g.id, (void*)ctx->d_mat})
+            ctx->owned.push_back(q);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(GPU-C state)");
+        ctx->gs_ready = true;
+    }
+    std::vector<DevMaterial> tab(ARMANDO_MAX_MATERIALS);
+    for (int k = 0; k < ARMANDO_MAX_MATERIALS; ++k) {
+        DevMaterial& M = tab[k];
+        std::memset(&M, 0, sizeof M);
+        if (ctx->materials.empty()) {
+            M.type = 4;
+            M.prop[0] = ctx->prm.rho0;
+            M.prop[1] = ctx->prm.c0;
+        } else if (k < (int)ctx->materials.size()) {
+            M.type = ctx->materials[k].eos;
+            std::memcpy(M.prop, ctx->materials[k].prop, sizeof M.prop);
+        }
+    }
+    CK(cudaMemcpy(ctx->d_mat, tab.data(), sizeof(DevMaterial) * tab.size(), cudaMemcpyHostToDevice));
+    return ARMANDO_OK;
+}
+
 armando_status check_flags(armando_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, kFlagWords * sizeof(unsigned),
                        cudaMemcpyDeviceToHost, ctx->stream));
@@ -951,6 +1048,7 @@ armando_status check_flags(armando_ctx* ctx) {
     if (f & FLAG_GRID_OVERFLOW) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "neighbour grid exceeded the context's cell capacity");
     if (f & FLAG_NONFINITE) return fail(ctx, ARMANDO_ERR_NONFINITE, "non-finite value in a fluid particle's state");
     if (f & FLAG_OUT_OF_GRID) return fail(ctx, ARMANDO_ERR_OUT_OF_GRID, "a particle left the periodic box by more than one period");
+    if (f & FLAG_BAD_MATERIAL) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "an |itype| outside the material table");
     return ARMANDO_OK;
 }
 
@@ -1230,7 +1328,7 @@ armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
 armando_status check_adjoint_support(armando_ctx* ctx) {
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
     const armando_params& p = ctx->prm;
-    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0)
+    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0 || p.scheme != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
                     "reverse mode supports pa_sph = 1, wall_model 0, without physical viscosity "
                     "and artificial heat");
@@ -1505,9 +1603,9 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
     ctx->mem_kind = mem_kind;
     if (n_inst > 1)
         for (int k = 0; k < n_inst; ++k)
-            if (params[k].wall_model == 3) {
+            if (params[k].wall_model == 3 || params[k].scheme != 0) {
                 delete ctx;
-                return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) are not available in batches");
+                return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "batches run the CERN scheme without mirror ghosts");
             }
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1550,8 +1648,8 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     if (vs != ARMANDO_OK) return fail(ctx, vs, why);
     if (params->wall_model == 3 && ctx->cap < ctx->n + ctx->nf)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) need a context created with wall_model 3");
-    if (params->wall_model == 3 && ctx->tune.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) sort every iteration: set a tuning with skin 0 first");
+    if ((params->wall_model == 3 || params->scheme != 0) && ctx->tune.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and the GPU-C schemes sort every iteration: set a tuning with skin 0 first");
     ctx->prm = *params;
     ctx->dp = make_dev_params(*params, ctx->tune.reach);
     ctx->dp.n_real = (int)ctx->n;
@@ -1581,8 +1679,8 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches run one thread per particle");
     if (ctx->n_inst > 1 && t.skin != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches sort every iteration (skin 0)");
-    if (ctx->prm.wall_model == 3 && t.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) sort every iteration (skin 0)");
+    if ((ctx->prm.wall_model == 3 || ctx->prm.scheme != 0) && t.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and the GPU-C schemes sort every iteration (skin 0)");
     return ARMANDO_OK;
 }
 
@@ -1685,7 +1783,7 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
             t.skin = skin;
         }
         float ms = -1.f;
-        if (t.skin != 0 && ctx->prm.wall_model == 3) {  // mirror ghosts sort every iteration
+        if (t.skin != 0 && (ctx->prm.wall_model == 3 || ctx->prm.scheme != 0)) {  // sort every iteration
             if (ms_per_step) ms_per_step[k] = -1.f;
             continue;
         }
@@ -1694,6 +1792,7 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
         st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
         if (st == ARMANDO_OK) st = plan_grid(ctx);
         if (st == ARMANDO_OK) st = build_wall_grid(ctx);
+        if (st == ARMANDO_OK) st = prepare_gpuc(ctx);
         // Two untimed iterations capture the graphs of the first and of the
         // following iterations; then the timed ones.
         for (int w = 0; w < 2 && st == ARMANDO_OK; ++w) st = run_step(ctx, make_args(ctx, dt, its0 + w));
@@ -1793,6 +1892,8 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     st = plan_grid(ctx);
     if (st != ARMANDO_OK) return st;
     st = build_wall_grid(ctx);
+    if (st != ARMANDO_OK) return st;
+    st = prepare_gpuc(ctx);
     if (st != ARMANDO_OK) return st;
     for (int k = 0; k < steps; ++k) {
         st = run_step(ctx, make_args(ctx, dt, its0 + k));
@@ -2101,8 +2202,8 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
     if (!ctx || !ms_per_phase || steps < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "bad argument");
     if (!ctx->start || ctx->next_its < 2 || !(ctx->last_dt > 0.f))
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "no device state: call armando_integrate first");
-    if (ctx->prm.wall_model == 3)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "phase timing does not cover mirror ghosts (wall_model 3)");
+    if (ctx->prm.wall_model == 3 || ctx->prm.scheme != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "phase timing covers the CERN scheme without mirror ghosts");
     CK(cudaSetDevice(ctx->device));
     cudaEvent_t ev[ARMANDO_N_PHASES + 1];
     for (auto& e : ev) CK(cudaEventCreate(&e));
@@ -2163,6 +2264,22 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
 
 const char* armando_last_error(const armando_ctx* ctx) {
     return ctx ? ctx->err.c_str() : g_last_error;
+}
+
+armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const armando_material* table) {
+    if (!ctx || !table) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if (count < 1 || count > ARMANDO_MAX_MATERIALS)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "material count must be 1..ARMANDO_MAX_MATERIALS");
+    for (int k = 0; k < count; ++k) {
+        if (table[k].eos < 0 || table[k].eos > 5)
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "material eos must be 0-5");
+        for (float q : table[k].prop)
+            if (!std::isfinite(q) && !(table[k].eos == 5 && std::isinf(q)))
+                return fail(ctx, ARMANDO_ERR_INVALID_ARG, "material properties must be finite");
+    }
+    ctx->materials.assign(table, table + count);
+    free_graphs(ctx);
+    return ARMANDO_OK;
 }
 
 armando_status armando_deck_count(const char* dir, int64_t* n_real, int64_t* n_virtual) {

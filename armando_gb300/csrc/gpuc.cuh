@@ -1,0 +1,297 @@
+// gpuc.cuh -- the GPU-C step variant (armando_params.scheme 1 and 2).
+//
+// Third-order TVD Runge-Kutta with continuity density and one neighbour list
+// per step, as the GPU-C codes run it (ArmandoThrust/acpu.c:2338-2379):
+// X = X0 + alpha (X + dt dX/dt - X0) for alpha = 1, 1/4, 2/3. Pair rates:
+//   scheme 1, the host path (acpu.c:346-437): every listed pair contributes
+//     continuity m_j (x_ij . v_ij) W'/r, pressure -(p_i + p_j)/(rho_i rho_j),
+//     the shock corrections of mass and momentum, and between different
+//     itype a push 0.02 (W/W0) c_i c_j / r scaled by m_j/(m_i + m_j);
+//   scheme 2, the device kernels (armando.cu:429-513): the same terms, with
+//     pressure -(p_i/rho_i^2 + p_j/rho_j^2), for pairs of equal itype only;
+//     pairs of different itype push 0.5 W m_j/(rho_j h_j) c_j^2.
+// Energy: de/dt = p drho/dt / rho^2 (acpu.c:510-534); gravity on itype > 0.
+// Update and EOS per material |itype| (acpu.c:873-966, armando.cu:987-1074).
+// Kernels with h_i. The list of a step holds the j != i with
+// sqrtf(|x0_i - x0_j|^2) < 2 h_i at the step's start (updateListHost,
+// acpu.c:2201-2240), without the reference's 21-entry cap; each stage tests
+// the candidates of the step's cell grid against the start positions (kept
+// for the step anyway) and evaluates the physics at the stage's positions.
+//
+// State in cell order: the step's start (x0, v0, rho0/u0) and two working
+// copies {x, v, (rho, u, p, c)} that the stages ping-pong between; the last
+// stage's rates go out as dv/dt, de/dt.
+#pragma once
+#include "kernels.cuh"
+
+namespace ag {
+
+struct DevMaterial {
+    int type;  // 0 boundary, 1 ideal gas, 2 polynomial, 3 shock, 4 Tait, 5 ESS
+    float prop[10];
+};
+
+struct GpucState {
+    float4* x0;    // {x, y, m, h} (2D) / {x, y, z, h} (3D) at the step's start
+    float4* v0;    // {v, -} (2D) / {v, m} (3D)
+    float2* q0;    // {rho, u} at the step's start
+    float4* xw[2];
+    float4* vw[2];
+    float4* sw[2];  // {rho, u, p, c}
+    float4* rates;  // {dv/dt, de/dt} of the last stage
+    int* itype;
+    int* id;
+};
+
+// The EOS of one particle after its update (acpu.c:932-962 with the property
+// functions of acpu.c:560-870; ESS of Code/armando.cu:572-598 on absolute
+// density). rho is clamped where the type clamps.
+__device__ __forceinline__ void gpuc_eos(const DevMaterial& M, float& rho, float u, float& p, float& c) {
+    const float* q = M.prop;
+    switch (M.type) {
+    case 0:  // boundary
+        if (rho < 0.9f * q[0]) rho = 0.9f * q[0];
+        p = 0.f;
+        c = q[1];
+        break;
+    case 1:  // ideal gas
+        p = __fadd_rn(__fmul_rn(__fmul_rn(q[1] - 1.0f, rho), u), q[2]);
+        c = sqrtf(__fmul_rn(__fmul_rn(q[1], q[1] - 1.0f), u));
+        break;
+    case 2: {  // Mie-Gruneisen polynomial
+        if (rho < 0.9f * q[0]) rho = 0.9f * q[0];
+        const float mu = __fdiv_rn(rho - q[0], q[0]);
+        const float mu2 = __fmul_rn(mu, mu);
+        if (mu < 0.f)
+            p = __fadd_rn(__fadd_rn(__fmul_rn(q[6], mu), __fmul_rn(q[7], mu2)),
+                          __fmul_rn(__fmul_rn(q[4], q[0]), u));
+        else
+            p = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(q[1], mu), __fmul_rn(q[2], mu2)),
+                                    __fmul_rn(q[3], __fmul_rn(mu2, mu))),
+                          __fmul_rn(__fmul_rn(__fadd_rn(q[4], __fmul_rn(q[5], mu)), q[0]), u));
+        c = sqrtf(__fdiv_rn(q[1], rho));
+        break;
+    }
+    case 3: {  // Mie-Gruneisen shock
+        if (rho < 0.9f * q[0]) rho = 0.9f * q[0];
+        const float mu = __fdiv_rn(rho - q[0], q[0]);
+        const float den = __fsub_rn(1.0f, __fmul_rn(q[3] - 1.0f, mu));
+        const float ph = __fdiv_rn(__fmul_rn(__fmul_rn(__fmul_rn(q[0], __fmul_rn(q[1], q[1])), mu),
+                                             1.0f + mu),
+                                   __fmul_rn(den, den));
+        const float corr = __fmul_rn(__fdiv_rn(__fmul_rn(0.5f, ph), q[0]), __fdiv_rn(mu, 1.0f + mu));
+        p = __fadd_rn(ph, __fmul_rn(__fmul_rn(q[2], q[0]), __fsub_rn(u, corr)));
+        c = q[1];
+        break;
+    }
+    case 4: {  // Tait
+        if (rho < 0.9f * q[0]) rho = 0.9f * q[0];
+        const float r = __fdiv_rn(rho, q[0]);
+        const float r2 = __fmul_rn(r, r), r4 = __fmul_rn(r2, r2);
+        const float r7 = __fmul_rn(__fmul_rn(r4, r2), r);
+        p = __fmul_rn(__fdiv_rn(__fmul_rn(q[0], __fmul_rn(q[1], q[1])), 7.0f), r7 - 1.0f);
+        c = q[1];
+        break;
+    }
+    case 5: {  // ESS
+        const float mu = __fdiv_rn(rho, q[0]) - 1.0f;
+        p = __fadd_rn(__fmul_rn(__fmul_rn(mu, q[0]), __fmul_rn(q[1], q[1])),
+                      __fmul_rn(__fmul_rn(u, q[0]), q[2]));
+        if (p < q[3]) p = q[3];
+        c = q[1];
+        break;
+    }
+    default:
+        p = 0.f;
+        break;
+    }
+}
+
+__device__ __forceinline__ int gpuc_material(int itype, int n_mat, unsigned* flags) {
+    const int k = itype < 0 ? -itype : itype;
+    if (k >= n_mat) {
+        atomicOr(flags, (unsigned)FLAG_BAD_MATERIAL);
+        return 0;
+    }
+    return k;
+}
+
+// Cell order of the step: start state, first working copy, sound speeds.
+template <int DIM>
+__global__ void k_gpuc_gather(StateA A, const int* __restrict__ perm, GpucState S,
+                              const DevMaterial* __restrict__ mat, int n_mat,
+                              unsigned* __restrict__ flags, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int j = perm[s];
+    const float4 xh = A.xh[j], vm = A.vm[j];
+    const int it = A.itype[j];
+    float rho = A.rho[j];
+    const float u = A.u[j], p = A.p[j];
+    float pp = 0.f, c = 0.f, r = rho;
+    gpuc_eos(mat[gpuc_material(it, n_mat, flags)], r, u, pp, c);  // Sound of the last update
+    S.x0[s] = xh;
+    S.v0[s] = vm;
+    S.q0[s] = make_float2(rho, u);
+    S.xw[0][s] = xh;
+    S.vw[0][s] = vm;
+    S.sw[0][s] = make_float4(rho, u, p, c);
+    S.itype[s] = it;
+    S.id[s] = A.id[j];
+}
+
+// Wendland C2 with h_i as the GPU-C codes evaluate it (acpu.c:146-201):
+// W = K/h^dim (1 - q/2)^4 (1 + 2q), dW/dr = K/h^(dim+1) 5/8 q (q - 2)^3.
+template <int DIM>
+__device__ __forceinline__ void gpuc_kernel(float r, float h, float K, float& w, float& dwdr) {
+    const float q = __fdiv_rn(r, h);
+    w = 0.f;
+    dwdr = 0.f;
+    if (!(q < 2.f)) return;
+    const float ih = __frcp_rn(h);
+    const float alpha = DIM == 2 ? __fmul_rn(K, __fmul_rn(ih, ih)) : __fmul_rn(K, __fmul_rn(__fmul_rn(ih, ih), ih));
+    float t = fmaf(-0.5f, q, 1.0f);
+    t = __fmul_rn(t, t);
+    t = __fmul_rn(t, t);
+    w = __fmul_rn(__fmul_rn(t, fmaf(2.0f, q, 1.0f)), alpha);
+    const float qm2 = q - 2.0f;
+    dwdr = __fmul_rn(__fmul_rn(__fmul_rn(0.625f, q), __fmul_rn(__fmul_rn(qm2, qm2), qm2)),
+                     __fmul_rn(alpha, ih));
+}
+
+// One RK3 stage: rates of every particle from working copy `cur`, update into
+// `nxt` (X0 + alpha (X + dt dX/dt - X0)), EOS. VAR 1: host path, 2: device.
+template <int DIM, int VAR>
+__global__ void __launch_bounds__(kPassThreads)
+    k_gpuc_stage(GpucState S, int cur, const unsigned* __restrict__ keys,
+                 const int* __restrict__ start, const DevGrid* __restrict__ gp, DevParams P,
+                 const DevMaterial* __restrict__ mat, int n_mat, unsigned* __restrict__ flags,
+                 float alpha, float dt, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const DevGrid g = *gp;
+    // working copies picked without indexing the parameter arrays (no stack)
+    const float4* __restrict__ xc = cur ? S.xw[1] : S.xw[0];
+    const float4* __restrict__ vc = cur ? S.vw[1] : S.vw[0];
+    const float4* __restrict__ sc = cur ? S.sw[1] : S.sw[0];
+    float4* __restrict__ xo = cur ? S.xw[0] : S.xw[1];
+    float4* __restrict__ vo = cur ? S.vw[0] : S.vw[1];
+    float4* __restrict__ so = cur ? S.sw[0] : S.sw[1];
+    const float4 x0i = S.x0[i], v0i = S.v0[i];
+    const float2 q0 = S.q0[i];
+    const float4 xi = xc[i], vi = vc[i], si = sc[i];
+    const int it = S.itype[i];
+    const float hi = x0i.w;
+    const float mi = mass_of<DIM>(x0i, v0i);
+    const float lim = __fmul_rn(2.0f, hi);
+    const float K = P.kw_hi;
+    float w0, d0;
+    gpuc_kernel<DIM>(0.f, hi, K, w0, d0);
+    float rd = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    if (g.ok) {
+        const CellCoord cc = decode_key<DIM>(keys[i], g);
+        for_candidates<DIM>(g, start, cc, [&](int k) {
+            if (k == i) return;
+            const float4 x0k = __ldg(S.x0 + k);
+            // updateListHost's test on the step's start positions
+            const float e0 = __fsub_rn(x0i.x, x0k.x), e1 = __fsub_rn(x0i.y, x0k.y);
+            float r2 = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
+            if (DIM == 3) {
+                const float e2 = __fsub_rn(x0i.z, x0k.z);
+                r2 = __fadd_rn(r2, __fmul_rn(e2, e2));
+            }
+            if (!(__fsqrt_rn(r2) < lim)) return;
+            const float4 xk = __ldg(xc + k), vk = __ldg(vc + k);
+            const float4 sk = __ldg(sc + k);
+            const int itk = __ldg(S.itype + k);
+            const float dx = xi.x - xk.x, dy = xi.y - xk.y, dz = (DIM == 3) ? xi.z - xk.z : 0.f;
+            const float dr = __fsqrt_rn(fmaf(dz, dz, fmaf(dy, dy, __fmul_rn(dx, dx))));
+            if (dr < __fmul_rn(0.01f, hi)) return;  // dr := 100 h: W = dW/dr = 0 (acpu.c:379)
+            float w, dwdr;
+            gpuc_kernel<DIM>(dr, hi, K, w, dwdr);
+            const float mk = (DIM == 2) ? __ldg(&S.x0[k].z) : __ldg(&S.v0[k].w);
+            const float dvr = fmaf(dz, vi.z - vk.z, fmaf(dy, vi.y - vk.y, __fmul_rn(dx, vi.x - vk.x)));
+            const float rhoi = si.x, rhok = sk.x;
+            const float ir = __fdiv_rn(1.0f, dr);
+            float f = 0.f;  // times dW/dr along (x_i - x_k)/dr
+            const bool same = it == itk;
+            if (VAR == 1 || same) {
+                rd = fmaf(__fmul_rn(mk, dvr), __fmul_rn(dwdr, ir), rd);
+                if (VAR == 1)
+                    f = __fmul_rn(mk, __fdiv_rn(-(si.z + sk.z), __fmul_rn(rhoi, rhok)));
+                else
+                    f = __fmul_rn(mk, -(__fdiv_rn(si.z, __fmul_rn(rhoi, rhoi)) +
+                                        __fdiv_rn(sk.z, __fmul_rn(rhok, rhok))));
+                const float cs = __fdiv_rn(__fmul_rn(2.0f, si.w), rhoi + rhok);
+                rd = fmaf(__fmul_rn(mk, __fmul_rn(rhoi - rhok, cs)), dwdr, rd);
+                if (dvr < 0.f) {
+                    const float sh = __fdiv_rn(__fmul_rn(dvr, hi), fmaf(0.01f * hi, hi, __fmul_rn(dr, dr)));
+                    f = fmaf(mk, __fmul_rn(__fmul_rn(sh, cs), 0.03f), f);
+                }
+            }
+            float push = 0.f;
+            if (!same) {
+                if (VAR == 1)
+                    push = __fmul_rn(__fdiv_rn(mk, mi + mk),
+                                     __fdiv_rn(__fmul_rn(__fmul_rn(0.02f, __fdiv_rn(w, w0)), __fmul_rn(si.w, sk.w)), dr));
+                else
+                    push = __fmul_rn(__fdiv_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, w), mk), rhok), __ldg(&S.x0[k].w)),
+                                     __fmul_rn(sk.w, sk.w));
+            }
+            const float tot = __fmul_rn(fmaf(f, dwdr, push), ir);
+            a0 = fmaf(tot, dx, a0);
+            a1 = fmaf(tot, dy, a1);
+            if (DIM == 3) a2 = fmaf(tot, dz, a2);
+        });
+    }
+    if (it > 0) {  // updateLoadsHost: gravity zone over every fluid particle
+        a0 += P.gravity[0];
+        a1 += P.gravity[1];
+        if (DIM == 3) a2 += P.gravity[2];
+    }
+    const float du = __fdiv_rn(__fmul_rn(si.z, rd), __fmul_rn(si.x, si.x));  // balanceEnergyHost
+    S.rates[i] = make_float4(a0, a1, a2, du);
+    float4 xn = xi, vn = vi, sn = si;
+    if (VAR == 2 || it != 0) {  // acpu.c:899 leaves itype 0 alone
+        xn.x = fmaf(alpha, fmaf(dt, vi.x, xi.x) - x0i.x, x0i.x);
+        xn.y = fmaf(alpha, fmaf(dt, vi.y, xi.y) - x0i.y, x0i.y);
+        if (DIM == 3) xn.z = fmaf(alpha, fmaf(dt, vi.z, xi.z) - x0i.z, x0i.z);
+        vn.x = fmaf(alpha, fmaf(dt, a0, vi.x) - v0i.x, v0i.x);
+        vn.y = fmaf(alpha, fmaf(dt, a1, vi.y) - v0i.y, v0i.y);
+        if (DIM == 3) vn.z = fmaf(alpha, fmaf(dt, a2, vi.z) - v0i.z, v0i.z);
+        float rho = fmaf(alpha, fmaf(dt, rd, si.x) - q0.x, q0.x);
+        const float u = fmaf(alpha, fmaf(dt, du, si.y) - q0.y, q0.y);
+        const DevMaterial& M = mat[gpuc_material(it, n_mat, flags)];
+        if ((VAR == 1 && it <= 0) || M.type == 0) {  // velocity kept
+            vn.x = v0i.x;
+            vn.y = v0i.y;
+            if (DIM == 3) vn.z = v0i.z;
+        }
+        float p = 0.f, c = si.w;
+        gpuc_eos(M, rho, u, p, c);
+        sn = make_float4(rho, u, p, c);
+        const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + rho + u + p;
+        if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
+    }
+    xo[i] = xn;
+    vo[i] = vn;
+    so[i] = sn;
+}
+
+// The step's result back to A (cell order of this step, like the force pass).
+template <int DIM>
+__global__ void k_gpuc_scatter(GpucState S, int cur, StateA A, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float4 sv = (cur ? S.sw[1] : S.sw[0])[s];
+    A.xh[s] = (cur ? S.xw[1] : S.xw[0])[s];
+    A.vm[s] = (cur ? S.vw[1] : S.vw[0])[s];
+    A.rho[s] = sv.x;
+    A.u[s] = sv.y;
+    A.p[s] = sv.z;
+    A.ap[s] = S.rates[s];
+    A.itype[s] = S.itype[s];
+    A.id[s] = S.id[s];
+}
+
+}  // namespace ag

@@ -41,6 +41,7 @@ enum DevFlag : unsigned {
     FLAG_NONFINITE = 2u,
     FLAG_OUT_OF_GRID = 4u,
     FLAG_PERIODIC_SMALL = 8u,
+    FLAG_BAD_MATERIAL = 16u,  // an itype outside the material table (GPU-C schemes)
 };
 
 struct DevGrid {

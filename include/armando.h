@@ -101,7 +101,41 @@ typedef struct armando_params {
                                      velocity). Needs a context created with wall_model 3,
                                      no periodic axis, no sort skin; not in batches or
                                      the reverse mode.                                    */
+    int32_t scheme;           /* the step's scheme:
+                                 0 = CERN-F77 leapfrog with summation density (the
+                                     default; CERNsource/time_integration.f:131-218);
+                                 1 = GPU-C third-order TVD Runge-Kutta with continuity
+                                     density and the host path's pair physics
+                                     (ArmandoThrust/acpu.c:346-437, 873-966, 2293-2379);
+                                 2 = the same with the device kernels' pair physics
+                                     (ArmandoThrust/armando.cu:429-513, 987-1074).
+                                 Schemes 1 and 2: one armando_step is one RK3 step (3
+                                 rate evaluations, the neighbour list of its start);
+                                 density evolves, EOS per material (|itype| indexes
+                                 the table of armando_set_materials), shock
+                                 corrections instead of art_visc/art_heat, h_i
+                                 kernels, gravity on itype > 0; pa_sph, visc,
+                                 visc_artificial, heat_*, pmin and wall_model do not
+                                 apply (wall_model must be 0). No periodic axis, sort
+                                 skin, batch or reverse mode.                        */
 } armando_params;
+
+/* EOS of one material of the GPU-C schemes (hMatType / hMatProp of
+ * ArmandoThrust/acpu.c; ESS of Code/armando.cu:572-598 on absolute density):
+ *   0 boundary  prop {rho0, c0}: rho >= 0.9 rho0, p = 0, c = c0, velocity kept
+ *   1 ideal gas {-, gamma, pshift}: p = (gamma - 1) rho u + pshift,
+ *               c = sqrt(gamma (gamma - 1) u)
+ *   2 Mie-Gruneisen polynomial {rho0, a1, a2, a3, b0, b1, t1, t2}
+ *   3 Mie-Gruneisen shock {rho0, c0, g0, s0}
+ *   4 Tait {rho0, c0}: p = rho0 c0^2/7 ((rho/rho0)^7 - 1), c = c0
+ *   5 ESS {rho0, c0, g0, pmin}: p = max(pmin, (rho/rho0 - 1) rho0 c0^2 + g0 rho0 u)
+ * (2 and 3 clamp rho >= 0.9 rho0 as 0 and 4 do.) */
+typedef struct armando_material {
+    int32_t eos;
+    float prop[10];
+} armando_material;
+
+#define ARMANDO_MAX_MATERIALS 64
 
 /* Per-step statistics of the last completed call. */
 typedef struct armando_stats {
@@ -351,6 +385,11 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
 armando_status armando_cell_ids_noalloc(const armando_params* params, const float* x,
                                         const float* hsml, int64_t n, int32_t* cell,
                                         void* stream);
+
+/* Material table of the GPU-C schemes (armando_params.scheme 1, 2), entry k for
+ * the particles with |itype| = k; count <= ARMANDO_MAX_MATERIALS. Until it is set,
+ * every entry is Tait with the context's rho0 and c0. */
+armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const armando_material* table);
 
 /* Blocks until the context's stream is idle and returns its sticky status. */
 armando_status armando_sync(armando_ctx* ctx);

@@ -17,7 +17,7 @@ _REPO = os.path.dirname(_HERE)
 if _REPO not in sys.path:
     sys.path.insert(0, _REPO)
 
-from armando_gb300._abi import Params  # noqa: E402  (shared C-ABI struct)
+from armando_gb300._abi import Material, Params  # noqa: E402  (shared C-ABI structs)
 
 LIB_PATH = os.path.join(_HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(_HERE, "_ref", "libacpu.so")
@@ -83,6 +83,11 @@ def lib() -> C.CDLL:
         L.ao_tangent_f64.restype = C.c_int
         L.ao_flops_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double] + [vp] * 11
         L.ao_flops_f64.restype = C.c_int
+        L.ao_gpuc_step_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material), i64,
+                                       C.c_int, C.c_double] + [vp] * 10 + [C.c_int]
+        L.ao_gpuc_step_f64.restype = C.c_int
+        L.ao_gpuc_eos_f64.argtypes = [C.POINTER(Material), i64, vp, vp, vp, vp, vp]
+        L.ao_gpuc_eos_f64.restype = None
         L.ao_ghosts_f64.argtypes = [C.POINTER(Params), i64, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp]
         L.ao_ghosts_f64.restype = i64
         L.ao_hardware_threads.argtypes = []
@@ -229,6 +234,35 @@ def ghosts(params: Params, x, v, h, itype, fp32=True):
     if ng < 0:
         raise RuntimeError("oracle ghosts failed")
     return owner[:ng], wall[:ng], xg[:ng * dim].reshape(ng, dim), vg[:ng * dim].reshape(ng, dim)
+
+
+def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = True):
+    """`steps` TVD-RK3 steps of the GPU-C scheme state.params.scheme (1 host-path,
+    2 device-kernel physics), in place. materials: list of _abi.Material by
+    |itype| (None: Tait with rho0, c0). Returns the last stage's (dvdt, dudt)."""
+    n, dim = state.n, state.dim
+    dv = np.zeros(n * dim)
+    du = np.zeros(n)
+    tab = None
+    nmat = 0
+    if materials is not None:
+        nmat = len(materials)
+        tab = (Material * nmat)(*materials)
+    rc = lib().ao_gpuc_step_f64(C.byref(state.params), nmat, tab, n, steps, dt, _p(state.x),
+                                _p(state.v), _p(state.m), _p(state.rho), _p(state.p), _p(state.u),
+                                _p(state.h), _p(state.itype), _p(dv), _p(du), int(fp32))
+    if rc:
+        raise RuntimeError("oracle gpuc step failed")
+    return dv, du
+
+
+def gpuc_eos(material, rho, u):
+    """EOS of one GPU-C material: (rho after its clamp, p, c)."""
+    rho = np.ascontiguousarray(rho, np.float64)
+    u = np.ascontiguousarray(np.broadcast_to(u, rho.shape), np.float64)
+    r, p, c = np.zeros_like(rho), np.zeros_like(rho), np.zeros_like(rho)
+    lib().ao_gpuc_eos_f64(C.byref(material), rho.size, _p(rho), _p(u), _p(r), _p(p), _p(c))
+    return r, p, c
 
 
 def hardware_threads() -> int:

@@ -8,6 +8,7 @@
 #include "armando_oracle.hpp"
 #include "armando_oracle_gather.hpp"
 #include "armando_oracle_flops.hpp"
+#include "armando_oracle_gpuc.hpp"
 #include "armando_oracle_tangent.hpp"
 
 namespace {
@@ -403,6 +404,66 @@ int64_t ao_ghosts_f64(const armando_params* prm, int64_t n, const double* x, con
         return emit(G);
     } catch (const std::exception&) {
         return -1;
+    }
+}
+
+// GPU-C scheme (params->scheme 1 or 2): `steps` TVD-RK3 steps in place. The
+// material table has nmat entries (NULL: Tait with rho0, c0 for every |itype|).
+// fp32 = 1: neighbour lists in FP32 coordinates (the library's). dvdt, dudt
+// (nullable): rates of the last stage.
+int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
+                     int64_t n, int steps, double dt, double* x, double* v, const double* m,
+                     double* rho, double* p, double* u, const double* h, const int* itype,
+                     double* dvdt, double* dudt, int fp32) {
+    if (prm->scheme != 1 && prm->scheme != 2) return 2;
+    ao::Params<double> P = to_params<double>(prm);
+    ao::GpucSetup<double> G;
+    G.variant = prm->scheme;
+    G.legacy3d = prm->kernel_3d_legacy;
+    for (int d = 0; d < 3; ++d) G.gravity[d] = prm->gravity[d];
+    if (table) {
+        G.mat.resize(nmat);
+        for (int k = 0; k < nmat; ++k) {
+            G.mat[k].type = table[k].eos;
+            for (int q = 0; q < 10; ++q) G.mat[k].prop[q] = table[k].prop[q];
+        }
+    } else {
+        G.mat.resize(ARMANDO_MAX_MATERIALS);
+        for (auto& M : G.mat) {
+            M.type = ao::EOS_TAIT;
+            M.prop[0] = prm->rho0;
+            M.prop[1] = prm->c0;
+        }
+    }
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, nullptr, nullptr);
+    std::vector<double> dv, du;
+    try {
+        for (int k = 0; k < steps; ++k) {
+            if (fp32) ao::gpuc_rk3_step<double, float>(s, G, dt, &dv, &du);
+            else ao::gpuc_rk3_step<double, double>(s, G, dt, &dv, &du);
+        }
+    } catch (const std::exception&) {
+        return 1;
+    }
+    store_state<double>(s, x, v, rho, p, u, nullptr, nullptr);
+    if (dvdt && !dv.empty()) std::memcpy(dvdt, dv.data(), sizeof(double) * n * P.dim);
+    if (dudt && !du.empty()) std::memcpy(dudt, du.data(), sizeof(double) * n);
+    return 0;
+}
+
+// EOS of the GPU-C schemes for one material: rho (clamped where the type
+// clamps), p and c for n states (rho_in, u).
+void ao_gpuc_eos_f64(const armando_material* mat, int64_t n, const double* rho_in, const double* u,
+                     double* rho, double* p, double* c) {
+    ao::GpucMaterial M;
+    M.type = mat->eos;
+    for (int q = 0; q < 10; ++q) M.prop[q] = mat->prop[q];
+    for (int64_t i = 0; i < n; ++i) {
+        double r = rho_in[i], pp = 0.0, cc = 0.0;
+        ao::gpuc_eos(M, r, u[i], pp, cc);
+        rho[i] = r;
+        p[i] = pp;
+        c[i] = cc;
     }
 }
 

@@ -1,0 +1,159 @@
+"""The GPU-C schemes (armando_params.scheme 1 and 2: TVD-RK3, continuity
+density) on the GPU, against the reference's own compiled C host path
+(ArmandoThrust/acpu.c golden vectors, tests/golden/acpu_rk3.npz) and against
+the FP64 oracle.
+
+Gates (normwise relative per output; acpu.c and the library compute in FP32):
+the integrated state x, rho, u within 1e-6 of the reference's; pressure and
+the velocity rates within 2e-4, velocity within 5e-5, because one FP32 ulp of
+rho ~ 1000 is 0.15 Pa of Tait pressure (c0 = 50 m/s).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import armando_gb300 as ag
+from armando_gb300 import cases
+from armando_gb300._abi import Material
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "acpu_rk3.npz")
+TOL = {"x": 1e-6, "rho": 1e-6, "u": 1e-6, "v": 5e-5, "p": 2e-4, "dv": 2e-4, "du": 2e-4}
+
+TAIT = Material.make(4, [1000.0, 50.0, -1.0e12])
+SHOCK = Material.make(3, [1000.0, 50.0, 0.5, 1.3])
+POLY = Material.make(2, [1000.0, 2.5e6, 1.0e6, 2.0e5, 0.2, 0.1, 2.5e6, 5.0e5])
+WALL = Material.make(0, [1000.0, 50.0])
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from armando_gb300 import build
+
+    build.build_library()
+    ag.load_library()
+
+
+@pytest.fixture(scope="module")
+def G():
+    return np.load(GOLD)
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    s = np.abs(b).max()
+    return np.abs(a - b).max() / s if s > 0 else np.abs(a).max()
+
+
+def golden_case(G, pre):
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
+    c.x, c.v, c.mass, c.rho = (G[pre + "_x0"].copy(), G[pre + "_v0"].copy(), G[pre + "_m"].copy(),
+                               G[pre + "_rho0"].copy())
+    c.h, c.itype = G[pre + "_h"].copy(), G[pre + "_itype"].copy()
+    if pre + "_u0" in G:
+        c.u = G[pre + "_u0"].copy()
+    c.dt = float(G[pre + "_dt"])
+    return c
+
+
+def run_gpu(c, steps, materials=None, tuning=None):
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        if materials is not None:
+            ctx.set_materials(materials)
+        if tuning is not None:
+            ctx.set_tuning(*tuning)
+        ctx.integrate(got, c.dt, 1, steps)
+    return got
+
+
+def fields(c):
+    return {"x": c.x, "v": c.v, "rho": c.rho, "p": c.p, "u": c.u, "dv": c.dvdt, "du": c.dudt}
+
+
+@pytest.mark.parametrize("steps", [1, 5])
+@pytest.mark.parametrize("pre", ["water", "multi"])
+def test_matches_acpu_golden(G, pre, steps):
+    c = golden_case(G, pre)
+    mats = [TAIT, TAIT] if pre == "water" else [WALL, TAIT, SHOCK, WALL, POLY]
+    got = fields(run_gpu(c, steps, mats))
+    for f in ("x", "v", "rho", "p", "u", "dv", "du"):
+        ref = G[f"{pre}_{f}_{steps}"]
+        # the water's u is pressure work from u = 0: it carries p's quantization
+        tol = TOL["p"] if (pre == "water" and f == "u") else TOL[f]
+        e = rel(got[f].reshape(ref.shape), ref)
+        assert e <= tol, (pre, steps, f, e)
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_published_dam_break_matches_the_oracle(O, scheme):
+    """The published 6,462-particle dam break (Tab.1 case 1), 10 RK3 steps,
+    both physics variants."""
+    c = cases.gpuc_dam_break(1, scheme=scheme)
+    rng = np.random.default_rng(90 + scheme)
+    v = c.v.reshape(-1, 2)
+    v[c.itype > 0] = rng.normal(0.0, 0.05, size=(c.n_fluid, 2))
+    c.v = v.ravel().astype(np.float32)
+    ref = O.State(c)
+    dv, du = O.gpuc_step(ref, 10, c.dt)
+    got = run_gpu(c, 10)
+    for f, a, b in (("x", got.x, ref.x), ("v", got.v, ref.v), ("rho", got.rho, ref.rho),
+                    ("p", got.p, ref.p), ("dv", got.dvdt, dv)):
+        assert rel(a, b) <= TOL[f] * 2, (scheme, f, rel(a, b))
+
+
+@pytest.mark.parametrize("tuning", [(2, 1, 256, 0), (3, 1, 128, 0)])
+def test_tunings(O, G, tuning):
+    c = golden_case(G, "multi")
+    mats = [WALL, TAIT, SHOCK, WALL, POLY]
+    got = fields(run_gpu(c, 5, mats, tuning))
+    for f in ("x", "v", "rho", "p", "u"):
+        ref = G[f"multi_{f}_5"]
+        assert rel(got[f].reshape(ref.shape), ref) <= TOL[f], (tuning, f)
+
+
+def test_integrate_equals_steps_and_is_deterministic():
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16), scheme=2)
+    a, b, d = c.copy(), c.copy(), c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.integrate(a, c.dt, 1, 6)
+        ctx.integrate(b, c.dt, 1, 6)
+        for its in range(1, 7):
+            ctx.step(d, c.dt, its)
+    for f in ("x", "v", "rho", "p", "u", "dvdt", "dudt"):
+        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        assert np.array_equal(getattr(a, f), getattr(d, f)), f
+
+
+def test_itype_outside_the_table_is_an_error():
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
+    c.itype[c.itype > 0] = 3
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_materials([TAIT, TAIT])
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.step(c.copy(), c.dt, 1)
+        assert e.value.status == ag._abi.ERR_INVALID_ARG
+
+
+def test_refusals():
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_tuning(1, 1, 128, 20)
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.forward_checkpointed(c.copy(), c.dt, 1, 4, 2)
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_materials([Material.make(9, [1.0])])
+        assert e.value.status == ag._abi.ERR_INVALID_ARG
+    with pytest.raises(ag.ArmandoError) as e:
+        ag.Batch([c.params, c.params], [c.n_fluid] * 2, [c.n_wall] * 2)
+    assert e.value.status == ag._abi.ERR_UNSUPPORTED
+    bad = c.params.copy()
+    bad.wall_model = 1
+    with pytest.raises(ag.ArmandoError) as e:
+        ag.Context(bad, c.n_fluid, c.n_wall)
+    assert e.value.status == ag._abi.ERR_INVALID_ARG
