@@ -79,7 +79,7 @@ def parse():
                     help="reach,threads_per_particle,block[,skin] instead of the autotuner")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--checkpoint-every", type=int, default=50)
-    ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint"],
+    ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint", "gpuc"],
                     help="run one extra workload alone and print its JSON")
     ap.add_argument("--config", default="dambreak2d", choices=["dambreak2d", "channel3d"])
     ap.add_argument("--dx", type=float, default=None,
@@ -411,6 +411,45 @@ def run_channel(args):
                                  step_bytes(3, cells_pp), peaks()[0])}
 
 
+# Published GPU-C numbers (ArmandoOnGPU.pdf p.5 Tab.1, Tesla C1060): particles,
+# steps, GPU seconds of the 2D dam break cases 1-3 (TVD-RK3 steps).
+GPUC_PUBLISHED = {1: (6462, 10000, 19.0), 2: (22899, 20000, 81.0), 4: (85773, 40000, 514.0)}
+
+
+def run_gpuc(args):
+    """The GPU-C codes' 2D dam break, the published Tab.1 cases 1-3 (6,462 /
+    22,899 / 85,773 particles), TVD-RK3 steps of scheme 1 (the host path's
+    physics) on device-resident state; the published C1060 rate beside each."""
+    import torch
+
+    import armando_gb300 as ag
+    from armando_gb300 import cases
+
+    out = []
+    for scale, (n_pub, steps_pub, sec_pub) in GPUC_PUBLISHED.items():
+        c = cases.gpuc_dam_break(scale)
+        assert c.n == n_pub
+        dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
+        with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+            tuned = tune(ctx, args, dev, c.dt)
+            tuned.pop("ms_per_step", None)
+            ctx.integrate(dev, c.dt, 1, 5)
+            steps = max(50, args.extra_steps * 10)
+            l0 = ctx.stats().gpu_launches
+            ms = timed_integrate(ctx, dev, c.dt, 6, steps)
+            launches = (ctx.stats().gpu_launches - l0) / steps
+        del dev
+        v = c.n * steps / (ms * 1e-3)
+        pub = n_pub * steps_pub / sec_pub
+        out.append({"case": f"dam break case {[1, 2, 4].index(scale) + 1}", "particles": c.n,
+                    "steps": steps, "ms_per_step": ms / steps, "value": v, "unit": METRIC,
+                    "published_c1060": pub, "ratio_to_published": v / pub,
+                    "launches_per_step": launches, "tuning": tuned})
+    torch.cuda.empty_cache()
+    return {"workload": "GPU-C TVD-RK3 dam break (scheme 1), the published Tab.1 cases; "
+                        "one step = 3 rate evaluations", "cases": out}
+
+
 def run_sweep(args):
     """Batched sweep vs the plain step run instance by instance on the same GPU."""
     import torch
@@ -657,7 +696,7 @@ def run_ours(args, rank, world, local_rank):
             out["cpu_baseline"] = cpu_baseline(make_case(args.config, args.dx), args.cpu_seconds)
     if not args.no_extras and rank == 0 and world == 1:
         out["workloads"] = {"channel3d": run_channel(args), "sweep": run_sweep(args),
-                            "adjoint": run_adjoint(args)}
+                            "adjoint": run_adjoint(args), "gpuc": run_gpuc(args)}
     return out
 
 
@@ -674,7 +713,8 @@ def main():
         import torch
 
         torch.cuda.set_device(local_rank)
-        run = {"channel3d": run_channel, "sweep": run_sweep, "adjoint": run_adjoint}[args.only]
+        run = {"channel3d": run_channel, "sweep": run_sweep, "adjoint": run_adjoint,
+               "gpuc": run_gpuc}[args.only]
         if rank == 0:
             print(json.dumps({"workload_only": args.only, **run(args)}), flush=True)
         return
