@@ -247,6 +247,16 @@ class Context:
             table[key] = float(ms[k])
         return best.as_tuple(), table
 
+    def get_hsml(self, out=None):
+        """Smoothing lengths after the last call, in caller order (evolved when
+        params.sle != 0)."""
+        if out is None:
+            if self.mem == MEM_DEVICE:
+                raise ValueError("pass a device array for a device-memory context")
+            out = np.zeros(self.n, np.float32)
+        self._check(self._lib.armando_get_hsml(self._h, _ptr(out)))
+        return out
+
     def set_materials(self, materials):
         """Material table of the GPU-C schemes: a list of _abi.Material (or
         (eos, props) pairs), entry k for the particles with |itype| = k."""

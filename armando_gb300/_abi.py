@@ -70,6 +70,9 @@ class Params(C.Structure):
         ("period_hi", F3),
         ("wall_model", C.c_int32),
         ("scheme", C.c_int32),
+        ("density_form", C.c_int32),
+        ("average_velocity", C.c_int32),
+        ("sle", C.c_int32),
     ]
 
     @classmethod
@@ -182,7 +185,7 @@ EXPORTED = [
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
     "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
-    "armando_set_materials",
+    "armando_set_materials", "armando_get_hsml",
 ]
 N_TUNINGS = 27
 N_PHASES = 6
@@ -265,6 +268,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_write_vtk.restype = C.c_int
     lib.armando_set_materials.argtypes = [vp, C.c_int32, C.POINTER(Material)]
     lib.armando_set_materials.restype = C.c_int
+    lib.armando_get_hsml.argtypes = [vp, vp]
+    lib.armando_get_hsml.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

@@ -152,6 +152,10 @@ struct armando_ctx {
         *d_ng = nullptr, *h_ng = nullptr;
     unsigned *g_tile_count = nullptr, *g_tile_off = nullptr;
     int64_t ghosts_last = 0;
+    // single_step options: drho/dt carried between calls in caller order
+    // (continuity density) and the buffers of the options, allocated on first use.
+    float* drho_caller = nullptr;
+    bool options_ready = false;
     // GPU-C schemes (scheme 1, 2): the RK3 working state in cell order and the
     // material table (default: Tait with rho0, c0 for every |itype|).
     GpucState gs{};
@@ -216,6 +220,11 @@ armando_status validate_params(const armando_params* p, int dim, std::string& wh
                 why = "mirror ghosts (wall_model 3) need a system without periodic axes";
                 return ARMANDO_ERR_INVALID_ARG;
             }
+    if (p->density_form < 0 || p->density_form > 2 || (p->average_velocity != 0 && p->average_velocity != 1) ||
+        p->sle < 0 || p->sle > 2) {
+        why = "density_form must be 0-2, average_velocity 0 or 1, sle 0-2";
+        return ARMANDO_ERR_INVALID_ARG;
+    }
     if (p->scheme < 0 || p->scheme > 2) {
         why = "scheme must be 0, 1 or 2";
         return ARMANDO_ERR_INVALID_ARG;
@@ -238,6 +247,9 @@ DevParams make_dev_params(const armando_params& p, int reach = 1) {
     DevParams d{};
     d.reach = reach;
     d.wall_model = p.wall_model;
+    d.density_form = p.density_form;
+    d.xsph = p.average_velocity;
+    d.sle = p.sle;
     d.dim = p.dim;
     d.pa_sph = p.pa_sph;
     d.visc = p.visc;
@@ -282,6 +294,7 @@ StepArgs make_args(const armando_ctx* c, float dt, int its) {
     s.kdt = (its == 1) ? 0.5f * dt : dt;
     s.hdt = (its == 1) ? 0.f : 0.5f * dt;
     s.heat_on = c->prm.heat_external && ((double)its * (double)dt <= (double)c->prm.heat_t_end);
+    s.dform = c->prm.density_form;
     return s;
 }
 
@@ -345,16 +358,18 @@ int launch_resort_advance(armando_ctx* ctx) {
     return 1;
 }
 
-// Calls f(tpp, block, periodic, lean) with the context's tuning, whether any
-// axis is periodic and whether the physics is lean (no physical viscosity, no
-// artificial heat) as compile-time constants. Lean variants exist for one
-// thread per particle.
+// Calls f(tpp, block, periodic, lean, opt) with the context's tuning, whether
+// any axis is periodic, whether the physics is lean (no physical viscosity, no
+// artificial heat, no wall push, no step option) and whether a single_step
+// option (continuity or normalised density, XSPH, h evolution) is on, as
+// compile-time constants. Lean variants exist for one thread per particle.
 template <class F>
-void with_tuning(const armando_tuning& t, bool per, bool lean, F&& f) {
+void with_tuning(const armando_tuning& t, bool per, bool lean, bool opt, F&& f) {
     using std::integral_constant;
     auto pick_lean = [&](auto tpp, auto bs, auto pr) {
-        if (decltype(tpp)::value == 1 && lean) f(tpp, bs, pr, std::true_type{});
-        else f(tpp, bs, pr, std::false_type{});
+        if (opt) f(tpp, bs, pr, std::false_type{}, std::true_type{});
+        else if (decltype(tpp)::value == 1 && lean) f(tpp, bs, pr, std::true_type{}, std::false_type{});
+        else f(tpp, bs, pr, std::false_type{}, std::false_type{});
     };
     auto pick_per = [&](auto tpp, auto bs) {
         if (per) pick_lean(tpp, bs, std::true_type{});
@@ -370,16 +385,24 @@ void with_tuning(const armando_tuning& t, bool per, bool lean, F&& f) {
 }
 
 bool any_periodic(const DevParams& p) { return p.periodic[0] || p.periodic[1] || p.periodic[2]; }
-bool lean_physics(const DevParams& p) { return !p.visc && !p.heat_art && p.wall_model == 0; }
+bool lean_physics(const DevParams& p) {
+    return !p.visc && !p.heat_art && p.wall_model == 0 && p.density_form == 0 && !p.xsph && !p.sle;
+}
+
+// Whether the parameters use a single_step option beyond summation density.
+bool step_options(const armando_params& p) {
+    return p.density_form != 0 || p.average_velocity != 0 || p.sle != 0;
+}
 
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
     const int n = (int)ctx->n_work;
-    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
-                [&](auto tpp, auto bs, auto per, auto lean) {
+    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
+                [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
-        k_density<DIM, T, BSZ, PER, LEAN><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool OPT = decltype(opt)::value;
+        k_density<DIM, T, BSZ, PER, LEAN, OPT><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
     });
 }
@@ -387,11 +410,12 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
 template <int DIM>
 void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     const int n = (int)ctx->n_work;
-    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp),
-                [&](auto tpp, auto bs, auto per, auto lean) {
+    with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
+                [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
-        k_force<DIM, T, BSZ, PER, LEAN><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool OPT = decltype(opt)::value;
+        k_force<DIM, T, BSZ, PER, LEAN, OPT><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
     });
 }
@@ -990,6 +1014,41 @@ armando_status build_wall_grid(armando_ctx* ctx) {
     return ctx->dim == 2 ? build_wall_grid_dim<2>(ctx) : build_wall_grid_dim<3>(ctx);
 }
 
+// single_step options: the buffers on first use (graphs that captured the old
+// pointers are dropped) and the carried drho/dt into A (caller order after
+// load_inputs).
+armando_status prepare_options(armando_ctx* ctx) {
+    if (!step_options(ctx->prm)) return ARMANDO_OK;
+    cudaError_t e = cudaSuccess;
+    if (!ctx->options_ready) {
+        const size_t n = (size_t)std::max<int64_t>(ctx->cap, 1);
+        ctx->A.drho = dalloc<float>(n, e);
+        ctx->B.q = dalloc<float>(n, e);
+        ctx->B.rlo = dalloc<float>(n, e);
+        ctx->drho_caller = dalloc<float>(n, e);
+        for (void* q : {(void*)ctx->A.drho, (void*)ctx->B.q, (void*)ctx->B.rlo, (void*)ctx->drho_caller})
+            ctx->owned.push_back(q);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(step options)");
+        CK(cudaMemsetAsync(ctx->drho_caller, 0, n * sizeof(float), ctx->stream));
+        ctx->options_ready = true;
+        free_graphs(ctx);
+    }
+    CK(cudaMemcpyAsync(ctx->A.drho, ctx->drho_caller, (size_t)ctx->n * sizeof(float),
+                       cudaMemcpyDeviceToDevice, ctx->stream));
+    return ARMANDO_OK;
+}
+
+// After a call: drho/dt back to caller order for the next call.
+armando_status keep_options(armando_ctx* ctx) {
+    if (!ctx->options_ready || ctx->n == 0) return ARMANDO_OK;
+    const int n = (int)ctx->n;
+    k_scatter_by_id<<<blocks_for(n, 256), 256, 0, ctx->stream>>>(ctx->A.drho, ctx->A.id,
+                                                                 ctx->drho_caller, n);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    return ARMANDO_OK;
+}
+
 // GPU-C schemes: the working state (first use) and the material table of
 // this call.
 armando_status prepare_gpuc(armando_ctx* ctx) {
@@ -1328,10 +1387,11 @@ armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
 armando_status check_adjoint_support(armando_ctx* ctx) {
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
     const armando_params& p = ctx->prm;
-    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0 || p.scheme != 0)
+    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0 || p.scheme != 0 ||
+        step_options(p))
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
-                    "reverse mode supports pa_sph = 1, wall_model 0, without physical viscosity "
-                    "and artificial heat");
+                    "reverse mode supports pa_sph = 1, wall_model 0, summation density, without "
+                    "physical viscosity, artificial heat, XSPH or h evolution");
     return ARMANDO_OK;
 }
 
@@ -1603,9 +1663,9 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
     ctx->mem_kind = mem_kind;
     if (n_inst > 1)
         for (int k = 0; k < n_inst; ++k)
-            if (params[k].wall_model == 3 || params[k].scheme != 0) {
+            if (params[k].wall_model == 3 || params[k].scheme != 0 || step_options(params[k])) {
                 delete ctx;
-                return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "batches run the CERN scheme without mirror ghosts");
+                return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "batches run the CERN summation-density step without mirror ghosts");
             }
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -1793,6 +1853,7 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
         if (st == ARMANDO_OK) st = plan_grid(ctx);
         if (st == ARMANDO_OK) st = build_wall_grid(ctx);
         if (st == ARMANDO_OK) st = prepare_gpuc(ctx);
+        if (st == ARMANDO_OK) st = prepare_options(ctx);
         // Two untimed iterations capture the graphs of the first and of the
         // following iterations; then the timed ones.
         for (int w = 0; w < 2 && st == ARMANDO_OK; ++w) st = run_step(ctx, make_args(ctx, dt, its0 + w));
@@ -1895,10 +1956,14 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     if (st != ARMANDO_OK) return st;
     st = prepare_gpuc(ctx);
     if (st != ARMANDO_OK) return st;
+    st = prepare_options(ctx);
+    if (st != ARMANDO_OK) return st;
     for (int k = 0; k < steps; ++k) {
         st = run_step(ctx, make_args(ctx, dt, its0 + k));
         if (st != ARMANDO_OK) return st;
     }
+    st = keep_options(ctx);
+    if (st != ARMANDO_OK) return st;
     ctx->last_dt = dt;
     ctx->next_its = its0 + steps;
     st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
@@ -2264,6 +2329,23 @@ armando_status armando_get_stats(const armando_ctx* cctx, armando_stats* out) {
 
 const char* armando_last_error(const armando_ctx* ctx) {
     return ctx ? ctx->err.c_str() : g_last_error;
+}
+
+armando_status armando_get_hsml(armando_ctx* ctx, float* hsml) {
+    if (!ctx || !hsml) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if (ctx->n == 0) return ARMANDO_OK;
+    CK(cudaSetDevice(ctx->device));
+    const int n = (int)ctx->n;
+    cudaStream_t st = ctx->stream;
+    float* dst = hsml;
+    if (ctx->mem_kind == ARMANDO_MEM_HOST) dst = ctx->s_h;
+    k_hsml_out<<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, dst, n);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    if (ctx->mem_kind == ARMANDO_MEM_HOST)
+        CK(cudaMemcpyAsync(hsml, ctx->s_h, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return ARMANDO_OK;
 }
 
 armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const armando_material* table) {

@@ -79,6 +79,9 @@ struct DevParams {
     // different itype; 3 like 0 plus mirror ghosts (particles with id >= n_real).
     int wall_model;
     int n_real;          // real particles; ids from n_real on are mirror ghosts
+    // single_step options: density 0 summation, 1 continuity, 2 normalised
+    // summation; XSPH; smoothing-length evolution 0, 1, 2.
+    int density_form, xsph, sle, pad2_;
 };
 
 __host__ __device__ inline bool repulsive_walls(const DevParams& P) {
@@ -90,6 +93,7 @@ struct StepArgs {
     float hdt;    // predictor half step: dt/2 (its > 1) or 0 (its == 1)
     float dt;     // drift
     int heat_on;  // external heat gate its*dt <= t_end
+    int dform;    // density form (1: the predictor advances rho with the carried drho/dt)
 };
 
 struct StateA {  // integrated state (slot order of the last sort)
@@ -102,6 +106,7 @@ struct StateA {  // integrated state (slot order of the last sort)
     int* itype;
     int* id;
     int* inst;  // instance of each slot (batches; nullptr for one system)
+    float* drho;  // drho/dt of the last iteration (continuity density; else nullptr)
 };
 
 struct StateB {  // working set of one step (cell order)
@@ -116,6 +121,8 @@ struct StateB {  // working set of one step (cell order)
     float4* tau2;  // {xz, yz, -, -}
     float* tds;    // T ds/dt
     float* ulo;    // rounding residual of the predicted energy u (rp.z + ulo exact)
+    float* q;      // density at the iteration's start (continuity and normalised density)
+    float* rlo;    // rounding residual of the predicted density (continuity)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
     float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour bits of each fluid slot over its first 32 * mask_words<DIM>()
@@ -691,6 +698,19 @@ __global__ void k_load_xh(const float* __restrict__ x, const float* __restrict__
 }
 
 // inv[id[s]] = s: the cell-order slot of each caller index.
+// dst[id[s]] = src[s]: a slot-order array back to caller order.
+__global__ void k_scatter_by_id(const float* __restrict__ src, const int* __restrict__ id,
+                                float* __restrict__ dst, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dst[id[s]] = src[s];
+}
+
+// Smoothing lengths of A in caller order.
+__global__ void k_hsml_out(StateA A, float* __restrict__ h, int n) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) h[A.id[s]] = A.xh[s].w;
+}
+
 __global__ void k_invert_ids(const int* __restrict__ id, int* __restrict__ inv, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < n) inv[id[s]] = s;
@@ -801,9 +821,19 @@ __global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, 
         }
     }
     if (B.ulo) B.ulo[s] = ulo;
+    // Continuity density: rho + dt/2 drho/dt as hi + lo (time_integration.f:
+    // 144-147), the start density kept for the corrector.
+    float rho = A.rho[j], rlo = 0.f;
+    if (B.q) B.q[s] = rho;
+    if (S.dform == 1 && it > 0 && S.hdt != 0.f) {
+        const sph::ff rh = sph::two_sum(rho, __fmul_rn(S.hdt, A.drho[j]));
+        rho = rh.hi;
+        rlo = rh.lo;
+    }
+    if (B.rlo) B.rlo[s] = rlo;
     B.xh[s] = xh;
     B.vm[s] = vm;
-    B.rp[s] = make_float4(A.rho[j], 0.f, u, 0.f);
+    B.rp[s] = make_float4(rho, 0.f, u, 0.f);
     B.p[s] = A.p[j];
     B.itype[s] = it;
     B.id[s] = A.id[j];
@@ -1214,7 +1244,7 @@ __device__ __forceinline__ int lane_len(const Cursor& cu) {
 // ---------------------------------------------------------------------------
 // LEAN: the parameters have no physical viscosity and no artificial heat, so
 // their operands and branches are compiled out.
-template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false>
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
@@ -1243,7 +1273,12 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     const float mi = mass_of<DIM>(xi, vi);
     // Self density m_i W(0, h_i) (density.f:39-42), on the particle's first lane.
     sph::ff S = sph::ff_mul_f(al_i, mi);
-    if (sub != 0) S = sph::ff{0.f, 0.f};
+    // Normalised summation (nor_density, density.f:65-158): the denominator
+    // m_i W(0)/rho_i + sum_j m_j/rho_j W_ij on the start densities, float-float.
+    const bool nor = OPT && P.density_form == 2 && fluid;
+    sph::ff Wn = sph::ff{0.f, 0.f};
+    if (nor) Wn = sph::ff_mul(S, sph::ff_recip(B.q[s]));
+    if (sub != 0) S = Wn = sph::ff{0.f, 0.f};
     const float ihf = ih_i.hi;
     const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
     const float kwf = P.kw_hi * (DIM == 2 ? ihf * ihf : ihf * ihf * ihf);
@@ -1315,7 +1350,11 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
                 al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
             }
-            if (fluid) sph::ff_acc(S, sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj));
+            if (fluid) {
+                const sph::ff wm = sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj);
+                sph::ff_acc(S, wm);
+                if (nor) sph::ff_acc(Wn, sph::ff_mul(wm, sph::ff_recip(__ldg(B.q + k))));
+            }
             if (need_div) {
                 const float dr2 = sph::dist2_exact<DIM>(dh);
                 const float gw = sph::wendland_grad_factor<DIM>(
@@ -1348,7 +1387,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 float tt = fmaf(-0.5f, q, 1.0f);
                 tt = tt * tt;
                 tt = tt * tt;
-                sph::ff_acc(S, sph::ff{kwh * mj * tt * fmaf(2.0f, q, 1.0f), 0.f});
+                const float wm = kwh * mj * tt * fmaf(2.0f, q, 1.0f);
+                sph::ff_acc(S, sph::ff{wm, 0.f});
+                if (nor) sph::ff_acc(Wn, sph::ff{__fdiv_rn(wm, __ldg(B.q + k)), 0.f});
             }
             if (need_div) {
                 const float t3 = q - 2.0f;
@@ -1365,6 +1406,10 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         for (int o = 1; o < TPP; o <<= 1) {
             const sph::ff t = {__shfl_xor_sync(gm, S.hi, o), __shfl_xor_sync(gm, S.lo, o)};
             sph::ff_acc(S, t);
+            if (OPT) {
+                const sph::ff tw = {__shfl_xor_sync(gm, Wn.hi, o), __shfl_xor_sync(gm, Wn.lo, o)};
+                sph::ff_acc(Wn, tw);
+            }
         }
         divs = group_sum<TPP>(divs);
     }
@@ -1389,7 +1434,16 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     }
     float rho = rp.x;
     if (fluid) {
-        float drho = __fadd_rn(__fsub_rn(S.hi, P.rho0), S.lo);
+        float drho;
+        if (OPT && P.density_form == 1) {  // continuity: the predicted density
+            drho = __fadd_rn(__fsub_rn(rp.x, P.rho0), B.rlo[s]);
+        } else if (nor) {  // S / Wn to float-float accuracy
+            const float qh = __fdiv_rn(S.hi, Wn.hi);
+            const float res = fmaf(-qh, Wn.hi, S.hi) + S.lo - qh * Wn.lo;
+            drho = __fadd_rn(__fsub_rn(qh, P.rho0), __fdiv_rn(res, Wn.hi));
+        } else {
+            drho = __fadd_rn(__fsub_rn(S.hi, P.rho0), S.lo);
+        }
         p = sph::tait_poly(__fmul_rn(drho, P.inv_rho0), P.B);
         if (p < P.pmin) {  // eos.f90:277-280
             p = 0.f;
@@ -1480,7 +1534,7 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // ---------------------------------------------------------------------------
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
-template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false>
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
@@ -1528,6 +1582,9 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     const float ulo_i = (work && heat_art) ? B.ulo[s] : 0.f;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, he_sum = 0.f, av_du = 0.f, ah_du = 0.f;
+    // single_step options: continuity drho/dt, XSPH velocity, div v for h
+    const bool cont = OPT && P.density_form == 1, xsph = OPT && P.xsph, sle2 = OPT && P.sle == 2;
+    float drho_s = 0.f, divh = 0.f, x0s = 0.f, x1s = 0.f, x2s = 0.f;
     constexpr int W = mask_words<DIM>() / TPP;  // mask words of this lane
     const size_t mlane = (size_t)s * TPP + sub;
     Cursor cu = cursor_begin<DIM>(g);
@@ -1656,6 +1713,22 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             const float gw = kgih * t3 * t3 * t3;
             const float w0 = gw * d[0], w1 = gw * d[1], w2 = (DIM == 3) ? gw * d[2] : 0.f;
             const float vx = vj.x - vi.x, vy = vj.y - vi.y, vz = (DIM == 3) ? vj.z - vi.z : 0.f;
+            if (cont || sle2) {  // (v_j - v_i) . grad_i W
+                float vdw = fmaf(vy, w1, __fmul_rn(vx, w0));
+                if (DIM == 3) vdw = fmaf(vz, w2, vdw);
+                if (cont) drho_s = fmaf(-mj, vdw, drho_s);  // con_density, density.f:203-216
+                if (sle2) divh = fmaf(__fdiv_rn(mj, rpj.x), vdw, divh);  // hsml.f:75-90
+            }
+            if (xsph) {  // av_vel.f:47-58: -eps m_j / rho_ij (v_i - v_j) W_ij, eps = 0.3
+                float tt = fmaf(-0.5f, q, 1.0f);
+                tt = tt * tt;
+                tt = tt * tt;
+                const float wv = P.kw_hi * (DIM == 2 ? ih * ih : ih * ih * ih) * tt * fmaf(2.0f, q, 1.0f);
+                const float c = __fdiv_rn(0.3f * mj * wv, 0.5f * (rpi.x + rpj.x));
+                x0s = fmaf(c, vx, x0s);
+                x1s = fmaf(c, vy, x1s);
+                if (DIM == 3) x2s = fmaf(c, vz, x2s);
+            }
             // Pressure (internal_force.f:309-428 for pa_sph 1, 179-306 for pa_sph 0).
             const float fs = -(rpi.y + rpj.y);
             // Products that feed a sum are written out (fmaf / __fmul_rn) so that
@@ -1726,6 +1799,13 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         he_sum = group_sum<TPP>(he_sum);
         av_du = group_sum<TPP>(av_du);
         ah_du = group_sum<TPP>(ah_du);
+        if (cont) drho_s = group_sum<TPP>(drho_s);
+        if (sle2) divh = group_sum<TPP>(divh);
+        if (xsph) {
+            x0s = group_sum<TPP>(x0s);
+            x1s = group_sum<TPP>(x1s);
+            if (DIM == 3) x2s = group_sum<TPP>(x2s);
+        }
     }
     if (!work || sub != 0) return;
     float du = __fadd_rn(fmaf(0.5f, he_sum, av_du), ah_du);  // internal_force.f:433-435
@@ -1748,9 +1828,23 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     vn.x = fmaf(S.kdt, a0, vmin.x);
     vn.y = fmaf(S.kdt, a1, vmin.y);
     if (DIM == 3) vn.z = fmaf(S.kdt, a2, vmin.z);
+    if (xsph && S.hdt != 0.f) {  // time_integration.f:195: v = v_min + dt dv + av
+        vn.x += x0s;
+        vn.y += x1s;
+        if (DIM == 3) vn.z += x2s;
+    }
     float un = fmaf(S.kdt, du, vmin.w);
     if (un < 0.f) un = 0.f;
     float4 xn = xi;
+    float rho_out = rpi.x;
+    if (cont) rho_out = fmaf(S.kdt, drho_s, B.q[s]);  // time_integration.f:191-193, 207-209
+    if (OPT && P.sle == 1) {  // hsml.f:45-48, exponent the single-precision 1./dim
+        const float mr = __fdiv_rn(mass_of<DIM>(xi, vi), rpi.x);
+        xn.w = 2.0f * (DIM == 2 ? sqrtf(mr) : powf(mr, 1.0f / 3.0f));
+    } else if (sle2) {  // hsml.f:92-96
+        const float hn = fmaf(S.dt, __fmul_rn(xi.w * (1.0f / DIM), divh), xi.w);
+        if (!(hn <= 0.f)) xn.w = hn;
+    }
     xn.x = fmaf(S.dt, vn.x, xi.x);
     xn.y = fmaf(S.dt, vn.y, xi.y);
     if (DIM == 3) xn.z = fmaf(S.dt, vn.z, xi.z);
@@ -1773,7 +1867,8 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     A.vm[o] = vn;
     A.u[o] = un;
     A.ap[o] = make_float4(a0, a1, a2, du);
-    A.rho[o] = rpi.x;
+    A.rho[o] = rho_out;
+    if (A.drho) A.drho[o] = drho_s;
     A.p[o] = B.p[s];
     A.itype[o] = it;
     A.id[o] = id;
@@ -1793,7 +1888,7 @@ __device__ __forceinline__ DevGrid load_grid(const DevGrid* __restrict__ gp) {
 }
 
 // One CTA per BS / TPP consecutive slots.
-template <int DIM, int TPP, int BS, bool PER, bool LEAN>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
@@ -1801,7 +1896,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_far[kListCapD][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    density_body<DIM, TPP, BS, LEAN>(B, keys, start, g, P, s, s < n, s_near, s_far);
+    density_body<DIM, TPP, BS, LEAN, OPT>(B, keys, start, g, P, s, s < n, s_near, s_far);
 }
 
 template <int DIM>
@@ -1813,7 +1908,7 @@ __global__ void __launch_bounds__(kPassThreads)
     shear_body<DIM>(B, keys, start, g, P, s, s < n);
 }
 
-template <int DIM, int TPP, int BS, bool PER, bool LEAN>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
@@ -1821,7 +1916,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_list[kListCap][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    force_body<DIM, TPP, BS, LEAN>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
+    force_body<DIM, TPP, BS, LEAN, OPT>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
 }
 
 // ---------------------------------------------------------------------------

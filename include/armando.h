@@ -118,6 +118,20 @@ typedef struct armando_params {
                                  visc_artificial, heat_*, pmin and wall_model do not
                                  apply (wall_model must be 0). No periodic axis, sort
                                  skin, batch or reverse mode.                        */
+    /* Options of the CERN scheme's single_step (zero: the summation-density step
+       above; CERNsource/single_step.f:106-116, 214-228):                         */
+    int32_t density_form;     /* 0 summation (sum_density, density.f:1-62; the
+                                 Fortran's density_method 1), 1 continuity
+                                 (con_density, density.f:161-218, integrated with
+                                 the leapfrog, time_integration.f:144-147, 191-197;
+                                 density_method 0), 2 normalised summation
+                                 (nor_density, density.f:65-158; density_method 2) */
+    int32_t average_velocity; /* 1: XSPH velocity correction of av_vel.f (eps 0.3),
+                                 added in the corrector from the second step on     */
+    int32_t sle;              /* smoothing-length evolution (h_upgrade, hsml.f):
+                                 0 fixed, 1 h = 2 (m/rho)^(1/dim), 2 dh/dt =
+                                 (h/dim) div v; fluid particles, after the rates;
+                                 armando_get_hsml reads the evolved h back        */
 } armando_params;
 
 /* EOS of one material of the GPU-C schemes (hMatType / hMatProp of
@@ -390,6 +404,12 @@ armando_status armando_cell_ids_noalloc(const armando_params* params, const floa
  * the particles with |itype| = k; count <= ARMANDO_MAX_MATERIALS. Until it is set,
  * every entry is Tait with the context's rho0 and c0. */
 armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const armando_material* table);
+
+/* Smoothing lengths of the context's particles after its last step or
+ * integrate call, in caller order (evolved when params.sle != 0; otherwise the
+ * ones passed in). With density_form 1 the context also keeps drho/dt between
+ * calls, as time_integration.f keeps it between its iterations. */
+armando_status armando_get_hsml(armando_ctx* ctx, float* hsml);
 
 /* Blocks until the context's stream is idle and returns its sticky status. */
 armando_status armando_sync(armando_ctx* ctx);

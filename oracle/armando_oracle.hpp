@@ -62,6 +62,9 @@ struct Params {
     // pushes between different itype (1 push only, 2 push and every sum),
     // 3 virtual particles plus mirror ghosts (ghost_particles).
     int wall_model = 0;
+    // single_step options: density 0 summation, 1 continuity, 2 normalised
+    // summation; XSPH (av_vel.f); smoothing-length evolution (hsml.f).
+    int density_form = 0, average_velocity = 0, sle = 0;
 };
 
 // Whether pairs of different itype push (wall_model 1 and 2).
@@ -317,12 +320,13 @@ struct State {
     std::vector<R> x, v, m, rho, p, u, h, c;
     std::vector<int> itype;
     std::vector<R> dvdt, dudt;  // rates of the last single_step (carried)
+    std::vector<R> drho;        // drho/dt of the last single_step (density_form 1; carried)
     bool fluid(int64_t i) const { return itype[i] > 0; }
 };
 
 template <class R>
 struct Rates {
-    std::vector<R> dv, du, tdsdt, divv;
+    std::vector<R> dv, du, tdsdt, divv, drho, av;
 };
 
 // Pair geometry shared by every pair loop: dx = x_i - x_j (minimum image),
@@ -365,6 +369,109 @@ void sum_density(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
         pair_geom(s, g, P, i, j, pg);
         if (s.fluid(i)) s.rho[i] = s.rho[i] + s.m[j] * pg.w;
         if (s.fluid(j)) s.rho[j] = s.rho[j] + s.m[i] * pg.w;
+    }
+}
+
+// density.f:161-218 (con_density): drho_i = sum_j m_j (v_i - v_j) . grad_i W_ij,
+// fluid only.
+template <class R, class Rc>
+void con_density(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+                 std::vector<R>& drho) {
+    const int dim = s.dim;
+    drho.assign(s.n, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        const int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        R vcc = R(0);
+        for (int d = 0; d < dim; ++d)
+            vcc = vcc + (s.v[(int64_t)i * dim + d] - s.v[(int64_t)j * dim + d]) * pg.dwdx[d];
+        if (s.fluid(i)) drho[i] = drho[i] + s.m[j] * vcc;
+        if (s.fluid(j)) drho[j] = drho[j] + s.m[i] * vcc;
+    }
+}
+
+// density.f:65-158 (nor_density): rho_i = (m_i W(0) + sum_j m_j W_ij) /
+// (m_i W(0)/rho_i + sum_j m_j/rho_j W_ij), the denominator on the densities
+// the iteration starts with; fluid only.
+template <class R, class Rc>
+void nor_density(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl) {
+    std::vector<R> wi(s.n, R(0)), num(s.n, R(0));
+    for (int64_t i = 0; i < s.n; ++i)
+        if (s.fluid(i)) {
+            const R w0 = kernel_w(R(0), s.h[i], s.dim, P.kernel_3d_legacy);
+            wi[i] = w0 * s.m[i] / s.rho[i];
+            num[i] = w0 * s.m[i];
+        }
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        const int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        if (s.fluid(i)) {
+            wi[i] = wi[i] + s.m[j] / s.rho[j] * pg.w;
+            num[i] = num[i] + s.m[j] * pg.w;
+        }
+        if (s.fluid(j)) {
+            wi[j] = wi[j] + s.m[i] / s.rho[i] * pg.w;
+            num[j] = num[j] + s.m[i] * pg.w;
+        }
+    }
+    for (int64_t i = 0; i < s.n; ++i)
+        if (s.fluid(i)) s.rho[i] = num[i] / wi[i];
+}
+
+// av_vel.f:1-62: XSPH, av_i = -eps sum_j m_j / rho_ij (v_i - v_j) W_ij with
+// rho_ij = (rho_i + rho_j)/2, eps = 0.3; fluid only.
+template <class R, class Rc>
+void av_vel(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl,
+            std::vector<R>& av) {
+    const int dim = s.dim;
+    const R eps = R(0.3);
+    av.assign(s.n * dim, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        const int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        const R mrho = (s.rho[i] + s.rho[j]) / R(2);
+        for (int d = 0; d < dim; ++d) {
+            const R dv = s.v[(int64_t)i * dim + d] - s.v[(int64_t)j * dim + d];
+            if (s.fluid(i)) av[(int64_t)i * dim + d] = av[(int64_t)i * dim + d] - eps * s.m[j] / mrho * dv * pg.w;
+            if (s.fluid(j)) av[(int64_t)j * dim + d] = av[(int64_t)j * dim + d] + eps * s.m[i] / mrho * dv * pg.w;
+        }
+    }
+}
+
+// hsml.f (h_upgrade) on the fluid particles, after the rates: sle 1,
+// h = 2 (m/rho)^(1/dim) (the exponent is the Fortran's single-precision 1./dim);
+// sle 2, dh/dt = (h/dim) div v with div v_i = sum_j m_j/rho_j (v_j - v_i) . grad_i W,
+// h += dt dh unless that leaves h <= 0.
+template <class R, class Rc>
+void h_upgrade(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairList& pl, double dt) {
+    using std::pow;
+    const int dim = s.dim;
+    if (P.sle == 1) {
+        const double e = (double)(1.0f / (float)dim);
+        for (int64_t i = 0; i < s.n; ++i)
+            if (s.fluid(i)) s.h[i] = R(2) * pow(s.m[i] / s.rho[i], e);
+        return;
+    }
+    if (P.sle != 2) return;
+    std::vector<R> divv(s.n, R(0));
+    PairGeom<R, Rc> pg;
+    for (size_t k = 0; k < pl.pi.size(); ++k) {
+        const int i = pl.pi[k], j = pl.pj[k];
+        pair_geom(s, g, P, i, j, pg);
+        R vdw = R(0);
+        for (int d = 0; d < dim; ++d)
+            vdw = vdw + (s.v[(int64_t)j * dim + d] - s.v[(int64_t)i * dim + d]) * pg.dwdx[d];
+        divv[i] = divv[i] + s.m[j] / s.rho[j] * vdw;
+        divv[j] = divv[j] + s.m[i] / s.rho[i] * vdw;
+    }
+    for (int64_t i = 0; i < s.n; ++i) {
+        if (!s.fluid(i)) continue;
+        const R dh = (s.h[i] / R(dim)) * divv[i];
+        const R hn = s.h[i] + R(dt) * dh;
+        if (!(hn <= R(0))) s.h[i] = hn;
     }
 }
 
@@ -747,7 +854,9 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
     const int64_t n = s.n;
     PairList same, other;
     const PairList& body = split_by_itype(s, P, pl, same, other);
-    sum_density(s, g, P, body);
+    if (P.density_form == 1) con_density(s, g, P, body, out.drho);  // single_step.f:106-108
+    else if (P.density_form == 2) nor_density(s, g, P, body);
+    else sum_density(s, g, P, body);
     for (int64_t i = 0; i < n; ++i) {
         s.c[i] = P.c0;
         if (s.fluid(i)) eos_tait(s.rho[i], s.p[i], P);
@@ -764,7 +873,9 @@ void single_step(State<R>& s, const Grid<Rc>& g, const Params<R>& P, const PairL
     if (P.visc_artificial) art_visc(s, g, P, body, avdvdt, avdudt);
     if (P.heat_artificial) art_heat(s, g, P, body, ahdudt, out.divv);
     if (repulsive_walls(P)) wall_repulsion(s, g, P, other, rpdvdt);
+    if (P.average_velocity) av_vel(s, g, P, body, out.av);  // single_step.f:214-216
     if (P.heat_external && (double(its) * dt <= P.heat_t_end)) ext_heat(s, P, exdudt);
+    if (P.sle) h_upgrade(s, g, P, body, dt);  // single_step.f:224-226
     out.dv.assign(n * dim, R(0));
     out.du.assign(n, R(0));
     for (int64_t i = 0; i < n; ++i) {
@@ -816,14 +927,18 @@ void leapfrog_step(State<R>& s, const Params<R>& P, int its, double dt, Rates<R>
     const int dim = s.dim;
     const int64_t n = s.n;
     const R hdt = R(dt / 2.0), fdt = R(dt);
-    std::vector<R> u_min, v_min;
+    std::vector<R> u_min, v_min, rho_min;
+    const bool cont = P.density_form == 1;
+    if (cont && (int64_t)s.drho.size() != n) s.drho.assign(n, R(0));
     if (its != 1) {
         u_min = s.u;
         v_min = s.v;
+        rho_min = s.rho;
         for (int64_t i = 0; i < n; ++i) {
             if (!s.fluid(i)) continue;
             s.u[i] = s.u[i] + hdt * s.dudt[i];
             if (s.u[i] < R(0)) s.u[i] = R(0);
+            if (cont) s.rho[i] = s.rho[i] + hdt * s.drho[i];  // time_integration.f:144-147
             for (int d = 0; d < dim; ++d) s.v[i * dim + d] = s.v[i * dim + d] + hdt * s.dvdt[i * dim + d];
         }
     }
@@ -838,19 +953,24 @@ void leapfrog_step(State<R>& s, const Params<R>& P, int its, double dt, Rates<R>
         drop_ghosts(s, G);
         r.dv.resize(n * dim);
         r.du.resize(n);
+        if (!r.drho.empty()) r.drho.resize(n);
+        if (!r.av.empty()) r.av.resize(n * dim);
     }
     for (int64_t i = 0; i < n; ++i) {
         if (!s.fluid(i)) continue;
         if (its != 1) {
             s.u[i] = u_min[i] + fdt * r.du[i];
             if (s.u[i] < R(0)) s.u[i] = R(0);
+            if (cont) s.rho[i] = rho_min[i] + fdt * r.drho[i];  // time_integration.f:191-193
             for (int d = 0; d < dim; ++d) {
                 s.v[i * dim + d] = v_min[i * dim + d] + fdt * r.dv[i * dim + d];
+                if (P.average_velocity) s.v[i * dim + d] = s.v[i * dim + d] + r.av[i * dim + d];
                 s.x[i * dim + d] = s.x[i * dim + d] + fdt * s.v[i * dim + d];
             }
         } else {
             s.u[i] = s.u[i] + hdt * r.du[i];
             if (s.u[i] < R(0)) s.u[i] = R(0);
+            if (cont) s.rho[i] = s.rho[i] + hdt * r.drho[i];  // time_integration.f:207-209
             for (int d = 0; d < dim; ++d) {
                 s.v[i * dim + d] = s.v[i * dim + d] + hdt * r.dv[i * dim + d];
                 s.x[i * dim + d] = s.x[i * dim + d] + fdt * s.v[i * dim + d];
@@ -860,6 +980,7 @@ void leapfrog_step(State<R>& s, const Params<R>& P, int its, double dt, Rates<R>
     }
     s.dvdt = r.dv;
     s.dudt = r.du;
+    if (cont) s.drho = r.drho;
     if (rates_out) *rates_out = r;
     if (pairs_out) *pairs_out = std::move(pl);
 }

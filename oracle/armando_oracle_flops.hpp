@@ -40,6 +40,7 @@ inline bool operator==(Flop a, Flop b) { return a.v == b.v; }
 inline bool operator!=(Flop a, Flop b) { return a.v != b.v; }
 inline Flop sqrt(Flop a) { ++Flop::count; return Flop(std::sqrt(a.v)); }
 inline Flop exp(Flop a) { ++Flop::count; return Flop(std::exp(a.v)); }
+inline Flop pow(Flop a, double e) { ++Flop::count; return Flop(std::pow(a.v, e)); }
 inline Flop fabs(Flop a) { return Flop(std::fabs(a.v)); }
 
 }  // namespace ao

