@@ -394,6 +394,13 @@ bool step_options(const armando_params& p) {
     return p.density_form != 0 || p.average_velocity != 0 || p.sle != 0;
 }
 
+// Whether every iteration must sort (no sort skin): mirror ghosts change every
+// iteration, the GPU-C schemes keep one list per step, and an evolving h
+// outgrows cells sized for the h of the last sort.
+bool sorts_every_step(const armando_params& p) {
+    return p.wall_model == 3 || p.scheme != 0 || p.sle != 0;
+}
+
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
     const int n = (int)ctx->n_work;
@@ -1708,8 +1715,8 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     if (vs != ARMANDO_OK) return fail(ctx, vs, why);
     if (params->wall_model == 3 && ctx->cap < ctx->n + ctx->nf)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) need a context created with wall_model 3");
-    if ((params->wall_model == 3 || params->scheme != 0) && ctx->tune.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and the GPU-C schemes sort every iteration: set a tuning with skin 0 first");
+    if (sorts_every_step(*params) && ctx->tune.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts, the GPU-C schemes and h evolution sort every iteration: set a tuning with skin 0 first");
     ctx->prm = *params;
     ctx->dp = make_dev_params(*params, ctx->tune.reach);
     ctx->dp.n_real = (int)ctx->n;
@@ -1739,8 +1746,8 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches run one thread per particle");
     if (ctx->n_inst > 1 && t.skin != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches sort every iteration (skin 0)");
-    if ((ctx->prm.wall_model == 3 || ctx->prm.scheme != 0) && t.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and the GPU-C schemes sort every iteration (skin 0)");
+    if (sorts_every_step(ctx->prm) && t.skin != 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts, the GPU-C schemes and h evolution sort every iteration (skin 0)");
     return ARMANDO_OK;
 }
 
@@ -1843,7 +1850,7 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
             t.skin = skin;
         }
         float ms = -1.f;
-        if (t.skin != 0 && (ctx->prm.wall_model == 3 || ctx->prm.scheme != 0)) {  // sort every iteration
+        if (t.skin != 0 && sorts_every_step(ctx->prm)) {  // sort every iteration
             if (ms_per_step) ms_per_step[k] = -1.f;
             continue;
         }

@@ -67,7 +67,7 @@ def lib() -> C.CDLL:
         L.ao_forces_f64.argtypes = [C.POINTER(Params), i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
         L.ao_forces_f64.restype = C.c_int
         L.ao_step_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double, vp, vp, vp, vp, vp,
-                                  vp, vp, vp, vp, vp, C.c_int, vp]
+                                  vp, vp, vp, vp, vp, vp, C.c_int, vp]
         L.ao_step_f64.restype = C.c_int
         L.ao_step_f32.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double, vp, vp, vp, vp, vp,
                                   vp, vp, vp, vp, vp]
@@ -177,6 +177,7 @@ class State:
         self.x, self.v, self.m = d(case.x), d(case.v), d(case.mass)
         self.rho, self.p, self.u, self.h = d(case.rho), d(case.p), d(case.u), d(case.h)
         self.dvdt, self.dudt = d(case.dvdt), d(case.dudt)
+        self.drho = np.zeros(self.m.shape[0], np.float64)  # carried drho/dt (continuity)
         self.itype = np.array(case.itype, np.int32)
         self.extra = None
 
@@ -192,8 +193,8 @@ def step(state: State, its: int, dt: float, nbr_fp32: bool = False, extra: bool 
     if state.x.dtype == np.float64:
         rc = lib().ao_step_f64(C.byref(state.params), n, its, dt, _p(state.x), _p(state.v),
                                _p(state.m), _p(state.rho), _p(state.p), _p(state.u), _p(state.h),
-                               _p(state.itype), _p(state.dvdt), _p(state.dudt), int(nbr_fp32),
-                               _p(ex) if extra else None)
+                               _p(state.itype), _p(state.dvdt), _p(state.dudt), _p(state.drho),
+                               int(nbr_fp32), _p(ex) if extra else None)
     else:
         rc = lib().ao_step_f32(C.byref(state.params), n, its, dt, _p(state.x), _p(state.v),
                                _p(state.m), _p(state.rho), _p(state.p), _p(state.u), _p(state.h),

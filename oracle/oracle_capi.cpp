@@ -197,10 +197,12 @@ int ao_forces_f64(const armando_params* prm, int64_t n, const double* x, const d
 // nbr_fp32 = 1 runs the neighbour search in FP32 coordinates (GPU mirror).
 // extra (optional, n*2): per particle tdsdt, divv of the step.
 int ao_step_f64(const armando_params* prm, int64_t n, int its, double dt, double* x, double* v,
-                const double* m, double* rho, double* p, double* u, const double* h,
-                const int* itype, double* dvdt, double* dudt, int nbr_fp32, double* extra) {
+                const double* m, double* rho, double* p, double* u, double* h,
+                const int* itype, double* dvdt, double* dudt, double* drho, int nbr_fp32,
+                double* extra) {
     ao::Params<double> P = to_params<double>(prm);
     ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
+    if (drho) s.drho.assign(drho, drho + n);
     ao::Rates<double> r;
     try {
         if (nbr_fp32) ao::leapfrog_step<double, float>(s, P, its, dt, &r);
@@ -209,6 +211,8 @@ int ao_step_f64(const armando_params* prm, int64_t n, int its, double dt, double
         return 1;
     }
     store_state(s, x, v, rho, p, u, dvdt, dudt);
+    std::memcpy(h, s.h.data(), sizeof(double) * n);  // evolved with params->sle
+    if (drho && !s.drho.empty()) std::memcpy(drho, s.drho.data(), sizeof(double) * n);
     if (extra) {
         for (int64_t i = 0; i < n; ++i) {
             extra[2 * i] = r.tdsdt.empty() ? 0.0 : r.tdsdt[i];
@@ -241,7 +245,8 @@ int ao_integrate_gather_f64(const armando_params* prm, int64_t n, int its0, int 
                             double* u, const double* h, const int* itype, double* dvdt,
                             double* dudt, int nthreads) {
     ao::Params<double> P = to_params<double>(prm);
-    if (P.wall_model != 0) return 2;  // the gather form restates wall_model 0 only
+    // the gather form restates wall_model 0 and summation density only
+    if (P.wall_model != 0 || P.density_form != 0 || P.average_velocity || P.sle) return 2;
     ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, dvdt, dudt);
     try {
         for (int k = 0; k < steps; ++k) ao::leapfrog_step_gather(s, P, its0 + k, dt, nthreads);

@@ -1,0 +1,146 @@
+"""single_step options on the GPU vs the FP64 oracle: continuity and
+normalised density, XSPH, smoothing-length evolution.
+
+One step from identical FP32 inputs (an oracle history state): TOL_STEP =
+1e-5 normwise relative on every output and on h. Continuity density carries
+drho/dt from one iteration to the next inside the context, so it is checked
+over 10 iterations against the oracle, within 20x the oracle's own change
+when its FP32 inputs move by one ulp (or 1e-5)."""
+import numpy as np
+import pytest
+
+import armando_gb300 as ag
+from armando_gb300 import cases
+from helpers import FIELDS, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_STEP = 1e-5
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from armando_gb300 import build
+
+    build.build_library()
+    ag.load_library()
+
+
+def dam(**opts):
+    c = cases.perturbed(cases.dam_break(dx=0.02), seed=95, dv=0.3)
+    for k, v in opts.items():
+        setattr(c.params, k, v)
+    return c
+
+
+def channel(**opts):
+    c = cases.perturbed(cases.channel(n_x=40, n_yz=12, length=40 * 7.9e-4, width=12 * 7.9e-4,
+                                      layers=3, jitter=0.01), seed=96, dv=0.05, du=50.0)
+    for k, v in opts.items():
+        setattr(c.params, k, v)
+    return c
+
+
+def history(O, c, steps):
+    """The FP32 state after `steps` oracle iterations (rates and h included)."""
+    st = O.State(c)
+    for its in range(1, steps + 1):
+        O.step(st, its, c.dt)
+    out = c.copy()
+    for f in FIELDS + ("h",):
+        setattr(out, f, getattr(st, f).astype(np.float32))
+    return out
+
+
+CASES = {
+    "normalised": lambda: dam(density_form=2),
+    "xsph": lambda: dam(average_velocity=1),
+    "sle1": lambda: dam(sle=1),
+    "sle2": lambda: dam(sle=2),
+    "all_3d": lambda: channel(density_form=2, average_velocity=1, sle=2),
+}
+
+
+@pytest.mark.parametrize("its", [1, 3])
+@pytest.mark.parametrize("name", list(CASES))
+def test_one_step_parity(O, name, its):
+    c = CASES[name]()
+    inp = c if its == 1 else history(O, c, its - 1)
+    ref = O.State(inp)
+    O.step(ref, its, inp.dt)
+    got = inp.copy()
+    with ag.Context(inp.params, inp.n_fluid, inp.n_wall) as ctx:
+        ctx.step(got, inp.dt, its)
+        h = ctx.get_hsml()
+    errs = {f: rel_err(getattr(got, f), getattr(ref, f)) for f in FIELDS}
+    errs["h"] = rel_err(h, ref.h)
+    bad = {f: e for f, e in errs.items() if not e <= TOL_STEP}
+    assert not bad, (name, its, bad)
+
+
+def test_normalised_density_with_lanes(O):
+    c = history(O, dam(density_form=2), 2)
+    ref = O.State(c)
+    O.step(ref, 3, c.dt)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(2, 4, 128, 0)
+        ctx.step(got, c.dt, 3)
+    for f in FIELDS:
+        assert rel_err(getattr(got, f), getattr(ref, f)) <= TOL_STEP, f
+
+
+@pytest.mark.parametrize("make", [lambda: dam(density_form=1), lambda: channel(density_form=1, sle=2)],
+                         ids=["dambreak", "channel3d"])
+def test_continuity_tracks_the_oracle(O, make):
+    c = make()
+    steps = 10
+    rng = np.random.default_rng(97)
+    c2 = c.copy()
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    c2.x = np.where(np.repeat(c.itype > 0, c.dim), np.nextafter(c.x, bump), c.x).astype(np.float32)
+    ref, pert = O.State(c), O.State(c2)
+    for its in range(1, steps + 1):
+        O.step(ref, its, c.dt)
+        O.step(pert, its, c.dt)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.integrate(got, c.dt, 1, steps)
+    for f in FIELDS:
+        cond = rel_err(getattr(pert, f), getattr(ref, f))
+        err = rel_err(getattr(got, f), getattr(ref, f))
+        assert err <= max(20.0 * cond, TOL_STEP), (f, err, cond)
+
+
+def test_continuity_carries_drho_between_calls():
+    """armando_step calls carry drho/dt in the context: ten one-step calls agree
+    with one ten-step call to rounding."""
+    c = dam(density_form=1, average_velocity=1)
+    a, b = c.copy(), c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.integrate(a, c.dt, 1, 10)
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        for its in range(1, 11):
+            ctx.step(b, c.dt, its)
+    for f in FIELDS:
+        assert rel_err(getattr(b, f), getattr(a, f)) <= 1e-6, f
+
+
+def test_options_refused_where_not_built():
+    c = dam(density_form=1)
+    with pytest.raises(ag.ArmandoError) as e:
+        ag.Batch([c.params, c.params], [c.n_fluid] * 2, [c.n_wall] * 2)
+    assert e.value.status == ag._abi.ERR_UNSUPPORTED
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.forward_checkpointed(c.copy(), c.dt, 1, 4, 2)
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
+    with ag.Context(dam(sle=1).params, c.n_fluid, c.n_wall) as ctx:
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_tuning(1, 1, 128, 20)  # h evolves: every iteration sorts
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED
+    bad = c.params.copy()
+    bad.sle = 3
+    with pytest.raises(ag.ArmandoError) as e:
+        ag.Context(bad, c.n_fluid, c.n_wall)
+    assert e.value.status == ag._abi.ERR_INVALID_ARG
