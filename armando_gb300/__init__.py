@@ -247,6 +247,30 @@ class Context:
             table[key] = float(ms[k])
         return best.as_tuple(), table
 
+    def set_open_boundaries(self, inlets=(), outlets=(), box=None):
+        """Inlets and outlets of the GPU-C schemes (lists of _abi.Inlet and
+        _abi.Outlet) and the box [lo, hi] outside which particles leave."""
+        from ._abi import Inlet, Outlet
+
+        tin = (Inlet * max(len(inlets), 1))(*inlets)
+        tout = (Outlet * max(len(outlets), 1))(*outlets)
+        lo = np.ascontiguousarray(box[0] if box else [-3.0e38] * 3, np.float32)
+        hi = np.ascontiguousarray(box[1] if box else [3.0e38] * 3, np.float32)
+        self._check(self._lib.armando_set_open_boundaries(self._h, len(inlets), tin, len(outlets),
+                                                          tout, _ptr(lo), _ptr(hi)))
+
+    def integrate_open(self, arrays, dt: float, its0: int, steps: int, n: int) -> int:
+        """`steps` GPU-C steps with the open boundaries on the first n particles of
+        capacity-sized arrays (dict or Case); returns the particle count after."""
+        a = arrays.arrays() if hasattr(arrays, "arrays") else arrays
+        self._validate(a)
+        cnt = C.c_int64(int(n))
+        self._check(self._lib.armando_integrate_open(
+            self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+            _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
+            float(dt), int(its0), int(steps), C.byref(cnt)))
+        return cnt.value
+
     def get_hsml(self, out=None):
         """Smoothing lengths after the last call, in caller order (evolved when
         params.sle != 0)."""

@@ -130,6 +130,38 @@ class Material(C.Structure):
 
 
 EOS_BOUNDARY, EOS_GAS, EOS_POLY, EOS_SHOCK, EOS_TAIT, EOS_ESS = range(6)
+
+
+class Inlet(C.Structure):
+    """``armando_inlet``: an inflow disk (3D) or segment (2D) of the GPU-C schemes."""
+
+    _fields_ = [("origin", F3), ("normal", F3), ("radius", C.c_float), ("itype", C.c_int32),
+                ("mass", C.c_float), ("hsml", C.c_float), ("speed", C.c_float),
+                ("rho", C.c_float), ("u", C.c_float)]
+
+    @classmethod
+    def make(cls, origin, normal, radius, itype, mass, hsml, speed, rho, u=0.0):
+        i = cls()
+        for d in range(3):
+            i.origin[d] = origin[d] if d < len(origin) else 0.0
+            i.normal[d] = normal[d] if d < len(normal) else 0.0
+        i.radius, i.itype, i.mass, i.hsml, i.speed, i.rho, i.u = radius, itype, mass, hsml, speed, rho, u
+        return i
+
+
+class Outlet(C.Structure):
+    """``armando_outlet``: particles behind its plane within its radius leave."""
+
+    _fields_ = [("origin", F3), ("normal", F3), ("radius", C.c_float)]
+
+    @classmethod
+    def make(cls, origin, normal, radius):
+        o = cls()
+        for d in range(3):
+            o.origin[d] = origin[d] if d < len(origin) else 0.0
+            o.normal[d] = normal[d] if d < len(normal) else 0.0
+        o.radius = radius
+        return o
 MAX_MATERIALS = 64
 
 
@@ -185,7 +217,8 @@ EXPORTED = [
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
     "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
-    "armando_set_materials", "armando_get_hsml",
+    "armando_set_materials", "armando_get_hsml", "armando_set_open_boundaries",
+    "armando_integrate_open",
 ]
 N_TUNINGS = 27
 N_PHASES = 6
@@ -270,6 +303,12 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_set_materials.restype = C.c_int
     lib.armando_get_hsml.argtypes = [vp, vp]
     lib.armando_get_hsml.restype = C.c_int
+    lib.armando_set_open_boundaries.argtypes = [vp, C.c_int32, C.POINTER(Inlet), C.c_int32,
+                                                C.POINTER(Outlet), vp, vp]
+    lib.armando_set_open_boundaries.restype = C.c_int
+    lib.armando_integrate_open.argtypes = [vp] * 11 + [C.c_float, C.c_int32, C.c_int32,
+                                                      C.POINTER(C.c_int64)]
+    lib.armando_integrate_open.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

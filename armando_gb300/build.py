@@ -12,6 +12,8 @@ NVCC_FLAGS = [
     "-std=c++17", "-O3", "-lineinfo",
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-Xcompiler", "-fPIC", "-shared",
+    # host code rounds like the oracle on x86 and on Arm (no fused multiply-add)
+    "-Xcompiler", "-ffp-contract=off",
 ]
 
 

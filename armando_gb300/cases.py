@@ -390,3 +390,47 @@ def gpuc_dam_break(scale: int = 1, fluid=(100, 50), tank=(269, 80), dr1: float =
                 _f32(np.zeros(n)), _f32(np.full(n, h)),
                 np.concatenate([np.ones(nf), -np.ones(n - nf)]).astype(np.int32),
                 dt=4.0e-4 / scale, steps=10000 * scale, meta=dict(dx=dr, scale=scale))
+
+
+def gpuc_open_channel(length: float = 0.3, height: float = 0.1, dr: float = 0.01,
+                      speed: float = 1.0, rho0: float = 1000.0, c0: float = 20.0,
+                      capacity: int = 2000, scheme: int = 1):
+    """A 2D open channel for the GPU-C open boundaries: water on a lattice
+    ((i + 1/2) dr, (j + 1/2) dr) filling [0, length] x [0, height] at `speed`
+    in +x, three wall rows under and over it (x from -3 dr to length + 3 dr),
+    an inlet segment across the channel at x = -dr/2 (normal +x, radius
+    height/2) emitting water at `speed`, an outlet at x = length (normal -x,
+    radius height/2) and a box 10 dr around everything. Returns (case padded
+    to `capacity`, n, inlets, outlets, box); h = 1.2 dr, dt = 0.2 h / c0."""
+    from ._abi import Inlet, Outlet
+
+    nx, ny = int(round(length / dr)), int(round(height / dr))
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    xf = np.stack([(i.ravel() + 0.5) * dr, (j.ravel() + 0.5) * dr], 1)
+    wx = np.arange(-3, nx + 4) * dr
+    walls = [np.stack([wx, np.full(wx.shape, y)], 1) for y in
+             [-0.5 * dr, -1.5 * dr, -2.5 * dr, height + 0.5 * dr, height + 1.5 * dr, height + 2.5 * dr]]
+    xw = np.concatenate(walls)
+    x = np.concatenate([xf, xw])
+    n, nf = len(x), len(xf)
+    h = 1.2 * dr
+    m = rho0 * dr * dr
+    v = np.zeros_like(x)
+    v[:nf, 0] = speed
+    P = Params.default(dim=2, rho0=rho0, c0=c0)
+    P.scheme = scheme
+
+    def pad(a, width=1, dtype=np.float32):
+        out = np.zeros(capacity * width, dtype)
+        out[:a.size] = np.asarray(a, dtype).ravel()
+        return out
+
+    c = Case("gpuc_open_channel", P, 2, pad(x, 2), pad(v, 2), pad(np.full(n, m)),
+             pad(np.full(n, rho0)), pad(np.zeros(n)), pad(np.zeros(n)), pad(np.full(n, h)),
+             pad(np.concatenate([np.ones(nf), -np.ones(n - nf)]), 1, np.int32),
+             dt=0.2 * h / c0, steps=200, meta=dict(dx=dr, n=n))
+    inlets = [Inlet.make((-0.5 * dr, 0.5 * height, 0.0), (1.0, 0.0, 0.0), 0.5 * height, 1, m, h,
+                         speed, rho0)]
+    outlets = [Outlet.make((length, 0.5 * height, 0.0), (-1.0, 0.0, 0.0), 0.5 * height)]
+    box = ((-10 * dr, -10 * dr, -1.0), (length + 10 * dr, height + 10 * dr, 1.0))
+    return c, n, inlets, outlets, box

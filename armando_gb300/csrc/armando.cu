@@ -152,6 +152,16 @@ struct armando_ctx {
         *d_ng = nullptr, *h_ng = nullptr;
     unsigned *g_tile_count = nullptr, *g_tile_off = nullptr;
     int64_t ghosts_last = 0;
+    // Open boundaries of the GPU-C schemes: inlets (with their distances since
+    // the last emission), outlets and box, the compaction buffers.
+    bool open_set = false;
+    std::vector<armando_inlet> inlets;
+    std::vector<float> inlet_dist;
+    OpenSpec open{};
+    StateA A2{};
+    bool open_ready = false;
+    int *open_keep = nullptr, *d_open_n = nullptr, *h_open_n = nullptr;
+    unsigned *open_tc = nullptr, *open_to = nullptr;
     // single_step options: drho/dt carried between calls in caller order
     // (continuity density) and the buffers of the options, allocated on first use.
     float* drho_caller = nullptr;
@@ -540,7 +550,7 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
 template <int DIM>
 int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S) {
     cudaStream_t st = ctx->stream;
-    const int n = (int)ctx->n;
+    const int n = (int)ctx->n_work;
     const int nm = ctx->materials.empty() ? ARMANDO_MAX_MATERIALS : (int)ctx->materials.size();
     int L = launch_grid_and_sort<DIM>(ctx, nullptr, st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
@@ -935,7 +945,7 @@ armando_status plan_grid(armando_ctx* ctx) {
     if (ctx->start) return ARMANDO_OK;
     if (ctx->n_inst > 1) return plan_grid_batch(ctx);
     cudaStream_t st = ctx->stream;
-    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, (int)ctx->n, ctx->dim, ctx->bbox_part);
+    k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, (int)ctx->n_work, ctx->dim, ctx->bbox_part);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, (long long)INT32_MAX,
                                     ctx->grid, ctx->flags);
     ctx->launches += 2;
@@ -1053,6 +1063,218 @@ armando_status keep_options(armando_ctx* ctx) {
                                                                  ctx->drho_caller, n);
     ctx->launches += 1;
     CK(cudaGetLastError());
+    return ARMANDO_OK;
+}
+
+armando_status alloc_stateA(armando_ctx* ctx, StateA& a);
+
+// Open boundaries: the compaction buffers (first use).
+armando_status prepare_open(armando_ctx* ctx) {
+    if (ctx->open_ready) return ARMANDO_OK;
+    armando_status st = alloc_stateA(ctx, ctx->A2);
+    if (st != ARMANDO_OK) return st;
+    cudaError_t e = cudaSuccess;
+    const size_t n = (size_t)std::max<int64_t>(ctx->n, 1);
+    const size_t tiles = (size_t)std::max(blocks_for(ctx->n, kGhostTile), 1);
+    ctx->open_keep = dalloc<int>(n, e);
+    ctx->open_tc = dalloc<unsigned>(tiles, e);
+    ctx->open_to = dalloc<unsigned>(tiles, e);
+    ctx->d_open_n = dalloc<int>(1, e);
+    for (void* q : {(void*)ctx->open_keep, (void*)ctx->open_tc, (void*)ctx->open_to, (void*)ctx->d_open_n})
+        ctx->owned.push_back(q);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(open boundaries)");
+    CK(cudaMallocHost((void**)&ctx->h_open_n, sizeof(int)));
+    ctx->open_ready = true;
+    return ARMANDO_OK;
+}
+
+// inletDevice (ArmandoThrust/armando.cu:2792-2845), on the host: each live
+// inlet advances its distance by speed dt; past hsml/1.2 it emits a lattice of
+// particles (3D: a disk across the normal w, rows along the axis u of w's
+// smallest |component| and v = w x u; 2D: a segment along (-w_y, w_x)), FP32 in
+// the reference's operation order. The new particles go to A at [n, n + p)
+// with serial numbers from *next_id on. Returns ARMANDO_ERR_INVALID_ARG when
+// they outgrow the context's capacity.
+armando_status emit_inlets(armando_ctx* ctx, float dt, int64_t& n, int64_t& next_id) {
+    const int dim = ctx->dim;
+    std::vector<float4> xh, vm;
+    std::vector<float> uu, rho;
+    std::vector<int> it, id;
+    for (size_t k = 0; k < ctx->inlets.size(); ++k) {
+        const armando_inlet& I = ctx->inlets[k];
+        if (I.itype == 0) continue;
+        float& dist = ctx->inlet_dist[k];
+        dist = dist + I.speed * dt;
+        if (!(dist > I.hsml / 1.2f)) continue;
+        dist = dist - I.hsml / 1.2f;
+        const float len = std::sqrt(I.normal[0] * I.normal[0] + I.normal[1] * I.normal[1] +
+                                    I.normal[2] * I.normal[2]);
+        const float w[3] = {I.normal[0] / len, I.normal[1] / len, I.normal[2] / len};
+        const float sp = I.hsml / 1.2f;
+        const int nn = (int)std::lround(1.2f * I.radius / I.hsml);
+        auto add = [&](const float r[3]) {
+            const float px = I.origin[0] + r[0], py = I.origin[1] + r[1], pz = I.origin[2] + r[2];
+            if (dim == 2) {
+                xh.push_back(make_float4(px, py, I.mass, I.hsml));
+                vm.push_back(make_float4(I.speed * w[0], I.speed * w[1], 0.f, 0.f));
+            } else {
+                xh.push_back(make_float4(px, py, pz, I.hsml));
+                vm.push_back(make_float4(I.speed * w[0], I.speed * w[1], I.speed * w[2], I.mass));
+            }
+            uu.push_back(I.u);
+            rho.push_back(I.rho);
+            it.push_back(I.itype);
+            id.push_back((int)next_id++);
+        };
+        if (dim == 2) {
+            const float u[2] = {-w[1], w[0]};
+            for (int iu = -nn; iu <= nn; ++iu) {
+                const float r[3] = {((float)iu * u[0]) * sp, ((float)iu * u[1]) * sp, 0.f};
+                if (std::sqrt(r[0] * r[0] + r[1] * r[1]) < I.radius) add(r);
+            }
+        } else {
+            float u[3] = {0.f, 0.f, 0.f};
+            const float a[3] = {std::fabs(w[0]), std::fabs(w[1]), std::fabs(w[2])};
+            if (a[0] <= a[1] && a[0] <= a[2]) u[0] = 1.f, u[1] = 0.f, u[2] = 0.f;
+            if (a[1] <= a[0] && a[1] <= a[2]) u[0] = 0.f, u[1] = 1.f, u[2] = 0.f;
+            if (a[2] <= a[0] && a[2] <= a[1]) u[0] = 0.f, u[1] = 0.f, u[2] = 1.f;
+            const float v[3] = {w[1] * u[2] - w[2] * u[1], w[2] * u[0] - w[0] * u[2],
+                                w[0] * u[1] - w[1] * u[0]};
+            for (int iv = -nn; iv <= nn; ++iv)
+                for (int iu = -nn; iu <= nn; ++iu) {
+                    float r[3];
+                    for (int d = 0; d < 3; ++d) r[d] = ((float)iu * u[d] + (float)iv * v[d]) * sp;
+                    if (std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) < I.radius) add(r);
+                }
+        }
+    }
+    const size_t p = xh.size();
+    if (p == 0) return ARMANDO_OK;
+    if (n + (int64_t)p > ctx->n)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "inflow exceeds the context's particle capacity");
+    cudaStream_t st = ctx->stream;
+    std::vector<float4> zero(p, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float> pz(p, 0.f);
+    auto H2D = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    CK(H2D(ctx->A.xh + n, xh.data(), p * sizeof(float4)));
+    CK(H2D(ctx->A.vm + n, vm.data(), p * sizeof(float4)));
+    CK(H2D(ctx->A.ap + n, zero.data(), p * sizeof(float4)));
+    CK(H2D(ctx->A.u + n, uu.data(), p * sizeof(float)));
+    CK(H2D(ctx->A.rho + n, rho.data(), p * sizeof(float)));
+    CK(H2D(ctx->A.p + n, pz.data(), p * sizeof(float)));
+    CK(H2D(ctx->A.itype + n, it.data(), p * sizeof(int)));
+    CK(H2D(ctx->A.id + n, id.data(), p * sizeof(int)));
+    n += (int64_t)p;
+    return ARMANDO_OK;
+}
+
+// checkOutDevice (armando.cu:2682-2722) and the removal of neighbourListDevice
+// (armando.cu:3137-3138): the particles that left are dropped, the others keep
+// their order (compacted into A2, which then becomes A).
+template <int DIM>
+armando_status remove_outflow(armando_ctx* ctx, int64_t& n) {
+    if (n == 0) return ARMANDO_OK;
+    cudaStream_t st = ctx->stream;
+    const int nn = (int)n;
+    const int tiles = blocks_for(nn, kGhostTile);
+    k_open_flags<DIM><<<tiles, kGhostThreads, 0, st>>>(ctx->A, nn, ctx->open, ctx->open_keep, ctx->open_tc);
+    k_ghost_scan<<<1, 1024, 0, st>>>(ctx->open_tc, tiles, ctx->open_to, ctx->d_open_n);
+    k_open_compact<<<tiles, kGhostThreads, 0, st>>>(ctx->A, ctx->A2, nn, ctx->open_keep, ctx->open_to);
+    ctx->launches += 3;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_open_n, ctx->d_open_n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    const int kept = *ctx->h_open_n;
+    if (kept < 0 || kept > nn) return fail(ctx, ARMANDO_ERR_CUDA, "open-boundary count out of range");
+    std::swap(ctx->A, ctx->A2);
+    n = kept;
+    return ARMANDO_OK;
+}
+
+// Enough cells for the open run's box at the grid's cell size.
+armando_status fit_cells_to_box(armando_ctx* ctx) {
+    const DevGrid g = *ctx->h_grid;
+    long long cells = 1;
+    for (int d = 0; d < ctx->dim; ++d) {
+        const double span = (double)ctx->open.hi[d] - (double)ctx->open.lo[d];
+        const double c = span / (double)g.size[d] + 3.0;
+        if (!(c < 1e9)) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "open-boundary box needs too many cells");
+        cells *= (long long)c;
+    }
+    if (cells <= ctx->cell_cap) return ARMANDO_OK;
+    if (cells > (1LL << 30)) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "open-boundary box needs more than 2^30 cells");
+    auto it = std::find(ctx->owned.begin(), ctx->owned.end(), (void*)ctx->start);
+    if (it != ctx->owned.end()) ctx->owned.erase(it);
+    cudaFree(ctx->start);
+    cudaError_t e = cudaSuccess;
+    ctx->start = dalloc<int>((size_t)cells + 1, e);
+    if (e != cudaSuccess) {
+        ctx->start = nullptr;
+        return cuda_fail(ctx, e, "cudaMalloc(cell table)");
+    }
+    ctx->owned.push_back(ctx->start);
+    ctx->cell_cap = cells;
+    int bits = 1;
+    while ((1LL << bits) < cells) ++bits;
+    ctx->passes = (bits + 7) / 8;
+    free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+// The output order of an open run: ascending serial number (survivors of the
+// input in input order, then the new particles in emission order).
+template <int DIM>
+armando_status store_open(armando_ctx* ctx, int64_t n, float* x, float* vx, float* mass,
+                          float* rho, float* p, float* u, float* hsml, int32_t* itype,
+                          float* dvdt, float* dudt) {
+    if (n == 0) return ARMANDO_OK;
+    cudaStream_t st = ctx->stream;
+    const int nn = (int)n;
+    const int tiles = blocks_for(nn, kSortTile);
+    k_open_id_keys<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, nn, ctx->keys[0]);
+    int L = 1;
+    for (int q = 0; q < 4; ++q) {
+        const int a = q & 1, b = (q + 1) & 1;
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ctx->keys[a], nn, 8 * q, ctx->hist, tiles);
+        k_radix_scan<<<kRadix, 256, 0, st>>>(ctx->hist, tiles, ctx->dtotal);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ctx->keys[a], q == 0 ? nullptr : ctx->vals[a],
+                                                        ctx->keys[b], ctx->vals[b], nn, 8 * q,
+                                                        ctx->hist, ctx->dtotal, tiles);
+        L += 3;
+    }
+    const bool host = ctx->mem_kind == ARMANDO_MEM_HOST;
+    float* dx = host ? ctx->s_x : x;
+    float* dv = host ? ctx->s_v : vx;
+    float* dm = host ? ctx->s_m : mass;
+    float* drho = host ? ctx->s_rho : rho;
+    float* dp = host ? ctx->s_p : p;
+    float* du = host ? ctx->s_u : u;
+    float* dh = host ? ctx->s_h : hsml;
+    int* dit = host ? ctx->s_itype : itype;
+    float* ddv = host ? ctx->s_dvdt : dvdt;
+    float* ddu = host ? ctx->s_dudt : dudt;
+    k_open_out<DIM><<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A, ctx->vals[0], nn, dx, dv, dm, drho,
+                                                         dp, du, dh, dit, ddv, ddu);
+    ctx->launches += L + 1;
+    CK(cudaGetLastError());
+    if (host) {
+        const size_t nd = (size_t)nn * DIM;
+        auto D2H = [&](void* dst, const void* src, size_t bytes) {
+            return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+        };
+        CK(D2H(x, ctx->s_x, nd * 4));
+        CK(D2H(vx, ctx->s_v, nd * 4));
+        CK(D2H(dvdt, ctx->s_dvdt, nd * 4));
+        CK(D2H(mass, ctx->s_m, (size_t)nn * 4));
+        CK(D2H(rho, ctx->s_rho, (size_t)nn * 4));
+        CK(D2H(p, ctx->s_p, (size_t)nn * 4));
+        CK(D2H(u, ctx->s_u, (size_t)nn * 4));
+        CK(D2H(hsml, ctx->s_h, (size_t)nn * 4));
+        CK(D2H(itype, ctx->s_itype, (size_t)nn * 4));
+        CK(D2H(dudt, ctx->s_dudt, (size_t)nn * 4));
+    }
     return ARMANDO_OK;
 }
 
@@ -1984,6 +2206,57 @@ armando_status armando_step(armando_ctx* ctx, float* x, float* vx, const float* 
     return armando_integrate(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its, 1);
 }
 
+armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, float* mass,
+                                      float* rho, float* p, float* u, float* hsml,
+                                      int32_t* itype, float* dvdt, float* dudt, float dt,
+                                      int32_t its0, int32_t steps, int64_t* n_particles) {
+    if (!ctx || !n_particles) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt, its0);
+    if (st != ARMANDO_OK) return st;
+    if (ctx->n_inst > 1 || ctx->prm.scheme == 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "open boundaries belong to the GPU-C schemes (scheme 1, 2) of one system");
+    if (!ctx->open_set) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "call armando_set_open_boundaries first");
+    if (steps < 0 || *n_particles < 0 || *n_particles > ctx->n)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps >= 0 and 0 <= *n_particles <= capacity");
+    CK(cudaSetDevice(ctx->device));
+    ctx->adj_ready = false;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if ((st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)) != ARMANDO_OK) return st;
+    int64_t n = *n_particles, next_id = n;
+    if ((st = prepare_open(ctx)) != ARMANDO_OK) return st;
+    if ((st = prepare_gpuc(ctx)) != ARMANDO_OK) return st;
+    ctx->n_work = std::max<int64_t>(n, 1);
+    st = plan_grid(ctx);
+    ctx->n_work = ctx->n;
+    if (st != ARMANDO_OK) return st;
+    if ((st = fit_cells_to_box(ctx)) != ARMANDO_OK) return st;
+    for (int k = 0; k < steps && st == ARMANDO_OK; ++k) {
+        if ((st = emit_inlets(ctx, dt, n, next_id)) != ARMANDO_OK) break;
+        st = ctx->dim == 2 ? remove_outflow<2>(ctx, n) : remove_outflow<3>(ctx, n);
+        if (st != ARMANDO_OK || n == 0) continue;
+        ctx->n_work = n;
+        ctx->num_tiles = blocks_for(n, kSortTile);
+        const StepArgs S = make_args(ctx, dt, its0 + k);
+        const int L = ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S) : launch_gpuc_step<3>(ctx, S);
+        ctx->launches += L;
+        ctx->steps_done += 1;
+        ctx->sorts_host += 1;
+        ctx->n_work = ctx->n;
+        ctx->num_tiles = blocks_for(ctx->n, kSortTile);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "kernel launch");
+    }
+    ctx->n_work = ctx->n;
+    ctx->num_tiles = blocks_for(ctx->n, kSortTile);
+    if (st != ARMANDO_OK) return st;
+    st = ctx->dim == 2 ? store_open<2>(ctx, n, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)
+                       : store_open<3>(ctx, n, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+    if (st != ARMANDO_OK) return st;
+    *n_particles = n;
+    ctx->next_its = 0;  // the device state is the open run's, in its own order
+    return check_flags(ctx);
+}
+
 armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* hsml, int32_t* cell) {
     if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "cell ids of one particle system only");
@@ -2338,6 +2611,41 @@ const char* armando_last_error(const armando_ctx* ctx) {
     return ctx ? ctx->err.c_str() : g_last_error;
 }
 
+armando_status armando_set_open_boundaries(armando_ctx* ctx, int32_t n_inlets,
+                                           const armando_inlet* inlets, int32_t n_outlets,
+                                           const armando_outlet* outlets, const float box_lo[3],
+                                           const float box_hi[3]) {
+    if (!ctx || !box_lo || !box_hi || (n_inlets && !inlets) || (n_outlets && !outlets))
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
+    if (n_inlets < 0 || n_inlets > ARMANDO_MAX_OPEN || n_outlets < 0 || n_outlets > ARMANDO_MAX_OPEN)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "at most ARMANDO_MAX_OPEN inlets and outlets");
+    for (int k = 0; k < n_inlets; ++k) {
+        const armando_inlet& I = inlets[k];
+        const float nn = I.normal[0] * I.normal[0] + I.normal[1] * I.normal[1] + I.normal[2] * I.normal[2];
+        if (I.itype != 0 && (!(nn > 0.f) || !(I.hsml > 0.f) || !(I.radius >= 0.f) || !(I.speed >= 0.f) ||
+                             !(I.mass > 0.f) || !(I.rho > 0.f)))
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "inlet needs a normal, hsml, mass, rho > 0 and radius, speed >= 0");
+    }
+    ctx->inlets.assign(inlets, inlets + n_inlets);
+    ctx->inlet_dist.assign(n_inlets, 0.f);
+    std::memset(&ctx->open, 0, sizeof ctx->open);
+    ctx->open.n_out = n_outlets;
+    for (int k = 0; k < n_outlets; ++k) {
+        for (int d = 0; d < 3; ++d) {
+            ctx->open.out[k].o[d] = outlets[k].origin[d];
+            ctx->open.out[k].n[d] = outlets[k].normal[d];
+        }
+        ctx->open.out[k].R = outlets[k].radius;
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (!(box_hi[d] >= box_lo[d])) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "box_hi must be >= box_lo");
+        ctx->open.lo[d] = box_lo[d];
+        ctx->open.hi[d] = box_hi[d];
+    }
+    ctx->open_set = true;
+    return ARMANDO_OK;
+}
+
 armando_status armando_get_hsml(armando_ctx* ctx, float* hsml) {
     if (!ctx || !hsml) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL argument");
     if (ctx->n == 0) return ARMANDO_OK;
@@ -2437,6 +2745,7 @@ armando_status armando_destroy(armando_ctx* ctx) {
     if (ctx->h_grid) cudaFreeHost(ctx->h_grid);
     if (ctx->h_wgrid) cudaFreeHost(ctx->h_wgrid);
     if (ctx->h_ng) cudaFreeHost(ctx->h_ng);
+    if (ctx->h_open_n) cudaFreeHost(ctx->h_open_n);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     delete ctx;

@@ -295,3 +295,122 @@ __global__ void k_gpuc_scatter(GpucState S, int cur, StateA A, int n) {
 }
 
 }  // namespace ag
+
+namespace ag {
+
+// ---------------------------------------------------------------------------
+// Open boundaries (armando.cu:2640-2856): outlets and the box remove particles,
+// keeping the order of the rest (a block scan over tiles of kGhostTile).
+// ---------------------------------------------------------------------------
+struct DevOutlet {
+    float o[3], n[3], R;
+};
+
+struct OpenSpec {
+    DevOutlet out[10];
+    int n_out;
+    float lo[3], hi[3];
+};
+
+// checkOutDevice (armando.cu:2682-2722) in FP32, operations in order, unfused.
+template <int DIM>
+__device__ __forceinline__ bool open_leaves(const float4& xh, const OpenSpec& O) {
+    const float x[3] = {xh.x, xh.y, DIM == 3 ? xh.z : 0.f};
+    for (int q = 0; q < O.n_out; ++q) {
+        const DevOutlet& Q = O.out[q];
+        float dn = 0.f;
+        for (int d = 0; d < DIM; ++d) dn = __fadd_rn(dn, __fmul_rn(__fsub_rn(x[d], Q.o[d]), Q.n[d]));
+        float dr = 0.f;
+        for (int d = 0; d < DIM; ++d) {
+            const float e = __fsub_rn(__fsub_rn(x[d], Q.o[d]), __fmul_rn(dn, Q.n[d]));
+            dr = __fadd_rn(dr, __fmul_rn(e, e));
+        }
+        if (dn < 0.f && __fsqrt_rn(dr) < Q.R) return true;
+    }
+    for (int d = 0; d < DIM; ++d)
+        if (x[d] > O.hi[d] || x[d] < O.lo[d]) return true;
+    return false;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kGhostThreads)
+    k_open_flags(StateA A, int n, OpenSpec O, int* __restrict__ keep,
+                 unsigned* __restrict__ tile_count) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned s_total;
+    unsigned mine = 0;
+    for (int it = 0; it < kGhostItems; ++it) {
+        const int i = blockIdx.x * kGhostTile + it * kGhostThreads + (int)threadIdx.x;
+        if (i >= n) break;
+        const int k = open_leaves<DIM>(A.xh[i], O) ? 0 : 1;
+        keep[i] = k;
+        mine += k;
+    }
+    block_excl_scan<kGhostThreads>(mine, s_warp, &s_total);
+    if (threadIdx.x == 0) tile_count[blockIdx.x] = s_total;
+}
+
+// The kept particles of A, in order, into D.
+__global__ void __launch_bounds__(kGhostThreads)
+    k_open_compact(StateA A, StateA D, int n, const int* __restrict__ keep,
+                   const unsigned* __restrict__ tile_off) {
+    __shared__ unsigned s_warp[32];
+    __shared__ unsigned s_total;
+    unsigned base = tile_off[blockIdx.x];
+    for (int it = 0; it < kGhostItems; ++it) {
+        const int i = blockIdx.x * kGhostTile + it * kGhostThreads + (int)threadIdx.x;
+        const int k = (i < n) ? keep[i] : 0;
+        const unsigned rank = block_excl_scan<kGhostThreads>((unsigned)k, s_warp, &s_total);
+        if (k) {
+            const int o = (int)(base + rank);
+            D.xh[o] = A.xh[i];
+            D.vm[o] = A.vm[i];
+            D.u[o] = A.u[i];
+            D.ap[o] = A.ap[i];
+            D.rho[o] = A.rho[i];
+            D.p[o] = A.p[i];
+            D.itype[o] = A.itype[i];
+            D.id[o] = A.id[i];
+        }
+        base += s_total;
+    }
+}
+
+// Keys of the output order: the particles' serial numbers.
+__global__ void k_open_id_keys(StateA A, int n, unsigned* __restrict__ keys) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) keys[s] = (unsigned)A.id[s];
+}
+
+// Output r = the particle of rank r in serial order: every field, staged.
+template <int DIM>
+__global__ void k_open_out(StateA A, const int* __restrict__ order, int n, float* __restrict__ x,
+                           float* __restrict__ v, float* __restrict__ m, float* __restrict__ rho,
+                           float* __restrict__ p, float* __restrict__ u, float* __restrict__ h,
+                           int* __restrict__ itype, float* __restrict__ dvdt,
+                           float* __restrict__ dudt) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const int s = order[r];
+    const float4 a = A.xh[s], b = A.vm[s], q = A.ap[s];
+    x[DIM * r] = a.x;
+    x[DIM * r + 1] = a.y;
+    v[DIM * r] = b.x;
+    v[DIM * r + 1] = b.y;
+    dvdt[DIM * r] = q.x;
+    dvdt[DIM * r + 1] = q.y;
+    if (DIM == 3) {
+        x[3 * r + 2] = a.z;
+        v[3 * r + 2] = b.z;
+        dvdt[3 * r + 2] = q.z;
+    }
+    m[r] = (DIM == 2) ? a.z : b.w;
+    h[r] = a.w;
+    dudt[r] = q.w;
+    u[r] = A.u[s];
+    rho[r] = A.rho[s];
+    p[r] = A.p[s];
+    itype[r] = A.itype[s];
+}
+
+}  // namespace ag

@@ -405,6 +405,45 @@ armando_status armando_cell_ids_noalloc(const armando_params* params, const floa
  * every entry is Tait with the context's rho0 and c0. */
 armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const armando_material* table);
 
+/* ---- open boundaries of the GPU-C schemes (scheme 1, 2) ---------------------------
+ * Inlets and outlets of ArmandoThrust/armando.cu:2640-2856. Every step, before its
+ * neighbour list:
+ *   inlets: distance += speed dt; past hsml/1.2 (the lattice spacing) it drops by
+ *     that much and the inlet emits a lattice of new particles in its plane (a
+ *     disk of radius `radius` in 3D, a segment across the normal in 2D), spacing
+ *     hsml/1.2, velocity speed along the normal, with the inlet's itype, mass,
+ *     hsml, rho and u;
+ *   outlets: a particle behind an outlet's plane ((x - origin) . normal < 0) within
+ *     `radius` of its axis leaves, and so does any particle outside [box_lo, box_hi].
+ * The particle count then varies up to the context's capacity (n_fluid + n_wall at
+ * creation); armando_integrate_open takes and returns it. Particles keep their
+ * order: the survivors of the input come first, in input order, then the new ones
+ * in emission order (inlets in table order, lattice rows in order). */
+typedef struct armando_inlet {
+    float origin[3], normal[3], radius;
+    int32_t itype;       /* 0: inlet off                                   */
+    float mass, hsml, speed, rho, u;
+} armando_inlet;
+
+typedef struct armando_outlet {
+    float origin[3], normal[3], radius;
+} armando_outlet;
+
+#define ARMANDO_MAX_OPEN 10
+
+/* Sets the open boundaries (at most ARMANDO_MAX_OPEN of each; resets the
+ * inlets' distances) and the box outside which particles leave. */
+armando_status armando_set_open_boundaries(armando_ctx* ctx, int32_t n_inlets,
+                                           const armando_inlet* inlets, int32_t n_outlets,
+                                           const armando_outlet* outlets, const float box_lo[3],
+                                           const float box_hi[3]);
+/* `steps` GPU-C steps with the open boundaries on *n_particles particles (in/out);
+ * every array holds room for the context's capacity. */
+armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, float* mass,
+                                      float* rho, float* p, float* u, float* hsml,
+                                      int32_t* itype, float* dvdt, float* dudt, float dt,
+                                      int32_t its0, int32_t steps, int64_t* n_particles);
+
 /* Smoothing lengths of the context's particles after its last step or
  * integrate call, in caller order (evolved when params.sle != 0; otherwise the
  * ones passed in). With density_form 1 the context also keeps drho/dt between

@@ -245,13 +245,147 @@ void gpuc_rates(const State<R>& s, const std::vector<std::vector<int>>& list,
     }
 }
 
+// Open boundaries (ArmandoThrust/armando.cu:2640-2856), applied at a step's
+// start, inlets before outlets as RKintegrateDevice calls them (armando.cu:
+// 3314-3318). Geometry in FP32 with the reference's operation order, so the
+// emitted positions are the library's bit for bit.
+struct GpucInlet {
+    float o[3], n[3], R;
+    int itype;
+    float mass, h, speed, rho, u;
+    float dist = 0.f;
+};
+struct GpucOutlet {
+    float o[3], n[3], R;
+};
+struct GpucOpen {
+    std::vector<GpucInlet> in;
+    std::vector<GpucOutlet> out;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// inletDevice (armando.cu:2792-2845): the lattice of one emission. 3D: the
+// inlet's unit normal w, u the coordinate axis of w's smallest |component|
+// (the last of x, y, z on ties), v = w x u, points (iu u + iv v) h/1.2 with
+// |r| < R, iu, iv in [-n, n], n = roundf(1.2 R/h). 2D: the same rows along
+// u = (-w_y, w_x) only (the 2D form of the disk: a segment across the inflow).
+inline void gpuc_inlet_lattice(const GpucInlet& I, int dim, std::vector<float>& pos, float w[3]) {
+    const float len = std::sqrt(I.n[0] * I.n[0] + I.n[1] * I.n[1] + I.n[2] * I.n[2]);
+    for (int d = 0; d < 3; ++d) w[d] = I.n[d] / len;
+    const float sp = I.h / 1.2f;
+    const int nn = (int)std::lround(1.2f * I.R / I.h);
+    pos.clear();
+    if (dim == 2) {
+        const float u[2] = {-w[1], w[0]};
+        for (int iu = -nn; iu <= nn; ++iu) {
+            const float r0 = ((float)iu * u[0]) * sp, r1 = ((float)iu * u[1]) * sp;
+            if (std::sqrt(r0 * r0 + r1 * r1) < I.R) {
+                pos.push_back(I.o[0] + r0);
+                pos.push_back(I.o[1] + r1);
+            }
+        }
+        return;
+    }
+    float u[3] = {0, 0, 0};
+    const float a[3] = {std::fabs(w[0]), std::fabs(w[1]), std::fabs(w[2])};
+    if (a[0] <= a[1] && a[0] <= a[2]) u[0] = 1.f, u[1] = 0.f, u[2] = 0.f;
+    if (a[1] <= a[0] && a[1] <= a[2]) u[0] = 0.f, u[1] = 1.f, u[2] = 0.f;
+    if (a[2] <= a[0] && a[2] <= a[1]) u[0] = 0.f, u[1] = 0.f, u[2] = 1.f;
+    const float v[3] = {w[1] * u[2] - w[2] * u[1], w[2] * u[0] - w[0] * u[2], w[0] * u[1] - w[1] * u[0]};
+    for (int iv = -nn; iv <= nn; ++iv)
+        for (int iu = -nn; iu <= nn; ++iu) {
+            float r[3];
+            for (int d = 0; d < 3; ++d) r[d] = ((float)iu * u[d] + (float)iv * v[d]) * sp;
+            if (std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]) < I.R)
+                for (int d = 0; d < 3; ++d) pos.push_back(I.o[d] + r[d]);
+        }
+}
+
+// checkOutDevice (armando.cu:2682-2722): behind an outlet within its radius,
+// or outside the box.
+inline bool gpuc_leaves(const float* x, int dim, const GpucOpen& O) {
+    for (const GpucOutlet& Q : O.out) {
+        float dn = 0.f;
+        for (int d = 0; d < dim; ++d) dn = dn + (x[d] - Q.o[d]) * Q.n[d];
+        float dr = 0.f;
+        for (int d = 0; d < dim; ++d) {
+            const float e = (x[d] - Q.o[d]) - dn * Q.n[d];
+            dr = dr + e * e;
+        }
+        if (dn < 0.f && std::sqrt(dr) < Q.R) return true;
+    }
+    for (int d = 0; d < dim; ++d)
+        if (x[d] > O.hi[d] || x[d] < O.lo[d]) return true;
+    return false;
+}
+
+// Emission then removal on the state (order kept: survivors, then the new
+// particles in emission order).
+template <class R>
+void gpuc_open(State<R>& s, GpucOpen& O, double dt) {
+    const int dim = s.dim;
+    std::vector<float> pos;
+    float w[3];
+    for (GpucInlet& I : O.in) {
+        if (I.itype == 0) continue;
+        I.dist = I.dist + I.speed * (float)dt;
+        if (!(I.dist > I.h / 1.2f)) continue;
+        I.dist = I.dist - I.h / 1.2f;
+        gpuc_inlet_lattice(I, dim, pos, w);
+        const int64_t k = (int64_t)pos.size() / dim;
+        for (int64_t q = 0; q < k; ++q) {
+            for (int d = 0; d < dim; ++d) {
+                s.x.push_back(R(pos[q * dim + d]));
+                s.v.push_back(R(I.speed * w[d]));
+                s.dvdt.push_back(R(0));
+            }
+            s.m.push_back(R(I.mass));
+            s.h.push_back(R(I.h));
+            s.rho.push_back(R(I.rho));
+            s.p.push_back(R(0));
+            s.u.push_back(R(I.u));
+            s.c.push_back(R(0));
+            s.itype.push_back(I.itype);
+            s.dudt.push_back(R(0));
+        }
+        s.n += k;
+    }
+    int64_t keep = 0;
+    for (int64_t i = 0; i < s.n; ++i) {
+        float xf[3];
+        for (int d = 0; d < dim; ++d) xf[d] = (float)s.x[i * dim + d];
+        if (gpuc_leaves(xf, dim, O)) continue;
+        for (int d = 0; d < dim; ++d) {
+            s.x[keep * dim + d] = s.x[i * dim + d];
+            s.v[keep * dim + d] = s.v[i * dim + d];
+            s.dvdt[keep * dim + d] = s.dvdt[i * dim + d];
+        }
+        s.m[keep] = s.m[i];
+        s.h[keep] = s.h[i];
+        s.rho[keep] = s.rho[i];
+        s.p[keep] = s.p[i];
+        s.u[keep] = s.u[i];
+        s.c[keep] = s.c[i];
+        s.itype[keep] = s.itype[i];
+        s.dudt[keep] = s.dudt[i];
+        ++keep;
+    }
+    s.n = keep;
+    s.x.resize(keep * dim);
+    s.v.resize(keep * dim);
+    s.dvdt.resize(keep * dim);
+    for (auto* a : {&s.m, &s.h, &s.rho, &s.p, &s.u, &s.c, &s.dudt}) a->resize(keep);
+    s.itype.resize(keep);
+}
+
 // One TVD-RK3 step (acpu.c:2360-2373): the list at the step's start, then
 // X = X0 + alpha (X + dt dX/dt - X0) for alpha = 1, 1/4, 2/3. s.p holds the
 // pressures of the previous update on entry; s.c is recomputed from rho, u.
 // rates_out: dv/dt [n*dim] and de/dt [n] of the last stage.
 template <class R, class Rc = R>
 void gpuc_rk3_step(State<R>& s, const GpucSetup<R>& G, double dt, std::vector<R>* dv_out = nullptr,
-                   std::vector<R>* du_out = nullptr) {
+                   std::vector<R>* du_out = nullptr, GpucOpen* open = nullptr) {
+    if (open) gpuc_open(s, *open, dt);
     const int dim = s.dim;
     const int64_t n = s.n;
     std::vector<Rc> xc(n * dim), hc(n);

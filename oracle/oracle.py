@@ -17,7 +17,7 @@ _REPO = os.path.dirname(_HERE)
 if _REPO not in sys.path:
     sys.path.insert(0, _REPO)
 
-from armando_gb300._abi import Material, Params  # noqa: E402  (shared C-ABI structs)
+from armando_gb300._abi import Inlet, Material, Outlet, Params  # noqa: E402  (shared C-ABI structs)
 
 LIB_PATH = os.path.join(_HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(_HERE, "_ref", "libacpu.so")
@@ -86,6 +86,11 @@ def lib() -> C.CDLL:
         L.ao_gpuc_step_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material), i64,
                                        C.c_int, C.c_double] + [vp] * 10 + [C.c_int]
         L.ao_gpuc_step_f64.restype = C.c_int
+        L.ao_gpuc_open_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material),
+                                       C.c_int32, C.POINTER(Inlet), C.c_int32, C.POINTER(Outlet),
+                                       vp, vp, i64, C.POINTER(i64), C.c_int, C.c_double] + \
+            [vp] * 10 + [C.c_int]
+        L.ao_gpuc_open_f64.restype = C.c_int
         L.ao_gpuc_eos_f64.argtypes = [C.POINTER(Material), i64, vp, vp, vp, vp, vp]
         L.ao_gpuc_eos_f64.restype = None
         L.ao_ghosts_f64.argtypes = [C.POINTER(Params), i64, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp]
@@ -255,6 +260,42 @@ def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = 
     if rc:
         raise RuntimeError("oracle gpuc step failed")
     return dv, du
+
+
+def gpuc_open(case, steps, dt, capacity, n=None, inlets=(), outlets=(), box=None,
+              materials=None, fp32=True):
+    """GPU-C steps with open boundaries from the first n particles of a case
+    (FP32 arrays; n = all of them by default): returns a dict of FP64 arrays
+    (x, v, mass, rho, p, u, h, itype, dvdt, dudt) of the particles left,
+    survivors in input order then new ones in emission order."""
+    dim = case.dim
+    n0 = case.n if n is None else int(n)
+    a = {}
+    for f, w, dt_ in (("x", dim, np.float64), ("v", dim, np.float64), ("mass", 1, np.float64),
+                      ("rho", 1, np.float64), ("p", 1, np.float64), ("u", 1, np.float64),
+                      ("h", 1, np.float64), ("itype", 1, np.int32), ("dvdt", dim, np.float64),
+                      ("dudt", 1, np.float64)):
+        arr = np.zeros(capacity * w, dt_)
+        src = np.asarray(getattr(case, f))[:n0 * w]
+        arr[:src.size] = src
+        a[f] = arr
+    n = C.c_int64(n0)
+    lo = np.array(box[0] if box else [-1e30] * 3, np.float32)
+    hi = np.array(box[1] if box else [1e30] * 3, np.float32)
+    tin = (Inlet * max(len(inlets), 1))(*inlets)
+    tout = (Outlet * max(len(outlets), 1))(*outlets)
+    tab, nmat = None, 0
+    if materials is not None:
+        nmat = len(materials)
+        tab = (Material * nmat)(*materials)
+    rc = lib().ao_gpuc_open_f64(C.byref(case.params), nmat, tab, len(inlets), tin, len(outlets),
+                                tout, _p(lo), _p(hi), capacity, C.byref(n), steps, dt,
+                                *[_p(a[f]) for f in ("x", "v", "mass", "rho", "p", "u", "h",
+                                                     "itype", "dvdt", "dudt")], int(fp32))
+    if rc:
+        raise RuntimeError(f"oracle open-boundary run failed ({rc})")
+    k = n.value
+    return {f: (v[:k * dim] if f in ("x", "v", "dvdt") else v[:k]) for f, v in a.items()}
 
 
 def gpuc_eos(material, rho, u):

@@ -459,6 +459,82 @@ int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_mate
     return 0;
 }
 
+// GPU-C scheme with open boundaries: `steps` steps on *n particles (in/out);
+// arrays hold `capacity` entries (x, v, dvdt: capacity*dim). Returns 0, 1 on a
+// failed step, 3 when the particles outgrow the capacity.
+int ao_gpuc_open_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
+                     int32_t n_in, const armando_inlet* inlets, int32_t n_out,
+                     const armando_outlet* outlets, const float* lo, const float* hi,
+                     int64_t capacity, int64_t* n, int steps, double dt, double* x, double* v,
+                     double* m, double* rho, double* p, double* u, double* h, int* itype,
+                     double* dvdt, double* dudt, int fp32) {
+    if (prm->scheme != 1 && prm->scheme != 2) return 2;
+    ao::GpucSetup<double> G;
+    G.variant = prm->scheme;
+    G.legacy3d = prm->kernel_3d_legacy;
+    for (int d = 0; d < 3; ++d) G.gravity[d] = prm->gravity[d];
+    G.mat.resize(table ? nmat : ARMANDO_MAX_MATERIALS);
+    for (size_t k = 0; k < G.mat.size(); ++k) {
+        if (table) {
+            G.mat[k].type = table[k].eos;
+            for (int q = 0; q < 10; ++q) G.mat[k].prop[q] = table[k].prop[q];
+        } else {
+            G.mat[k].type = ao::EOS_TAIT;
+            G.mat[k].prop[0] = prm->rho0;
+            G.mat[k].prop[1] = prm->c0;
+        }
+    }
+    ao::GpucOpen O;
+    for (int k = 0; k < n_in; ++k) {
+        ao::GpucInlet I;
+        for (int d = 0; d < 3; ++d) {
+            I.o[d] = inlets[k].origin[d];
+            I.n[d] = inlets[k].normal[d];
+        }
+        I.R = inlets[k].radius;
+        I.itype = inlets[k].itype;
+        I.mass = inlets[k].mass;
+        I.h = inlets[k].hsml;
+        I.speed = inlets[k].speed;
+        I.rho = inlets[k].rho;
+        I.u = inlets[k].u;
+        O.in.push_back(I);
+    }
+    for (int k = 0; k < n_out; ++k) {
+        ao::GpucOutlet Q;
+        for (int d = 0; d < 3; ++d) {
+            Q.o[d] = outlets[k].origin[d];
+            Q.n[d] = outlets[k].normal[d];
+        }
+        Q.R = outlets[k].radius;
+        O.out.push_back(Q);
+    }
+    for (int d = 0; d < 3; ++d) {
+        O.lo[d] = lo[d];
+        O.hi[d] = hi[d];
+    }
+    const int dim = prm->dim;
+    ao::State<double> s = load_state<double>(dim, *n, x, v, m, rho, p, u, h, itype, nullptr, nullptr);
+    std::vector<double> dv, du;
+    try {
+        for (int k = 0; k < steps; ++k) {
+            if (fp32) ao::gpuc_rk3_step<double, float>(s, G, dt, &dv, &du, &O);
+            else ao::gpuc_rk3_step<double, double>(s, G, dt, &dv, &du, &O);
+            if (s.n > capacity) return 3;
+        }
+    } catch (const std::exception&) {
+        return 1;
+    }
+    *n = s.n;
+    store_state<double>(s, x, v, rho, p, u, nullptr, nullptr);
+    std::memcpy(m, s.m.data(), sizeof(double) * s.n);
+    std::memcpy(h, s.h.data(), sizeof(double) * s.n);
+    std::memcpy(itype, s.itype.data(), sizeof(int) * s.n);
+    if (!dv.empty()) std::memcpy(dvdt, dv.data(), sizeof(double) * s.n * dim);
+    if (!du.empty()) std::memcpy(dudt, du.data(), sizeof(double) * s.n);
+    return 0;
+}
+
 // EOS of the GPU-C schemes for one material: rho (clamped where the type
 // clamps), p and c for n states (rho_in, u).
 void ao_gpuc_eos_f64(const armando_material* mat, int64_t n, const double* rho_in, const double* u,
