@@ -254,8 +254,11 @@ class Context:
 
         tin = (Inlet * max(len(inlets), 1))(*inlets)
         tout = (Outlet * max(len(outlets), 1))(*outlets)
-        lo = np.ascontiguousarray(box[0] if box else [-3.0e38] * 3, np.float32)
-        hi = np.ascontiguousarray(box[1] if box else [3.0e38] * 3, np.float32)
+        lo = np.full(3, -3.0e38, np.float32)  # axes the box leaves out: unbounded
+        hi = np.full(3, 3.0e38, np.float32)
+        if box:
+            lo[:len(box[0])] = box[0]
+            hi[:len(box[1])] = box[1]
         self._check(self._lib.armando_set_open_boundaries(self._h, len(inlets), tin, len(outlets),
                                                           tout, _ptr(lo), _ptr(hi)))
 
@@ -289,6 +292,15 @@ class Context:
         ms = [m if isinstance(m, Material) else Material.make(*m) for m in materials]
         tab = (Material * len(ms))(*ms)
         self._check(self._lib.armando_set_materials(self._h, len(ms), tab))
+
+    def set_zones(self, loads=(), fixes=()):
+        """Load and fix zones of the GPU-C schemes: lists of _abi.LoadZone and
+        _abi.FixZone (``armando_set_zones``)."""
+        from ._abi import FixZone, LoadZone
+
+        lt = (LoadZone * max(len(loads), 1))(*loads)
+        ft = (FixZone * max(len(fixes), 1))(*fixes)
+        self._check(self._lib.armando_set_zones(self._h, len(loads), lt, len(fixes), ft))
 
     def sync(self):
         self._check(self._lib.armando_sync(self._h))

@@ -162,6 +162,49 @@ class Outlet(C.Structure):
             o.normal[d] = normal[d] if d < len(normal) else 0.0
         o.radius = radius
         return o
+
+
+MAX_OPEN = 10
+
+
+def _box(z, lo, hi):
+    for d in range(3):
+        z.lo[d] = lo[d] if d < len(lo) else -float("inf")
+        z.hi[d] = hi[d] if d < len(hi) else float("inf")
+
+
+class LoadZone(C.Structure):
+    """``armando_load_zone``: inside the open box lo < x < hi a particle with
+    itype > 0 gains accel on dv/dt and w on de/dt."""
+
+    _fields_ = [("lo", F3), ("hi", F3), ("accel", F3), ("w", C.c_float)]
+
+    @classmethod
+    def make(cls, lo, hi, accel=(0.0, 0.0, 0.0), w=0.0):
+        z = cls()
+        _box(z, lo, hi)
+        for d in range(3):
+            z.accel[d] = accel[d] if d < len(accel) else 0.0
+        z.w = w
+        return z
+
+
+class FixZone(C.Structure):
+    """``armando_fix_zone``: inside the open box a particle takes velocity vel
+    after each stage's update."""
+
+    _fields_ = [("lo", F3), ("hi", F3), ("vel", F3)]
+
+    @classmethod
+    def make(cls, lo, hi, vel):
+        z = cls()
+        _box(z, lo, hi)
+        for d in range(3):
+            z.vel[d] = vel[d] if d < len(vel) else 0.0
+        return z
+
+
+MAX_ZONES = 10
 MAX_MATERIALS = 64
 
 
@@ -218,7 +261,7 @@ EXPORTED = [
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
     "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
     "armando_set_materials", "armando_get_hsml", "armando_set_open_boundaries",
-    "armando_integrate_open",
+    "armando_integrate_open", "armando_set_zones",
 ]
 N_TUNINGS = 27
 N_PHASES = 6
@@ -309,6 +352,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_integrate_open.argtypes = [vp] * 11 + [C.c_float, C.c_int32, C.c_int32,
                                                       C.POINTER(C.c_int64)]
     lib.armando_integrate_open.restype = C.c_int
+    lib.armando_set_zones.argtypes = [vp, C.c_int32, C.POINTER(LoadZone), C.c_int32, C.POINTER(FixZone)]
+    lib.armando_set_zones.restype = C.c_int
     del fp, ip
     _lib = lib
     return lib

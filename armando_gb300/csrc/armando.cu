@@ -172,6 +172,9 @@ struct armando_ctx {
     bool gs_ready = false;
     DevMaterial* d_mat = nullptr;
     std::vector<armando_material> materials;  // set by armando_set_materials
+    DevZones* d_zones = nullptr;               // load and fix zones (armando_set_zones)
+    std::vector<armando_load_zone> loads;
+    std::vector<armando_fix_zone> fixes;
 };
 
 namespace {
@@ -560,14 +563,18 @@ int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S) {
     static const float alphas[3] = {1.0f, 0.25f, 2.0f / 3.0f};
     for (int q = 0; q < 3; ++q) {
         const int cur = q & 1;
-        if (ctx->prm.scheme == 1)
-            k_gpuc_stage<DIM, 1><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-                ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->flags,
-                alphas[q], S.dt, n);
-        else
-            k_gpuc_stage<DIM, 2><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-                ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->flags,
-                alphas[q], S.dt, n);
+        with_tuning(ctx->tune, false, false, false, [&](auto tpp, auto bs, auto, auto, auto) {
+            constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
+            const int blocks = blocks_for((int64_t)n * T, BSZ);
+            if (ctx->prm.scheme == 1)
+                k_gpuc_stage<DIM, 1, T, BSZ><<<blocks, BSZ, 0, st>>>(
+                    ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->d_zones,
+                    ctx->flags, alphas[q], S.dt, n);
+            else
+                k_gpuc_stage<DIM, 2, T, BSZ><<<blocks, BSZ, 0, st>>>(
+                    ctx->gs, cur, skeys, ctx->start, ctx->grid, ctx->dp, ctx->d_mat, nm, ctx->d_zones,
+                    ctx->flags, alphas[q], S.dt, n);
+        });
     }
     k_gpuc_scatter<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->gs, 1, ctx->A, n);
     return L + 5;
@@ -1298,9 +1305,11 @@ armando_status prepare_gpuc(armando_ctx* ctx) {
         g.itype = dalloc<int>(n, e);
         g.id = dalloc<int>(n, e);
         ctx->d_mat = dalloc<DevMaterial>(ARMANDO_MAX_MATERIALS, e);
+        ctx->d_zones = dalloc<DevZones>(1, e);
         for (void* q : {(void*)g.x0, (void*)g.v0, (void*)g.q0, (void*)g.xw[0], (void*)g.xw[1],
                         (void*)g.vw[0], (void*)g.vw[1], (void*)g.sw[0], (void*)g.sw[1],
-                        (void*)g.rates, (void*)g.itype, (void*)g.id, (void*)ctx->d_mat})
+                        (void*)g.rates, (void*)g.itype, (void*)g.id, (void*)ctx->d_mat,
+                        (void*)ctx->d_zones})
             ctx->owned.push_back(q);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(GPU-C state)");
         ctx->gs_ready = true;
@@ -1319,6 +1328,28 @@ armando_status prepare_gpuc(armando_ctx* ctx) {
         }
     }
     CK(cudaMemcpy(ctx->d_mat, tab.data(), sizeof(DevMaterial) * tab.size(), cudaMemcpyHostToDevice));
+    DevZones z;
+    std::memset(&z, 0, sizeof z);
+    z.n_load = (int)ctx->loads.size();
+    z.n_fix = (int)ctx->fixes.size();
+    for (int k = 0; k < z.n_load; ++k) {
+        const armando_load_zone& L = ctx->loads[k];
+        for (int d = 0; d < 3; ++d) {
+            z.load[k].lo[d] = L.lo[d];
+            z.load[k].hi[d] = L.hi[d];
+            z.load[k].g[d] = L.accel[d];
+        }
+        z.load[k].w = L.w;
+    }
+    for (int k = 0; k < z.n_fix; ++k) {
+        const armando_fix_zone& F = ctx->fixes[k];
+        for (int d = 0; d < 3; ++d) {
+            z.fix[k].lo[d] = F.lo[d];
+            z.fix[k].hi[d] = F.hi[d];
+            z.fix[k].v[d] = F.vel[d];
+        }
+    }
+    CK(cudaMemcpy(ctx->d_zones, &z, sizeof z, cudaMemcpyHostToDevice));
     return ARMANDO_OK;
 }
 
@@ -2676,6 +2707,36 @@ armando_status armando_set_materials(armando_ctx* ctx, int32_t count, const arma
     }
     ctx->materials.assign(table, table + count);
     free_graphs(ctx);
+    return ARMANDO_OK;
+}
+
+armando_status armando_set_zones(armando_ctx* ctx, int32_t n_loads, const armando_load_zone* loads,
+                                 int32_t n_fixes, const armando_fix_zone* fixes) {
+    if (!ctx) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL context");
+    if (ctx->prm.scheme == 0)
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "load and fix zones belong to the GPU-C schemes (scheme 1, 2)");
+    if (n_loads < 0 || n_loads > ARMANDO_MAX_ZONES || n_fixes < 0 || n_fixes > ARMANDO_MAX_ZONES)
+        return fail(ctx, ARMANDO_ERR_INVALID_ARG, "zone counts must be 0..ARMANDO_MAX_ZONES");
+    if ((n_loads && !loads) || (n_fixes && !fixes)) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "NULL zone table");
+    auto box_ok = [](const float* lo, const float* hi) {
+        for (int d = 0; d < 3; ++d)
+            if (std::isnan(lo[d]) || std::isnan(hi[d])) return false;
+        return true;
+    };
+    for (int k = 0; k < n_loads; ++k) {
+        const armando_load_zone& L = loads[k];
+        if (!box_ok(L.lo, L.hi) || !std::isfinite(L.accel[0]) || !std::isfinite(L.accel[1]) ||
+            !std::isfinite(L.accel[2]) || !std::isfinite(L.w))
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "load zone: NaN bound or non-finite accel / w");
+    }
+    for (int k = 0; k < n_fixes; ++k) {
+        const armando_fix_zone& F = fixes[k];
+        if (!box_ok(F.lo, F.hi) || !std::isfinite(F.vel[0]) || !std::isfinite(F.vel[1]) ||
+            !std::isfinite(F.vel[2]))
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "fix zone: NaN bound or non-finite velocity");
+    }
+    ctx->loads.assign(loads, loads + n_loads);
+    ctx->fixes.assign(fixes, fixes + n_fixes);
     return ARMANDO_OK;
 }
 

@@ -10,7 +10,8 @@
 //   scheme 2, the device kernels (armando.cu:429-513): the same terms, with
 //     pressure -(p_i/rho_i^2 + p_j/rho_j^2), for pairs of equal itype only;
 //     pairs of different itype push 0.5 W m_j/(rho_j h_j) c_j^2.
-// Energy: de/dt = p drho/dt / rho^2 (acpu.c:510-534); gravity on itype > 0.
+// Energy: de/dt = p drho/dt / rho^2 (acpu.c:510-534); gravity and the load
+// zones on itype > 0 (acpu.c:1047-1076); fix zones after the update.
 // Update and EOS per material |itype| (acpu.c:873-966, armando.cu:987-1074).
 // Kernels with h_i. The list of a step holds the j != i with
 // sqrtf(|x0_i - x0_j|^2) < 2 h_i at the step's start (updateListHost,
@@ -30,6 +31,27 @@ struct DevMaterial {
     int type;  // 0 boundary, 1 ideal gas, 2 polynomial, 3 shock, 4 Tait, 5 ESS
     float prop[10];
 };
+
+// Load and fix zones (acpu.c:33-48; armando.cu:43-58): open boxes lo < x < hi,
+// x and y only in 2D (armando2D.cu:756-762).
+struct DevLoadZone {
+    float lo[3], hi[3], g[3], w;
+};
+struct DevFixZone {
+    float lo[3], hi[3], v[3];
+};
+struct DevZones {
+    int n_load, n_fix;
+    DevLoadZone load[10];
+    DevFixZone fix[10];
+};
+
+template <int DIM>
+__device__ __forceinline__ bool in_zone(const float* lo, const float* hi, const float4& x) {
+    bool in = x.x > __ldg(lo) && x.x < __ldg(hi) && x.y > __ldg(lo + 1) && x.y < __ldg(hi + 1);
+    if (DIM == 3) in = in && x.z > __ldg(lo + 2) && x.z < __ldg(hi + 2);
+    return in;
+}
 
 struct GpucState {
     float4* x0;    // {x, y, m, h} (2D) / {x, y, z, h} (3D) at the step's start
@@ -142,14 +164,20 @@ __global__ void k_gpuc_gather(StateA A, const int* __restrict__ perm, GpucState 
 
 // Wendland C2 with h_i as the GPU-C codes evaluate it (acpu.c:146-201):
 // W = K/h^dim (1 - q/2)^4 (1 + 2q), dW/dr = K/h^(dim+1) 5/8 q (q - 2)^3.
+// The particle's factors: ih = 1/h, alpha = K/h^dim (as K ih^dim).
 template <int DIM>
-__device__ __forceinline__ void gpuc_kernel(float r, float h, float K, float& w, float& dwdr) {
+__device__ __forceinline__ void gpuc_kernel_norm(float h, float K, float& ih, float& alpha) {
+    ih = __frcp_rn(h);
+    alpha = DIM == 2 ? __fmul_rn(K, __fmul_rn(ih, ih)) : __fmul_rn(K, __fmul_rn(__fmul_rn(ih, ih), ih));
+}
+
+template <int DIM>
+__device__ __forceinline__ void gpuc_kernel(float r, float h, float ih, float alpha, float& w,
+                                            float& dwdr) {
     const float q = __fdiv_rn(r, h);
     w = 0.f;
     dwdr = 0.f;
     if (!(q < 2.f)) return;
-    const float ih = __frcp_rn(h);
-    const float alpha = DIM == 2 ? __fmul_rn(K, __fmul_rn(ih, ih)) : __fmul_rn(K, __fmul_rn(__fmul_rn(ih, ih), ih));
     float t = fmaf(-0.5f, q, 1.0f);
     t = __fmul_rn(t, t);
     t = __fmul_rn(t, t);
@@ -159,16 +187,52 @@ __device__ __forceinline__ void gpuc_kernel(float r, float h, float K, float& w,
                      __fmul_rn(alpha, ih));
 }
 
+// The smallest t with sqrt_rn(t) >= lim, so that sqrt_rn(r2) < lim exactly when
+// r2 < t (sqrt_rn is monotone): updateListHost's test without a square root
+// per candidate. lim^2 rounded lies within one step of t (checked on random
+// FP32 lims over [1e-30, 1e19] against IEEE square roots, in the CPU tests);
+// the loops allow four. lim <= 0 or NaN: no r2 passes.
+__device__ __forceinline__ float sqrt_less_bound(float lim) {
+    if (!(lim > 0.f)) return -INFINITY;
+    float t = __fmul_rn(lim, lim);
+    if (isinf(t)) return t;  // every finite r2 has sqrt_rn(r2) < lim
+#pragma unroll 1
+    for (int q = 0; q < 4 && __fsqrt_rn(t) < lim; ++q) t = nextafterf(t, INFINITY);
+#pragma unroll 1
+    for (int q = 0; q < 4; ++q) {
+        const float d = nextafterf(t, 0.f);
+        if (!(__fsqrt_rn(d) >= lim)) break;
+        t = d;
+    }
+    return t;
+}
+
+// Neighbours a lane collects before it evaluates them (a longer list is
+// evaluated in pieces of this length): about the lane's share of the 2D / 3D
+// neighbours, at least 8, within 48 KB of static shared memory per CTA.
+template <int DIM, int TPP, int BS>
+__host__ __device__ constexpr int gpuc_list_len() {
+    constexpr int want = (DIM == 2 ? 32 : 64) / TPP < 8 ? 8 : (DIM == 2 ? 32 : 64) / TPP;
+    return want * BS * 4 > 48 * 1024 ? 48 * 1024 / (4 * BS) : want;
+}
+
 // One RK3 stage: rates of every particle from working copy `cur`, update into
 // `nxt` (X0 + alpha (X + dt dX/dt - X0)), EOS. VAR 1: host path, 2: device.
-template <int DIM, int VAR>
-__global__ void __launch_bounds__(kPassThreads)
+// TPP lanes per particle split its candidates (lane `sub` takes slots
+// k0 + sub, k0 + sub + TPP, ... of every cell range) and sum their rates with
+// an xor butterfly; lane 0 updates. TPP = 1 sums in candidate order. Each lane
+// first lists the candidates that pass the start-position test (in shared
+// memory, candidate order kept) and then evaluates the list, so the lanes of a
+// warp run the pair physics together instead of idling through candidates.
+template <int DIM, int VAR, int TPP = 1, int BS = kPassThreads>
+__global__ void __launch_bounds__(BS)
     k_gpuc_stage(GpucState S, int cur, const unsigned* __restrict__ keys,
                  const int* __restrict__ start, const DevGrid* __restrict__ gp, DevParams P,
-                 const DevMaterial* __restrict__ mat, int n_mat, unsigned* __restrict__ flags,
-                 float alpha, float dt, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+                 const DevMaterial* __restrict__ mat, int n_mat, const DevZones* __restrict__ zones,
+                 unsigned* __restrict__ flags, float alpha, float dt, int n) {
+    const int i = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
+    const int sub = (TPP == 1) ? 0 : (int)(threadIdx.x & (TPP - 1));
+    if (i >= n) return;  // whole groups: the lanes of a particle share i
     const DevGrid g = *gp;
     // working copies picked without indexing the parameter arrays (no stack)
     const float4* __restrict__ xc = cur ? S.xw[1] : S.xw[0];
@@ -177,82 +241,120 @@ __global__ void __launch_bounds__(kPassThreads)
     float4* __restrict__ xo = cur ? S.xw[0] : S.xw[1];
     float4* __restrict__ vo = cur ? S.vw[0] : S.vw[1];
     float4* __restrict__ so = cur ? S.sw[0] : S.sw[1];
-    const float4 x0i = S.x0[i], v0i = S.v0[i];
-    const float2 q0 = S.q0[i];
+    const float4 x0i = S.x0[i];
     const float4 xi = xc[i], vi = vc[i], si = sc[i];
     const int it = S.itype[i];
     const float hi = x0i.w;
-    const float mi = mass_of<DIM>(x0i, v0i);
-    const float lim = __fmul_rn(2.0f, hi);
-    const float K = P.kw_hi;
+    const float mi = (DIM == 2) ? x0i.z : S.v0[i].w;
+    const float r2_bound = sqrt_less_bound(__fmul_rn(2.0f, hi));
+    float ih, kal;
+    gpuc_kernel_norm<DIM>(hi, P.kw_hi, ih, kal);
     float w0, d0;
-    gpuc_kernel<DIM>(0.f, hi, K, w0, d0);
+    gpuc_kernel<DIM>(0.f, hi, ih, kal, w0, d0);
+    // the device variant's own pressure term (armando.cu:483-485)
+    const float p_i = (VAR == 2) ? __fdiv_rn(si.z, __fmul_rn(si.x, si.x)) : 0.f;
     float rd = 0.f, a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    if (g.ok) {
-        const CellCoord cc = decode_key<DIM>(keys[i], g);
-        for_candidates<DIM>(g, start, cc, [&](int k) {
-            if (k == i) return;
-            const float4 x0k = __ldg(S.x0 + k);
-            // updateListHost's test on the step's start positions
-            const float e0 = __fsub_rn(x0i.x, x0k.x), e1 = __fsub_rn(x0i.y, x0k.y);
-            float r2 = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
-            if (DIM == 3) {
-                const float e2 = __fsub_rn(x0i.z, x0k.z);
-                r2 = __fadd_rn(r2, __fmul_rn(e2, e2));
+    auto pair = [&](int k) {
+        const float4 xk = __ldg(xc + k), vk = __ldg(vc + k);
+        const float4 sk = __ldg(sc + k);
+        const int itk = __ldg(S.itype + k);
+        const float dx = xi.x - xk.x, dy = xi.y - xk.y, dz = (DIM == 3) ? xi.z - xk.z : 0.f;
+        const float dr = __fsqrt_rn(fmaf(dz, dz, fmaf(dy, dy, __fmul_rn(dx, dx))));
+        if (dr < __fmul_rn(0.01f, hi)) return;  // dr := 100 h: W = dW/dr = 0 (acpu.c:379)
+        float w, dwdr;
+        gpuc_kernel<DIM>(dr, hi, ih, kal, w, dwdr);
+        const float mk = (DIM == 2) ? __ldg(&S.x0[k].z) : __ldg(&S.v0[k].w);
+        const float dvr = fmaf(dz, vi.z - vk.z, fmaf(dy, vi.y - vk.y, __fmul_rn(dx, vi.x - vk.x)));
+        const float rhoi = si.x, rhok = sk.x;
+        const float ir = __fdiv_rn(1.0f, dr);
+        float f = 0.f;  // times dW/dr along (x_i - x_k)/dr
+        const bool same = it == itk;
+        if (VAR == 1 || same) {
+            rd = fmaf(__fmul_rn(mk, dvr), __fmul_rn(dwdr, ir), rd);
+            if (VAR == 1)
+                f = __fmul_rn(mk, __fdiv_rn(-(si.z + sk.z), __fmul_rn(rhoi, rhok)));
+            else
+                f = __fmul_rn(mk, -(p_i + __fdiv_rn(sk.z, __fmul_rn(rhok, rhok))));
+            const float cs = __fdiv_rn(__fmul_rn(2.0f, si.w), rhoi + rhok);
+            rd = fmaf(__fmul_rn(mk, __fmul_rn(rhoi - rhok, cs)), dwdr, rd);
+            if (dvr < 0.f) {
+                const float sh = __fdiv_rn(__fmul_rn(dvr, hi), fmaf(0.01f * hi, hi, __fmul_rn(dr, dr)));
+                f = fmaf(mk, __fmul_rn(__fmul_rn(sh, cs), 0.03f), f);
             }
-            if (!(__fsqrt_rn(r2) < lim)) return;
-            const float4 xk = __ldg(xc + k), vk = __ldg(vc + k);
-            const float4 sk = __ldg(sc + k);
-            const int itk = __ldg(S.itype + k);
-            const float dx = xi.x - xk.x, dy = xi.y - xk.y, dz = (DIM == 3) ? xi.z - xk.z : 0.f;
-            const float dr = __fsqrt_rn(fmaf(dz, dz, fmaf(dy, dy, __fmul_rn(dx, dx))));
-            if (dr < __fmul_rn(0.01f, hi)) return;  // dr := 100 h: W = dW/dr = 0 (acpu.c:379)
-            float w, dwdr;
-            gpuc_kernel<DIM>(dr, hi, K, w, dwdr);
-            const float mk = (DIM == 2) ? __ldg(&S.x0[k].z) : __ldg(&S.v0[k].w);
-            const float dvr = fmaf(dz, vi.z - vk.z, fmaf(dy, vi.y - vk.y, __fmul_rn(dx, vi.x - vk.x)));
-            const float rhoi = si.x, rhok = sk.x;
-            const float ir = __fdiv_rn(1.0f, dr);
-            float f = 0.f;  // times dW/dr along (x_i - x_k)/dr
-            const bool same = it == itk;
-            if (VAR == 1 || same) {
-                rd = fmaf(__fmul_rn(mk, dvr), __fmul_rn(dwdr, ir), rd);
-                if (VAR == 1)
-                    f = __fmul_rn(mk, __fdiv_rn(-(si.z + sk.z), __fmul_rn(rhoi, rhok)));
-                else
-                    f = __fmul_rn(mk, -(__fdiv_rn(si.z, __fmul_rn(rhoi, rhoi)) +
-                                        __fdiv_rn(sk.z, __fmul_rn(rhok, rhok))));
-                const float cs = __fdiv_rn(__fmul_rn(2.0f, si.w), rhoi + rhok);
-                rd = fmaf(__fmul_rn(mk, __fmul_rn(rhoi - rhok, cs)), dwdr, rd);
-                if (dvr < 0.f) {
-                    const float sh = __fdiv_rn(__fmul_rn(dvr, hi), fmaf(0.01f * hi, hi, __fmul_rn(dr, dr)));
-                    f = fmaf(mk, __fmul_rn(__fmul_rn(sh, cs), 0.03f), f);
+        }
+        float push = 0.f;
+        if (!same) {
+            if (VAR == 1)
+                push = __fmul_rn(__fdiv_rn(mk, mi + mk),
+                                 __fdiv_rn(__fmul_rn(__fmul_rn(0.02f, __fdiv_rn(w, w0)), __fmul_rn(si.w, sk.w)), dr));
+            else
+                push = __fmul_rn(__fdiv_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, w), mk), rhok), __ldg(&S.x0[k].w)),
+                                 __fmul_rn(sk.w, sk.w));
+        }
+        const float tot = __fmul_rn(fmaf(f, dwdr, push), ir);
+        a0 = fmaf(tot, dx, a0);
+        a1 = fmaf(tot, dy, a1);
+        if (DIM == 3) a2 = fmaf(tot, dz, a2);
+    };
+    if (g.ok) {
+        constexpr int ML = gpuc_list_len<DIM, TPP, BS>();
+        __shared__ int s_list[ML][BS];
+        const int tid = threadIdx.x;
+        int nl = 0;
+        const CellCoord cc = decode_key<DIM>(keys[i], g);
+        Cursor cu = cursor_begin<DIM>(g);
+        while (cursor_next<DIM>(g, start, cc, cu))
+            for (int k = cu.k + sub; k < cu.ke; k += TPP) {
+                if (k == i) continue;
+                // updateListHost's test on the step's start positions
+                const float4 x0k = __ldg(S.x0 + k);
+                const float e0 = __fsub_rn(x0i.x, x0k.x), e1 = __fsub_rn(x0i.y, x0k.y);
+                float r2 = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
+                if (DIM == 3) {
+                    const float e2 = __fsub_rn(x0i.z, x0k.z);
+                    r2 = __fadd_rn(r2, __fmul_rn(e2, e2));
+                }
+                if (!(r2 < r2_bound)) continue;
+                s_list[nl++][tid] = k;
+                if (nl == ML) {  // a full list: evaluate it and go on collecting
+                    for (int q = 0; q < ML; ++q) pair(s_list[q][tid]);
+                    nl = 0;
                 }
             }
-            float push = 0.f;
-            if (!same) {
-                if (VAR == 1)
-                    push = __fmul_rn(__fdiv_rn(mk, mi + mk),
-                                     __fdiv_rn(__fmul_rn(__fmul_rn(0.02f, __fdiv_rn(w, w0)), __fmul_rn(si.w, sk.w)), dr));
-                else
-                    push = __fmul_rn(__fdiv_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, w), mk), rhok), __ldg(&S.x0[k].w)),
-                                     __fmul_rn(sk.w, sk.w));
-            }
-            const float tot = __fmul_rn(fmaf(f, dwdr, push), ir);
-            a0 = fmaf(tot, dx, a0);
-            a1 = fmaf(tot, dy, a1);
-            if (DIM == 3) a2 = fmaf(tot, dz, a2);
-        });
+        for (int q = 0; q < nl; ++q) pair(s_list[q][tid]);
     }
-    if (it > 0) {  // updateLoadsHost: gravity zone over every fluid particle
-        a0 += P.gravity[0];
-        a1 += P.gravity[1];
-        if (DIM == 3) a2 += P.gravity[2];
+    if (TPP > 1) {  // the particle's lanes reach this point together
+        rd = group_sum<TPP>(rd);
+        a0 = group_sum<TPP>(a0);
+        a1 = group_sum<TPP>(a1);
+        if (DIM == 3) a2 = group_sum<TPP>(a2);
+        if (sub != 0) return;
     }
-    const float du = __fdiv_rn(__fmul_rn(si.z, rd), __fmul_rn(si.x, si.x));  // balanceEnergyHost
+    // the start state, read after the pair loop (not held in registers across it)
+    const float4 v0i = S.v0[i];
+    const float2 q0 = S.q0[i];
+    float wz = 0.f;
+    if (it > 0) {  // updateLoadsHost: gravity over every fluid particle, then the zones
+        float g0 = P.gravity[0], g1 = P.gravity[1], g2 = P.gravity[2];
+        const int nl = __ldg(&zones->n_load);
+#pragma unroll 1
+        for (int q = 0; q < nl; ++q) {
+            const DevLoadZone* Z = zones->load + q;
+            if (!in_zone<DIM>(Z->lo, Z->hi, xi)) continue;
+            g0 = __fadd_rn(g0, __ldg(&Z->g[0]));
+            g1 = __fadd_rn(g1, __ldg(&Z->g[1]));
+            g2 = __fadd_rn(g2, __ldg(&Z->g[2]));
+            wz = __fadd_rn(wz, __ldg(&Z->w));
+        }
+        a0 += g0;
+        a1 += g1;
+        if (DIM == 3) a2 += g2;
+    }
+    // balanceEnergyHost on top of the loads' w
+    const float du = __fadd_rn(wz, __fdiv_rn(__fmul_rn(si.z, rd), __fmul_rn(si.x, si.x)));
     S.rates[i] = make_float4(a0, a1, a2, du);
     float4 xn = xi, vn = vi, sn = si;
-    if (VAR == 2 || it != 0) {  // acpu.c:899 leaves itype 0 alone
+    if (VAR == 2 || it != 0) {  // acpu.c:894 leaves itype 0 alone
         xn.x = fmaf(alpha, fmaf(dt, vi.x, xi.x) - x0i.x, x0i.x);
         xn.y = fmaf(alpha, fmaf(dt, vi.y, xi.y) - x0i.y, x0i.y);
         if (DIM == 3) xn.z = fmaf(alpha, fmaf(dt, vi.z, xi.z) - x0i.z, x0i.z);
@@ -262,7 +364,21 @@ __global__ void __launch_bounds__(kPassThreads)
         float rho = fmaf(alpha, fmaf(dt, rd, si.x) - q0.x, q0.x);
         const float u = fmaf(alpha, fmaf(dt, du, si.y) - q0.y, q0.y);
         const DevMaterial& M = mat[gpuc_material(it, n_mat, flags)];
-        if ((VAR == 1 && it <= 0) || M.type == 0) {  // velocity kept
+        if (VAR == 1 && it <= 0) {  // acpu.c:910-914
+            vn.x = v0i.x;
+            vn.y = v0i.y;
+            if (DIM == 3) vn.z = v0i.z;
+        }
+        const int nf = __ldg(&zones->n_fix);
+#pragma unroll 1
+        for (int q = 0; q < nf; ++q) {  // fix zones at the new position
+            const DevFixZone* Z = zones->fix + q;
+            if (!in_zone<DIM>(Z->lo, Z->hi, xn)) continue;
+            vn.x = __ldg(&Z->v[0]);
+            vn.y = __ldg(&Z->v[1]);
+            if (DIM == 3) vn.z = __ldg(&Z->v[2]);
+        }
+        if (M.type == 0) {  // boundary materials keep their velocity
             vn.x = v0i.x;
             vn.y = v0i.y;
             if (DIM == 3) vn.z = v0i.z;

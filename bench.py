@@ -93,6 +93,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 3D channel and batched-sweep workloads")
     ap.add_argument("--extra-steps", type=int, default=20)
+    ap.add_argument("--gpuc-cases", default="1,2,3",
+                    help="with --only gpuc: which published dam-break cases (1-3) to time")
     ap.add_argument("--sweep-instances", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=10)
     return ap.parse_args()
@@ -426,7 +428,10 @@ def run_gpuc(args):
     from armando_gb300 import cases
 
     out = []
-    for scale, (n_pub, steps_pub, sec_pub) in GPUC_PUBLISHED.items():
+    wanted = {int(k) for k in args.gpuc_cases.split(",")}
+    for num, (scale, (n_pub, steps_pub, sec_pub)) in enumerate(GPUC_PUBLISHED.items(), start=1):
+        if num not in wanted:
+            continue
         c = cases.gpuc_dam_break(scale)
         assert c.n == n_pub
         dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
@@ -441,7 +446,7 @@ def run_gpuc(args):
         del dev
         v = c.n * steps / (ms * 1e-3)
         pub = n_pub * steps_pub / sec_pub
-        out.append({"case": f"dam break case {[1, 2, 4].index(scale) + 1}", "particles": c.n,
+        out.append({"case": f"dam break case {num}", "particles": c.n,
                     "steps": steps, "ms_per_step": ms / steps, "value": v, "unit": METRIC,
                     "published_c1060": pub, "ratio_to_published": v / pub,
                     "launches_per_step": launches, "tuning": tuned})

@@ -444,6 +444,37 @@ armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, flo
                                       int32_t* itype, float* dvdt, float* dudt, float dt,
                                       int32_t its0, int32_t steps, int64_t* n_particles);
 
+/* ---- load and fix zones of the GPU-C schemes (scheme 1, 2) ------------------------
+ * The GPU-C codes' `struct load` and `struct fix` tables (ArmandoThrust/acpu.c:33-48,
+ * hLoad / hFix; armando.cu:43-58). A zone is the open box lo < x < hi (every bound
+ * strict; in 2D x and y only, as armando2D.cu:756-762 tests them):
+ *   load: every rate evaluation, a particle with itype > 0 inside the box gains
+ *     accel on dv/dt and w on de/dt (updateLoadsHost, acpu.c:1047-1076), zones in
+ *     table order after params.gravity (the reference's load 0 over the whole box);
+ *   fix: after every stage's update, a particle inside the box at its new position
+ *     takes the velocity vel (acpu.c:916-926, armando.cu:1026-1036; the last
+ *     matching zone wins); scheme 1 applies it to itype != 0 after resetting the
+ *     velocity of itype <= 0, scheme 2 to every particle; boundary-type materials
+ *     then keep their start velocity in both.
+ * Bounds may be infinite; the other fields must be finite. */
+typedef struct armando_load_zone {
+    float lo[3], hi[3];
+    float accel[3];
+    float w;
+} armando_load_zone;
+
+typedef struct armando_fix_zone {
+    float lo[3], hi[3];
+    float vel[3];
+} armando_fix_zone;
+
+#define ARMANDO_MAX_ZONES 10
+
+/* Sets the zones (at most ARMANDO_MAX_ZONES of each; zero counts clear them).
+ * ARMANDO_ERR_UNSUPPORTED for the CERN scheme (params.scheme 0). */
+armando_status armando_set_zones(armando_ctx* ctx, int32_t n_loads, const armando_load_zone* loads,
+                                 int32_t n_fixes, const armando_fix_zone* fixes);
+
 /* Smoothing lengths of the context's particles after its last step or
  * integrate call, in caller order (evolved when params.sle != 0; otherwise the
  * ones passed in). With density_form 1 the context also keeps drho/dt between

@@ -46,9 +46,14 @@ class Simulation(C.Structure):  # acpu.c:23-32
                [("tsn", C.c_int), ("ssi", C.c_int), ("nsi", C.c_int)]
 
 
-class Load(C.Structure):  # acpu.c:34-42
+class Load(C.Structure):  # acpu.c:33-41
     _fields_ = [(k, C.c_float) for k in ("minX", "maxX", "minY", "maxY", "minZ", "maxZ",
                                          "gx", "gy", "gz", "w")]
+
+
+class Fix(C.Structure):  # acpu.c:43-48
+    _fields_ = [(k, C.c_float) for k in ("minX", "maxX", "minY", "maxY", "minZ", "maxZ",
+                                         "velX", "velY", "velZ")]
 
 
 MODEL_FLOATS = ["Mass", "Smooth", "PosX", "PosY", "PosZ", "VelX", "VelY", "VelZ", "Density",
@@ -82,12 +87,15 @@ def _ptr(a, t):
 class AcpuRun:
     """A 2D particle system stepped by acpu.c. x, v: [n, 2]; materials:
     {index: (type, [props])} set into hMatType / hMatProp; gravity a load zone
-    over the whole box (acpu.c:1047-1076 applies it to Material > 0)."""
+    over the whole box (acpu.c:1047-1076 applies it to Material > 0), then
+    `loads` [(lo2, hi2, (gx, gy), w)] in hLoad[1:] and `fixes` [(lo2, hi2,
+    (vx, vy))] in hFix, z bounds -1, 1 (the 2D system lies at z = 0)."""
 
     SORTED = ["Mass", "Smooth", "PosX", "PosY", "PosZ", "VelX", "VelY", "VelZ", "Density",
               "Energy", "Pressure", "Sound"]
 
-    def __init__(self, x, v, mass, rho, p, u, h, material, sound, materials, dt, gravity=(0.0, 0.0)):
+    def __init__(self, x, v, mass, rho, p, u, h, material, sound, materials, dt, gravity=(0.0, 0.0),
+                 loads=(), fixes=()):
         self.L = L = load_acpu()
         n = len(mass)
         self.n = n
@@ -102,16 +110,26 @@ class AcpuRun:
             for q, val in enumerate(props):
                 mat_prop[k][q] = val
         Simulation.in_dll(L, "hRun").dt = float(dt)
-        loads = (Load * 10).in_dll(L, "hLoad")
+        tab_l = (Load * 10).in_dll(L, "hLoad")
         for k in range(10):
-            C.memset(C.byref(loads[k]), 0, C.sizeof(Load))
+            C.memset(C.byref(tab_l[k]), 0, C.sizeof(Load))
         h0 = float(np.max(h))
         lo, hi = x.min(axis=0) - 8 * h0, x.max(axis=0) + 8 * h0
-        loads[0].minX, loads[0].maxX, loads[0].minY, loads[0].maxY = lo[0], hi[0], lo[1], hi[1]
-        loads[0].minZ, loads[0].maxZ = -1.0, 1.0
-        loads[0].gx, loads[0].gy = gravity[0], gravity[1]
-        fixes = (C.c_char * (C.sizeof(C.c_float) * 9 * 10)).in_dll(L, "hFix")
-        C.memset(fixes, 0, C.sizeof(fixes))
+        tab_l[0].minX, tab_l[0].maxX, tab_l[0].minY, tab_l[0].maxY = lo[0], hi[0], lo[1], hi[1]
+        tab_l[0].minZ, tab_l[0].maxZ = -1.0, 1.0
+        tab_l[0].gx, tab_l[0].gy = gravity[0], gravity[1]
+        assert len(loads) <= 9 and len(fixes) <= 10
+        for k, (zlo, zhi, g, w) in enumerate(loads, start=1):
+            z = tab_l[k]
+            z.minX, z.maxX, z.minY, z.maxY, z.minZ, z.maxZ = zlo[0], zhi[0], zlo[1], zhi[1], -1.0, 1.0
+            z.gx, z.gy, z.w = g[0], g[1], w
+        tab = (Fix * 10).in_dll(L, "hFix")
+        for k in range(10):
+            C.memset(C.byref(tab[k]), 0, C.sizeof(Fix))
+        for k, (zlo, zhi, vel) in enumerate(fixes):
+            z = tab[k]
+            z.minX, z.maxX, z.minY, z.maxY, z.minZ, z.maxZ = zlo[0], zhi[0], zlo[1], zhi[1], -1.0, 1.0
+            z.velX, z.velY = vel[0], vel[1]
         self.a = {k: np.zeros(n, np.float32) for k in MODEL_FLOATS}
         a = self.a
         a["Mass"][:], a["Smooth"][:] = mass, h

@@ -9,7 +9,8 @@
 //   pair rates, variant 1 (host path)    acpu.c:346-437  balanceMassMomentumHost
 //   pair rates, variant 2 (device path)  ArmandoThrust/armando.cu:429-513
 //   energy rate        acpu.c:510-534    de/dt = p drho/dt / rho^2
-//   loads              acpu.c:1047-1076  (gravity on itype > 0)
+//   loads              acpu.c:1047-1076  (gravity, then load zones, on itype > 0)
+//   fix zones          acpu.c:916-926, armando.cu:1026-1036 (after the update)
 //   update + EOS       acpu.c:873-966 (variant 1), armando.cu:987-1074 (variant 2)
 //   EOS functions      acpu.c:560-870; ESS from Code/armando.cu:572-598, 703-723
 //   Wendland W, dW/dr  acpu.c:146-201 with h_i (2D alpha 7/(4 pi h^2); 3D as
@@ -37,12 +38,30 @@ struct GpucMaterial {
     double prop[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 };
 
+// Load and fix zones (acpu.c:33-48): the open box lo < x < hi, x and y only
+// in 2D (armando2D.cu:756-762).
+struct GpucLoad {
+    float lo[3], hi[3], g[3], w;
+};
+struct GpucFix {
+    float lo[3], hi[3], v[3];
+};
+
+template <class R>
+inline bool gpuc_in_zone(const float* lo, const float* hi, const R* x, int dim) {
+    for (int d = 0; d < dim; ++d)
+        if (!(x[d] > R(lo[d]) && x[d] < R(hi[d]))) return false;
+    return true;
+}
+
 template <class R>
 struct GpucSetup {
     int variant = 1;  // 1: host path (acpu.c), 2: device kernels (armando.cu)
     int legacy3d = 0;
     R gravity[3] = {R(0), R(0), R(0)};
     std::vector<GpucMaterial> mat;  // by |itype|
+    std::vector<GpucLoad> loads;
+    std::vector<GpucFix> fixes;
 };
 
 // Density clamp rho >= 0.9 rho0 (densityTait/Poly/Shock, acpu.c:843-870).
@@ -195,8 +214,15 @@ void gpuc_rates(const State<R>& s, const std::vector<std::vector<int>>& list,
     drho.assign(n, R(0));
     du.assign(n, R(0));
     for (int64_t i = 0; i < n; ++i) {
-        if (s.itype[i] > 0)  // updateLoadsHost: gravity zone over every fluid particle
+        R wz = R(0);
+        if (s.itype[i] > 0) {  // updateLoadsHost: gravity over every fluid particle, then the zones
             for (int d = 0; d < dim; ++d) dv[i * dim + d] = G.gravity[d];
+            for (const GpucLoad& Z : G.loads) {
+                if (!gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim)) continue;
+                for (int d = 0; d < dim; ++d) dv[i * dim + d] = dv[i * dim + d] + R(Z.g[d]);
+                wz = wz + R(Z.w);
+            }
+        }
         const R hi = s.h[i];
         const R w0 = kernel_w(R(0), hi, dim, G.legacy3d);
         R rd = R(0), a[3] = {R(0), R(0), R(0)};
@@ -241,7 +267,7 @@ void gpuc_rates(const State<R>& s, const std::vector<std::vector<int>>& list,
         }
         drho[i] = rd;
         for (int d = 0; d < dim; ++d) dv[i * dim + d] = dv[i * dim + d] + a[d];
-        du[i] = s.p[i] * rd / (s.rho[i] * s.rho[i]);  // balanceEnergyHost
+        du[i] = wz + s.p[i] * rd / (s.rho[i] * s.rho[i]);  // balanceEnergyHost on the loads' w
     }
 }
 
@@ -388,6 +414,11 @@ void gpuc_rk3_step(State<R>& s, const GpucSetup<R>& G, double dt, std::vector<R>
     if (open) gpuc_open(s, *open, dt);
     const int dim = s.dim;
     const int64_t n = s.n;
+    if (n == 0) {  // every particle left: nothing to step until an inlet emits
+        if (dv_out) dv_out->clear();
+        if (du_out) du_out->clear();
+        return;
+    }
     std::vector<Rc> xc(n * dim), hc(n);
     for (int64_t i = 0; i < n * dim; ++i) xc[i] = Rc(s.x[i]);
     for (int64_t i = 0; i < n; ++i) hc[i] = Rc(s.h[i]);
@@ -401,7 +432,7 @@ void gpuc_rk3_step(State<R>& s, const GpucSetup<R>& G, double dt, std::vector<R>
         gpuc_rates(s, list, G, dv, drho, du);
         for (int64_t i = 0; i < n; ++i) {
             const int it = s.itype[i];
-            if (G.variant == 1 && it == 0) continue;  // acpu.c:899
+            if (G.variant == 1 && it == 0) continue;  // acpu.c:894
             for (int d = 0; d < dim; ++d) {
                 const int64_t k = i * dim + d;
                 s.x[k] = x0[k] + alpha * (s.x[k] + Rdt * s.v[k] - x0[k]);
@@ -413,7 +444,12 @@ void gpuc_rk3_step(State<R>& s, const GpucSetup<R>& G, double dt, std::vector<R>
             s.rho[i] = rho0[i] + alpha * (s.rho[i] + Rdt * drho[i] - rho0[i]);
             s.u[i] = u0[i] + alpha * (s.u[i] + Rdt * du[i] - u0[i]);
             const GpucMaterial& M = gpuc_material(G.mat, it);
-            if ((G.variant == 1 && it <= 0) || M.type == EOS_BOUNDARY)
+            if (G.variant == 1 && it <= 0)  // acpu.c:910-914
+                for (int d = 0; d < dim; ++d) s.v[i * dim + d] = v0[i * dim + d];
+            for (const GpucFix& Z : G.fixes)  // acpu.c:916-926 at the new position
+                if (gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim))
+                    for (int d = 0; d < dim; ++d) s.v[i * dim + d] = R(Z.v[d]);
+            if (M.type == EOS_BOUNDARY)
                 for (int d = 0; d < dim; ++d) s.v[i * dim + d] = v0[i * dim + d];
             gpuc_eos(M, s.rho[i], s.u[i], s.p[i], s.c[i]);
         }

@@ -17,7 +17,7 @@ _REPO = os.path.dirname(_HERE)
 if _REPO not in sys.path:
     sys.path.insert(0, _REPO)
 
-from armando_gb300._abi import Inlet, Material, Outlet, Params  # noqa: E402  (shared C-ABI structs)
+from armando_gb300._abi import FixZone, Inlet, LoadZone, Material, Outlet, Params  # noqa: E402  (shared C-ABI structs)
 
 LIB_PATH = os.path.join(_HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(_HERE, "_ref", "libacpu.so")
@@ -83,11 +83,12 @@ def lib() -> C.CDLL:
         L.ao_tangent_f64.restype = C.c_int
         L.ao_flops_f64.argtypes = [C.POINTER(Params), i64, C.c_int, C.c_double] + [vp] * 11
         L.ao_flops_f64.restype = C.c_int
-        L.ao_gpuc_step_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material), i64,
-                                       C.c_int, C.c_double] + [vp] * 10 + [C.c_int]
+        zones = [C.c_int32, C.POINTER(LoadZone), C.c_int32, C.POINTER(FixZone)]
+        L.ao_gpuc_step_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material)] + zones + \
+            [i64, C.c_int, C.c_double] + [vp] * 10 + [C.c_int]
         L.ao_gpuc_step_f64.restype = C.c_int
-        L.ao_gpuc_open_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material),
-                                       C.c_int32, C.POINTER(Inlet), C.c_int32, C.POINTER(Outlet),
+        L.ao_gpuc_open_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material)] + zones + \
+                                      [C.c_int32, C.POINTER(Inlet), C.c_int32, C.POINTER(Outlet),
                                        vp, vp, i64, C.POINTER(i64), C.c_int, C.c_double] + \
             [vp] * 10 + [C.c_int]
         L.ao_gpuc_open_f64.restype = C.c_int
@@ -242,10 +243,17 @@ def ghosts(params: Params, x, v, h, itype, fp32=True):
     return owner[:ng], wall[:ng], xg[:ng * dim].reshape(ng, dim), vg[:ng * dim].reshape(ng, dim)
 
 
-def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = True):
+def _zones(loads, fixes):
+    return (len(loads), (LoadZone * max(len(loads), 1))(*loads), len(fixes),
+            (FixZone * max(len(fixes), 1))(*fixes))
+
+
+def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = True, loads=(),
+              fixes=()):
     """`steps` TVD-RK3 steps of the GPU-C scheme state.params.scheme (1 host-path,
     2 device-kernel physics), in place. materials: list of _abi.Material by
-    |itype| (None: Tait with rho0, c0). Returns the last stage's (dvdt, dudt)."""
+    |itype| (None: Tait with rho0, c0); loads, fixes: _abi.LoadZone / FixZone
+    lists. Returns the last stage's (dvdt, dudt)."""
     n, dim = state.n, state.dim
     dv = np.zeros(n * dim)
     du = np.zeros(n)
@@ -254,7 +262,8 @@ def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = 
     if materials is not None:
         nmat = len(materials)
         tab = (Material * nmat)(*materials)
-    rc = lib().ao_gpuc_step_f64(C.byref(state.params), nmat, tab, n, steps, dt, _p(state.x),
+    rc = lib().ao_gpuc_step_f64(C.byref(state.params), nmat, tab, *_zones(loads, fixes), n, steps, dt,
+                                _p(state.x),
                                 _p(state.v), _p(state.m), _p(state.rho), _p(state.p), _p(state.u),
                                 _p(state.h), _p(state.itype), _p(dv), _p(du), int(fp32))
     if rc:
@@ -263,7 +272,7 @@ def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = 
 
 
 def gpuc_open(case, steps, dt, capacity, n=None, inlets=(), outlets=(), box=None,
-              materials=None, fp32=True):
+              materials=None, fp32=True, loads=(), fixes=()):
     """GPU-C steps with open boundaries from the first n particles of a case
     (FP32 arrays; n = all of them by default): returns a dict of FP64 arrays
     (x, v, mass, rho, p, u, h, itype, dvdt, dudt) of the particles left,
@@ -280,15 +289,19 @@ def gpuc_open(case, steps, dt, capacity, n=None, inlets=(), outlets=(), box=None
         arr[:src.size] = src
         a[f] = arr
     n = C.c_int64(n0)
-    lo = np.array(box[0] if box else [-1e30] * 3, np.float32)
-    hi = np.array(box[1] if box else [1e30] * 3, np.float32)
+    lo = np.full(3, -3.0e38, np.float32)
+    hi = np.full(3, 3.0e38, np.float32)
+    if box:
+        lo[:len(box[0])] = box[0]
+        hi[:len(box[1])] = box[1]
     tin = (Inlet * max(len(inlets), 1))(*inlets)
     tout = (Outlet * max(len(outlets), 1))(*outlets)
     tab, nmat = None, 0
     if materials is not None:
         nmat = len(materials)
         tab = (Material * nmat)(*materials)
-    rc = lib().ao_gpuc_open_f64(C.byref(case.params), nmat, tab, len(inlets), tin, len(outlets),
+    rc = lib().ao_gpuc_open_f64(C.byref(case.params), nmat, tab, *_zones(loads, fixes),
+                                len(inlets), tin, len(outlets),
                                 tout, _p(lo), _p(hi), capacity, C.byref(n), steps, dt,
                                 *[_p(a[f]) for f in ("x", "v", "mass", "rho", "p", "u", "h",
                                                      "itype", "dvdt", "dudt")], int(fp32))

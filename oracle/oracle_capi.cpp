@@ -415,34 +415,60 @@ int64_t ao_ghosts_f64(const armando_params* prm, int64_t n, const double* x, con
     }
 }
 
-// GPU-C scheme (params->scheme 1 or 2): `steps` TVD-RK3 steps in place. The
-// material table has nmat entries (NULL: Tait with rho0, c0 for every |itype|).
-// fp32 = 1: neighbour lists in FP32 coordinates (the library's). dvdt, dudt
-// (nullable): rates of the last stage.
-int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
-                     int64_t n, int steps, double dt, double* x, double* v, const double* m,
-                     double* rho, double* p, double* u, const double* h, const int* itype,
-                     double* dvdt, double* dudt, int fp32) {
-    if (prm->scheme != 1 && prm->scheme != 2) return 2;
-    ao::Params<double> P = to_params<double>(prm);
+// Setup of the GPU-C schemes: variant, kernel switch, gravity, the material
+// table (nmat entries; NULL: Tait with rho0, c0 for every |itype|) and the
+// load and fix zones.
+static ao::GpucSetup<double> gpuc_setup(const armando_params* prm, int32_t nmat, const armando_material* table,
+                                        int32_t n_load, const armando_load_zone* loads, int32_t n_fix,
+                                        const armando_fix_zone* fixes) {
     ao::GpucSetup<double> G;
     G.variant = prm->scheme;
     G.legacy3d = prm->kernel_3d_legacy;
     for (int d = 0; d < 3; ++d) G.gravity[d] = prm->gravity[d];
-    if (table) {
-        G.mat.resize(nmat);
-        for (int k = 0; k < nmat; ++k) {
+    G.mat.resize(table ? nmat : ARMANDO_MAX_MATERIALS);
+    for (size_t k = 0; k < G.mat.size(); ++k) {
+        if (table) {
             G.mat[k].type = table[k].eos;
             for (int q = 0; q < 10; ++q) G.mat[k].prop[q] = table[k].prop[q];
-        }
-    } else {
-        G.mat.resize(ARMANDO_MAX_MATERIALS);
-        for (auto& M : G.mat) {
-            M.type = ao::EOS_TAIT;
-            M.prop[0] = prm->rho0;
-            M.prop[1] = prm->c0;
+        } else {
+            G.mat[k].type = ao::EOS_TAIT;
+            G.mat[k].prop[0] = prm->rho0;
+            G.mat[k].prop[1] = prm->c0;
         }
     }
+    for (int k = 0; k < n_load; ++k) {
+        ao::GpucLoad Z;
+        for (int d = 0; d < 3; ++d) {
+            Z.lo[d] = loads[k].lo[d];
+            Z.hi[d] = loads[k].hi[d];
+            Z.g[d] = loads[k].accel[d];
+        }
+        Z.w = loads[k].w;
+        G.loads.push_back(Z);
+    }
+    for (int k = 0; k < n_fix; ++k) {
+        ao::GpucFix Z;
+        for (int d = 0; d < 3; ++d) {
+            Z.lo[d] = fixes[k].lo[d];
+            Z.hi[d] = fixes[k].hi[d];
+            Z.v[d] = fixes[k].vel[d];
+        }
+        G.fixes.push_back(Z);
+    }
+    return G;
+}
+
+// GPU-C scheme (params->scheme 1 or 2): `steps` TVD-RK3 steps in place, with
+// the setup of gpuc_setup. fp32 = 1: neighbour lists in FP32 coordinates (the
+// library's). dvdt, dudt (nullable): rates of the last stage.
+int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
+                     int32_t n_load, const armando_load_zone* loads, int32_t n_fix,
+                     const armando_fix_zone* fixes, int64_t n, int steps, double dt, double* x,
+                     double* v, const double* m, double* rho, double* p, double* u, const double* h,
+                     const int* itype, double* dvdt, double* dudt, int fp32) {
+    if (prm->scheme != 1 && prm->scheme != 2) return 2;
+    ao::Params<double> P = to_params<double>(prm);
+    const ao::GpucSetup<double> G = gpuc_setup(prm, nmat, table, n_load, loads, n_fix, fixes);
     ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, nullptr, nullptr);
     std::vector<double> dv, du;
     try {
@@ -463,27 +489,14 @@ int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_mate
 // arrays hold `capacity` entries (x, v, dvdt: capacity*dim). Returns 0, 1 on a
 // failed step, 3 when the particles outgrow the capacity.
 int ao_gpuc_open_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
-                     int32_t n_in, const armando_inlet* inlets, int32_t n_out,
-                     const armando_outlet* outlets, const float* lo, const float* hi,
+                     int32_t n_load, const armando_load_zone* loads, int32_t n_fix,
+                     const armando_fix_zone* fixes, int32_t n_in, const armando_inlet* inlets,
+                     int32_t n_out, const armando_outlet* outlets, const float* lo, const float* hi,
                      int64_t capacity, int64_t* n, int steps, double dt, double* x, double* v,
                      double* m, double* rho, double* p, double* u, double* h, int* itype,
                      double* dvdt, double* dudt, int fp32) {
     if (prm->scheme != 1 && prm->scheme != 2) return 2;
-    ao::GpucSetup<double> G;
-    G.variant = prm->scheme;
-    G.legacy3d = prm->kernel_3d_legacy;
-    for (int d = 0; d < 3; ++d) G.gravity[d] = prm->gravity[d];
-    G.mat.resize(table ? nmat : ARMANDO_MAX_MATERIALS);
-    for (size_t k = 0; k < G.mat.size(); ++k) {
-        if (table) {
-            G.mat[k].type = table[k].eos;
-            for (int q = 0; q < 10; ++q) G.mat[k].prop[q] = table[k].prop[q];
-        } else {
-            G.mat[k].type = ao::EOS_TAIT;
-            G.mat[k].prop[0] = prm->rho0;
-            G.mat[k].prop[1] = prm->c0;
-        }
-    }
+    const ao::GpucSetup<double> G = gpuc_setup(prm, nmat, table, n_load, loads, n_fix, fixes);
     ao::GpucOpen O;
     for (int k = 0; k < n_in; ++k) {
         ao::GpucInlet I;

@@ -15,6 +15,12 @@ Writes tests/golden/acpu_rk3.npz:
     walls of a boundary-type material, u = 100 J/kg;
   * eos_*: known answers of acpu.c's EOS functions (pressure, sound, density
     clamp) for every type on a grid of (rho, u).
+and tests/golden/acpu_zones.npz:
+  * zones_*: the water tank with two overlapping load zones (acceleration and
+    heating, acpu.c:1047-1076) and a fix zone over the left of the water and
+    part of the left wall (prescribed velocity, acpu.c:916-926), the zones as
+    zones_load (rows lo_x, lo_y, hi_x, hi_y, gx, gy, w) and zones_fix (rows
+    lo_x, lo_y, hi_x, hi_y, vx, vy); the state after 1 and after 5 steps.
 No neighbour list needs more than the reference's MAXN = 21 entries (checked).
 """
 import ctypes as C
@@ -31,6 +37,11 @@ from acpu_driver import MAXN, AcpuRun, load_acpu  # noqa: E402
 from armando_gb300 import cases  # noqa: E402
 
 OUT = os.path.join(HERE, "acpu_rk3.npz")
+OUT_ZONES = os.path.join(HERE, "acpu_zones.npz")
+INF = float("inf")
+LOADS = [((0.10, -INF), (0.24, INF), (3.0, 1.5), 250.0),
+         ((0.20, -INF), (0.50, 0.08), (-1.0, 0.0), 40.0)]
+FIXES = [((-0.10, -0.03), (0.06, 0.12), (0.5, 0.0))]
 
 TAIT = (4, [1000.0, 50.0, -1.0e12])
 SHOCK = (3, [1000.0, 50.0, 0.5, 1.3])
@@ -56,7 +67,7 @@ def tank(seed):
     return c
 
 
-def run(c, material, materials, u, steps_list):
+def run(c, material, materials, u, steps_list, loads=(), fixes=()):
     x = c.x.reshape(-1, 2).astype(np.float32)
     v = c.v.reshape(-1, 2).astype(np.float32)
     snd = np.zeros(c.n, np.float32)
@@ -64,7 +75,7 @@ def run(c, material, materials, u, steps_list):
         sel = np.abs(material) == k
         snd[sel] = sound(t, props, c.rho[sel], u[sel])
     r = AcpuRun(x, v, c.mass, c.rho, c.p, u, c.h, material, snd, materials, c.dt,
-                gravity=(0.0, -9.81))
+                gravity=(0.0, -9.81), loads=loads, fixes=fixes)
     out = {}
     done = 0
     for s in steps_list:
@@ -134,6 +145,21 @@ def main():
         data["eos_" + k] = val
     np.savez_compressed(OUT, **data)
     print("wrote", OUT, len(data), "arrays")
+    zones = {}
+    c = tank(13)
+    u = np.zeros(c.n, np.float32)
+    out = run(c, c.itype.copy(), {1: TAIT}, u, [1, 5], LOADS, FIXES)
+    zones.update({"zones_x0": c.x, "zones_v0": c.v, "zones_m": c.mass, "zones_rho0": c.rho,
+                  "zones_h": c.h, "zones_itype": c.itype, "zones_dt": np.float64(c.dt),
+                  "zones_load": np.array([list(lo) + list(hi) + list(g) + [w] for lo, hi, g, w in LOADS],
+                                         np.float32),
+                  "zones_fix": np.array([list(lo) + list(hi) + list(v) for lo, hi, v in FIXES],
+                                        np.float32)})
+    for s, st in out.items():
+        for k, val in st.items():
+            zones[f"zones_{k}_{s}"] = val
+    np.savez_compressed(OUT_ZONES, **zones)
+    print("wrote", OUT_ZONES, len(zones), "arrays")
 
 
 if __name__ == "__main__":

@@ -109,8 +109,11 @@ def test_published_dam_break_matches_the_oracle(O, scheme):
         assert rel(a, b) <= TOL[f] * 2, (scheme, f, rel(a, b))
 
 
-@pytest.mark.parametrize("tuning", [(2, 1, 256, 0), (3, 1, 128, 0)])
+@pytest.mark.parametrize("tuning", [(2, 1, 256, 0), (3, 1, 128, 0), (1, 2, 128, 0), (1, 4, 256, 0),
+                                    (2, 4, 128, 0)])
 def test_tunings(O, G, tuning):
+    """Cell reach, lanes per particle (their sums in another order) and CTA
+    size against acpu.c."""
     c = golden_case(G, "multi")
     mats = [WALL, TAIT, SHOCK, WALL, POLY]
     got = fields(run_gpu(c, 5, mats, tuning))
@@ -166,3 +169,127 @@ def test_refusals():
     with pytest.raises(ag.ArmandoError) as e:
         ag.Context(bad, c.n_fluid, c.n_wall)
     assert e.value.status == ag._abi.ERR_INVALID_ARG
+
+
+GOLD_ZONES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "acpu_zones.npz")
+
+
+def zones_of(Z):
+    from armando_gb300._abi import FixZone, LoadZone
+
+    loads = [LoadZone.make(r[0:2], r[2:4], (r[4], r[5], 0.0), r[6]) for r in Z["zones_load"]]
+    fixes = [FixZone.make(r[0:2], r[2:4], (r[4], r[5], 0.0)) for r in Z["zones_fix"]]
+    return loads, fixes
+
+
+@pytest.mark.parametrize("steps", [1, 5])
+def test_zones_match_acpu_golden(steps):
+    """Two overlapping load zones and a fix zone over water and part of the
+    left wall, against acpu.c (u: pressure work next to the fixed water, gated
+    like the water tank's)."""
+    Z = np.load(GOLD_ZONES)
+    loads, fixes = zones_of(Z)
+    c = golden_case(Z, "zones")
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_materials([TAIT, TAIT])
+        ctx.set_zones(loads, fixes)
+        ctx.integrate(got, c.dt, 1, steps)
+    g = fields(got)
+    bad = {}
+    for f in ("x", "v", "rho", "p", "u", "dv", "du"):
+        ref = Z[f"zones_{f}_{steps}"]
+        tol = 5e-4 if f in ("u", "du") else TOL[f]
+        e = rel(g[f].reshape(ref.shape), ref)
+        if not e <= tol:
+            bad[f] = e
+    assert not bad, (steps, bad)
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_zone_known_answers(dim, scheme):
+    """Isolated particles, one RK3 step: the load zones' v = dt a, u = u0 + dt w
+    (overlapping zones adding; in 3D the z bounds decide), the fix zone's
+    x = x0 + (5/6) dt vel from rest."""
+    from armando_gb300._abi import FixZone, LoadZone
+
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16), scheme=scheme)
+    pts = np.array([[0.1, 0.2, 0.3], [1.1, 0.2, -0.4], [2.1, -0.9, 0.3]])[:, :dim]
+    c.params.dim = c.dim = dim
+    c.params.gravity[:] = (0.0, 0.0, 0.0)
+    for f in ("mass", "rho", "p", "u", "h", "itype", "dudt"):
+        setattr(c, f, getattr(c, f)[:3].copy())
+    c.itype[:] = 1
+    c.x = pts.ravel().astype(np.float32)
+    c.v = np.zeros(3 * dim, np.float32)
+    c.dvdt = np.zeros(3 * dim, np.float32)
+    c.u = np.full(3, 5.0, np.float32)
+    dt = 1e-3
+    a1, a2 = np.array([2.0, -1.0, 0.5]), np.array([0.25, 0.5, -4.0])
+    loads = [LoadZone.make((0.0, 0.0, -0.1), (1.5, 0.5, 0.5), a1, 300.0),
+             LoadZone.make((1.0, 0.0, -0.1), (1.5, 0.5, 0.5), a2, 20.0)]
+    vel = np.array([0.7, -0.3, 0.2])
+    fixes = [FixZone.make((2.0, -1.0, 0.0), (2.5, -0.5, 0.5), vel)]
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_zones(loads, fixes)
+        ctx.integrate(got, dt, 1, 1)
+    x0 = c.x.reshape(3, dim).astype(np.float64)
+    x, v = got.x.reshape(3, dim), got.v.reshape(3, dim)
+    acc = [a1[:dim], (a1 + a2)[:dim]]
+    w = [300.0, 320.0]
+    if dim == 3:
+        acc[1], w[1] = np.zeros(3), 0.0
+    for k in range(2):
+        np.testing.assert_allclose(v[k], dt * acc[k], rtol=1e-6, atol=1e-9)
+        np.testing.assert_allclose(x[k], x0[k] + 0.5 * dt * dt * acc[k], rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(got.u[k], 5.0 + dt * w[k], rtol=1e-6)
+    np.testing.assert_allclose(v[2], vel[:dim], rtol=1e-6)
+    np.testing.assert_allclose(x[2], x0[2] + dt * 5.0 / 6.0 * vel[:dim], rtol=1e-6, atol=1e-7)
+
+
+def test_zones_3d_channel_matches_the_oracle(O):
+    """A 3D block of water, device-variant physics, with a heated
+    accelerating load zone and a fix zone over its inflow end: 3 RK3 steps
+    against the FP64 oracle."""
+    from armando_gb300._abi import FixZone, LoadZone
+
+    c = cases.channel(n_x=14, n_yz=6, length=14 * 7.9e-4, width=6 * 7.9e-4, layers=2, jitter=0.01)
+    c.params.scheme = 2
+    c.params.periodic[:] = (0, 0, 0)
+    c.params.heat_external = 0
+    c.params.gravity[:] = (0.0, 0.0, -9.81)
+    L = 14 * 7.9e-4
+    loads = [LoadZone.make((0.4 * L, -1.0, -1.0), (0.8 * L, 1.0, 1.0), (30.0, 0.0, 5.0), 2.0e3)]
+    fixes = [FixZone.make((-1.0, -1.0, -1.0), (0.15 * L, 1.0, 1.0), (0.8, 0.0, 0.0))]
+    ref = O.State(c)
+    dv, du = O.gpuc_step(ref, 3, c.dt, loads=loads, fixes=fixes)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_zones(loads, fixes)
+        ctx.integrate(got, c.dt, 1, 3)
+    for f, a, b in (("x", got.x, ref.x), ("v", got.v, ref.v), ("rho", got.rho, ref.rho),
+                    ("p", got.p, ref.p), ("u", got.u, ref.u), ("dv", got.dvdt, dv)):
+        assert rel(a, b) <= TOL[f] * 2, (f, rel(a, b))
+
+
+def test_zone_refusals():
+    from armando_gb300._abi import FixZone, LoadZone
+
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
+    z = LoadZone.make((0.0, 0.0), (1.0, 1.0), (1.0, 0.0), 0.0)
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_zones([z] * 11, [])
+        assert e.value.status == ag._abi.ERR_INVALID_ARG
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_zones([], [FixZone.make((0.0, 0.0), (1.0, 1.0), (float("nan"), 0.0))])
+        assert e.value.status == ag._abi.ERR_INVALID_ARG
+        ctx.set_zones([], [])
+    p0 = c.params.copy()
+    p0.scheme = 0
+    with ag.Context(p0, c.n_fluid, c.n_wall) as ctx:
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.set_zones([z], [])
+        assert e.value.status == ag._abi.ERR_UNSUPPORTED

@@ -7,7 +7,7 @@ import pytest
 
 import armando_gb300 as ag
 from armando_gb300 import cases
-from armando_gb300._abi import Inlet
+from armando_gb300._abi import Inlet, Outlet
 from helpers import rel_err
 
 pytestmark = pytest.mark.gpu
@@ -38,8 +38,9 @@ def compare(O, c, n, inlets, outlets, box, steps, tol_scale=1.0):
     assert m == len(ref["mass"])
     assert np.array_equal(a["itype"][:m], ref["itype"])
     bad = {}
-    for f, g in (("x", a["x"][:2 * m]), ("v", a["v"][:2 * m]), ("rho", a["rho"][:m]),
-                 ("p", a["p"][:m]), ("dvdt", a["dvdt"][:2 * m])):
+    d = c.dim
+    for f, g in (("x", a["x"][:d * m]), ("v", a["v"][:d * m]), ("rho", a["rho"][:m]),
+                 ("p", a["p"][:m]), ("dvdt", a["dvdt"][:d * m])):
         e = rel_err(g, ref[f])
         if not e <= TOL[f] * tol_scale:
             bad[f] = e
@@ -71,11 +72,38 @@ def test_open_channel_over_100_steps(O):
     assert m == n - 10 + 11
 
 
-def test_device_variant_and_3d_box():
-    """Scheme 2 runs the same open channel; a 3D duct with a disk inlet emits."""
+def test_device_variant(O):
+    """Scheme 2 runs the same open channel; its wall push differs from scheme
+    1's and a second column leaves by step 80 (the oracle agrees)."""
     c, n, inl, outl, box = cases.gpuc_open_channel(scheme=2)
-    m, a = run_gpu(c, n, inl, outl, box, 100)
-    assert m == n - 10 + 11 and np.all(np.isfinite(a["x"][:2 * m]))
+    m = compare(O, c, n, inl, outl, box, 100, tol_scale=5.0)
+    assert m == n - 20 + 11
+
+
+def test_disk_inlet_3d(O):
+    """A 3D duct with a disk inlet across its start (normal +x) and an outlet
+    at its end: the first steps emit disks of the reference's lattice; counts,
+    order and fields against the oracle."""
+    c = cases.channel(n_x=10, n_yz=4, length=10 * 7.9e-4, width=4 * 7.9e-4, layers=2, jitter=0.01)
+    c.params.scheme = 2
+    c.params.periodic[:] = (0, 0, 0)
+    c.params.heat_external = 0
+    n = c.n
+    h = float(c.h[0])
+    I = Inlet.make((0.0, 0.0016, 0.0016), (1.0, 0.0, 0.0), 1.5 * h, 1, float(c.mass[0]), h,
+                   0.6 * h / 1.2 / c.dt, 10500.0, float(c.u[0]))
+    L = 10 * 7.9e-4
+    outl = [Outlet.make((L - 1.0e-4, 0.0016, 0.0016), (-1.0, 0.0, 0.0), 0.01)]
+    box = ((-0.01, -0.01, -0.01), (0.02, 0.02, 0.02))
+    padded = c.copy()
+    for f, w in (("x", 3), ("v", 3), ("mass", 1), ("rho", 1), ("p", 1), ("u", 1), ("h", 1),
+                 ("itype", 1), ("dvdt", 3), ("dudt", 1)):
+        a = getattr(c, f)
+        out = np.zeros(CAP * w, a.dtype)
+        out[:a.size] = a
+        setattr(padded, f, out)
+    m = compare(O, padded, n, [I], outl, box, 4)
+    assert m > n
 
 
 def test_refusals():
@@ -98,3 +126,20 @@ def test_refusals():
         with pytest.raises(ag.ArmandoError) as e:
             ctx.integrate_open(small, c.dt, 1, 100, n)
         assert e.value.status == ag._abi.ERR_INVALID_ARG
+
+
+def test_empty_system_refills(O):
+    """Every particle leaves in the first step; steps on no particles launch
+    nothing; the inlet refills the system in the third step."""
+    c, n, inl, _, _ = cases.gpuc_open_channel()
+    I = inl[0]
+    o = np.array(I.origin[:2])
+    box = (tuple(o - 0.06), tuple(o + 0.06 + [0.02, 0.0]))
+    fast = Inlet.make(tuple(I.origin), tuple(I.normal), I.radius, 1, I.mass, I.hsml,
+                      0.4 * I.hsml / 1.2 / c.dt, I.rho)
+    x = c.x.reshape(-1, 2)
+    inside = np.all((x[:n] >= box[0]) & (x[:n] <= box[1]), axis=1)
+    c.x[:2 * n] = np.where(np.repeat(inside, 2), c.x[:2 * n] + 1.0, c.x[:2 * n])
+    m, _ = run_gpu(c, n, [fast], [], box, 2)
+    assert m == 0
+    assert compare(O, c, n, [fast], [], box, 3) == 11

@@ -5,8 +5,8 @@ One step from identical FP32 inputs (an oracle history state): TOL_STEP =
 1e-5 normwise relative on every output and on h. Continuity density carries
 drho/dt from one iteration to the next inside the context, so it is checked
 over 10 iterations against the oracle, within 20x the oracle's own change
-when its FP32 state (positions, density, h) moves by one ulp (or 1e-5): the
-library carries density and h between iterations in FP32."""
+when its FP32 state (positions, velocities, u, density, h) moves by one ulp
+(or 1e-5): the library carries that state between iterations in FP32."""
 import numpy as np
 import pytest
 
@@ -101,8 +101,11 @@ def test_normalised_density_with_lanes(O):
 def test_continuity_tracks_the_oracle(O, make):
     c = make()
     steps = 10
-    # The twin moves every FP32 state the step carries by one ulp: positions
-    # and, with continuity density and h evolution, the density and h too.
+    # The twin moves every FP32 state the step carries by one ulp: positions,
+    # velocities, internal energy and, with continuity density and h
+    # evolution, the density and h too. u matters in the heated channel: art.
+    # heat conducts on u_i - u_j ~ 150 J/kg of u ~ 9e4 J/kg, where one FP32
+    # ulp (0.008) is 5e-5 of the difference.
     rng = np.random.default_rng(97)
     c2 = c.copy()
     fl = c.itype > 0
@@ -112,6 +115,8 @@ def test_continuity_tracks_the_oracle(O, make):
         return np.where(mask, np.nextafter(a, bump), a).astype(np.float32)
 
     c2.x = ulp(c.x, np.repeat(fl, c.dim))
+    c2.v = ulp(c.v, np.repeat(fl, c.dim))
+    c2.u = ulp(c.u, fl)
     c2.rho = ulp(c.rho, fl)
     c2.h = ulp(c.h, fl)
     ref, pert = O.State(c), O.State(c2)

@@ -104,3 +104,92 @@ def test_device_variant_gates_pairs_by_material(O, G):
     assert inner.sum() > 20 and near.sum() > 10
     assert not np.allclose(a.rho[near], b.rho[near], rtol=0, atol=1e-9)
     np.testing.assert_allclose(a.rho[inner], b.rho[inner], rtol=2e-6)
+
+
+GOLD_ZONES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "acpu_zones.npz")
+
+
+def golden_zones(Z):
+    """The load and fix zones of the golden run as C-ABI structs (2D: the z
+    bounds do not enter)."""
+    from armando_gb300._abi import FixZone, LoadZone
+
+    loads = [LoadZone.make(r[0:2], r[2:4], (r[4], r[5], 0.0), r[6]) for r in Z["zones_load"]]
+    fixes = [FixZone.make(r[0:2], r[2:4], (r[4], r[5], 0.0)) for r in Z["zones_fix"]]
+    return loads, fixes
+
+
+@pytest.mark.parametrize("steps", [1, 5])
+def test_load_and_fix_zones_match_acpu(O, steps):
+    """Two overlapping load zones (acceleration and heating) and a fix zone
+    over the left of the water and part of the left wall, which then moves
+    (acpu.c resets wall velocities before the fix zones)."""
+    Z = np.load(GOLD_ZONES)
+    loads, fixes = golden_zones(Z)
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
+    c.x, c.v, c.mass, c.rho = Z["zones_x0"], Z["zones_v0"], Z["zones_m"], Z["zones_rho0"]
+    c.h, c.itype = Z["zones_h"], Z["zones_itype"]
+    st = O.State(c)
+    dv, du = O.gpuc_step(st, steps, float(Z["zones_dt"]), materials=[MATS["tait"]] * 2,
+                         loads=loads, fixes=fixes)
+    for f, got in (("x", st.x.reshape(-1, 2)), ("v", st.v.reshape(-1, 2)), ("rho", st.rho),
+                   ("p", st.p), ("u", st.u), ("dv", dv.reshape(-1, 2)), ("du", du)):
+        # u starts at 0: next to the fixed water its pressure work carries p's
+        # quantization, as in the water tank
+        tol = TOL["p"] if f == "u" else TOL[f]
+        e = rel(got, Z[f"zones_{f}_{steps}"])
+        assert e <= tol, (f, steps, e)
+    moved = np.abs(st.x.reshape(-1, 2) - c.x.reshape(-1, 2)).max(1) > 1e-6
+    assert (moved & (c.itype <= 0)).sum() > 10
+
+
+def isolated(dim, scheme):
+    """Three particles far beyond each other's reach (no pair terms), fluid,
+    at rest, no gravity."""
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16), scheme=scheme)
+    pts = np.array([[0.1, 0.2, 0.3], [1.1, 0.2, -0.4], [2.1, -0.9, 0.3]])[:, :dim]
+    c.params.dim = c.dim = dim
+    c.params.gravity[:] = (0.0, 0.0, 0.0)
+    keep = np.arange(3)
+    for f in ("mass", "rho", "p", "u", "h", "itype", "dudt"):
+        setattr(c, f, getattr(c, f)[keep].copy())
+    c.itype[:] = 1
+    c.x = pts.ravel().astype(np.float32)
+    c.v = np.zeros(3 * dim, np.float32)
+    c.dvdt = np.zeros(3 * dim, np.float32)
+    c.u = np.full(3, 5.0, np.float32)
+    return c
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_zone_known_answers(O, dim, scheme):
+    """Isolated particles, one RK3 step (exact for constant rates): inside a
+    load zone v = dt a, x = x0 + dt^2 a / 2, u = u0 + dt w, overlapping zones
+    adding; inside a fix zone v = vel after every stage, so x = x0 + (5/6) dt
+    vel from rest; in 3D the z bounds decide (particle 2 lies below the
+    load zones' z range); in 2D z does not enter."""
+    from armando_gb300._abi import FixZone, LoadZone
+
+    c = isolated(dim, scheme)
+    dt = 1e-3
+    a1, a2 = np.array([2.0, -1.0, 0.5]), np.array([0.25, 0.5, -4.0])
+    loads = [LoadZone.make((0.0, 0.0, -0.1), (1.5, 0.5, 0.5), a1, 300.0),
+             LoadZone.make((1.0, 0.0, -0.1), (1.5, 0.5, 0.5), a2, 20.0)]
+    vel = np.array([0.7, -0.3, 0.2])
+    fixes = [FixZone.make((2.0, -1.0, 0.0), (2.5, -0.5, 0.5), vel)]
+    st = O.State(c)
+    O.gpuc_step(st, 1, dt, loads=loads, fixes=fixes)
+    x0 = c.x.reshape(3, dim).astype(np.float64)
+    x, v = st.x.reshape(3, dim), st.v.reshape(3, dim)
+    acc = [a1[:dim], (a1 + a2)[:dim]]
+    w = [300.0, 320.0]
+    if dim == 3:  # particle 2 (z = -0.4) below the z range of the load zones
+        acc[1], w[1] = np.zeros(3), 0.0
+    for k in range(2):
+        np.testing.assert_allclose(v[k], dt * acc[k], rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(x[k], x0[k] + 0.5 * dt * dt * acc[k], rtol=1e-12, atol=1e-15)
+        np.testing.assert_allclose(st.u[k], 5.0 + dt * w[k], rtol=1e-12)
+    np.testing.assert_allclose(v[2], vel[:dim], rtol=1e-7)
+    np.testing.assert_allclose(x[2], x0[2] + dt * 5.0 / 6.0 * vel[:dim], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(st.u[2], 5.0, rtol=1e-12)

@@ -82,3 +82,21 @@ def test_open_channel_flow_counts(O):
     out = O.gpuc_open(c, 100, c.dt, 4000, n=n, inlets=inl, outlets=outl, box=box)
     assert len(out["mass"]) == n - 10 + 11
     assert np.all(np.isfinite(out["x"])) and np.all(np.isfinite(out["rho"]))
+
+
+def test_empty_system_refills(O):
+    """A box that holds none of the particles empties the system in the first
+    step; steps on nothing do nothing until the inlet (inside the box) emits."""
+    c, n, inl, _, _ = still_channel()
+    I = inl[0]
+    o = np.array(I.origin[:2])
+    box = (tuple(o - 0.06), tuple(o + 0.06 + [0.02, 0.0]))
+    fast = Inlet.make(tuple(I.origin), tuple(I.normal), I.radius, 1, I.mass, I.hsml,
+                      0.4 * I.hsml / 1.2 / c.dt, I.rho)
+    x = c.x.reshape(-1, 2)
+    inside = np.all((x[:n] >= box[0]) & (x[:n] <= box[1]), axis=1)
+    c.x[:2 * n] = np.where(np.repeat(inside, 2), c.x[:2 * n] + 1.0, c.x[:2 * n])  # move them out
+    out = O.gpuc_open(c, 2, c.dt, 4000, n=n, inlets=[fast], outlets=[], box=box)
+    assert len(out["mass"]) == 0
+    out = O.gpuc_open(c, 3, c.dt, 4000, n=n, inlets=[fast], outlets=[], box=box)
+    assert len(out["mass"]) == 11 and np.all(np.isfinite(out["x"]))
