@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(BS)
         if (dr < __fmul_rn(0.01f, hi)) return;  // dr := 100 h: W = dW/dr = 0 (acpu.c:379)
         float w, dwdr;
         gpuc_kernel<DIM>(dr, hi, ih, kal, w, dwdr);
-        const float mk = (DIM == 2) ? __ldg(&S.x0[k].z) : __ldg(&S.v0[k].w);
+        const float mk = mass_of<DIM>(xk, vk);  // the working copies carry m and h
         const float dvr = fmaf(dz, vi.z - vk.z, fmaf(dy, vi.y - vk.y, __fmul_rn(dx, vi.x - vk.x)));
         const float rhoi = si.x, rhok = sk.x;
         const float ir = __fdiv_rn(1.0f, dr);
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(BS)
                 push = __fmul_rn(__fdiv_rn(mk, mi + mk),
                                  __fdiv_rn(__fmul_rn(__fmul_rn(0.02f, __fdiv_rn(w, w0)), __fmul_rn(si.w, sk.w)), dr));
             else
-                push = __fmul_rn(__fdiv_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, w), mk), rhok), __ldg(&S.x0[k].w)),
+                push = __fmul_rn(__fdiv_rn(__fdiv_rn(__fmul_rn(__fmul_rn(0.5f, w), mk), rhok), xk.w),
                                  __fmul_rn(sk.w, sk.w));
         }
         const float tot = __fmul_rn(fmaf(f, dwdr, push), ir);
