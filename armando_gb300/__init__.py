@@ -47,6 +47,15 @@ def _check_host(a, n, dtype, name):
         raise ValueError(f"{name} has {a.size} elements, expected {n}")
 
 
+def _sized(a, n, dtype, name):
+    """a as a C-contiguous host array of dtype with exactly n elements (the C
+    side reads n of them)."""
+    a = np.ascontiguousarray(a, dtype)
+    if a.size != n:
+        raise ValueError(f"{name} has {a.size} elements, expected {n}")
+    return a
+
+
 class Context:
     """One particle system on the current CUDA device (``armando_create``)."""
 
@@ -144,8 +153,10 @@ class Context:
         """Cotangents of the initial state and of the parameters for cotangents of the
         final state of the last forward_checkpointed (host memory kind: numpy)."""
         n, nd = self.n, self.n * self.dim
-        f32 = lambda a: None if a is None else np.ascontiguousarray(a, np.float32)  # noqa: E731
-        ins = [f32(a) for a in (x_bar, v_bar, u_bar, p_bar, dvdt_bar, dudt_bar)]
+        ins = [None if a is None else _sized(a, size, np.float32, name)
+               for a, size, name in ((x_bar, nd, "x_bar"), (v_bar, nd, "v_bar"), (u_bar, n, "u_bar"),
+                                     (p_bar, n, "p_bar"), (dvdt_bar, nd, "dvdt_bar"),
+                                     (dudt_bar, n, "dudt_bar"))]
         outs = {"x": np.zeros(nd, np.float32), "v": np.zeros(nd, np.float32),
                 "u": np.zeros(n, np.float32), "dvdt": np.zeros(nd, np.float32),
                 "dudt": np.zeros(n, np.float32)}
@@ -161,7 +172,10 @@ class Context:
     def cell_ids(self, x, h):
         """Cell id per particle (caller order) under the link_list grid of x."""
         out = np.zeros(self.n, np.int32) if self.mem == MEM_HOST else None
-        if self.mem != MEM_HOST:
+        if self.mem == MEM_HOST:
+            x = _sized(x, self.n * self.dim, np.float32, "x")
+            h = _sized(h, self.n, np.float32, "h")
+        else:
             import torch
             out = torch.zeros(self.n, dtype=torch.int32, device="cuda")
         self._check(self._lib.armando_cell_ids(self._h, _ptr(x), _ptr(h), _ptr(out)))
@@ -169,8 +183,8 @@ class Context:
 
     def neighbours(self, x, h):
         """CSR (offs[n+1], nbr) of neighbour sets j != i, ascending (host arrays)."""
-        x = np.ascontiguousarray(x, np.float32)
-        h = np.ascontiguousarray(h, np.float32)
+        x = _sized(x, self.n * self.dim, np.float32, "x")
+        h = _sized(h, self.n, np.float32, "h")
         offs = np.zeros(self.n + 1, np.int64)
         total = C.c_int64(0)
         st = self._lib.armando_neighbours(self._h, _ptr(x), _ptr(h), _ptr(offs), None, 0,
@@ -314,8 +328,8 @@ class Batch(Context):
         lib = load_library()
         k = len(params_list)
         arr = (Params * k)(*[p.copy() for p in params_list])
-        nf = np.ascontiguousarray(n_fluid, np.int64)
-        nw = np.ascontiguousarray(n_wall, np.int64)
+        nf = _sized(n_fluid, k, np.int64, "n_fluid")
+        nw = _sized(n_wall, k, np.int64, "n_wall")
         dim = int(params_list[0].dim)
         h = C.c_void_p()
         st = lib.armando_batch_create(C.byref(h), k, arr, dim, nf.ctypes.data_as(C.c_void_p),
@@ -378,7 +392,7 @@ def write_deck(directory: str, dim: int, n_real: int, arrays) -> None:
     n = int(np.asarray(a["mass"]).size)
     if not 0 <= n_real <= n:
         raise ValueError("n_real out of range")
-    arrs = [np.ascontiguousarray(a[f], np.int32 if f == "itype" else np.float32)
+    arrs = [_sized(a[f], n * (dim if f in ("x", "v") else 1), np.int32 if f == "itype" else np.float32, f)
             for f in DECK_FIELDS]
     _io_check(lib, lib.armando_deck_write(str(directory).encode(), dim, n_real, n - n_real,
                                           *[_ptr(q) for q in arrs]))
@@ -389,6 +403,6 @@ def write_vtk(path: str, dim: int, arrays) -> None:
     lib = load_library()
     a = arrays.arrays() if hasattr(arrays, "arrays") else arrays
     n = int(np.asarray(a["mass"]).size)
-    arrs = [np.ascontiguousarray(a[f], np.int32 if f == "itype" else np.float32)
+    arrs = [_sized(a[f], n * (dim if f in ("x", "v") else 1), np.int32 if f == "itype" else np.float32, f)
             for f in ("x", "v", "rho", "p", "u", "itype")]
     _io_check(lib, lib.armando_write_vtk(str(path).encode(), dim, n, *[_ptr(q) for q in arrs]))

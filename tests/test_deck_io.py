@@ -172,3 +172,15 @@ def test_vtk_snapshot(tmp_path):
     with pytest.raises(ag.ArmandoError) as e:
         ag.write_vtk(tmp_path / "no" / "such" / "dir.vtk", 2, c)
     assert e.value.status == ag._abi.ERR_IO
+
+
+def test_short_arrays_are_refused_before_the_library_reads_them(tmp_path):
+    """The writers read n*dim positions and velocities and n of the rest:
+    shorter arrays raise ValueError in Python instead of reaching C."""
+    c = cases.dam_break(dx=0.1)
+    a = {k: v.copy() for k, v in c.arrays().items()}
+    a["x"] = a["x"][:-1]
+    with pytest.raises(ValueError):
+        ag.write_deck(str(tmp_path), c.dim, c.n_fluid, a)
+    with pytest.raises(ValueError):
+        ag.write_vtk(str(tmp_path / "s.vtk"), c.dim, a)
