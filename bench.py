@@ -191,6 +191,68 @@ def traffic_per_particle(kernel, config):
     return d.get(config, {}).get(kernel)
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event reasons read through NVML (the driver's
+    libnvidia-ml, read-only queries) every 2 ms during the timed region, so a
+    region of tens of milliseconds still gets dozens of samples."""
+
+    # nvmlClocksEventReasons bits
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, gpu_index):
+        import ctypes as C
+
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(gpu_index), C.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint(0)
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, C.c_int(1), C.byref(mx))  # NVML_CLOCK_SM
+        self.max_mhz = float(mx.value) or None
+        self.sm, self.reasons = [], set()
+        self.stop = threading.Event()
+
+    def _poll(self):
+        C = self.C
+        clk, rs = C.c_uint(0), C.c_ulonglong(0)
+        while not self.stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.h, C.c_int(1), C.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if self.reasons_fn(self.h, C.byref(rs)) == 0:
+                for bit, name in self.BITS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            self.stop.wait(0.002)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._poll, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self.stop.set()
+        self.t.join(timeout=5)
+
+    def summary(self):
+        return {"sm_mhz": float(np.median(self.sm)) if self.sm else None,
+                "sm_max_mhz": self.max_mhz, "reasons": sorted(self.reasons),
+                "samples": len(self.sm), "source": "nvml, 2 ms"}
+
+
+def clock_sampler(gpu_index):
+    """NVML sampler where the driver library loads, else nvidia-smi's."""
+    try:
+        return NvmlClockSampler(gpu_index)
+    except (OSError, AttributeError):
+        return ClockSampler(gpu_index)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -601,7 +663,7 @@ def run_ours(args, rank, world, local_rank):
     launches0 = ctx.stats().gpu_launches
     sorts0 = ctx.stats().sorts_done
     barrier()
-    with ClockSampler(local_rank) as clk:
+    with clock_sampler(local_rank) as clk:
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
