@@ -24,17 +24,20 @@ def _lib():
     ag.load_library()
 
 
-def run_gpu(c, n, inlets, outlets, box, steps):
+def run_gpu(c, n, inlets, outlets, box, steps, loads=(), fixes=()):
     a = {k: v.copy() for k, v in c.arrays().items()}
     with ag.Context(c.params, CAP, 0) as ctx:
         ctx.set_open_boundaries(inlets, outlets, box)
+        if loads or fixes:
+            ctx.set_zones(list(loads), list(fixes))
         m = ctx.integrate_open(a, c.dt, 1, steps, n)
     return m, a
 
 
-def compare(O, c, n, inlets, outlets, box, steps, tol_scale=1.0):
-    m, a = run_gpu(c, n, inlets, outlets, box, steps)
-    ref = O.gpuc_open(c, steps, c.dt, CAP, n=n, inlets=inlets, outlets=outlets, box=box)
+def compare(O, c, n, inlets, outlets, box, steps, tol_scale=1.0, loads=(), fixes=()):
+    m, a = run_gpu(c, n, inlets, outlets, box, steps, loads, fixes)
+    ref = O.gpuc_open(c, steps, c.dt, CAP, n=n, inlets=inlets, outlets=outlets, box=box,
+                      loads=loads, fixes=fixes)
     assert m == len(ref["mass"])
     assert np.array_equal(a["itype"][:m], ref["itype"])
     bad = {}
@@ -143,3 +146,18 @@ def test_empty_system_refills(O):
     m, _ = run_gpu(c, n, [fast], [], box, 2)
     assert m == 0
     assert compare(O, c, n, [fast], [], box, 3) == 11
+
+
+def test_open_channel_with_zones(O):
+    """The open channel driven like the reference's channel runs: a fix zone
+    over the water of the inflow strip (initChannel's hFix) and a heated,
+    accelerated band downstream, 20 steps against the oracle. No particle
+    comes near a zone's edge in that time: a particle on an edge (a wall
+    column at x = 0.04, say) enters or stays out on one ulp of its position."""
+    from armando_gb300._abi import FixZone, LoadZone
+
+    c, n, inl, outl, box = cases.gpuc_open_channel()
+    fixes = [FixZone.make((-1.0, 0.0), (0.04, 0.1), (1.2, 0.0))]
+    loads = [LoadZone.make((0.15, -1.0), (0.22, 1.0), (2.0, 0.0), 500.0)]
+    m = compare(O, c, n, inl, outl, box, 20, tol_scale=5.0, loads=loads, fixes=fixes)
+    assert m == n
