@@ -408,10 +408,11 @@ bool step_options(const armando_params& p) {
 }
 
 // Whether every iteration must sort (no sort skin): mirror ghosts change every
-// iteration, the GPU-C schemes keep one list per step, and an evolving h
-// outgrows cells sized for the h of the last sort.
+// iteration and an evolving h outgrows cells sized for the h of the last sort.
+// (The GPU-C schemes sort lazily like the CERN step: their stage test against
+// the step's start positions needs the same cells; open runs sort every step.)
 bool sorts_every_step(const armando_params& p) {
-    return p.wall_model == 3 || p.scheme != 0 || p.sle != 0;
+    return p.wall_model == 3 || p.sle != 0;
 }
 
 template <int DIM>
@@ -481,6 +482,9 @@ int launch_step(armando_ctx* ctx, const StepArgs& S) {
 // from the flag, so iterations that do not sort launch none of them. The body
 // is captured from a second stream into the node's child graph.
 template <int DIM>
+int launch_gpuc_passes(armando_ctx* ctx, const StepArgs& S, const int* rs);
+
+template <int DIM>
 armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphExec_t* out,
                                 int* launches) {
     cudaError_t e = cudaSuccess;
@@ -531,7 +535,8 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
     e = cudaStreamEndCapture(ctx->stream2, &body_out);
     body_cap = false;
     if (e != cudaSuccess) return fail_graph(e, "cudaStreamEndCapture(body)");
-    L += launch_passes<DIM>(ctx, S, resort_flags(ctx));
+    L += ctx->prm.scheme != 0 ? launch_gpuc_passes<DIM>(ctx, S, resort_flags(ctx))
+                              : launch_passes<DIM>(ctx, S, resort_flags(ctx));
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_graph(e, "kernel launch during capture");
     cudaGraph_t g_out = nullptr;
     e = cudaStreamEndCapture(ctx->stream, &g_out);
@@ -551,15 +556,15 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
 // order state, three stages ping-ponging between the working copies, the
 // result back to A.
 template <int DIM>
-int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S) {
+int launch_gpuc_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n_work;
     const int nm = ctx->materials.empty() ? ARMANDO_MAX_MATERIALS : (int)ctx->materials.size();
-    int L = launch_grid_and_sort<DIM>(ctx, nullptr, st);
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
+    ctx->gs.xsort = rs ? ctx->xsort_buf : nullptr;
     k_gpuc_gather<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->gs, ctx->d_mat, nm,
-                                                           ctx->flags, n);
+                                                           ctx->flags, n, rs);
     static const float alphas[3] = {1.0f, 0.25f, 2.0f / 3.0f};
     for (int q = 0; q < 3; ++q) {
         const int cur = q & 1;
@@ -576,13 +581,24 @@ int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S) {
                     ctx->flags, alphas[q], S.dt, n);
         });
     }
-    k_gpuc_scatter<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->gs, 1, ctx->A, n);
-    return L + 5;
+    k_gpuc_scatter<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->gs, 1, ctx->A, n, ctx->grid,
+                                                            ctx->flags);
+    int L = 5;
+    if (rs) L += launch_resort_advance(ctx);
+    return L;
+}
+
+// rs: the lazy-sorting flags (nullptr: the step sorts).
+template <int DIM>
+int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S, const int* rs) {
+    const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream);
+    return L + launch_gpuc_passes<DIM>(ctx, S, rs);
 }
 
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
+    const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
     if (ctx->prm.scheme != 0)
-        return ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S) : launch_gpuc_step<3>(ctx, S);
+        return ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S, rs) : launch_gpuc_step<3>(ctx, S, rs);
     return ctx->dim == 2 ? launch_step<2>(ctx, S) : launch_step<3>(ctx, S);
 }
 
@@ -1969,7 +1985,7 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
     if (params->wall_model == 3 && ctx->cap < ctx->n + ctx->nf)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts (wall_model 3) need a context created with wall_model 3");
     if (sorts_every_step(*params) && ctx->tune.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts, the GPU-C schemes and h evolution sort every iteration: set a tuning with skin 0 first");
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and h evolution sort every iteration: set a tuning with skin 0 first");
     ctx->prm = *params;
     ctx->dp = make_dev_params(*params, ctx->tune.reach);
     ctx->dp.n_real = (int)ctx->n;
@@ -2000,7 +2016,7 @@ armando_status check_tuning(armando_ctx* ctx, const armando_tuning& t) {
     if (ctx->n_inst > 1 && t.skin != 0)
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "batches sort every iteration (skin 0)");
     if (sorts_every_step(ctx->prm) && t.skin != 0)
-        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts, the GPU-C schemes and h evolution sort every iteration (skin 0)");
+        return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "mirror ghosts and h evolution sort every iteration (skin 0)");
     return ARMANDO_OK;
 }
 
@@ -2268,7 +2284,8 @@ armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, flo
         ctx->n_work = n;
         ctx->num_tiles = blocks_for(n, kSortTile);
         const StepArgs S = make_args(ctx, dt, its0 + k);
-        const int L = ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S) : launch_gpuc_step<3>(ctx, S);
+        const int L = ctx->dim == 2 ? launch_gpuc_step<2>(ctx, S, nullptr)
+                                    : launch_gpuc_step<3>(ctx, S, nullptr);  // the count changes: sort
         ctx->launches += L;
         ctx->steps_done += 1;
         ctx->sorts_host += 1;

@@ -63,6 +63,7 @@ struct GpucState {
     float4* rates;  // {dv/dt, de/dt} of the last stage
     int* itype;
     int* id;
+    float4* xsort;  // lazy sorting: positions at the last sort (nullptr: every step sorts)
 };
 
 // The EOS of one particle after its update (acpu.c:932-962 with the property
@@ -139,14 +140,19 @@ __device__ __forceinline__ int gpuc_material(int itype, int n_mat, unsigned* fla
 }
 
 // Cell order of the step: start state, first working copy, sound speeds.
+// A is in the cell order of the last sort, so a step that does not sort
+// (lazy sorting) takes it slot for slot.
 template <int DIM>
 __global__ void k_gpuc_gather(StateA A, const int* __restrict__ perm, GpucState S,
                               const DevMaterial* __restrict__ mat, int n_mat,
-                              unsigned* __restrict__ flags, int n) {
+                              unsigned* __restrict__ flags, int n,
+                              const int* __restrict__ resort = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
-    const int j = perm[s];
+    const bool sorted = !sort_skipped(resort);
+    const int j = sorted ? perm[s] : s;
     const float4 xh = A.xh[j], vm = A.vm[j];
+    if (sorted && S.xsort) S.xsort[s] = xh;
     const int it = A.itype[j];
     float rho = A.rho[j];
     const float u = A.u[j], p = A.p[j];
@@ -395,12 +401,25 @@ __global__ void __launch_bounds__(BS)
 }
 
 // The step's result back to A (cell order of this step, like the force pass).
+// Lazy sorting: a particle farther than half the skin from where it was binned
+// makes the next step sort (the cells of the last sort hold every pair within
+// 2 max(h) of the step's start positions only while none is).
 template <int DIM>
-__global__ void k_gpuc_scatter(GpucState S, int cur, StateA A, int n) {
+__global__ void k_gpuc_scatter(GpucState S, int cur, StateA A, int n,
+                               const DevGrid* __restrict__ gp = nullptr,
+                               unsigned* __restrict__ flags = nullptr) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const float4 sv = (cur ? S.sw[1] : S.sw[0])[s];
-    A.xh[s] = (cur ? S.xw[1] : S.xw[0])[s];
+    const float4 xn = (cur ? S.xw[1] : S.xw[0])[s];
+    if (S.xsort && gp && flags) {
+        const float h2 = gp->half_skin2;
+        const float4 xb = S.xsort[s];
+        const float e0 = xn.x - xb.x, e1 = xn.y - xb.y, e2 = (DIM == 3) ? xn.z - xb.z : 0.f;
+        if (h2 > 0.f && e0 * e0 + e1 * e1 + e2 * e2 > h2 && *(volatile unsigned*)(flags + 2) == 0u)
+            atomicExch(flags + 2, 1u);
+    }
+    A.xh[s] = xn;
     A.vm[s] = (cur ? S.vw[1] : S.vw[0])[s];
     A.rho[s] = sv.x;
     A.u[s] = sv.y;

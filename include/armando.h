@@ -116,8 +116,11 @@ typedef struct armando_params {
                                  corrections instead of art_visc/art_heat, h_i
                                  kernels, gravity on itype > 0; pa_sph, visc,
                                  visc_artificial, heat_*, pmin and wall_model do not
-                                 apply (wall_model must be 0). No periodic axis, sort
-                                 skin, batch or reverse mode.                        */
+                                 apply (wall_model must be 0). No periodic axis,
+                                 batch or reverse mode. A sort skin keeps the cells
+                                 of the last sort as for scheme 0 (the candidate
+                                 test against the step's start positions is exact
+                                 in them); armando_integrate_open sorts every step. */
     /* Options of the CERN scheme's single_step (zero: the summation-density step
        above; CERNsource/single_step.f:106-116, 214-228):                         */
     int32_t density_form;     /* 0 summation (sum_density, density.f:1-62; the

@@ -129,8 +129,8 @@ def test_batch_rejects_single_only_calls():
     insts = _instances_2d()[:2]
     with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
                   [c.n_wall for c in insts]) as b:
-        with pytest.raises(ag.ArmandoError) as e:
-            b.cell_ids(insts[0].x, insts[0].h)
+        with pytest.raises(ag.ArmandoError) as e:  # packed arrays of the batch's size
+            b.cell_ids(np.zeros(b.n * b.dim, np.float32), np.ones(b.n, np.float32))
         assert e.value.status == ag._abi.ERR_UNSUPPORTED
 
 

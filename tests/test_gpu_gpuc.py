@@ -110,7 +110,7 @@ def test_published_dam_break_matches_the_oracle(O, scheme):
 
 
 @pytest.mark.parametrize("tuning", [(2, 1, 256, 0), (3, 1, 128, 0), (1, 2, 128, 0), (1, 4, 256, 0),
-                                    (2, 4, 128, 0)])
+                                    (2, 4, 128, 0), (2, 1, 128, 20), (1, 2, 256, 40)])
 def test_tunings(O, G, tuning):
     """Cell reach, lanes per particle (their sums in another order) and CTA
     size against acpu.c."""
@@ -152,9 +152,6 @@ def test_itype_outside_the_table_is_an_error():
 def test_refusals():
     c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16))
     with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
-        with pytest.raises(ag.ArmandoError) as e:
-            ctx.set_tuning(1, 1, 128, 20)
-        assert e.value.status == ag._abi.ERR_UNSUPPORTED
         with pytest.raises(ag.ArmandoError) as e:
             ctx.forward_checkpointed(c.copy(), c.dt, 1, 4, 2)
         assert e.value.status == ag._abi.ERR_UNSUPPORTED
@@ -293,3 +290,35 @@ def test_zone_refusals():
         with pytest.raises(ag.ArmandoError) as e:
             ctx.set_zones([z], [])
         assert e.value.status == ag._abi.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_lazy_sorting_matches_sorting_every_step(scheme):
+    """A sort skin: the published 6,462-particle dam break over 40 steps sorts
+    on a few of them and agrees with the every-step run to rounding: the
+    neighbour lists are the same; only the summation order follows the older
+    cells. Gate: 20x the every-step run's own change when its positions move
+    by one ulp (u and de/dt are pure pressure work from u = 0 and carry p's
+    quantization)."""
+    c = cases.gpuc_dam_break(1, scheme=scheme)
+    rng = np.random.default_rng(70 + scheme)
+    v = c.v.reshape(-1, 2)
+    v[c.itype > 0] = rng.normal(0.0, 0.05, size=(c.n_fluid, 2))
+    c.v = v.ravel().astype(np.float32)
+    every, lazy, twin = c.copy(), c.copy(), c.copy()
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    twin.x = np.nextafter(c.x, bump).astype(np.float32)
+    for run in (every, twin):
+        with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+            ctx.set_tuning(2, 1, 128, 0)
+            ctx.integrate(run, c.dt, 1, 40)
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(2, 1, 128, 20)
+        s0 = ctx.stats().sorts_done
+        ctx.integrate(lazy, c.dt, 1, 40)
+        sorts = ctx.stats().sorts_done - s0
+    assert 1 <= sorts < 40
+    for f in ("x", "v", "rho", "p", "u", "dvdt", "dudt"):
+        cond = rel(getattr(twin, f), getattr(every, f))
+        err = rel(getattr(lazy, f), getattr(every, f))
+        assert err <= max(20.0 * cond, 1e-6), (f, err, cond)
