@@ -392,6 +392,50 @@ def gpuc_dam_break(scale: int = 1, fluid=(100, 50), tank=(269, 80), dr1: float =
                 dt=4.0e-4 / scale, steps=10000 * scale, meta=dict(dx=dr, scale=scale))
 
 
+# Mercury for the pressure-wave workload: rho0 13,540 kg/m^3, c0 1,490 m/s and
+# Grueneisen gamma 1.96 (the reference's mercury material, FORTRANsource/sph.f90:
+# 158-163), as the GPU-C polynomial EOS {rho0, a1, a2, a3, b0, b1, t1, t2} with
+# a1 = t1 = rho0 c0^2, b0 = gamma.
+MERCURY_RHO0, MERCURY_C0, MERCURY_GAMMA = 13540.0, 1490.0, 1.96
+
+
+def mercury_poly():
+    """The polynomial-EOS material of the pressure-wave workload."""
+    from ._abi import Material
+
+    a1 = MERCURY_RHO0 * MERCURY_C0 ** 2
+    return Material.make(2, [MERCURY_RHO0, a1, 0.0, 0.0, MERCURY_GAMMA, 0.0, a1, 0.0])
+
+
+def gpuc_pressure_wave(n_side: int = 401, size: float = 0.1, radius: float = 4.0e-3,
+                       e0: float = 1400.0, t_end: float = 1.0e-4, steps: int = None,
+                       scheme: int = 1) -> Case:
+    """Stand-in for the published pressure-wave workload of the GPU-C code
+    (ArmandoOnGPU.pdf section 6.2, Tab.3): a square section of a mercury tank,
+    `size` wide, free on every side (no walls), on an n_side x n_side lattice
+    (401 / 501 / 601 give the published 160,801 / 251,001 / 361,201
+    particles), with an instantaneous energy deposit at its centre, Gaussian
+    around the axis: u = e0 exp(-(r / radius)^2). Polynomial EOS of mercury
+    (`mercury_poly`, itype 1), h = 1.2 dr, m = rho0 dr^2, no gravity; `steps`
+    (default 2 n_side, the published 800 / 1,000 / 1,200) cover t_end = 0.1 ms.
+    The deposit's amplitude is not published: e0 = 1,400 J/kg is a 10 K rise
+    (cp 140 J/(kg K))."""
+    dr = size / (n_side - 1)
+    i, j = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    x = np.stack([i.ravel() * dr, j.ravel() * dr], 1) - 0.5 * size
+    n = len(x)
+    r2 = (x * x).sum(1)
+    u = e0 * np.exp(-r2 / (radius * radius))
+    steps = 2 * (n_side - 1) if steps is None else steps
+    P = Params.default(dim=2, rho0=MERCURY_RHO0, c0=MERCURY_C0, gravity=(0.0, 0.0, 0.0))
+    P.scheme = scheme
+    return Case(f"gpuc_pressure_wave_{n_side}", P, 2, _f32(x.ravel()), _f32(np.zeros(2 * n)),
+                _f32(np.full(n, MERCURY_RHO0 * dr * dr)), _f32(np.full(n, MERCURY_RHO0)),
+                _f32(np.zeros(n)), _f32(u), _f32(np.full(n, 1.2 * dr)),
+                np.ones(n, np.int32), dt=t_end / steps, steps=steps,
+                meta=dict(dx=dr, n_side=n_side))
+
+
 def gpuc_open_channel(length: float = 0.3, height: float = 0.1, dr: float = 0.01,
                       speed: float = 1.0, rho0: float = 1000.0, c0: float = 20.0,
                       capacity: int = 2000, scheme: int = 1):

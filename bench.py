@@ -93,8 +93,9 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 3D channel and batched-sweep workloads")
     ap.add_argument("--extra-steps", type=int, default=20)
-    ap.add_argument("--gpuc-cases", default="1,2,3",
-                    help="with --only gpuc: which published dam-break cases (1-3) to time")
+    ap.add_argument("--gpuc-cases", default="1,2,3,w1,w2,w3",
+                    help="with --only gpuc: which published cases to time (dam break 1-3, "
+                         "pressure wave w1-w3)")
     ap.add_argument("--sweep-instances", type=int, default=512)
     ap.add_argument("--plain-steps", type=int, default=10)
     return ap.parse_args()
@@ -478,26 +479,40 @@ def run_channel(args):
 # Published GPU-C numbers (ArmandoOnGPU.pdf p.5 Tab.1, Tesla C1060): particles,
 # steps, GPU seconds of the 2D dam break cases 1-3 (TVD-RK3 steps).
 GPUC_PUBLISHED = {1: (6462, 10000, 19.0), 2: (22899, 20000, 81.0), 4: (85773, 40000, 514.0)}
+# Tab.3 of the same report: lattice side -> (particles, steps, GPU seconds)
+GPUC_WAVE_PUBLISHED = {401: (160801, 800, 33.5), 501: (251001, 1000, 55.1), 601: (361201, 1200, 74.0)}
 
 
 def run_gpuc(args):
-    """The GPU-C codes' 2D dam break, the published Tab.1 cases 1-3 (6,462 /
-    22,899 / 85,773 particles), TVD-RK3 steps of scheme 1 (the host path's
-    physics) on device-resident state; the published C1060 rate beside each."""
+    """The GPU-C codes' published workloads, TVD-RK3 steps of scheme 1 (the
+    host path's physics) on device-resident state, the published C1060 rate
+    beside each: the 2D dam break, Tab.1 cases 1-3 (6,462 / 22,899 / 85,773
+    particles, the reference's geometry), and the pressure wave, Tab.3 cases
+    1-3 (160,801 / 251,001 / 361,201 particles; a stand-in with the published
+    size, material model and free surfaces, `cases.gpuc_pressure_wave`)."""
     import torch
 
     import armando_gb300 as ag
     from armando_gb300 import cases
 
+    work = []
+    for num, (scale, pub) in enumerate(GPUC_PUBLISHED.items(), start=1):
+        work.append((str(num), f"dam break case {num}", lambda s=scale: cases.gpuc_dam_break(s),
+                     None, pub))
+    for num, (side, pub) in enumerate(GPUC_WAVE_PUBLISHED.items(), start=1):
+        work.append((f"w{num}", f"pressure wave case {num}",
+                     lambda s=side: cases.gpuc_pressure_wave(s), [cases.mercury_poly()] * 2, pub))
+    wanted = set(args.gpuc_cases.split(","))
     out = []
-    wanted = {int(k) for k in args.gpuc_cases.split(",")}
-    for num, (scale, (n_pub, steps_pub, sec_pub)) in enumerate(GPUC_PUBLISHED.items(), start=1):
-        if num not in wanted:
+    for key, label, make, mats, (n_pub, steps_pub, sec_pub) in work:
+        if key not in wanted:
             continue
-        c = cases.gpuc_dam_break(scale)
+        c = make()
         assert c.n == n_pub
         dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
         with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+            if mats:
+                ctx.set_materials(mats)
             tuned = tune(ctx, args, dev, c.dt)
             tuned.pop("ms_per_step", None)
             ctx.integrate(dev, c.dt, 1, 5)
@@ -508,13 +523,13 @@ def run_gpuc(args):
         del dev
         v = c.n * steps / (ms * 1e-3)
         pub = n_pub * steps_pub / sec_pub
-        out.append({"case": f"dam break case {num}", "particles": c.n,
+        out.append({"case": label, "particles": c.n,
                     "steps": steps, "ms_per_step": ms / steps, "value": v, "unit": METRIC,
                     "published_c1060": pub, "ratio_to_published": v / pub,
                     "launches_per_step": launches, "tuning": tuned})
     torch.cuda.empty_cache()
-    return {"workload": "GPU-C TVD-RK3 dam break (scheme 1), the published Tab.1 cases; "
-                        "one step = 3 rate evaluations", "cases": out}
+    return {"workload": "GPU-C TVD-RK3 (scheme 1), the published Tab.1 dam break and Tab.3 "
+                        "pressure-wave cases; one step = 3 rate evaluations", "cases": out}
 
 
 def run_sweep(args):

@@ -322,3 +322,31 @@ def test_lazy_sorting_matches_sorting_every_step(scheme):
         cond = rel(getattr(twin, f), getattr(every, f))
         err = rel(getattr(lazy, f), getattr(every, f))
         assert err <= max(20.0 * cond, 1e-6), (f, err, cond)
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+def test_pressure_wave_matches_the_oracle(O, scheme):
+    """The pressure-wave stand-in (polynomial EOS of mercury, free surfaces,
+    a Gaussian energy deposit) on a 41 x 41 lattice, 10 RK3 steps. Mercury is
+    stiff: one FP32 ulp of rho = 13,540 is 2,200 Pa at c0 = 1,490 m/s, and
+    the library rounds its state to FP32 after every stage. Gate: the gates
+    above or 20x the oracle's own change when every FP32 input (x, v, rho, u)
+    moves by one ulp, whichever is larger."""
+    c = cases.gpuc_pressure_wave(41, radius=0.02, scheme=scheme)
+    mats = [cases.mercury_poly()] * 2
+    ref = O.State(c)
+    dv, du = O.gpuc_step(ref, 10, c.dt, materials=mats)
+    rng = np.random.default_rng(60 + scheme)
+    twin = c.copy()
+    for f in ("x", "v", "rho", "u"):
+        a = getattr(c, f)
+        bump = np.where(rng.random(a.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+        setattr(twin, f, np.nextafter(a, bump).astype(np.float32))
+    tw = O.State(twin)
+    dvt, _ = O.gpuc_step(tw, 10, c.dt, materials=mats)
+    got = run_gpu(c, 10, mats)
+    for f, a, b, t in (("x", got.x, ref.x, tw.x), ("v", got.v, ref.v, tw.v),
+                       ("rho", got.rho, ref.rho, tw.rho), ("p", got.p, ref.p, tw.p),
+                       ("u", got.u, ref.u, tw.u), ("dv", got.dvdt, dv, dvt)):
+        err, cond = rel(a, b), rel(t, b)
+        assert err <= max(TOL[f], 20.0 * cond), (scheme, f, err, cond)

@@ -193,3 +193,18 @@ def test_zone_known_answers(O, dim, scheme):
     np.testing.assert_allclose(v[2], vel[:dim], rtol=1e-7)
     np.testing.assert_allclose(x[2], x0[2] + dt * 5.0 / 6.0 * vel[:dim], rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(st.u[2], 5.0, rtol=1e-12)
+
+
+def test_pressure_wave_is_symmetric(O):
+    """The pressure-wave stand-in (a Gaussian energy deposit at the centre of
+    a free square of mercury, polynomial EOS) stays symmetric under the
+    square's reflections, and the deposit drives a compression outward."""
+    c = cases.gpuc_pressure_wave(41, radius=0.02)
+    st = O.State(c)
+    O.gpuc_step(st, 10, c.dt, materials=[cases.mercury_poly()] * 2)
+    p = st.p.reshape(41, 41)  # [i, j] with x = i dr, y = j dr
+    scale = np.abs(p).max()
+    assert np.abs(p - p[::-1, :]).max() <= 1e-9 * scale
+    assert np.abs(p - p.T).max() <= 1e-9 * scale
+    v = st.v.reshape(41, 41, 2)
+    assert v[30, 20, 0] > 0 and v[10, 20, 0] < 0  # outward on both sides of the centre
