@@ -390,7 +390,7 @@ def run_reference(args, rank):
     O = _oracle()
     threads = O.hardware_threads()
     st = O.State(case)
-    w = max(1, min(args.warmup, 2))
+    w = max(1, min(args.warmup, 3))  # warm-up steps are whole CPU steps: at most 3
     t0 = time.perf_counter()
     O.integrate_gather(st, 1, w, case.dt, threads)
     t_w = (time.perf_counter() - t0) / w
