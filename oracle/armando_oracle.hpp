@@ -339,6 +339,7 @@ struct PairGeom {
 template <class R, class Rc>
 inline void pair_geom(const State<R>& s, const Grid<Rc>& g, const Params<R>& P, int i, int j,
                       PairGeom<R, Rc>& pg) {
+    (void)g;  // the geometry needs no grid: the minimum image uses the period of P
     const int dim = s.dim;
     pg.r2 = R(0);
     for (int d = 0; d < dim; ++d) {
