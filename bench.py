@@ -79,7 +79,8 @@ def parse():
                     help="reach,threads_per_particle,block[,skin] instead of the autotuner")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--checkpoint-every", type=int, default=50)
-    ap.add_argument("--only", default=None, choices=[None, "channel3d", "sweep", "adjoint", "gpuc"],
+    ap.add_argument("--only", default=None,
+                    choices=[None, "channel3d", "sweep", "adjoint", "gpuc", "variants"],
                     help="run one extra workload alone and print its JSON")
     ap.add_argument("--config", default="dambreak2d", choices=["dambreak2d", "channel3d"])
     ap.add_argument("--dx", type=float, default=None,
@@ -532,6 +533,57 @@ def run_gpuc(args):
                         "pressure-wave cases; one step = 3 rate evaluations", "cases": out}
 
 
+def run_variants(args):
+    """The single_step options and wall treatments of the CERN step, each on
+    the 2D dam break (2,030,018 particles) beside the default step at one
+    fixed tuning (no sort skin: mirror ghosts and h evolution sort every
+    iteration): ms per leapfrog iteration and particle-steps/s, CUDA events
+    around `extra_steps` device-resident iterations after 3 warm-up ones."""
+    import torch
+
+    import armando_gb300 as ag
+    from armando_gb300 import cases
+
+    tuning = [int(x) for x in (args.tuning or "3,1,256,0").split(",")]
+    tuning[3] = 0
+    base = cases.dam_break() if args.dx is None else cases.dam_break(dx=args.dx)
+    tank_w = 4.0
+    variants = [
+        ("default (summation density, CERN virtual particles)", {}),
+        ("wall_model 1 (GPU-C device repulsion)", {"wall_model": 1}),
+        ("wall_model 2 (GPU-C host-path repulsion)", {"wall_model": 2}),
+        ("wall_model 3 (mirror ghosts)", "ghosts"),
+        ("density_form 1 (continuity)", {"density_form": 1}),
+        ("density_form 2 (normalised summation)", {"density_form": 2}),
+        ("average_velocity 1 (XSPH)", {"average_velocity": 1}),
+        ("sle 2 (h evolution by div v)", {"sle": 2}),
+    ]
+    out = []
+    for label, opt in variants:
+        if opt == "ghosts":
+            c = cases.with_mirror_ghosts(base, lo=(0.0, 0.0), hi=(tank_w, None))
+        else:
+            c = base.copy()
+            for k, v in opt.items():
+                setattr(c.params, k, v)
+        dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
+        with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+            ctx.set_tuning(*tuning)
+            ctx.integrate(dev, c.dt, 1, 3)
+            ms = timed_integrate(ctx, dev, c.dt, 4, args.extra_steps)
+            ghosts = ctx.stats().ghosts
+        del dev
+        torch.cuda.empty_cache()
+        row = {"variant": label, "ms_per_step": ms / args.extra_steps,
+               "value": c.n * args.extra_steps / (ms * 1e-3), "unit": METRIC}
+        if opt == "ghosts":
+            row["ghosts_per_step"] = int(ghosts)
+        out.append(row)
+    for row in out:
+        row["relative_to_default"] = out[0]["ms_per_step"] / row["ms_per_step"]
+    return {"workload": f"{base.name}: {base.n} particles, tuning {tuning}", "variants": out}
+
+
 def run_sweep(args):
     """Batched sweep vs the plain step run instance by instance on the same GPU."""
     import torch
@@ -796,7 +848,7 @@ def main():
 
         torch.cuda.set_device(local_rank)
         run = {"channel3d": run_channel, "sweep": run_sweep, "adjoint": run_adjoint,
-               "gpuc": run_gpuc}[args.only]
+               "gpuc": run_gpuc, "variants": run_variants}[args.only]
         if rank == 0:
             print(json.dumps({"workload_only": args.only, **run(args)}), flush=True)
         return
