@@ -581,7 +581,28 @@ def run_variants(args):
         out.append(row)
     for row in out:
         row["relative_to_default"] = out[0]["ms_per_step"] / row["ms_per_step"]
-    return {"workload": f"{base.name}: {base.n} particles, tuning {tuning}", "variants": out}
+    # Particle decks (input.f / output.f formats) and the VTK snapshot: host code
+    # of the library, timed on a 0.23 M-particle dam break in a temporary folder.
+    import shutil
+    import tempfile
+
+    d = cases.dam_break(dx=3.0e-3)
+    tmp = tempfile.mkdtemp(prefix="armando_deck_")
+    try:
+        t0 = time.perf_counter()
+        ag.write_deck(tmp, d.dim, d.n_fluid, d)
+        t1 = time.perf_counter()
+        back = ag.read_deck(tmp, d.dim)
+        t2 = time.perf_counter()
+        ag.write_vtk(os.path.join(tmp, "snap.vtk"), d.dim, d)
+        t3 = time.perf_counter()
+        nbytes = sum(os.path.getsize(os.path.join(tmp, f)) for f in os.listdir(tmp))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    io = {"particles": d.n, "deck_write_s": t1 - t0, "deck_read_s": t2 - t1, "vtk_write_s": t3 - t2,
+          "bytes_on_disk": nbytes, "round_trip_particles": int(np.asarray(back["mass"]).size)}
+    return {"workload": f"{base.name}: {base.n} particles, tuning {tuning}", "variants": out,
+            "deck_io": io}
 
 
 def run_sweep(args):
