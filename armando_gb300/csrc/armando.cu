@@ -97,6 +97,7 @@ struct armando_ctx {
     std::string err = "no error";
     int64_t steps_done = 0, launches = 0;
     int launches_per_step = 0;
+    int lazy_body = 0;  // kernels in the conditional body of the lazy step graph (run on sorting steps)
     DevGrid last_grid{};
     bool have_grid = false;
     float last_dt = 0.f;  // dt and next its of the state left on the device
@@ -530,7 +531,8 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
                                            nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return fail_graph(e, "cudaStreamBeginCaptureToGraph(body)");
     body_cap = true;
-    int L = 1 + launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2);
+    const int body = launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2);
+    int L = 1 + body;
     cudaGraph_t body_out = nullptr;
     e = cudaStreamEndCapture(ctx->stream2, &body_out);
     body_cap = false;
@@ -549,6 +551,7 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
         return cuda_fail(ctx, e, "cudaGraphInstantiate(conditional)");
     }
     *launches = L;
+    ctx->lazy_body = body;
     return ARMANDO_OK;
 }
 
@@ -826,11 +829,13 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
         if (ie != cudaSuccess) return cuda_fail(ctx, ie, "cudaGraphInstantiate");
         ctx->graphs[key] = exec;
         ctx->launches_per_step = L;
+        ctx->lazy_body = 0;
     } else {
         exec = itg->second;
     }
     CK(cudaGraphLaunch(exec, ctx->stream));
-    ctx->launches += ctx->launches_per_step;
+    // the conditional body's kernels are counted when the device reports its sorts
+    ctx->launches += ctx->launches_per_step - ctx->lazy_body;
     ctx->steps_done += 1;
     if (!lazy(ctx)) ctx->sorts_host += 1;
     return ARMANDO_OK;
@@ -1377,6 +1382,8 @@ armando_status check_flags(armando_ctx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->last_grid = *ctx->h_grid;
     ctx->have_grid = true;
+    if ((int64_t)ctx->h_flags[3] >= ctx->sorts_done)
+        ctx->launches += ((int64_t)ctx->h_flags[3] - ctx->sorts_done) * ctx->lazy_body;
     ctx->sorts_done = ctx->h_flags[3];
     const unsigned f = *ctx->h_flags;
     if (f & FLAG_PERIODIC_SMALL) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "periodic box shorter than 3 cells of 2*max(h)");
