@@ -1003,12 +1003,13 @@ template <int DIM>
 armando_status build_wall_grid_dim(armando_ctx* ctx) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n;
-    k_wall_grid<DIM><<<1, kWallGridThreads, 0, st>>>(ctx->A, n, 1LL << 28, ctx->wgrid);
+    k_wall_grid_partial<DIM><<<kBBoxBlocks, 256, 0, st>>>(ctx->A, n, ctx->bbox_part);
+    k_wall_grid<DIM><<<1, kWallGridThreads, 0, st>>>(ctx->bbox_part, kBBoxBlocks, 1LL << 28, ctx->wgrid);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ctx->h_wgrid, ctx->wgrid, sizeof(WallGrid), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     const WallGrid g = *ctx->h_wgrid;
-    ctx->launches += 1;
+    ctx->launches += 2;
     if (g.ncells < 0) return fail(ctx, ARMANDO_ERR_GRID_OVERFLOW, "wall grid of the mirror ghosts needs more than 2^28 cells");
     ctx->wall_cells = g.ncells;
     if (g.ncells == 0) return ARMANDO_OK;

@@ -35,15 +35,16 @@ constexpr int kGhostThreads = 256;
 constexpr int kGhostItems = 4;
 constexpr int kGhostTile = kGhostThreads * kGhostItems;
 
-// Box of the wall particles and max h of all particles (one block).
+// Box of the wall particles, their count and max h of all particles: partial
+// results per CTA (8 floats each: min[3], max[3], max h, the count's bits).
 template <int DIM>
-__global__ void __launch_bounds__(kWallGridThreads)
-    k_wall_grid(StateA A, int n, long long max_cells, WallGrid* __restrict__ wg) {
-    __shared__ float s_red[7][32];
-    __shared__ int s_cnt[32];
+__global__ void __launch_bounds__(256)
+    k_wall_grid_partial(StateA A, int n, float* __restrict__ part) {
+    __shared__ float s_red[7][8];
+    __shared__ int s_cnt[8];
     float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
     int cnt = 0;
-    for (int i = threadIdx.x; i < n; i += kWallGridThreads) {
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) {
         const float4 xh = A.xh[i];
         v[6] = fmaxf(v[6], xh.w);
         if (A.itype[i] <= 0) {
@@ -54,6 +55,44 @@ __global__ void __launch_bounds__(kWallGridThreads)
             }
             ++cnt;
         }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int off = 16; off > 0; off >>= 1) {
+        for (int d = 0; d < 3; ++d) v[d] = fminf(v[d], __shfl_xor_sync(0xffffffffu, v[d], off));
+        for (int d = 3; d < 7; ++d) v[d] = fmaxf(v[d], __shfl_xor_sync(0xffffffffu, v[d], off));
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+    }
+    if (lane == 0) {
+        for (int d = 0; d < 7; ++d) s_red[d][warp] = v[d];
+        s_cnt[warp] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int w = 1; w < 8; ++w) {
+        for (int d = 0; d < 3; ++d) v[d] = fminf(v[d], s_red[d][w]);
+        for (int d = 3; d < 7; ++d) v[d] = fmaxf(v[d], s_red[d][w]);
+        cnt += s_cnt[w];
+    }
+    float* o = part + 8 * blockIdx.x;
+    for (int d = 0; d < 7; ++d) o[d] = v[d];
+    o[7] = __int_as_float(cnt);
+}
+
+// The wall grid from the partials (one block): min / max / count are exact in
+// any order, so the grid does not depend on how the particles were split.
+template <int DIM>
+__global__ void __launch_bounds__(kWallGridThreads)
+    k_wall_grid(const float* __restrict__ part, int nparts, long long max_cells,
+                WallGrid* __restrict__ wg) {
+    __shared__ float s_red[7][32];
+    __shared__ int s_cnt[32];
+    float v[7] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX, 0.f};
+    int cnt = 0;
+    for (int b = threadIdx.x; b < nparts; b += kWallGridThreads) {
+        const float* q = part + 8 * b;
+        for (int d = 0; d < 3; ++d) v[d] = fminf(v[d], q[d]);
+        for (int d = 3; d < 7; ++d) v[d] = fmaxf(v[d], q[d]);
+        cnt += __float_as_int(q[7]);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int off = 16; off > 0; off >>= 1) {
