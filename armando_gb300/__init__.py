@@ -116,18 +116,23 @@ class Context:
         self._check(self._lib.armando_set_params(self._h, C.byref(params)))
         self.params = params.copy()
 
-    def step(self, s, dt: float, its: int):
-        """One leapfrog iteration `its` on state `s` (a Case or dict of arrays), in place."""
+    def step(self, s, dt: float, its: int, wait: bool = True):
+        """One leapfrog iteration `its` on state `s` (a Case or dict of arrays), in
+        place. With device memory the C call is asynchronous; ``wait`` then
+        blocks for it and raises its device status (``armando_sync``)."""
         a = s.arrays() if hasattr(s, "arrays") else s
         self._validate(a)
         self._check(self._lib.armando_step(self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]),
                                            _ptr(a["rho"]), _ptr(a["p"]), _ptr(a["u"]),
                                            _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]),
                                            _ptr(a["dudt"]), float(dt), int(its)))
+        if wait and self.mem == MEM_DEVICE:
+            self.sync()
         return s
 
-    def integrate(self, s, dt: float, its0: int, steps: int):
-        """`steps` leapfrog iterations its0.. on state `s`, in place."""
+    def integrate(self, s, dt: float, its0: int, steps: int, wait: bool = True):
+        """`steps` leapfrog iterations its0.. on state `s`, in place (``wait`` as
+        for step)."""
         a = s.arrays() if hasattr(s, "arrays") else s
         self._validate(a)
         self._check(self._lib.armando_integrate(self._h, _ptr(a["x"]), _ptr(a["v"]),
@@ -135,6 +140,8 @@ class Context:
                                                 _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]),
                                                 _ptr(a["dvdt"]), _ptr(a["dudt"]), float(dt),
                                                 int(its0), int(steps)))
+        if wait and self.mem == MEM_DEVICE:
+            self.sync()
         return s
 
     # -- reverse mode -----------------------------------------------------------
@@ -317,7 +324,13 @@ class Context:
         self._check(self._lib.armando_set_zones(self._h, len(loads), lt, len(fixes), ft))
 
     def sync(self):
+        """Blocks for the context's stream; raises the device status of the
+        asynchronous calls since the last report (``armando_sync``)."""
         self._check(self._lib.armando_sync(self._h))
+
+    def set_stream(self, stream_handle: int):
+        """Launch on the caller's cudaStream_t (0: the context's own stream)."""
+        self._check(self._lib.armando_set_stream(self._h, C.c_void_p(int(stream_handle) or None)))
 
 
 class Batch(Context):
@@ -343,8 +356,9 @@ class Batch(Context):
         self.counts = nf + nw
         self.offsets = np.concatenate([[0], np.cumsum(self.counts)])
 
-    def integrate_batch(self, s, dts, its0: int, steps: int):
-        """`steps` iterations of every instance, dts[k] the time step of instance k."""
+    def integrate_batch(self, s, dts, its0: int, steps: int, wait: bool = True):
+        """`steps` iterations of every instance, dts[k] the time step of instance k
+        (``wait`` as for Context.step)."""
         a = s.arrays() if hasattr(s, "arrays") else s
         self._validate(a)
         d = np.ascontiguousarray(dts, np.float32)
@@ -354,6 +368,8 @@ class Batch(Context):
             self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
             _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
             d.ctypes.data_as(C.c_void_p), int(its0), int(steps)))
+        if wait and self.mem == MEM_DEVICE:
+            self.sync()
         return s
 
 

@@ -191,16 +191,18 @@ class LoadZone(C.Structure):
 
 class FixZone(C.Structure):
     """``armando_fix_zone``: inside the open box a particle takes velocity vel
-    after each stage's update."""
+    after each stage's update (tau = 0), or relaxes towards it, dv/dt +=
+    (vel - v) / tau, in every rate evaluation (tau > 0: a pump zone)."""
 
-    _fields_ = [("lo", F3), ("hi", F3), ("vel", F3)]
+    _fields_ = [("lo", F3), ("hi", F3), ("vel", F3), ("tau", C.c_float)]
 
     @classmethod
-    def make(cls, lo, hi, vel):
+    def make(cls, lo, hi, vel, tau=0.0):
         z = cls()
         _box(z, lo, hi)
         for d in range(3):
             z.vel[d] = vel[d] if d < len(vel) else 0.0
+        z.tau = tau
         return z
 
 
@@ -254,7 +256,8 @@ EXPORTED = [
     "armando_params_default", "armando_create", "armando_set_params",
     "armando_step", "armando_integrate", "armando_cell_ids",
     "armando_neighbours", "armando_sync", "armando_get_stats",
-    "armando_last_error", "armando_destroy", "armando_abi_version",
+    "armando_last_error", "armando_destroy", "armando_abi_version", "armando_binary_version",
+    "armando_set_stream",
     "armando_get_stream", "armando_profile_phases", "armando_cell_ids_noalloc",
     "armando_batch_create", "armando_batch_integrate",
     "armando_forward_checkpointed", "armando_backward",
@@ -309,6 +312,10 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_destroy.restype = C.c_int
     lib.armando_abi_version.argtypes = []
     lib.armando_abi_version.restype = C.c_int32
+    lib.armando_binary_version.argtypes = [ip]
+    lib.armando_binary_version.restype = C.c_int
+    lib.armando_set_stream.argtypes = [vp, vp]
+    lib.armando_set_stream.restype = C.c_int
     lib.armando_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
     lib.armando_get_stream.restype = C.c_int
     lib.armando_profile_phases.argtypes = [vp, C.c_int32, C.POINTER(C.c_float)]

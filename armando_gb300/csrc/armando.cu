@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -19,6 +20,7 @@
 
 #include "../../include/armando.h"
 #include "kernels.cuh"
+#include "staged.cuh"
 #include "adjoint.cuh"
 #include "ghosts.cuh"
 #include "gpuc.cuh"
@@ -62,7 +64,19 @@ constexpr int kFlagWords = 4;
 
 struct armando_ctx {
     int device = 0;
+    // The stream the context launches on: its own stream (created blocking, so
+    // it is ordered with the legacy default stream both ways), or the caller's
+    // (armando_set_stream). Graphs are captured on cap_stream and launched here.
     cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    // A device-memory call returned before its work completed: its device
+    // status words are being copied to h_flags; armando_sync reports them.
+    bool pending = false;
+    // Stage the neighbour passes' candidates in shared memory where the
+    // variant allows it (ARMANDO_STAGING=1 at creation; otherwise global
+    // memory through L1; both give the same bits).
+    bool staging = false;
     armando_params prm{};
     DevParams dp{};
     int dim = 2;
@@ -319,6 +333,17 @@ void free_graphs(armando_ctx* c) {
     c->batch_graph = nullptr;
 }
 
+// Captures on the context's private capture stream for the scope's life; the
+// launch stream (the context's own or the caller's) is never put in capture
+// mode, so a caller's stream that synchronises with the legacy default stream
+// needs no care, and the instantiated graph is launched on it afterwards.
+struct CaptureScope {
+    armando_ctx* c;
+    cudaStream_t run;
+    explicit CaptureScope(armando_ctx* ctx) : c(ctx), run(ctx->stream) { c->stream = c->cap_stream; }
+    ~CaptureScope() { c->stream = run; }
+};
+
 // ---- launch sequences -------------------------------------------------------
 
 // The context's lazy-sort flags (see sort_skipped); nullptr: always sort.
@@ -416,9 +441,44 @@ bool sorts_every_step(const armando_params& p) {
     return p.wall_model == 3 || p.sle != 0;
 }
 
+// The staged passes serve one thread per particle, lean physics, no periodic
+// axis, no single_step option and no mirror ghosts (the other variants read
+// their candidates from global memory).
+bool staged_passes(const armando_ctx* ctx) {
+    return ctx->staging && ctx->tune.threads_per_particle == 1 && lean_physics(ctx->dp) && !any_periodic(ctx->dp) &&
+           !step_options(ctx->prm) && ctx->n_inst == 1 && ctx->prm.wall_model != 3;
+}
+
+template <int DIM, int BS>
+void launch_density_staged(armando_ctx* ctx, const unsigned* skeys) {
+    const int n = (int)ctx->n_work;
+    const int reach = ctx->tune.reach;
+    const int cap = stage_cap(DIM, reach, BS, false);
+    const int bytes = stage_smem_bytes(DIM, reach, BS, false);
+    cudaFuncSetAttribute(k_density_st<DIM, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    k_density_st<DIM, BS><<<blocks_for(n, BS), BS, bytes, ctx->stream>>>(
+        ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n, cap, ctx->flags);
+}
+
+template <int DIM, int BS>
+void launch_force_staged(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
+    const int n = (int)ctx->n_work;
+    const int reach = ctx->tune.reach;
+    const int cap = stage_cap(DIM, reach, BS, true);
+    const int bytes = stage_smem_bytes(DIM, reach, BS, true);
+    cudaFuncSetAttribute(k_force_st<DIM, BS>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    k_force_st<DIM, BS><<<blocks_for(n, BS), BS, bytes, ctx->stream>>>(
+        ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n, cap);
+}
+
 template <int DIM>
 void launch_density(armando_ctx* ctx, const unsigned* skeys) {
     const int n = (int)ctx->n_work;
+    if (staged_passes(ctx)) {
+        if (ctx->tune.block == 256) launch_density_staged<DIM, 256>(ctx, skeys);
+        else launch_density_staged<DIM, 128>(ctx, skeys);
+        return;
+    }
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
                 [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
@@ -432,6 +492,11 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
 template <int DIM>
 void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     const int n = (int)ctx->n_work;
+    if (staged_passes(ctx)) {
+        if (ctx->tune.block == 256) launch_force_staged<DIM, 256>(ctx, skeys, S);
+        else launch_force_staged<DIM, 128>(ctx, skeys, S);
+        return;
+    }
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
                 [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
@@ -739,6 +804,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
 armando_status run_batch_step(armando_ctx* ctx) {
     if (!ctx->batch_graph) {
         cudaGraph_t graph = nullptr;
+        CaptureScope cap(ctx);
         CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         int L = launch_batch_step_any(ctx, nullptr);
         cudaError_t le = cudaGetLastError();
@@ -805,8 +871,12 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     cudaGraphExec_t exec = nullptr;
     if (itg == ctx->graphs.end() && lazy(ctx) && !ctx->no_conditional) {
         int L = 0;
-        armando_status gs = ctx->dim == 2 ? build_lazy_graph<2>(ctx, S, &exec, &L)
-                                          : build_lazy_graph<3>(ctx, S, &exec, &L);
+        armando_status gs;
+        {
+            CaptureScope cap(ctx);
+            gs = ctx->dim == 2 ? build_lazy_graph<2>(ctx, S, &exec, &L)
+                               : build_lazy_graph<3>(ctx, S, &exec, &L);
+        }
         if (gs == ARMANDO_OK) {
             ctx->graphs[key] = exec;
             ctx->launches_per_step = L;
@@ -818,10 +888,15 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     }
     if (itg == ctx->graphs.end()) {
         cudaGraph_t graph = nullptr;
-        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        int L = launch_step_any(ctx, S);
-        cudaError_t le = cudaGetLastError();
-        cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+        int L = 0;
+        cudaError_t le = cudaSuccess, ce = cudaSuccess;
+        {
+            CaptureScope cap(ctx);
+            CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            L = launch_step_any(ctx, S);
+            le = cudaGetLastError();
+            ce = cudaStreamEndCapture(ctx->stream, &graph);
+        }
         if (le != cudaSuccess) return cuda_fail(ctx, le, "kernel launch during capture");
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "cudaStreamEndCapture");
         cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
@@ -1370,17 +1445,53 @@ armando_status prepare_gpuc(armando_ctx* ctx) {
             z.fix[k].hi[d] = F.hi[d];
             z.fix[k].v[d] = F.vel[d];
         }
+        z.fix[k].tau = F.tau;
     }
     CK(cudaMemcpy(ctx->d_zones, &z, sizeof z, cudaMemcpyHostToDevice));
     return ARMANDO_OK;
 }
 
-armando_status check_flags(armando_ctx* ctx) {
+// Enqueues the copy of the device status words and the last grid to the
+// pinned host mirrors (complete once the stream passes this point).
+armando_status copy_flags(armando_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->h_flags, ctx->flags, kFlagWords * sizeof(unsigned),
                        cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_grid, ctx->n_inst > 1 ? ctx->d_grids : ctx->grid, sizeof(DevGrid),
                        cudaMemcpyDeviceToHost, ctx->stream));
+    return ARMANDO_OK;
+}
+
+armando_status eval_flags(armando_ctx* ctx);
+
+// Synchronous status of a call: waits for the stream, then reads the flags.
+armando_status check_flags(armando_ctx* ctx) {
+    armando_status st = copy_flags(ctx);
+    if (st != ARMANDO_OK) return st;
     CK(cudaStreamSynchronize(ctx->stream));
+    ctx->pending = false;
+    return eval_flags(ctx);
+}
+
+// End of a call. Device memory: stream-ordered and asynchronous, the status
+// words follow the work and armando_sync reports them. Host memory: the
+// outputs are in the caller's arrays on return, so the call waits.
+armando_status finish_call(armando_ctx* ctx) {
+    if (ctx->mem_kind != ARMANDO_MEM_DEVICE) return check_flags(ctx);
+    armando_status st = copy_flags(ctx);
+    if (st != ARMANDO_OK) return st;
+    ctx->pending = true;
+    return ARMANDO_OK;
+}
+
+// Clears the error word at a call's start, unless an asynchronous call's
+// status has not been reported yet (device errors stay until armando_sync).
+armando_status clear_flags(armando_ctx* ctx) {
+    if (!ctx->pending) CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    return ARMANDO_OK;
+}
+
+// Host side of the status words copied by copy_flags (the copy has landed).
+armando_status eval_flags(armando_ctx* ctx) {
     ctx->last_grid = *ctx->h_grid;
     ctx->have_grid = true;
     if ((int64_t)ctx->h_flags[3] >= ctx->sorts_done)
@@ -1392,6 +1503,7 @@ armando_status check_flags(armando_ctx* ctx) {
     if (f & FLAG_NONFINITE) return fail(ctx, ARMANDO_ERR_NONFINITE, "non-finite value in a fluid particle's state");
     if (f & FLAG_OUT_OF_GRID) return fail(ctx, ARMANDO_ERR_OUT_OF_GRID, "a particle left the periodic box by more than one period");
     if (f & FLAG_BAD_MATERIAL) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "an |itype| outside the material table");
+    if (f & FLAG_TIMEOUT) return fail(ctx, ARMANDO_ERR_TIMEOUT, "a bounded wait on a shared-memory staging copy gave up");
     return ARMANDO_OK;
 }
 
@@ -1455,9 +1567,10 @@ armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, co
         itype = ctx->s_itype;
         dvdt = dvdt ? ctx->s_dvdt : nullptr;
         dudt = dudt ? ctx->s_dudt : nullptr;
-    } else {
-        CK(cudaDeviceSynchronize());  // caller's producers of the arrays are complete
     }
+    // Device memory: stream order only. The context's own stream is ordered
+    // after earlier work on the legacy default stream; a caller producing the
+    // arrays on another stream passes it with armando_set_stream.
     if (dvdt && !dudt) dvdt = nullptr;
     const int nn = (int)ctx->n;
     if (ctx->dim == 2)
@@ -1894,6 +2007,19 @@ void armando_params_default(armando_params* p) {
 
 int32_t armando_abi_version(void) { return ARMANDO_ABI_VERSION; }
 
+armando_status armando_binary_version(int32_t* version) {
+    if (!version) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "version is NULL");
+    cudaFuncAttributes a{};
+    const cudaError_t e = cudaFuncGetAttributes(&a, k_advance_its);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(nullptr, e == cudaErrorNoDevice ? ARMANDO_ERR_NO_DEVICE : ARMANDO_ERR_CUDA,
+                    cudaGetErrorString(e));
+    }
+    *version = a.binaryVersion;
+    return ARMANDO_OK;
+}
+
 static armando_status create_impl(armando_ctx** out, int32_t n_inst, const armando_params* params,
                                   int32_t dim, const int64_t* n_fluid, const int64_t* n_wall,
                                   int32_t mem_kind) {
@@ -1951,12 +2077,16 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
                 delete ctx;
                 return fail(nullptr, ARMANDO_ERR_UNSUPPORTED, "batches run the CERN summation-density step without mirror ghosts");
             }
-    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamDefault);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         armando_status st = cuda_fail(ctx, e, "cudaStreamCreate");
+        if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
         delete ctx;
         return st;
     }
+    ctx->stream = ctx->own_stream;
+    if (const char* sv = std::getenv("ARMANDO_STAGING")) ctx->staging = std::strcmp(sv, "1") == 0;
     armando_status st = alloc_state(ctx);
     if (st == ARMANDO_OK && n_inst > 1) st = alloc_batch(ctx);
     if (st != ARMANDO_OK) {
@@ -2132,7 +2262,7 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
             continue;
         }
         if ((st = apply_tuning(ctx, t)) != ARMANDO_OK) break;
-        CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+        if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
         st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
         if (st == ARMANDO_OK) st = plan_grid(ctx);
         if (st == ARMANDO_OK) st = build_wall_grid(ctx);
@@ -2198,7 +2328,7 @@ armando_status armando_batch_integrate(armando_ctx* ctx, float* x, float* vx, co
         st = upload_batch_params(ctx);
         if (st != ARMANDO_OK) return st;
     }
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
     if (st != ARMANDO_OK) return st;
     st = plan_grid(ctx);
@@ -2213,7 +2343,7 @@ armando_status armando_batch_integrate(armando_ctx* ctx, float* x, float* vx, co
     ctx->next_its = its0 + steps;
     st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
     if (st != ARMANDO_OK) return st;
-    return check_flags(ctx);
+    return finish_call(ctx);
 }
 
 armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const float* mass,
@@ -2231,7 +2361,7 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     if (steps < 0) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps must be >= 0");
     CK(cudaSetDevice(ctx->device));
     if (ctx->n == 0 || steps == 0) return ARMANDO_OK;
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
     if (st != ARMANDO_OK) return st;
     st = plan_grid(ctx);
@@ -2252,7 +2382,7 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     ctx->next_its = its0 + steps;
     st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
     if (st != ARMANDO_OK) return st;
-    return check_flags(ctx);
+    return finish_call(ctx);
 }
 
 armando_status armando_step(armando_ctx* ctx, float* x, float* vx, const float* mass, float* rho,
@@ -2275,7 +2405,7 @@ armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, flo
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps >= 0 and 0 <= *n_particles <= capacity");
     CK(cudaSetDevice(ctx->device));
     ctx->adj_ready = false;
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     if ((st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)) != ARMANDO_OK) return st;
     int64_t n = *n_particles, next_id = n;
     if ((st = prepare_open(ctx)) != ARMANDO_OK) return st;
@@ -2322,7 +2452,7 @@ armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* h
     const int nn = (int)ctx->n;
     const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
     cudaStream_t st = ctx->stream;
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     const float* dx = x;
     const float* dh = hsml;
     int* dcell = reinterpret_cast<int*>(cell);
@@ -2332,8 +2462,6 @@ armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* h
         dx = ctx->s_x;
         dh = ctx->s_h;
         dcell = ctx->s_itype;  // scratch int[n]
-    } else {
-        CK(cudaDeviceSynchronize());
     }
     if (ctx->dim == 2) k_load_xh<2><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
     else k_load_xh<3><<<blocks_for(nn, 256), 256, 0, st>>>(dx, dh, ctx->A, nn);
@@ -2343,6 +2471,7 @@ armando_status armando_cell_ids(armando_ctx* ctx, const float* x, const float* h
     if (s != ARMANDO_OK) return s;
     DevParams dp1 = ctx->dp;  // link_list's own grid, whatever the tuning
     dp1.reach = 1;
+    dp1.skin = 0.f;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, nn, ctx->dim, ctx->bbox_part);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, dp1, ctx->cell_cap, ctx->grid,
                                     ctx->flags);
@@ -2367,7 +2496,7 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float*
     offs[0] = 0;
     if (nn == 0) return ARMANDO_OK;
     cudaStream_t st = ctx->stream;
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), st));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     float* dx = nullptr;
     float* dh = nullptr;
     cudaError_t e = cudaSuccess;
@@ -2459,7 +2588,7 @@ armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* v
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps and checkpoint_every must be >= 1");
     CK(cudaSetDevice(ctx->device));
     ctx->adj_ready = false;
-    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     if ((st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)) != ARMANDO_OK) return st;
     if ((st = plan_grid(ctx)) != ARMANDO_OK) return st;
     if ((st = alloc_adjoint(ctx)) != ARMANDO_OK) return st;
@@ -2522,7 +2651,7 @@ armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const floa
             dev_in[k] = stage[k];
         }
     }
-    if (!host) CK(cudaDeviceSynchronize());
+    // Device memory: ordered by the context's stream (see load_inputs).
     if (ctx->dim == 2)
         k_adj_load<2><<<blocks_for(nn, 256), 256, 0, sm>>>(ctx->A.id, dev_in[0], dev_in[1], dev_in[2],
                                                          dev_in[4], dev_in[5], dev_in[3], ctx->adjG,
@@ -2637,7 +2766,30 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
 
 armando_status armando_sync(armando_ctx* ctx) {
     if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (!ctx->pending) return ARMANDO_OK;
+    // The status of the asynchronous calls since the last report (the error
+    // word is sticky until then): report it once, then start clean.
+    ctx->pending = false;
+    armando_status st = eval_flags(ctx);
+    if (st != ARMANDO_OK) CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->stream));
+    return st;
+}
+
+armando_status armando_set_stream(armando_ctx* ctx, void* stream) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    if (next == ctx->stream) return ARMANDO_OK;
+    // Work already enqueued on the previous stream comes first.
+    cudaEvent_t ev = nullptr;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(next, ev, 0);
+    cudaEventDestroy(ev);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "armando_set_stream");
+    ctx->stream = next;
     return ARMANDO_OK;
 }
 
@@ -2757,8 +2909,8 @@ armando_status armando_set_zones(armando_ctx* ctx, int32_t n_loads, const armand
     for (int k = 0; k < n_fixes; ++k) {
         const armando_fix_zone& F = fixes[k];
         if (!box_ok(F.lo, F.hi) || !std::isfinite(F.vel[0]) || !std::isfinite(F.vel[1]) ||
-            !std::isfinite(F.vel[2]))
-            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "fix zone: NaN bound or non-finite velocity");
+            !std::isfinite(F.vel[2]) || !std::isfinite(F.tau) || F.tau < 0.f)
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "fix zone: NaN bound, non-finite velocity or tau < 0");
     }
     ctx->loads.assign(loads, loads + n_loads);
     ctx->fixes.assign(fixes, fixes + n_fixes);
@@ -2832,7 +2984,8 @@ armando_status armando_destroy(armando_ctx* ctx) {
     if (ctx->h_wgrid) cudaFreeHost(ctx->h_wgrid);
     if (ctx->h_ng) cudaFreeHost(ctx->h_ng);
     if (ctx->h_open_n) cudaFreeHost(ctx->h_open_n);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
     delete ctx;
     return ARMANDO_OK;

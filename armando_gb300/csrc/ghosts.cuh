@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kWallGridThreads)
             const float span = (v[3 + d] - v[d] + 2.0f * g.size) / g.size;
             g.n[d] = (span < 1.0e9f) ? (int)span + 1 : 1000000000;
         }
-        cells *= g.n[d];
+        if (cells <= max_cells) cells *= g.n[d];  // saturates (no overflow)
     }
     if (cnt == 0 || !(g.size > 0.f)) g.ncells = 0;
     else g.ncells = (cells > max_cells) ? -1 : (int)cells;

@@ -39,6 +39,7 @@ struct DevLoadZone {
 };
 struct DevFixZone {
     float lo[3], hi[3], v[3];
+    float tau;  // 0: fix zone (velocity set after the update); > 0: pump zone (a rate)
 };
 struct DevZones {
     int n_load, n_fix;
@@ -352,6 +353,16 @@ __global__ void __launch_bounds__(BS)
             g2 = __fadd_rn(g2, __ldg(&Z->g[2]));
             wz = __fadd_rn(wz, __ldg(&Z->w));
         }
+        const int np = __ldg(&zones->n_fix);
+#pragma unroll 1
+        for (int q = 0; q < np; ++q) {  // pump zones: (vel - v) / tau (Code/armando.cu:1046-1055)
+            const DevFixZone* Z = zones->fix + q;
+            const float tau = __ldg(&Z->tau);
+            if (!(tau > 0.f) || !in_zone<DIM>(Z->lo, Z->hi, xi)) continue;
+            g0 = __fadd_rn(g0, __fdiv_rn(__fsub_rn(__ldg(&Z->v[0]), vi.x), tau));
+            g1 = __fadd_rn(g1, __fdiv_rn(__fsub_rn(__ldg(&Z->v[1]), vi.y), tau));
+            if (DIM == 3) g2 = __fadd_rn(g2, __fdiv_rn(__fsub_rn(__ldg(&Z->v[2]), vi.z), tau));
+        }
         a0 += g0;
         a1 += g1;
         if (DIM == 3) a2 += g2;
@@ -379,7 +390,7 @@ __global__ void __launch_bounds__(BS)
 #pragma unroll 1
         for (int q = 0; q < nf; ++q) {  // fix zones at the new position
             const DevFixZone* Z = zones->fix + q;
-            if (!in_zone<DIM>(Z->lo, Z->hi, xn)) continue;
+            if (__ldg(&Z->tau) > 0.f || !in_zone<DIM>(Z->lo, Z->hi, xn)) continue;  // pumps: above
             vn.x = __ldg(&Z->v[0]);
             vn.y = __ldg(&Z->v[1]);
             if (DIM == 3) vn.z = __ldg(&Z->v[2]);

@@ -42,6 +42,7 @@ enum DevFlag : unsigned {
     FLAG_OUT_OF_GRID = 4u,
     FLAG_PERIODIC_SMALL = 8u,
     FLAG_BAD_MATERIAL = 16u,  // an itype outside the material table (GPU-C schemes)
+    FLAG_TIMEOUT = 32u,       // a bounded wait on a bulk copy gave up
 };
 
 struct DevGrid {
@@ -371,7 +372,9 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
                 fl |= FLAG_GRID_OVERFLOW;
             }
         }
-        ncells *= g.n[d];
+        // Saturates once above the capacity: three axes of up to 1e9 cells
+        // each would overflow the product (a far outlier in 3D).
+        if (ncells <= capacity) ncells *= g.n[d];
     }
     g.ok = 1;
     g.cell_off = 0;
@@ -1239,16 +1242,38 @@ __device__ __forceinline__ int lane_len(const Cursor& cu) {
     return cu.k < cu.ke ? (cu.ke - cu.k + TPP - 1) / TPP : 0;
 }
 
+// Candidates of a CTA staged in shared memory (staged passes, one thread per
+// particle, no periodic axis): slot k of stencil row r sits at k + shift[r].
+struct StageView {
+    const float4* x;    // xh of the staged slots
+    const float4* v;    // density 3D: vm (mass); force 2D: vr; force 3D: vm
+    const float4* r;    // force 3D: rp
+    const int* shift;   // per stencil row, cursor order
+};
+
+// Stencil row of the cursor's current range (non-periodic grids: one piece
+// per row), r = (dz + f) (2f + 1) + (dy + f).
+template <int DIM>
+__device__ __forceinline__ int cursor_row(const Cursor& cu, int f) {
+    const int dy = (cu.st & 15) - 8, dz = ((cu.st >> 4) & 15) - 8;
+    return DIM == 2 ? dy + f : (dz + f) * (2 * f + 1) + (dy + f);
+}
+
 // ---------------------------------------------------------------------------
 // Pass 1: summation density (float-float near pairs), Tait EOS, div v.
 // ---------------------------------------------------------------------------
 // LEAN: the parameters have no physical viscosity and no artificial heat, so
 // their operands and branches are compiled out.
-template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false>
+// STG: the candidates come from the CTA's staged copy SV (LT: the list entry
+// type, staged indices), else from global memory through L1.
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
+          bool STG = false, class LT = int>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
-                                             int (*s_near)[BS], int (*s_far)[BS]) {
+                                             LT (*s_near)[BS], LT (*s_far)[BS],
+                                             const StageView& SV = StageView{}) {
+    static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     const bool need_div = !LEAN && P.heat_art != 0;
@@ -1291,6 +1316,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     int ord = 0;  // candidate ordinal (cursor order, self included)
     int wb = 0;   // the accumulator holds the bits of ordinals 32 wb .. 32 wb + 63
     unsigned long long cur = 0ull;
+    int shift = 0;  // staged index - slot in the cursor's row
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
         // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
@@ -1300,6 +1326,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                     done = true;
                     break;
                 }
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
                 if (TPP > 1) {
                     cu.k += sub;
                     continue;
@@ -1310,8 +1337,10 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             const int cnt = min(kTestBatch, lane_len<TPP>(cu));
             float4 xb[kTestBatch];
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u)
-                xb[u] = __ldg(B.xh + min(k0 + u * TPP, cu.ke - 1));
+            for (int u = 0; u < kTestBatch; ++u) {
+                const int ku = min(k0 + u * TPP, cu.ke - 1);
+                xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+            }
             cu.k += cnt * TPP;
             unsigned pb = 0u;  // pass bits of this batch
 #pragma unroll
@@ -1321,8 +1350,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 if (u >= cnt || k == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
                 pb |= 1u << u;
                 const float hs = xi.w + xb[u].w;  // near: q < kNearQ with h = hs/2
-                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = k;
-                else s_far[nf++][tid] = k;
+                const LT e = (LT)(STG ? k + shift : k);
+                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = e;
+                else s_far[nf++][tid] = e;
             }
             if (ord - 32 * wb >= 32) {  // word wb is complete
                 if (mask_on && wb < W) B.nmask[mask_word_index<W>(wb, B.mstride, mlane)] = (unsigned)cur;
@@ -1337,11 +1367,11 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         // Near pairs: float-float weights on the exact pair difference.
         for (int t = 0; t < mn; ++t) {
             if (t >= nn) continue;
-            const int k = s_near[t][tid];
+            const int k = (int)s_near[t][tid];
             if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;  // push only
-            const float4 xj = __ldg(B.xh + k);
+            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
+            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(B.vm + k);
             const float mj = mass_of<DIM>(xj, vj);
             float dh[3], dl[3];
             exact_delta<DIM>(xi, xj, g, dh, dl);
@@ -1367,11 +1397,11 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         // Far pairs: FP32 weights (each below ~1% of the self term).
         for (int t = 0; t < mf; ++t) {
             if (t >= nf) continue;
-            const int k = s_far[t][tid];
+            const int k = (int)s_far[t][tid];
             if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;
-            const float4 xj = __ldg(B.xh + k);
+            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (DIM == 3 || need_div) vj = __ldg(B.vm + k);
+            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(B.vm + k);
             const float mj = mass_of<DIM>(xj, vj);
             float d[3], dr2;
             pair_delta<DIM>(xi, xj, g, d, dr2);
@@ -1534,13 +1564,17 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // ---------------------------------------------------------------------------
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
-template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false>
+// STG: neighbours from the CTA's staged copy SV (see density_body).
+template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
+          bool STG = false, class LT = int>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
                                            const DevParams& P, const StepArgs& S,
                                            unsigned* __restrict__ flags, const int s,
-                                           const bool valid, int (*s_list)[BS]) {
+                                           const bool valid, LT (*s_list)[BS],
+                                           const StageView& SV = StageView{}) {
+    static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
@@ -1600,6 +1634,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         from_mask = !(ch.x == ~0u && (W == 1 || ch.y == ~0u));
     }
     int wi = 0, rbase = 0;  // index of wbits; ordinal of the cursor row's first slot
+    int shift = 0;          // staged index - slot in the cursor's row
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
         while (!done && from_mask) {
@@ -1623,12 +1658,13 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     break;
                 }
                 cu.k += sub;
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
             }
             if (!in_rows) {  // cannot happen for a mask of this step's candidates
                 done = true;
                 break;
             }
-            s_list[nl++][tid] = cu.k + TPP * (o - rbase);
+            s_list[nl++][tid] = (LT)(cu.k + TPP * (o - rbase) + (STG ? shift : 0));
         }
         while (!done && !from_mask) {
             if (cu.k >= cu.ke) {
@@ -1636,6 +1672,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     done = true;
                     break;
                 }
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
                 if (TPP > 1) {
                     cu.k += sub;
                     continue;
@@ -1646,24 +1683,27 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             const int cnt = min(kTestBatch, lane_len<TPP>(cu));
             float4 xb[kTestBatch];
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u)
-                xb[u] = __ldg(B.xh + min(k0 + u * TPP, cu.ke - 1));
+            for (int u = 0; u < kTestBatch; ++u) {
+                const int ku = min(k0 + u * TPP, cu.ke - 1);
+                xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+            }
             cu.k += cnt * TPP;
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 float d[3], dr2;
                 const int k = k0 + u * TPP;
-                if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2)) s_list[nl++][tid] = k;
+                if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
+                    s_list[nl++][tid] = (LT)(STG ? k + shift : k);
             }
         }
         const int ml = __reduce_max_sync(0xffffffffu, nl);
         for (int t = 0; t < ml; ++t) {
             if (t >= nl) continue;
-            const int k = s_list[t][tid];
-            const float4 xj = __ldg(B.xh + k);
+            const int k = (int)s_list[t][tid];
+            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
             float4 vj, rpj;
             if (DIM == 2) {  // {vx, vy, rho, P}; u and psi only for art_heat
-                const float4 vr = __ldg(B.vr + k);
+                const float4 vr = STG ? SV.v[k] : __ldg(B.vr + k);
                 vj = make_float4(vr.x, vr.y, 0.f, 0.f);
                 rpj = make_float4(vr.z, vr.w, 0.f, 0.f);
                 if (heat_art) {
@@ -1672,8 +1712,8 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     rpj.w = r.w;
                 }
             } else {
-                vj = __ldg(B.vm + k);
-                rpj = __ldg(B.rp + k);
+                vj = STG ? SV.v[k] : __ldg(B.vm + k);
+                rpj = STG ? SV.r[k] : __ldg(B.rp + k);
             }
             float d[3], dr2;
             pair_delta<DIM>(xi, xj, g, d, dr2);

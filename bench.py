@@ -440,12 +440,14 @@ def timed_integrate(ctx, arrays, dts, its0, steps, batch=False):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
+    # Device memory: the calls return once enqueued; the status is read after.
     if batch:
-        ctx.integrate_batch(arrays, dts, its0, steps)
+        ctx.integrate_batch(arrays, dts, its0, steps, wait=False)
     else:
-        ctx.integrate(arrays, dts, its0, steps)
+        ctx.integrate(arrays, dts, its0, steps, wait=False)
     e1.record(stream)
     e1.synchronize()
+    ctx.sync()
     return e0.elapsed_time(e1)
 
 
@@ -755,9 +757,10 @@ def run_ours(args, rank, world, local_rank):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        ctx.integrate(dev, case.dt, its, args.steps)
+        ctx.integrate(dev, case.dt, its, args.steps, wait=False)
         e1.record(stream)
         e1.synchronize()
+    ctx.sync()
     barrier()
     ms = e0.elapsed_time(e1)
     its += args.steps

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define ARMANDO_ABI_VERSION 1
+#define ARMANDO_ABI_VERSION 2
 
 typedef enum armando_status {
     ARMANDO_OK = 0,
@@ -458,8 +458,12 @@ armando_status armando_integrate_open(armando_ctx* ctx, float* x, float* vx, flo
  *     takes the velocity vel (acpu.c:916-926, armando.cu:1026-1036; the last
  *     matching zone wins); scheme 1 applies it to itype != 0 after resetting the
  *     velocity of itype <= 0, scheme 2 to every particle; boundary-type materials
- *     then keep their start velocity in both.
- * Bounds may be infinite; the other fields must be finite. */
+ *     then keep their start velocity in both;
+ *   pump (a fix zone with tau > 0, the pump / relaxation zones of
+ *     Code/armando.cu:1046-1055): every rate evaluation, a particle with
+ *     itype > 0 inside the box at the stage's position gains (vel - v) / tau on
+ *     dv/dt, v its stage velocity; pump zones in table order after the loads.
+ * Bounds may be infinite; the other fields must be finite, tau >= 0. */
 typedef struct armando_load_zone {
     float lo[3], hi[3];
     float accel[3];
@@ -469,6 +473,7 @@ typedef struct armando_load_zone {
 typedef struct armando_fix_zone {
     float lo[3], hi[3];
     float vel[3];
+    float tau;  /* 0: fix zone; > 0: pump zone relaxing to vel over time tau */
 } armando_fix_zone;
 
 #define ARMANDO_MAX_ZONES 10
@@ -484,13 +489,36 @@ armando_status armando_set_zones(armando_ctx* ctx, int32_t n_loads, const armand
  * calls, as time_integration.f keeps it between its iterations. */
 armando_status armando_get_hsml(armando_ctx* ctx, float* hsml);
 
-/* Blocks until the context's stream is idle and returns its sticky status. */
+/* Calls are stream-ordered on the context's stream. With ARMANDO_MEM_DEVICE,
+ * armando_step / armando_integrate / armando_batch_integrate return as soon as
+ * their work is enqueued (the first call on a context, and calls with mirror
+ * ghosts or open boundaries, read device counts back and block); the device
+ * status of those calls (non-finite state, grid overflow, a particle out of
+ * the periodic box) is sticky until armando_sync reports it, and
+ * armando_get_stats is current after armando_sync. With ARMANDO_MEM_HOST a
+ * call returns once its outputs are in the caller's arrays. The context's own
+ * stream is created blocking, so it is ordered both ways with work on the
+ * legacy default stream (where PyTorch's default stream puts its kernels).
+ * Replaces the Fortran's synchronous calls (CERNsource/time_integration.f:1-8),
+ * which have no notion of a stream. */
+
+/* Blocks until the context's stream is idle and returns the status of the
+ * asynchronous calls since the last report. */
 armando_status armando_sync(armando_ctx* ctx);
+/* Launch the context's work on the caller's stream (a cudaStream_t of the
+ * context's device; NULL: the context's own stream). Work already enqueued on
+ * the previous stream is ordered before later calls. Graphs are captured on a
+ * private stream, so any stream may be passed. No counterpart in the
+ * reference (its GPU code uses the default stream, ArmandoThrust/armando.cu). */
+armando_status armando_set_stream(armando_ctx* ctx, void* stream);
 armando_status armando_get_stats(const armando_ctx* ctx, armando_stats* out);
 /* Last error message of the context (static string when ctx is NULL). */
 const char* armando_last_error(const armando_ctx* ctx);
 armando_status armando_destroy(armando_ctx* ctx);
 int32_t armando_abi_version(void);
+/* cudaFuncAttributes::binaryVersion of the library's device code on the
+ * current device (103: built for sm_103a). No counterpart in the reference. */
+armando_status armando_binary_version(int32_t* version);
 
 /* ---- particle decks and snapshots (host only; no context, no GPU) --------------
  * Decks of the CERN-F77 code, in directory dir: real particles in f_xv.dat,

@@ -45,6 +45,7 @@ struct GpucLoad {
 };
 struct GpucFix {
     float lo[3], hi[3], v[3];
+    float tau = 0.f;  // > 0: a pump zone, Code/armando.cu:1046-1055 (a rate, not a set velocity)
 };
 
 template <class R>
@@ -221,6 +222,12 @@ void gpuc_rates(const State<R>& s, const std::vector<std::vector<int>>& list,
                 if (!gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim)) continue;
                 for (int d = 0; d < dim; ++d) dv[i * dim + d] = dv[i * dim + d] + R(Z.g[d]);
                 wz = wz + R(Z.w);
+            }
+            // pump zones (Code/armando.cu:1046-1055): dv/dt += (vel - v) / tau
+            for (const GpucFix& Z : G.fixes) {
+                if (!(Z.tau > 0.f) || !gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim)) continue;
+                for (int d = 0; d < dim; ++d)
+                    dv[i * dim + d] = dv[i * dim + d] + (R(Z.v[d]) - s.v[i * dim + d]) / R(Z.tau);
             }
         }
         const R hi = s.h[i];
@@ -447,7 +454,7 @@ void gpuc_rk3_step(State<R>& s, const GpucSetup<R>& G, double dt, std::vector<R>
             if (G.variant == 1 && it <= 0)  // acpu.c:910-914
                 for (int d = 0; d < dim; ++d) s.v[i * dim + d] = v0[i * dim + d];
             for (const GpucFix& Z : G.fixes)  // acpu.c:916-926 at the new position
-                if (gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim))
+                if (Z.tau == 0.f && gpuc_in_zone(Z.lo, Z.hi, &s.x[i * dim], dim))
                     for (int d = 0; d < dim; ++d) s.v[i * dim + d] = R(Z.v[d]);
             if (M.type == EOS_BOUNDARY)
                 for (int d = 0; d < dim; ++d) s.v[i * dim + d] = v0[i * dim + d];

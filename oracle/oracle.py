@@ -87,6 +87,9 @@ def lib() -> C.CDLL:
         L.ao_gpuc_step_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material)] + zones + \
             [i64, C.c_int, C.c_double] + [vp] * 10 + [C.c_int]
         L.ao_gpuc_step_f64.restype = C.c_int
+        L.ao_gpuc_rates_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material), i64] + \
+            [vp] * 11 + [C.c_int]
+        L.ao_gpuc_rates_f64.restype = C.c_int
         L.ao_gpuc_open_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material)] + zones + \
                                       [C.c_int32, C.POINTER(Inlet), C.c_int32, C.POINTER(Outlet),
                                        vp, vp, i64, C.POINTER(i64), C.c_int, C.c_double] + \
@@ -269,6 +272,25 @@ def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = 
     if rc:
         raise RuntimeError("oracle gpuc step failed")
     return dv, du
+
+
+def gpuc_rates(params: Params, x, v, m, rho, p, u, h, itype, materials=None, fp32: bool = True):
+    """Pair rates (drho/dt, dv/dt, de/dt) of the GPU-C scheme params.scheme at one
+    state, p as given; the first stage of a step evaluates these."""
+    f = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    x, v, m, rho, p, u, h = (f(a) for a in (x, v, m, rho, p, u, h))
+    it = np.ascontiguousarray(itype, np.int32)
+    n, dim = m.shape[0], int(params.dim)
+    drho, dv, du = np.zeros(n), np.zeros(n * dim), np.zeros(n)
+    tab, nmat = None, 0
+    if materials is not None:
+        nmat = len(materials)
+        tab = (Material * nmat)(*materials)
+    rc = lib().ao_gpuc_rates_f64(C.byref(params), nmat, tab, n, _p(x), _p(v), _p(m), _p(rho),
+                                 _p(p), _p(u), _p(h), _p(it), _p(drho), _p(dv), _p(du), int(fp32))
+    if rc:
+        raise RuntimeError("oracle gpuc rates failed")
+    return drho, dv, du
 
 
 def gpuc_open(case, steps, dt, capacity, n=None, inlets=(), outlets=(), box=None,

@@ -453,6 +453,7 @@ static ao::GpucSetup<double> gpuc_setup(const armando_params* prm, int32_t nmat,
             Z.hi[d] = fixes[k].hi[d];
             Z.v[d] = fixes[k].vel[d];
         }
+        Z.tau = fixes[k].tau;
         G.fixes.push_back(Z);
     }
     return G;
@@ -482,6 +483,34 @@ int ao_gpuc_step_f64(const armando_params* prm, int32_t nmat, const armando_mate
     store_state<double>(s, x, v, rho, p, u, nullptr, nullptr);
     if (dvdt && !dv.empty()) std::memcpy(dvdt, dv.data(), sizeof(double) * n * P.dim);
     if (dudt && !du.empty()) std::memcpy(dudt, du.data(), sizeof(double) * n);
+    return 0;
+}
+
+// Pair rates of the GPU-C scheme at one state, as the first stage of a step
+// evaluates them (the list of gpuc_list, gpuc_rates): drho/dt, dv/dt (loads
+// included) and de/dt, with p as given (not from the EOS) and c from the
+// material's EOS. fp32 = 1: the list in FP32 coordinates.
+int ao_gpuc_rates_f64(const armando_params* prm, int32_t nmat, const armando_material* table,
+                      int64_t n, const double* x, const double* v, const double* m,
+                      const double* rho, const double* p, const double* u, const double* h,
+                      const int* itype, double* drho, double* dvdt, double* dudt, int fp32) {
+    if (prm->scheme != 1 && prm->scheme != 2) return 2;
+    ao::Params<double> P = to_params<double>(prm);
+    const ao::GpucSetup<double> G = gpuc_setup(prm, nmat, table, 0, nullptr, 0, nullptr);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, p, u, h, itype, nullptr, nullptr);
+    const int dim = P.dim;
+    std::vector<float> xf(n * dim), hf(n);
+    for (int64_t i = 0; i < n * dim; ++i) xf[i] = (float)x[i];
+    for (int64_t i = 0; i < n; ++i) hf[i] = (float)h[i];
+    const std::vector<std::vector<int>> list =
+        fp32 ? ao::gpuc_list<float>(n, dim, xf.data(), hf.data()) : ao::gpuc_list<double>(n, dim, x, h);
+    for (int64_t i = 0; i < n; ++i)
+        s.c[i] = ao::gpuc_sound(ao::gpuc_material(G.mat, s.itype[i]), s.rho[i], s.u[i]);
+    std::vector<double> dv, dr, du;
+    ao::gpuc_rates(s, list, G, dv, dr, du);
+    std::memcpy(drho, dr.data(), sizeof(double) * n);
+    std::memcpy(dvdt, dv.data(), sizeof(double) * n * dim);
+    std::memcpy(dudt, du.data(), sizeof(double) * n);
     return 0;
 }
 

@@ -12,7 +12,7 @@ import os
 import sys
 
 RECORDS = 40
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ARMANDO_REF_DIR", "/root/reference")
 SRC = os.path.join(ROOT, "FORTRANsource")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "deck")
 

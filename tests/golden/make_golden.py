@@ -45,7 +45,7 @@ def fp(a, off=0):
     return C.c_void_p(a.ctypes.data + off * a.itemsize)
 
 
-def main(ref_dir="/root/reference"):
+def main(ref_dir=os.environ.get("ARMANDO_REF_DIR", "/root/reference")):
     subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_DIR={ref_dir}"],
                    check=True)
     L = C.CDLL(os.path.join(REPO, "oracle", "_ref", "libacpu.so"))

@@ -47,12 +47,20 @@ def test_library_exports_every_declared_symbol(lib):
         assert hasattr(lib, name)
 
 
-def test_library_built_for_sm103a(lib):
-    # The fatbin of an sm_103a build carries the arch name in its ELF notes.
-    out = subprocess.run(["cuobjdump", "--list-elf", ag.LIB_PATH], capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in out.stdout
+def test_library_built_for_sm103a_only():
+    from armando_gb300 import build
+
+    flags = " ".join(build.NVCC_FLAGS)
+    assert "-gencode arch=compute_103a,code=sm_103a" in flags
+    assert flags.count("-gencode") == 1
+
+
+@pytest.mark.gpu
+def test_device_code_is_sm103(lib):
+    """cudaFuncGetAttributes of a library kernel: binaryVersion 103."""
+    v = C.c_int32(0)
+    assert lib.armando_binary_version(C.byref(v)) == _abi.OK, lib.armando_last_error(None)
+    assert v.value == 103
 
 
 def test_struct_layout_matches_c():
@@ -86,7 +94,7 @@ def test_params_default_matches_python(lib):
 
 
 def test_abi_version(lib):
-    assert lib.armando_abi_version() == 1
+    assert lib.armando_abi_version() == 2
 
 
 def test_create_without_gpu_reports_status(lib):

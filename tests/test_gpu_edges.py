@@ -87,3 +87,24 @@ def test_isolated_particle_beside_a_block(O):
         assert rel_err(getattr(got, f), getattr(ref, f)) <= 1e-5, f
     w0 = cases.wendland_w(0.0, float(c.h[k]), 2)
     np.testing.assert_allclose(got.rho[k], c.mass[k] * w0, rtol=1e-6)
+
+
+@pytest.mark.parametrize("tuning", [(1, 1, 128, 0), (3, 1, 256, 10)])
+def test_far_outlier_reports_grid_overflow(tuning):
+    """One particle 1e4 m out on every axis of a 3D block: the cell count per
+    axis is ~5e6, whose product over three axes exceeds every capacity (and a
+    64-bit integer). The call must fail with GRID_OVERFLOW, not run on a
+    wrapped count."""
+    c = cases.channel(n_x=12, n_yz=6, length=12 * 7.9e-4, width=6 * 7.9e-4, layers=1,
+                      jitter=0.01)
+    c.params.periodic[:] = [0, 0, 0]
+    i = int(np.flatnonzero(c.itype > 0)[0])
+    c.x.reshape(-1, 3)[i] = [1.0e4, 1.0e4, 1.0e4]
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(*tuning)
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.step(c.copy(), c.dt, 1)
+        assert e.value.status == ag._abi.ERR_GRID_OVERFLOW
+        with pytest.raises(ag.ArmandoError) as e:
+            ctx.cell_ids(c.x, c.h)
+        assert e.value.status == ag._abi.ERR_GRID_OVERFLOW

@@ -350,3 +350,38 @@ def test_pressure_wave_matches_the_oracle(O, scheme):
                        ("u", got.u, ref.u, tw.u), ("dv", got.dvdt, dv, dvt)):
         err, cond = rel(a, b), rel(t, b)
         assert err <= max(TOL[f], 20.0 * cond), (scheme, f, err, cond)
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_pump_zone_known_answer(O, dim, scheme):
+    """A pump zone relaxing an isolated particle towards vel (dv/dt = (vel - v)
+    / tau, Code/armando.cu:1046-1055): ten RK3 steps against the exact RK3
+    answer of the linear system and against the oracle; particles outside the
+    zone stay at rest."""
+    from armando_gb300._abi import FixZone
+
+    c = cases.gpuc_dam_break(1, fluid=(20, 10), tank=(54, 16), scheme=scheme)
+    pts = np.array([[0.1, 0.2, 0.3], [1.1, 0.2, -0.4], [2.1, -0.9, 0.3]])[:, :dim]
+    c.params.dim = c.dim = dim
+    c.params.gravity[:] = (0.0, 0.0, 0.0)
+    for f in ("mass", "rho", "p", "u", "h", "itype", "dudt"):
+        setattr(c, f, getattr(c, f)[:3].copy())
+    c.itype[:] = 1
+    c.x = pts.ravel().astype(np.float32)
+    c.v = np.zeros(3 * dim, np.float32)
+    c.dvdt = np.zeros(3 * dim, np.float32)
+    dt, tau, steps = 1e-3, 5e-3, 10
+    vel = np.array([0.7, -0.3, 0.2])
+    pumps = [FixZone.make((0.0, 0.0, 0.0), (0.5, 0.5, 0.5), vel, tau)]
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_zones([], pumps)
+        ctx.integrate(got, dt, 1, steps)
+    ref = O.State(c)
+    O.gpuc_step(ref, steps, dt, fixes=pumps)
+    v, x = got.v.reshape(3, dim), got.x.reshape(3, dim)
+    np.testing.assert_allclose(v, ref.v.reshape(3, dim), rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(x, ref.x.reshape(3, dim), rtol=1e-6, atol=1e-7)
+    assert np.all(v[1:] == 0.0)
+    np.testing.assert_allclose(v[0], vel[:dim] * (1.0 - np.exp(-steps * dt / tau)), rtol=1e-3)

@@ -208,3 +208,44 @@ def test_pressure_wave_is_symmetric(O):
     assert np.abs(p - p.T).max() <= 1e-9 * scale
     v = st.v.reshape(41, 41, 2)
     assert v[30, 20, 0] > 0 and v[10, 20, 0] < 0  # outward on both sides of the centre
+
+
+def rk3_relaxation(v_target, tau, dt, steps, x0):
+    """The TVD-RK3 step on x' = v, v' = (V - v) / tau from rest: for this
+    linear system the step is y + dt f + dt^2/2 A f + dt^3/6 A^2 f, f = A y + b."""
+    A = np.array([[0.0, 1.0], [0.0, -1.0 / tau]])
+    out = []
+    for x, V in zip(x0, v_target):
+        y = np.array([x, 0.0])
+        b = np.array([0.0, V / tau])
+        for _ in range(steps):
+            f = A @ y + b
+            y = y + dt * f + dt * dt / 2 * (A @ f) + dt ** 3 / 6 * (A @ (A @ f))
+        out.append(y)
+    return np.array(out)  # [dim, (x, v)]
+
+
+@pytest.mark.parametrize("scheme", [1, 2])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_pump_zone_known_answer(O, dim, scheme):
+    """A pump zone (a fix zone with tau > 0, Code/armando.cu:1046-1055):
+    isolated particle 0 inside relaxes towards vel with dv/dt = (vel - v)/tau,
+    which ten RK3 steps integrate exactly as the third-order Taylor step of
+    the linear system; particles 1 and 2 lie outside and stay at rest."""
+    from armando_gb300._abi import FixZone
+
+    c = isolated(dim, scheme)
+    dt, steps = 1e-3, 10
+    tau = float(np.float32(5e-3))  # the zone record holds FP32 values
+    vel = np.array([0.7, -0.3, 0.2], np.float32).astype(np.float64)
+    pumps = [FixZone.make((0.0, 0.0, 0.0), (0.5, 0.5, 0.5), vel, tau)]
+    st = O.State(c)
+    O.gpuc_step(st, steps, dt, fixes=pumps)
+    x0 = c.x.reshape(3, dim).astype(np.float64)
+    ref = rk3_relaxation(vel[:dim], tau, dt, steps, x0[0])
+    x, v = st.x.reshape(3, dim), st.v.reshape(3, dim)
+    np.testing.assert_allclose(v[0], ref[:, 1], rtol=1e-12)
+    np.testing.assert_allclose(x[0], ref[:, 0], rtol=1e-12, atol=1e-15)
+    assert np.all(v[1:] == 0.0) and np.array_equal(x[1:], x0[1:])
+    # approaching vel like 1 - exp(-t / tau)
+    np.testing.assert_allclose(v[0], vel[:dim] * (1.0 - np.exp(-steps * dt / tau)), rtol=1e-3)

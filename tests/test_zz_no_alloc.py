@@ -64,3 +64,16 @@ def test_noalloc_rejects_sizes_beyond_its_limit(lib):
     assert b"2^30" in lib.armando_last_error(None)
     st = lib.armando_cell_ids_noalloc(C.byref(c.params), None, None, -1, None, None)
     assert st == _abi.ERR_INVALID_ARG
+
+
+def test_cell_ids_keep_link_list_grid_under_any_tuning(lib, O):
+    """A tuning with a sort skin (or a wider reach) changes the step's cells but
+    not the cell ids either entry point returns: both stay link_list's grid."""
+    c = cases.dam_break(dx=0.02)
+    _, _, ref, _ = O.link_list(c.x, c.h, c.dim, fp32=True, params=c.params)
+    for tuning in ((1, 1, 128, 10), (3, 1, 256, 40), (2, 2, 128, 20)):
+        with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+            ctx.set_tuning(*tuning)
+            got = ctx.cell_ids(c.x, c.h)
+        assert np.array_equal(got.astype(np.int64), ref), tuning
+        assert np.array_equal(_noalloc(lib, c), got), tuning
