@@ -77,6 +77,9 @@ struct armando_ctx {
     // variant allows it (ARMANDO_STAGING=1 at creation; otherwise global
     // memory through L1; both give the same bits).
     bool staging = false;
+    // Neighbour lists between sorts (ARMANDO_NEIGHBOUR_LISTS=0 at creation:
+    // walk the cells every iteration; 2D results are the same bits).
+    bool lists = true;
     armando_params prm{};
     DevParams dp{};
     int dim = 2;
@@ -356,8 +359,13 @@ armando_status force_sort(armando_ctx* ctx) {
     return ARMANDO_OK;
 }
 
+bool use_lists(const armando_ctx* ctx);
 template <int DIM>
-int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st) {
+int launch_build_list(armando_ctx* ctx, const int* rs, cudaStream_t st);
+
+// lists: also rebuild the neighbour lists (a lazily sorting step).
+template <int DIM>
+int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st, bool lists = false) {
     const int n = (int)ctx->n_work;
     int L = 0;
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
@@ -383,11 +391,34 @@ int launch_grid_and_sort(armando_ctx* ctx, const int* rs, cudaStream_t st) {
     k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(ctx->keys[ctx->passes & 1], n,
                                                                    &ctx->grid->ncells, (int)ctx->cell_cap,
                                                                    ctx->start, rs);
+    if (lists) L += launch_build_list<DIM>(ctx, rs, st);
     return L + 1;
 }
 
 // Whether the context sorts lazily (a sort skin; one particle system).
 bool lazy(const armando_ctx* ctx) { return ctx->tune.skin > 0 && ctx->n_inst == 1; }
+
+// Neighbour lists: a lazily sorting CERN step with one lane per particle and
+// the lists allocated (ensure_lists); the iterations between sorts then read
+// the lists instead of walking the cells.
+bool use_lists(const armando_ctx* ctx) {
+    return lazy(ctx) && ctx->tune.threads_per_particle == 1 && ctx->prm.scheme == 0 &&
+           ctx->B.nlist != nullptr;
+}
+
+template <int DIM>
+int launch_build_list(armando_ctx* ctx, const int* rs, cudaStream_t st) {
+    const int n = (int)ctx->n_work;
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    if (ctx->dp.periodic[0] || ctx->dp.periodic[1] || ctx->dp.periodic[2])
+        k_build_list<DIM, true><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+            ctx->A, perm, ctx->B, skeys, ctx->start, ctx->grid, n, rs);
+    else
+        k_build_list<DIM, false><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+            ctx->A, perm, ctx->B, skeys, ctx->start, ctx->grid, n, rs);
+    return 1;
+}
 
 // End of a lazily sorting iteration: the next one sorts if this one flagged
 // it; counts this iteration's sort.
@@ -403,12 +434,21 @@ int launch_resort_advance(armando_ctx* ctx) {
 // option (continuity or normalised density, XSPH, h evolution) is on, as
 // compile-time constants. Lean variants exist for one thread per particle.
 template <class F>
-void with_tuning(const armando_tuning& t, bool per, bool lean, bool opt, F&& f) {
+void with_tuning(const armando_tuning& t, bool per, bool lean, bool opt, bool lst, F&& f) {
     using std::integral_constant;
+    // lists (one lane per particle only) as a compile-time flag, last argument
+    auto pick_lst = [&](auto tpp, auto bs, auto pr, auto ln, auto op) {
+        if constexpr (decltype(tpp)::value == 1) {
+            if (lst) f(tpp, bs, pr, ln, op, std::true_type{});
+            else f(tpp, bs, pr, ln, op, std::false_type{});
+        } else {
+            f(tpp, bs, pr, ln, op, std::false_type{});
+        }
+    };
     auto pick_lean = [&](auto tpp, auto bs, auto pr) {
-        if (opt) f(tpp, bs, pr, std::false_type{}, std::true_type{});
-        else if (decltype(tpp)::value == 1 && lean) f(tpp, bs, pr, std::true_type{}, std::false_type{});
-        else f(tpp, bs, pr, std::false_type{}, std::false_type{});
+        if (opt) pick_lst(tpp, bs, pr, std::false_type{}, std::true_type{});
+        else if (decltype(tpp)::value == 1 && lean) pick_lst(tpp, bs, pr, std::true_type{}, std::false_type{});
+        else pick_lst(tpp, bs, pr, std::false_type{}, std::false_type{});
     };
     auto pick_per = [&](auto tpp, auto bs) {
         if (per) pick_lean(tpp, bs, std::true_type{});
@@ -445,7 +485,7 @@ bool sorts_every_step(const armando_params& p) {
 // axis, no single_step option and no mirror ghosts (the other variants read
 // their candidates from global memory).
 bool staged_passes(const armando_ctx* ctx) {
-    return ctx->staging && ctx->tune.threads_per_particle == 1 && lean_physics(ctx->dp) && !any_periodic(ctx->dp) &&
+    return ctx->staging && !use_lists(ctx) && ctx->tune.threads_per_particle == 1 && lean_physics(ctx->dp) && !any_periodic(ctx->dp) &&
            !step_options(ctx->prm) && ctx->n_inst == 1 && ctx->prm.wall_model != 3;
 }
 
@@ -480,11 +520,11 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
         return;
     }
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
-                [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
+                use_lists(ctx), [&](auto tpp, auto bs, auto per, auto lean, auto opt, auto lst) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
-        constexpr bool OPT = decltype(opt)::value;
-        k_density<DIM, T, BSZ, PER, LEAN, OPT><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool OPT = decltype(opt)::value, LST = decltype(lst)::value;
+        k_density<DIM, T, BSZ, PER, LEAN, OPT, LST><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
     });
 }
@@ -498,11 +538,11 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
         return;
     }
     with_tuning(ctx->tune, any_periodic(ctx->dp), lean_physics(ctx->dp), step_options(ctx->prm),
-                [&](auto tpp, auto bs, auto per, auto lean, auto opt) {
+                use_lists(ctx), [&](auto tpp, auto bs, auto per, auto lean, auto opt, auto lst) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
-        constexpr bool OPT = decltype(opt)::value;
-        k_force<DIM, T, BSZ, PER, LEAN, OPT><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
+        constexpr bool OPT = decltype(opt)::value, LST = decltype(lst)::value;
+        k_force<DIM, T, BSZ, PER, LEAN, OPT, LST><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
             ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
     });
 }
@@ -539,7 +579,7 @@ int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
 template <int DIM>
 int launch_step(armando_ctx* ctx, const StepArgs& S) {
     const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
-    const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream);
+    const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream, use_lists(ctx));
     return L + launch_passes<DIM>(ctx, S, rs);
 }
 
@@ -596,7 +636,8 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
                                            nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return fail_graph(e, "cudaStreamBeginCaptureToGraph(body)");
     body_cap = true;
-    const int body = launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2);
+    const int body = launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2,
+                                               ctx->prm.scheme == 0 && use_lists(ctx));
     int L = 1 + body;
     cudaGraph_t body_out = nullptr;
     e = cudaStreamEndCapture(ctx->stream2, &body_out);
@@ -636,7 +677,7 @@ int launch_gpuc_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     static const float alphas[3] = {1.0f, 0.25f, 2.0f / 3.0f};
     for (int q = 0; q < 3; ++q) {
         const int cur = q & 1;
-        with_tuning(ctx->tune, false, false, false, [&](auto tpp, auto bs, auto, auto, auto) {
+        with_tuning(ctx->tune, false, false, false, false, [&](auto tpp, auto bs, auto, auto, auto, auto) {
             constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
             const int blocks = blocks_for((int64_t)n * T, BSZ);
             if (ctx->prm.scheme == 1)
@@ -784,6 +825,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     const int* perm = ctx->vals[ctx->passes & 1];
     k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(skeys, n, &ctx->grid->ncells,
                                                                    (int)ctx->cell_cap, ctx->start, rs);
+    if (use_lists(ctx)) L += launch_build_list<DIM>(ctx, rs, st);
     k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
     cudaEventRecord(ev[3], st);
     launch_density<DIM>(ctx, skeys);
@@ -2087,6 +2129,7 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
     }
     ctx->stream = ctx->own_stream;
     if (const char* sv = std::getenv("ARMANDO_STAGING")) ctx->staging = std::strcmp(sv, "1") == 0;
+    if (const char* lv = std::getenv("ARMANDO_NEIGHBOUR_LISTS")) ctx->lists = std::strcmp(lv, "0") != 0;
     armando_status st = alloc_state(ctx);
     if (st == ARMANDO_OK && n_inst > 1) st = alloc_batch(ctx);
     if (st != ARMANDO_OK) {
@@ -2188,6 +2231,23 @@ armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
     ctx->adj_ready = false;
     ctx->next_its = 0;  // the device state no longer belongs to the last call
     free_graphs(ctx);
+    // Neighbour lists for a lazily sorting CERN step with one lane per
+    // particle, allocated on first use and kept.
+    if (ctx->lists && lazy(ctx) && t.threads_per_particle == 1 && ctx->prm.scheme == 0 &&
+        !ctx->B.nlist && ctx->prm.wall_model != 3) {
+        const int lcap = ctx->dim == 2 ? kListCap2 : kListCap3;
+        cudaError_t e = cudaSuccess;
+        int* nl = dalloc<int>((size_t)lcap * (size_t)std::max<int64_t>(ctx->cap, 1), e);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(neighbour lists)");
+        ctx->owned.push_back(nl);
+        int* nc = dalloc<int>((size_t)std::max<int64_t>(ctx->cap, 1), e);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(neighbour counts)");
+        ctx->owned.push_back(nc);
+        ctx->B.nlist = nl;
+        ctx->B.ncount = nc;
+        ctx->B.lcap = lcap;
+        ctx->B.lstride = (int)ctx->cap;
+    }
     return ARMANDO_OK;
 }
 

@@ -54,6 +54,7 @@ struct DevGrid {
     int cell_off;  // first cell of this grid in the shared cell table (batches)
     int reach;       // stencil half-width in cells: cell size (2 max(h) + skin) / reach
     float half_skin2;  // (skin / 2)^2: a particle this far from its binned position forces a sort
+    float skin;        // sort skin (length): neighbour lists hold pairs within h_i + h_j + skin
 };
 
 // A unit of work of the persistent passes: slots [s0, s1) of one instance.
@@ -126,6 +127,14 @@ struct StateB {  // working set of one step (cell order)
     float* rlo;    // rounding residual of the predicted density (continuity)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
     float4* xsort; // position of each slot when the particles were last sorted
+    // Neighbour lists of a lazily sorting context (built on the iterations that
+    // sort): entry t of slot s at nlist[t * n + s], the candidates within
+    // h_i + h_j + skin in cursor order; ncount[s] entries, -1 when more than
+    // lcap (that slot walks its cells instead).
+    int* nlist;
+    int* ncount;
+    int lcap;      // list entries per slot
+    int lstride;   // slots per list row (the context's capacity)
     // Neighbour bits of each fluid slot over its first 32 * mask_words<DIM>()
     // candidates (cursor order); words 0 and 1 all ones: more candidates than
     // bits. With TPP lanes per particle, lane L = s * TPP + sub keeps
@@ -380,6 +389,7 @@ __device__ __forceinline__ DevGrid grid_from_bbox(const float* mm, const DevPara
     g.cell_off = 0;
     g.reach = f;
     g.half_skin2 = 0.25f * skin * skin;
+    g.skin = skin;
     if (ncells > capacity || (fl & FLAG_GRID_OVERFLOW) || (fl & FLAG_PERIODIC_SMALL)) {
         fl |= (ncells > capacity) ? FLAG_GRID_OVERFLOW : 0u;
         g.ok = 0;
@@ -1108,6 +1118,14 @@ __device__ __forceinline__ float pow_grad(float ih) {
 // particle with more neighbours takes several rounds.
 // ---------------------------------------------------------------------------
 constexpr int kListCap = 32;      // force pass list
+// Neighbour-list entries per particle of a lazily sorting context (pairs
+// within h_i + h_j + skin; the lattice counts are ~20 / ~85 at a 10% skin,
+// ~28 / ~125 at 40%); a particle with more walks its cells. Each must fit the
+// neighbour bits of one lane (mask_words * 32).
+constexpr int kListCap2 = 64;
+constexpr int kListCap3 = 256;
+static_assert(kListCap2 <= 32 * mask_words<2>() && kListCap3 <= 32 * mask_words<3>(),
+              "a list's neighbour bits fit one lane's mask");
 constexpr int kListCapD = 24;     // density pass: near and far lists each
 constexpr int kTestBatch = 4;     // candidate loads issued together
 // Density pairs with q = r/h < kNearQ are evaluated in float-float, the others
@@ -1266,14 +1284,17 @@ __device__ __forceinline__ int cursor_row(const Cursor& cu, int f) {
 // their operands and branches are compiled out.
 // STG: the candidates come from the CTA's staged copy SV (LT: the list entry
 // type, staged indices), else from global memory through L1.
+// LST: a lazily sorting context's neighbour lists (B.nlist) replace the cell
+// walk for slots whose list fits; the neighbour bits then index list entries.
 template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
-          bool STG = false, class LT = int>
+          bool STG = false, class LT = int, bool LST = false>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
                                              LT (*s_near)[BS], LT (*s_far)[BS],
                                              const StageView& SV = StageView{}) {
     static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
+    static_assert(!LST || (TPP == 1 && !STG), "lists: one lane per particle, unstaged");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     const bool need_div = !LEAN && P.heat_art != 0;
@@ -1317,36 +1338,56 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     int wb = 0;   // the accumulator holds the bits of ordinals 32 wb .. 32 wb + 63
     unsigned long long cur = 0ull;
     int shift = 0;  // staged index - slot in the cursor's row
+    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // list entries (-1: walk the cells)
+    int lt = 0;
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
         // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
         while (!done) {
-            if (cu.k >= cu.ke) {
-                if (!cursor_next<DIM>(g, start, cc, cu)) {
+            int kb[kTestBatch];
+            int cnt;
+            float4 xb[kTestBatch];
+            if (LST && lc >= 0) {
+                if (lt >= lc) {
                     done = true;
                     break;
                 }
-                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
-                if (TPP > 1) {
-                    cu.k += sub;
-                    continue;
-                }
-            }
-            if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
-            const int k0 = cu.k;
-            const int cnt = min(kTestBatch, lane_len<TPP>(cu));
-            float4 xb[kTestBatch];
+                if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
+                cnt = min(kTestBatch, lc - lt);
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u) {
-                const int ku = min(k0 + u * TPP, cu.ke - 1);
-                xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                for (int u = 0; u < kTestBatch; ++u)
+                    kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
+#pragma unroll
+                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + kb[u]);
+                lt += cnt;
+            } else {
+                if (cu.k >= cu.ke) {
+                    if (!cursor_next<DIM>(g, start, cc, cu)) {
+                        done = true;
+                        break;
+                    }
+                    if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
+                    if (TPP > 1) {
+                        cu.k += sub;
+                        continue;
+                    }
+                }
+                if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
+                const int k0 = cu.k;
+                cnt = min(kTestBatch, lane_len<TPP>(cu));
+#pragma unroll
+                for (int u = 0; u < kTestBatch; ++u) {
+                    const int ku = min(k0 + u * TPP, cu.ke - 1);
+                    kb[u] = k0 + u * TPP;
+                    xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                }
+                cu.k += cnt * TPP;
             }
-            cu.k += cnt * TPP;
             unsigned pb = 0u;  // pass bits of this batch
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 float d[3], dr2;
-                const int k = k0 + u * TPP;
+                const int k = kb[u];
                 if (u >= cnt || k == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
                 pb |= 1u << u;
                 const float hs = xi.w + xb[u].w;  // near: q < kNearQ with h = hs/2
@@ -1566,7 +1607,7 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // ---------------------------------------------------------------------------
 // STG: neighbours from the CTA's staged copy SV (see density_body).
 template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
-          bool STG = false, class LT = int>
+          bool STG = false, class LT = int, bool LST = false>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
@@ -1575,6 +1616,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const bool valid, LT (*s_list)[BS],
                                            const StageView& SV = StageView{}) {
     static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
+    static_assert(!LST || (TPP == 1 && !STG), "lists: one lane per particle, unstaged");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
@@ -1635,6 +1677,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     int wi = 0, rbase = 0;  // index of wbits; ordinal of the cursor row's first slot
     int shift = 0;          // staged index - slot in the cursor's row
+    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // bits index list entries
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
         while (!done && from_mask) {
@@ -1650,6 +1693,10 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             }
             const int o = 32 * wi + __ffs(wbits) - 1;
             wbits &= wbits - 1u;
+            if (LST && lc >= 0) {
+                s_list[nl++][tid] = (LT)__ldg(B.nlist + (size_t)o * B.lstride + s);
+                continue;
+            }
             bool in_rows = true;
             while (o >= rbase + lane_len<TPP>(cu)) {  // move to the range holding ordinal o
                 rbase += lane_len<TPP>(cu);
@@ -1928,7 +1975,7 @@ __device__ __forceinline__ DevGrid load_grid(const DevGrid* __restrict__ gp) {
 }
 
 // One CTA per BS / TPP consecutive slots.
-template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n) {
@@ -1936,7 +1983,56 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_far[kListCapD][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    density_body<DIM, TPP, BS, LEAN, OPT>(B, keys, start, g, P, s, s < n, s_near, s_far);
+    density_body<DIM, TPP, BS, LEAN, OPT, false, int, LST>(B, keys, start, g, P, s, s < n, s_near,
+                                                           s_far);
+}
+
+// Neighbour lists of an iteration that sorts (lazy sorting), built in the
+// sort's conditional body after the cell table: for each slot s of the new
+// order, the candidates k != s (cursor order) within h_s + h_k + skin, the
+// bound widened by 2^-14 over the rounding of the FP32 distances. Positions
+// are read through the sort's permutation (the reorder into cell order comes
+// later in the iteration). Until the next sort every particle stays within
+// half the skin of where it was binned, so every pair the exact test accepts
+// (r < h_i + h_j) on those iterations is in the list.
+template <int DIM, bool PER>
+__global__ void __launch_bounds__(kPassThreads)
+    k_build_list(StateA A, const int* __restrict__ perm, StateB B,
+                 const unsigned* __restrict__ keys, const int* __restrict__ start,
+                 const DevGrid* __restrict__ gp, int n, const int* __restrict__ resort = nullptr) {
+    if (sort_skipped(resort)) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DevGrid g = load_grid<PER>(gp);
+    if (!g.ok) {
+        B.ncount[s] = 0;
+        return;
+    }
+    const float4 xi = A.xh[perm[s]];
+    const CellCoord cc = decode_key<DIM>(keys[s], g);
+    const float pad = (1.0f + 0x1p-14f);
+    int cnt = 0;
+    Cursor cu = cursor_begin<DIM>(g);
+    while (cursor_next<DIM>(g, start, cc, cu)) {
+        for (int k0 = cu.k; k0 < cu.ke; k0 += kTestBatch) {
+            float4 xb[kTestBatch];
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u)
+                xb[u] = __ldg(A.xh + __ldg(perm + min(k0 + u, cu.ke - 1)));
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                const int k = k0 + u;
+                if (k >= cu.ke || k == s) continue;
+                float d[3], dr2;
+                pair_delta<DIM>(xi, xb[u], g, d, dr2);
+                const float lim = __fmul_rn(__fadd_rn(__fadd_rn(xi.w, xb[u].w), g.skin), pad);
+                if (!(dr2 < __fmul_rn(lim, lim))) continue;
+                if (cnt < B.lcap) B.nlist[(size_t)cnt * B.lstride + s] = k;
+                ++cnt;
+            }
+        }
+    }
+    B.ncount[s] = cnt <= B.lcap ? cnt : -1;
 }
 
 template <int DIM>
@@ -1948,7 +2044,7 @@ __global__ void __launch_bounds__(kPassThreads)
     shear_body<DIM>(B, keys, start, g, P, s, s < n);
 }
 
-template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
@@ -1956,7 +2052,8 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     __shared__ int s_list[kListCap][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    force_body<DIM, TPP, BS, LEAN, OPT>(B, A, keys, start, g, P, S, flags, s, s < n, s_list);
+    force_body<DIM, TPP, BS, LEAN, OPT, false, int, LST>(B, A, keys, start, g, P, S, flags, s,
+                                                         s < n, s_list);
 }
 
 // ---------------------------------------------------------------------------

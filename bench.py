@@ -43,6 +43,8 @@ METRIC = "particle-steps/s"
 # cross-pass rho/p, the neighbour-search key + permutation and the cell table.
 #   force pass:  read x, v, u, m, h, itype + rho, p; write x, v, dv, u, rho, p, du
 B_FORCE = {2: (2 + 2 + 4) * 4 + 8 + (3 * 2 + 4) * 4, 3: (3 + 3 + 4) * 4 + 8 + (3 * 3 + 4) * 4}
+#   density pass: read x, m, h; write rho, p
+B_DENSITY = {2: (2 + 2) * 4 + 8, 3: (3 + 2) * 4 + 8}
 
 
 def link_list_cells(case) -> int:
@@ -191,6 +193,31 @@ def traffic_per_particle(kernel, config):
         return None
     d = json.load(open(p))
     return d.get(config, {}).get(kernel)
+
+
+def pass_counters(kernel, config):
+    """FP32-pipe utilisation and instructions per particle of a pass, from the
+    committed ncu summary (profiles/passes.json), or None."""
+    p = os.path.join(REPO, "profiles", "passes.json")
+    if not os.path.exists(p):
+        return None
+    return json.load(open(p)).get(config, {}).get(kernel)
+
+
+def pass_rooflines(phases, dim, n, hbm, config):
+    """Each neighbour pass against the HBM roof: algorithmic bytes, achieved
+    GB/s and fraction, with its ncu counters; the larger pass first."""
+    out = []
+    for kernel, key, b in (("k_density", "density", B_DENSITY[dim]),
+                           ("k_force", "force", B_FORCE[dim])):
+        t = phases[key] * 1e-3
+        ach = b * n / t / 1e9
+        tr = traffic_per_particle(kernel, config)
+        out.append({"kernel": kernel, "ms": phases[key], "alg_bytes_per_particle": b,
+                    "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                    "traffic": (tr * n if tr is not None else None),
+                    "ncu": pass_counters(kernel, config)})
+    return sorted(out, key=lambda r: -r["ms"])
 
 
 class NvmlClockSampler:
@@ -391,7 +418,7 @@ def run_reference(args, rank):
     O = _oracle()
     threads = O.hardware_threads()
     st = O.State(case)
-    w = max(1, min(args.warmup, 3))  # warm-up steps are whole CPU steps: at most 3
+    w = max(1, args.warmup)  # the same warm-up count as the GPU arm
     t0 = time.perf_counter()
     O.integrate_gather(st, 1, w, case.dt, threads)
     t_w = (time.perf_counter() - t0) / w
@@ -781,10 +808,8 @@ def run_ours(args, rank, world, local_rank):
     out = None
     if rank == 0:
         hbm, peak_kind = peaks()
-        t_force = phases["force"] * 1e-3
-        alg_force = B_FORCE[case.dim] * case.n
-        achieved = alg_force / t_force / 1e9
-        tr = traffic_per_particle("k_force", args.config)
+        passes = pass_rooflines(phases, case.dim, case.n, hbm, args.config)
+        top = passes[0]  # the larger pass
         cells_pp = link_list_cells(case) / case.n  # the reference algorithm's cell table
         b_step = step_bytes(case.dim, cells_pp)
         step_s = ms * 1e-3 / args.steps
@@ -794,11 +819,11 @@ def run_ours(args, rank, world, local_rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded lattice, no dataset)",
             "config": config_dict(case, args),
-            "roofline": {"bound": "hbm", "kernel": "k_force (pass 2: forces + leapfrog)",
-                         "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "alg_bytes_per_particle": B_FORCE[case.dim],
-                         "traffic": (tr * case.n if tr is not None else None)},
+            "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": top["achieved"],
+                         "peak": hbm, "unit": "GB/s", "frac": top["frac"],
+                         "peak_kind": peak_kind, "alg_bytes_per_particle": top["alg_bytes_per_particle"],
+                         "traffic": top["traffic"], "ncu": top["ncu"],
+                         "passes": passes},
             "step_roofline": {"alg_bytes_per_particle": b_step,
                               "achieved_gbs": b_step * case.n / step_s / 1e9,
                               "frac_of_measured_hbm": b_step * case.n / step_s / 1e9 / hbm},
@@ -855,7 +880,33 @@ def run_ours(args, rank, world, local_rank):
     if not args.no_extras and rank == 0 and world == 1:
         out["workloads"] = {"channel3d": run_channel(args), "sweep": run_sweep(args),
                             "adjoint": run_adjoint(args), "gpuc": run_gpuc(args)}
+    if rank == 0:
+        out["summary"] = summary(out)
     return out
+
+
+def summary(out):
+    """The headline numbers of every workload in a few keys, last in the line."""
+    s = {"dambreak2d": {"ms_per_step": round(out["ms_per_step"], 4), "value": out["value"],
+                        "e2e": out.get("e2e", {}).get("value"),
+                        "two_roof_frac": (out.get("two_roof") or {}).get("frac"),
+                        "passes_ms": {p["kernel"]: round(p["ms"], 4) for p in out["roofline"]["passes"]},
+                        "tuning": out["tuning"]["tuning"]}}
+    w = out.get("workloads", {})
+    if "channel3d" in w:
+        c = w["channel3d"]
+        s["channel3d"] = {"ms_per_step": round(c["ms_per_step"], 3), "value": c["value"],
+                          "two_roof_frac": (c.get("two_roof") or {}).get("frac")}
+    if "sweep" in w:
+        s["sweep"] = {"value": w["sweep"]["value"], "speedup_vs_plain": w["sweep"]["speedup_vs_plain"]}
+    if "adjoint" in w:
+        a = w["adjoint"]
+        s["adjoint"] = {"backward_over_forward": a["backward_over_forward"],
+                        "forward_plus_backward_over_forward": a["forward_plus_backward_over_forward"]}
+    if "gpuc" in w:
+        s["gpuc"] = {c["case"]: round(c.get("ratio_to_published", float("nan")), 1)
+                     for c in w["gpuc"].get("cases", []) if "case" in c}
+    return s
 
 
 def main():

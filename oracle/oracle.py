@@ -90,6 +90,8 @@ def lib() -> C.CDLL:
         L.ao_gpuc_rates_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material), i64] + \
             [vp] * 11 + [C.c_int]
         L.ao_gpuc_rates_f64.restype = C.c_int
+        L.ao_con_density_f64.argtypes = [C.POINTER(Params), i64] + [vp] * 7
+        L.ao_con_density_f64.restype = C.c_int
         L.ao_gpuc_open_f64.argtypes = [C.POINTER(Params), C.c_int32, C.POINTER(Material)] + zones + \
                                       [C.c_int32, C.POINTER(Inlet), C.c_int32, C.POINTER(Outlet),
                                        vp, vp, i64, C.POINTER(i64), C.c_int, C.c_double] + \
@@ -272,6 +274,19 @@ def gpuc_step(state: State, steps: int, dt: float, materials=None, fp32: bool = 
     if rc:
         raise RuntimeError("oracle gpuc step failed")
     return dv, du
+
+
+def con_density(params: Params, x, v, m, rho, h, itype):
+    """con_density (density.f:161-218): drho/dt of the fluid particles (FP64)."""
+    d = lambda a: np.ascontiguousarray(a, np.float64)  # noqa: E731
+    x, v, m, rho, h = map(d, (x, v, m, rho, h))
+    it = np.ascontiguousarray(itype, np.int32)
+    out = np.zeros(m.shape[0])
+    rc = lib().ao_con_density_f64(C.byref(params), m.shape[0], _p(x), _p(v), _p(m), _p(rho),
+                                  _p(h), _p(it), _p(out))
+    if rc:
+        raise RuntimeError("oracle con_density failed")
+    return out
 
 
 def gpuc_rates(params: Params, x, v, m, rho, p, u, h, itype, materials=None, fp32: bool = True):

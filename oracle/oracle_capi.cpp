@@ -193,6 +193,28 @@ int ao_forces_f64(const armando_params* prm, int64_t n, const double* x, const d
     return 0;
 }
 
+// con_density (density.f:161-218): drho/dt[n] of the fluid particles for the
+// given velocities. Pairs from link_list.
+int ao_con_density_f64(const armando_params* prm, int64_t n, const double* x, const double* v,
+                       const double* m, const double* rho, const double* h, const int* itype,
+                       double* drho) {
+    ao::Params<double> P = to_params<double>(prm);
+    std::vector<double> zero(n, 0.0);
+    ao::State<double> s = load_state<double>(P.dim, n, x, v, m, rho, zero.data(), zero.data(), h,
+                                             itype, nullptr, nullptr);
+    ao::PairList pl;
+    ao::Grid<double> g;
+    try {
+        g = ao::neighbour_search<double, double>(s, P, pl);
+    } catch (const std::exception&) {
+        return 1;
+    }
+    std::vector<double> dr;
+    ao::con_density(s, g, P, pl, dr);
+    std::memcpy(drho, dr.data(), sizeof(double) * n);
+    return 0;
+}
+
 // One leapfrog iteration `its` (time_integration.f:131-218), pair-loop form.
 // nbr_fp32 = 1 runs the neighbour search in FP32 coordinates (GPU mirror).
 // extra (optional, n*2): per particle tdsdt, divv of the step.

@@ -10,7 +10,9 @@ oracle/_ref/libacpu.so from ArmandoThrust/acpu.c (oracle/Makefile, target
   balanceMassMomentumHost (v = 0, one material: only the pressure action
                            -(P_i + P_j)/(rho_i rho_j) dW/dr (x_i - x_j)/r acts;
                            two materials: plus the boundary repulsion of
-                           different-material pairs, acpu.c:424-429)
+                           different-material pairs, acpu.c:424-429;
+                           v != 0 at uniform density: plus the momentum
+                           shock correction, and the continuity rate)
                                             acpu.c:346-437
 The cell tables are padded with empty guard cells because updateListHost
 visits cell ids ic +- nX*nY without bounds checks in 2D.
@@ -174,6 +176,28 @@ def main(ref_dir=os.environ.get("ARMANDO_REF_DIR", "/root/reference")):
     acc_m[order, 1] = vdy
     out["force_mat"] = mat2
     out["force_acc_two_materials"] = acc_m.ravel()
+    # Moving particles, one material, uniform density: the continuity rate
+    # drho/dt = sum_j m_j (x_i - x_j).(v_i - v_j) dW/dr / r (the mass shock
+    # correction vanishes at uniform density) and, beside the pressure action,
+    # the momentum shock correction of acpu.c:413-422, which is art_visc with
+    # alpha = 0.03, beta = 0, eta = 0.1, c = c0 for uniform h.
+    vel = rng.normal(0.0, 0.5, (n, 2)).astype(np.float32)
+    vxs, vys = vel[order, 0].copy(), vel[order, 1].copy()
+    msort[:] = 1
+    dsort[:] = 1000.0
+    for a in (ddot, vdx, vdy, vdz):
+        a[:] = 0.0
+    args_v = [fp(lst), fp(msort), fp(masssort), fp(smooth), fp(sx), fp(sy), fp(sz), fp(vxs),
+              fp(vys), fp(z), fp(dsort), fp(psort), fp(csort), fp(ddot), fp(vdx), fp(vdy), fp(vdz)]
+    L.balanceMassMomentumHost(n, *args_v)
+    acc_v = np.zeros((n, 2), np.float32)
+    acc_v[order, 0] = vdx
+    acc_v[order, 1] = vdy
+    drho_v = np.zeros(n, np.float32)
+    drho_v[order] = ddot
+    out["moving_v"] = vel.ravel()
+    out["moving_acc_uniform_rho"] = acc_v.ravel()
+    out["moving_drho_uniform_rho"] = drho_v
     path = os.path.join(HERE, "acpu_pins.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, {k: v.shape for k, v in out.items()})

@@ -58,6 +58,39 @@ def test_pressure_force_pa_sph1_matches_acpu_uniform_rho(O, golden):
     assert np.abs(dv - golden["force_acc_uniform_rho"]).max() <= 2e-6 * np.abs(dv).max()
 
 
+def test_art_visc_matches_acpu_momentum_shock_correction(O, golden):
+    """Moving particles at uniform density: acpu.c's momentum shock correction
+    (acpu.c:413-422) is art_visc (art_visc.f:55-101) with alpha = 0.03,
+    beta = 0, eta = 0.1 and c = c0 at uniform h, so the oracle's pa_sph 0
+    pressure action plus art_visc must equal the compiled host path's rate."""
+    n = golden["lattice_h"].size
+    x, v = golden["lattice_x"], golden["moving_v"]
+    P = Params.default(dim=2, pa_sph=0, rho0=1000.0, c0=20.0)
+    P.visc_artificial = 1
+    P.av_alpha, P.av_beta, P.av_eta = 0.03, 0.0, 0.1
+    dv, _ = O.forces(P, x, v, golden["force_mass"], np.full(n, 1000.0), golden["force_p"],
+                     np.zeros(n), golden["lattice_h"], np.ones(n, np.int32))
+    ref = golden["moving_acc_uniform_rho"]
+    assert np.abs(dv - ref).max() <= 2e-6 * np.abs(ref).max()
+    # the viscous term is a visible part of the result, not rounding
+    assert np.abs(ref - golden["force_acc_uniform_rho"]).max() > 1e-2 * np.abs(ref).max()
+    P.visc_artificial = 0
+    dv0, _ = O.forces(P, x, v, golden["force_mass"], np.full(n, 1000.0), golden["force_p"],
+                      np.zeros(n), golden["lattice_h"], np.ones(n, np.int32))
+    assert np.abs(dv0 - ref).max() > 1e-2 * np.abs(ref).max()
+
+
+def test_con_density_matches_acpu_continuity_rate(O, golden):
+    """con_density (density.f:161-218) against acpu.c's drho/dt at uniform
+    density, where its mass shock correction vanishes (acpu.c:396, 407-411)."""
+    n = golden["lattice_h"].size
+    P = Params.default(dim=2, rho0=1000.0, c0=20.0)
+    drho = O.con_density(P, golden["lattice_x"], golden["moving_v"], golden["force_mass"],
+                         np.full(n, 1000.0), golden["lattice_h"], np.ones(n, np.int32))
+    ref = golden["moving_drho_uniform_rho"]
+    assert np.abs(drho - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
 def test_boundary_repulsion_matches_acpu_two_materials(O, golden):
     """wall_model 2 (acpu.c:424-429): pressure action of every pair plus the
     repulsion 0.02 (W/W0) c_i c_j m_j / ((m_i + m_j) r) between particles of
