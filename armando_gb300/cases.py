@@ -281,6 +281,13 @@ def adjoint_dam_break(n_target: int = 250_000, seed: int = 5, v_std: float = 0.0
     return c
 
 
+# Probe of the reverse-mode loss (mean pressure over a 5 cm patch): centred 10 cm
+# inside the column's right face, near the floor. On the face itself the
+# surface particles sit at the pmin = 0 clamp of the EOS, where the loss has
+# no derivative at FP32 resolution.
+ADJOINT_PROBE = ((0.9, 0.05, 0.0), 0.05)
+
+
 FIELDS = ("x", "v", "mass", "rho", "p", "u", "h", "itype", "dvdt", "dudt")
 
 

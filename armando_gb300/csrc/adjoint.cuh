@@ -14,7 +14,15 @@
 //                  cotangents, scatter to the slot order of the step's input
 // Non-smooth points follow the value: art_visc acts while v_ij . r_ij < 0,
 // u = max(0, .) and the Tait clamp pass no gradient where they bind.
-// Supported: pa_sph = 1, no physical viscosity, no artificial heat.
+// Artificial heat (art_heat.f:42-97), when on: du_i += sum_j m_j (psi_i + psi_j)
+// A_ij (u_i - u_j), A = G r^2 / (rho_bar (r^2 + (eta h_bar)^2)), psi_i =
+// g1 h_i c0 + g2 h_i^2 (|divv_i| - divv_i), divv_i = sum_j m_j G_ij (vh_j - vh_i)
+// . (x_i - x_j) / rho_i. k_adj_force takes the psi, u_half, rho, x cotangents of
+// those pair terms (walls included: their psi enters their neighbours' rates)
+// and turns psi_bar into the cotangent of each particle's divergence sum;
+// k_adj_density gathers that sum's reverse onto velocities and positions. |divv|
+// follows its sign (no gradient at divv = 0 from one side).
+// Supported: pa_sph = 1, no physical viscosity.
 #pragma once
 #include "kernels.cuh"
 
@@ -47,6 +55,7 @@ struct TapeSlot {
     float* du;
     int* start;
     DevGrid* grid;
+    float* ulo;  // rounding residual of the predicted energy (artificial heat only)
 };
 
 template <int DIM>
@@ -70,6 +79,7 @@ __global__ void k_tape_save(StateB B, const unsigned* __restrict__ keys,
     T.keys[s] = keys[s];
     T.perm[s] = perm[s];
     T.du[s] = ap[s].w;
+    if (T.ulo) T.ulo[s] = B.ulo ? B.ulo[s] : 0.f;
 }
 
 // The working set of a taped iteration as the pass kernels see it.
@@ -82,6 +92,7 @@ inline StateB tape_view(StateB B, const TapeSlot& T, int n) {
     B.itype = T.itype;
     B.nmask = T.nmask;
     B.mstride = n;
+    B.ulo = T.ulo;
     return B;
 }
 
@@ -223,16 +234,18 @@ struct NbrStream {
     uint4 ch;
 };
 
+// use_mask: the density pass left this slot's bits (fluid particles); walls
+// test their candidates.
 template <int DIM>
 __device__ __forceinline__ void nbr_init(NbrStream<DIM>& ns, const StateB& B, const DevGrid& g,
-                                         int s, bool work) {
+                                         int s, bool work, bool use_mask = true) {
     ns.cu = cursor_begin<DIM>(g);
     ns.done = !work;
     ns.from_mask = false;
     ns.wbits = 0u;
     ns.ch = make_uint4(0u, 0u, 0u, 0u);
     // masks of several lanes per particle are not in this layout: test instead
-    if (work && B.mtpp == 1) {
+    if (work && use_mask && B.mtpp == 1) {
         ns.ch = mask_load_chunk<mask_words<DIM>()>(B.nmask, B.mstride, s, 0);
         ns.wbits = ns.ch.x;
         ns.from_mask = !(ns.ch.x == ~0u && ns.ch.y == ~0u);
@@ -317,30 +330,44 @@ __global__ void __launch_bounds__(kPassThreads)
                 const DevGrid* __restrict__ gp, DevParams P, StepArgs S,
                 const float4* __restrict__ abar, const float* __restrict__ pbar_loss,
                 float* __restrict__ rhobar, float4* __restrict__ xF, float4* __restrict__ vhb,
-                float* __restrict__ block_part, int n) {
+                float* __restrict__ divsb, double* __restrict__ block_part, int n) {
     __shared__ int s_list[kListCap][kPassThreads];
-    __shared__ float s_red[ADJ_NPARAM][kPassThreads / 32];
+    __shared__ double s_red[ADJ_NPARAM][kPassThreads / 32];
     const int tid = threadIdx.x;
     const int s = blockIdx.x * blockDim.x + tid;
     const bool valid = s < n;
     const DevGrid g = *gp;
-    const bool work = valid && g.ok && B.itype[s] > 0;
-    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi, abi = xi;
-    float pi = 0.f;
-    if (work) {
+    const bool ah = P.heat_art != 0;
+    const int it = valid ? B.itype[s] : 0;
+    const bool work = valid && g.ok && it > 0;
+    // walls take part for artificial heat only: their psi enters their
+    // neighbours' energy rates
+    const bool act = valid && g.ok && (it > 0 || ah);
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi, abi = make_float4(0.f, 0.f, 0.f, 0.f);
+    float pi = 0.f, uloi = 0.f;
+    if (act) {
         xi = B.xh[s];
         vi = B.vm[s];
         rpi = B.rp[s];
         pi = B.p[s];
-        abi = abar[s];
+        if (work) abi = abar[s];
+        if (ah && B.ulo) uloi = B.ulo[s];
     }
     const float mi = mass_of<DIM>(xi, vi);
     CellCoord cc = {{0, 0, 0}};
-    if (work) cc = decode_key<DIM>(keys[s], g);
+    if (act) cc = decode_key<DIM>(keys[s], g);
     float xb[3] = {0.f, 0.f, 0.f}, vb[3] = {0.f, 0.f, 0.f}, Pb = 0.f, rb = 0.f;
-    float pa[ADJ_NPARAM] = {0.f, 0.f, 0.f, 0.f};
+    float psib = 0.f, uhb = 0.f;  // artificial heat: psi_bar, u_half_bar of this particle
+    // parameter cotangents, float-float (hi in pa, rounding residuals in palo):
+    // pair terms of both signs cancel in these sums
+    float pa[ADJ_NPARAM] = {0.f, 0.f, 0.f, 0.f}, palo[ADJ_NPARAM] = {0.f, 0.f, 0.f, 0.f};
+    auto pacc = [&](int q, float v) {
+        const sph::ff t = sph::two_sum(pa[q], v);
+        pa[q] = t.hi;
+        palo[q] += t.lo;
+    };
     NbrStream<DIM> ns;
-    nbr_init<DIM>(ns, B, g, s, work);
+    nbr_init<DIM>(ns, B, g, s, act, work);
     while (__any_sync(0xffffffffu, !ns.done)) {
         const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
         const int ml = __reduce_max_sync(0xffffffffu, nl);
@@ -357,33 +384,66 @@ __global__ void __launch_bounds__(kPassThreads)
             const float rho_bar = 0.5f * (rpi.x + rpj.x);
             float w[3] = {vj.x - vi.x, vj.y - vi.y, DIM == 3 ? vj.z - vi.z : 0.f};
             PairAdj o;
-            // Pair (s, j): the rates of s.
-            pair_adjoint<DIM>(pg.d, w, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpi.y, rpj.y, mj,
-                              abi, P, o);
-#pragma unroll
-            for (int k = 0; k < DIM; ++k) {
-                xb[k] += o.db[k];
-                vb[k] -= o.wb[k];
-            }
-            Pb += o.Pb;
-            rb += o.rb;
-            pa[ADJ_ALPHA] += o.al;
-            pa[ADJ_BETA] += o.be;
-            pa[ADJ_C0] += o.c0;
-            // Pair (j, s): the rates of j (zero cotangents for walls).
-            if (abj.x != 0.f || abj.y != 0.f || abj.z != 0.f || abj.w != 0.f) {
-                float dn[3] = {-pg.d[0], -pg.d[1], -pg.d[2]};
-                float wn[3] = {-w[0], -w[1], -w[2]};
-                pair_adjoint<DIM>(dn, wn, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpj.y, rpi.y,
-                                  mi, abj, P, o);
+            if (work) {
+                // Pair (s, j): the rates of s.
+                pair_adjoint<DIM>(pg.d, w, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpi.y, rpj.y,
+                                  mj, abi, P, o);
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) {
-                    xb[k] -= o.db[k];
-                    vb[k] += o.wb[k];
+                    xb[k] += o.db[k];
+                    vb[k] -= o.wb[k];
                 }
                 Pb += o.Pb;
                 rb += o.rb;
+                pacc(ADJ_ALPHA, o.al);
+                pacc(ADJ_BETA, o.be);
+                pacc(ADJ_C0, o.c0);
+                // Pair (j, s): the rates of j (zero cotangents for walls).
+                if (abj.x != 0.f || abj.y != 0.f || abj.z != 0.f || abj.w != 0.f) {
+                    float dn[3] = {-pg.d[0], -pg.d[1], -pg.d[2]};
+                    float wn[3] = {-w[0], -w[1], -w[2]};
+                    pair_adjoint<DIM>(dn, wn, pg.dr2, pg.G, pg.dGdr_r, pg.mh, rho_bar, rpj.y,
+                                      rpi.y, mi, abj, P, o);
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k) {
+                        xb[k] -= o.db[k];
+                        vb[k] += o.wb[k];
+                    }
+                    Pb += o.Pb;
+                    rb += o.rb;
+                }
             }
+            if (ah) {
+                // du_s and du_j terms m (psi_s + psi_j) A (u_s - u_j), A(r^2):
+                // weights du_bar_s m_j - du_bar_j m_s on the pair (s, j).
+                const float e = pg.mh * pg.mh * P.ah_eta2;
+                const float den = rho_bar * (e + pg.dr2);
+                const float A = pg.G * pg.dr2 / den;
+                const float dAds = (0.5f * pg.dGdr_r * pg.dr2 + pg.G) / den - A / (e + pg.dr2);
+                const float ps = rpi.w + rpj.w;
+                const float ulj = B.ulo ? __ldg(B.ulo + j) : 0.f;
+                const float du = (rpi.z - rpj.z) + (uloi - ulj);
+                const float cdu = abi.w * mj - abj.w * mi;
+                psib = fmaf(A * du, cdu, psib);
+                uhb = fmaf(ps * A, cdu, uhb);
+                rb -= 0.5f * ps * A * du * cdu / rho_bar;
+                const float cx = 2.f * dAds * ps * du * cdu;
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) xb[k] = fmaf(cx, pg.d[k], xb[k]);
+            }
+        }
+    }
+    float dsb = 0.f;  // cotangent of the divergence sum (artificial heat)
+    if (act && ah) {
+        // psi = g1 h c0 + g2 h^2 (|divv| - divv), divv = divs / rho: divv from psi
+        const float h = xi.w, base = P.ah_g1 * h * P.c0;
+        pacc(ADJ_C0, psib * P.ah_g1 * h);
+        if (P.ah_g2 != 0.f && rpi.w > base) {  // divv < 0
+            const float k2 = 2.f * P.ah_g2 * h * h;
+            const float divv = -(rpi.w - base) / k2;
+            const float divvb = -k2 * psib;
+            dsb = divvb / rpi.x;
+            if (work) rb -= divvb * divv / rpi.x;
         }
     }
     if (work) {
@@ -393,7 +453,7 @@ __global__ void __launch_bounds__(kPassThreads)
             const float e2 = (DIM == 3) ? xi.z - P.heat_center[2] : 0.f;
             const float ex = expf(-(e0 * e0 + e1 * e1 + e2 * e2) * P.heat_k);
             const float dub = abi.w;
-            pa[ADJ_Q0] += dub * ex / rho;
+            pacc(ADJ_Q0, dub * ex / rho);
             rb -= dub * P.heat_q0 * ex / (rho * rho);
             const float gx = -2.f * P.heat_k * dub * P.heat_q0 * ex / rho;
             xb[0] += gx * e0;
@@ -408,42 +468,47 @@ __global__ void __launch_bounds__(kPassThreads)
             const float ratio = rho * P.inv_rho0;
             const float r3 = ratio * ratio * ratio;
             rtot = rb - 2.f * Pb * pi / (rho * rho * rho) + pb * P.c0 * P.c0 * r3 * r3;
-            if (P.c0 > 0.f) pa[ADJ_C0] += pb * 2.f * pi / P.c0;
+            if (P.c0 > 0.f) pacc(ADJ_C0, pb * 2.f * pi / P.c0);
         }
         rhobar[s] = rtot;
         xF[s] = make_float4(xb[0], xb[1], xb[2], 0.f);
-        vhb[s] = make_float4(vb[0], vb[1], vb[2], 0.f);
+        // .w: u_half_bar (the predicted energy of artificial heat)
+        vhb[s] = make_float4(vb[0], vb[1], vb[2], ah ? uhb : 0.f);
     } else if (valid) {
         rhobar[s] = 0.f;
         xF[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         vhb[s] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    // Deterministic per-block partial sums of the parameter cotangents.
+    if (valid && divsb) divsb[s] = dsb;
+    // Deterministic per-block partial sums of the parameter cotangents, in
+    // double (a fixed shuffle order, then the warps in order).
 #pragma unroll
     for (int q = 0; q < ADJ_NPARAM; ++q) {
-        float v = pa[q];
+        double v = (double)pa[q] + (double)palo[q];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if ((tid & 31) == 0) s_red[q][tid >> 5] = v;
     }
     __syncthreads();
     if (tid < ADJ_NPARAM) {
-        float v = 0.f;
+        double v = 0.0;
         for (int w2 = 0; w2 < kPassThreads / 32; ++w2) v += s_red[tid][w2];
         block_part[blockIdx.x * ADJ_NPARAM + tid] = v;
     }
 }
 
-// Density reverse (rho_i = m_i W(0) + sum m_j W_ij), assembly, scatter to the
-// slot order of the step's input (perm: cell slot -> input slot).
+// Density reverse (rho_i = m_i W(0) + sum m_j W_ij), the reverse of the
+// divergence sums of artificial heat (divs_i = sum_j m_j G_ij (vh_j - vh_i) .
+// d_ij, cotangents divsb), assembly, scatter to the slot order of the step's
+// input (perm: cell slot -> input slot).
 template <int DIM>
 __global__ void __launch_bounds__(kPassThreads)
     k_adj_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
                   const DevGrid* __restrict__ gp, DevParams P, StepArgs S,
                   const float* __restrict__ rhobar, const float4* __restrict__ xF,
                   const float4* __restrict__ vhb, const float4* __restrict__ xpart,
-                  const float4* __restrict__ vpart, const int* __restrict__ perm, AdjState Gp,
-                  int n) {
+                  const float4* __restrict__ vpart, const float* __restrict__ divsb,
+                  const int* __restrict__ perm, AdjState Gp, int n) {
     __shared__ int s_list[kListCap][kPassThreads];
     const int tid = threadIdx.x;
     const int s = blockIdx.x * blockDim.x + tid;
@@ -460,7 +525,9 @@ __global__ void __launch_bounds__(kPassThreads)
     const float mi = mass_of<DIM>(xi, vi);
     CellCoord cc = {{0, 0, 0}};
     if (work) cc = decode_key<DIM>(keys[s], g);
-    float xb[3] = {0.f, 0.f, 0.f};
+    const bool ah = P.heat_art != 0 && divsb != nullptr;
+    const float dsi = (work && ah) ? divsb[s] : 0.f;
+    float xb[3] = {0.f, 0.f, 0.f}, vdb[3] = {0.f, 0.f, 0.f};
     NbrStream<DIM> ns;
     nbr_init<DIM>(ns, B, g, s, work);
     while (__any_sync(0xffffffffu, !ns.done)) {
@@ -470,25 +537,44 @@ __global__ void __launch_bounds__(kPassThreads)
             if (t >= nl) continue;
             const int j = s_list[t][tid];
             const float4 xj = __ldg(B.xh + j);
-            float mj;
-            if (DIM == 2) mj = xj.z;
-            else mj = __ldg(&B.vm[j].w);
+            float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 3 || ah) vj = __ldg(B.vm + j);
+            const float mj = mass_of<DIM>(xj, vj);
             const float rbj = __ldg(rhobar + j);
             PairGeo<DIM> pg;
             pair_geo<DIM>(xi, xj, g, P, pg);
             const float c = (rbi * mj + rbj * mi) * pg.G;
 #pragma unroll
             for (int k = 0; k < DIM; ++k) xb[k] = fmaf(c, pg.d[k], xb[k]);
+            if (ah) {
+                // d/d(vh_s), d/d(x_s) of divs_s (weight dsb_s m_j) and of divs_j
+                // (weight dsb_j m_s, d_js = -d, w_js = -w): the same forms.
+                const float cd = dsi * mj + __ldg(divsb + j) * mi;
+                const float w[3] = {vj.x - vi.x, vj.y - vi.y, DIM == 3 ? vj.z - vi.z : 0.f};
+                float wd = w[0] * pg.d[0] + w[1] * pg.d[1];
+                if (DIM == 3) wd += w[2] * pg.d[2];
+#pragma unroll
+                for (int k = 0; k < DIM; ++k) {
+                    vdb[k] = fmaf(-cd * pg.G, pg.d[k], vdb[k]);
+                    xb[k] = fmaf(cd, pg.G * w[k] + pg.dGdr_r * pg.d[k] * wd, xb[k]);
+                }
+            }
         }
     }
     if (!valid) return;
     float4 gx = make_float4(0.f, 0.f, 0.f, 0.f), gv = gx, ga = gx;
     if (work) {
-        const float4 xp = xpart[s], f = xF[s], vh = vhb[s], vp = vpart[s];
+        const float4 xp = xpart[s], f = xF[s], vp = vpart[s];
+        float4 vh = vhb[s];
+        vh.x += vdb[0];
+        vh.y += vdb[1];
+        vh.z += vdb[2];
+        // u_half = max(0, u + hdt du_prev): no gradient where it clamped to 0
+        const float uh = (ah && B.rp[s].z != 0.f) ? vh.w : 0.f;
         gx = make_float4(xp.x + f.x + xb[0], xp.y + f.y + xb[1], xp.z + f.z + xb[2], 0.f);
         // predictor: vh = v + hdt a_prev (v_bar gets vh_bar; a_prev_bar = hdt vh_bar)
-        gv = make_float4(vp.x + vh.x, vp.y + vh.y, vp.z + vh.z, vp.w);
-        ga = make_float4(S.hdt * vh.x, S.hdt * vh.y, S.hdt * vh.z, 0.f);
+        gv = make_float4(vp.x + vh.x, vp.y + vh.y, vp.z + vh.z, vp.w + uh);
+        ga = make_float4(S.hdt * vh.x, S.hdt * vh.y, S.hdt * vh.z, S.hdt * uh);
     }
     const int j = perm[s];
     Gp.xb[j] = gx;
@@ -498,11 +584,11 @@ __global__ void __launch_bounds__(kPassThreads)
 
 // Adds the step's parameter cotangents (block partials, fixed order) to acc.
 __global__ void __launch_bounds__(256)
-    k_adj_params(const float* __restrict__ block_part, int nblocks, double* __restrict__ acc) {
+    k_adj_params(const double* __restrict__ block_part, int nblocks, double* __restrict__ acc) {
     __shared__ double s[ADJ_NPARAM][256];
     for (int q = 0; q < ADJ_NPARAM; ++q) {
         double v = 0.0;
-        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += (double)block_part[b * ADJ_NPARAM + q];
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v += block_part[b * ADJ_NPARAM + q];
         s[q][threadIdx.x] = v;
     }
     __syncthreads();

@@ -152,7 +152,9 @@ struct armando_ctx {
     AdjState adjG{}, adjGp{};            // cotangents (output / input slot order)
     float4 *adj_abar = nullptr, *adj_xpart = nullptr, *adj_vpart = nullptr, *adj_xF = nullptr,
            *adj_vhb = nullptr;
-    float *adj_rhobar = nullptr, *adj_pbar = nullptr, *adj_blk = nullptr;
+    float *adj_rhobar = nullptr, *adj_pbar = nullptr;
+    double* adj_blk = nullptr;   // per-block parameter cotangents
+    float* adj_divsb = nullptr;  // cotangents of the divergence sums (artificial heat)
     double* adj_pacc = nullptr;
     int adj_its0 = 0, adj_steps = 0, adj_K = 0;
     float adj_dt = 0.f;
@@ -1737,11 +1739,13 @@ armando_status alloc_adjoint(armando_ctx* ctx) {
     ctx->adj_vhb = dalloc<float4>(n, e);
     ctx->adj_rhobar = dalloc<float>(n, e);
     ctx->adj_pbar = dalloc<float>(n, e);
-    ctx->adj_blk = dalloc<float>((size_t)blocks_for(ctx->n, kPassThreads) * ADJ_NPARAM + 4, e);
+    ctx->adj_blk = dalloc<double>((size_t)blocks_for(ctx->n, kPassThreads) * ADJ_NPARAM + 4, e);
     ctx->adj_pacc = dalloc<double>(ADJ_NPARAM, e);
+    if (ctx->prm.heat_artificial) ctx->adj_divsb = dalloc<float>(n, e);
     for (void* p : {(void*)ctx->adj_abar, (void*)ctx->adj_xpart, (void*)ctx->adj_vpart,
                     (void*)ctx->adj_xF, (void*)ctx->adj_vhb, (void*)ctx->adj_rhobar,
-                    (void*)ctx->adj_pbar, (void*)ctx->adj_blk, (void*)ctx->adj_pacc})
+                    (void*)ctx->adj_pbar, (void*)ctx->adj_blk, (void*)ctx->adj_pacc,
+                    (void*)ctx->adj_divsb})
         ctx->owned.push_back(p);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(adjoint)");
     return ARMANDO_OK;
@@ -1764,9 +1768,10 @@ armando_status alloc_tape(armando_ctx* ctx, int count) {
         T.du = dalloc<float>(n, e);
         T.start = dalloc<int>((size_t)ctx->cell_cap + 1, e);
         T.grid = dalloc<DevGrid>(1, e);
+        if (ctx->prm.heat_artificial) T.ulo = dalloc<float>(n, e);
         for (void* p : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
                         (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm, (void*)T.du,
-                        (void*)T.start, (void*)T.grid})
+                        (void*)T.start, (void*)T.grid, (void*)T.ulo})
             ctx->owned.push_back(p);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "cudaMalloc(adjoint tape; a smaller checkpoint_every needs less)");
@@ -1806,11 +1811,12 @@ int launch_adjoint(armando_ctx* ctx, const StepArgs& S, const TapeSlot& T) {
                                                   ctx->adj_xpart, ctx->adj_vpart, n);
     k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
                                                  ctx->adj_abar, ctx->adj_pbar, ctx->adj_rhobar,
-                                                 ctx->adj_xF, ctx->adj_vhb, ctx->adj_blk, n);
+                                                 ctx->adj_xF, ctx->adj_vhb, ctx->adj_divsb,
+                                                 ctx->adj_blk, n);
     k_adj_density<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
                                                    ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb,
-                                                   ctx->adj_xpart, ctx->adj_vpart, T.perm,
-                                                   ctx->adjGp, n);
+                                                   ctx->adj_xpart, ctx->adj_vpart, ctx->adj_divsb,
+                                                   T.perm, ctx->adjGp, n);
     k_adj_params<<<1, 256, 0, st>>>(ctx->adj_blk, nb, ctx->adj_pacc);
     return 4;
 }
@@ -1826,11 +1832,10 @@ armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
 armando_status check_adjoint_support(armando_ctx* ctx) {
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
     const armando_params& p = ctx->prm;
-    if (p.pa_sph != 1 || p.visc || p.heat_artificial || p.wall_model != 0 || p.scheme != 0 ||
-        step_options(p))
+    if (p.pa_sph != 1 || p.visc || p.wall_model != 0 || p.scheme != 0 || step_options(p))
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
                     "reverse mode supports pa_sph = 1, wall_model 0, summation density, without "
-                    "physical viscosity, artificial heat, XSPH or h evolution");
+                    "physical viscosity, XSPH or h evolution");
     return ARMANDO_OK;
 }
 
@@ -2223,7 +2228,7 @@ armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
         for (const TapeSlot& T : ctx->tape)
             for (void* q : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
                             (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm,
-                            (void*)T.du, (void*)T.start, (void*)T.grid})
+                            (void*)T.du, (void*)T.start, (void*)T.grid, (void*)T.ulo})
                 release(ctx, q);
         ctx->tape.clear();
     }

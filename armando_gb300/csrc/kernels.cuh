@@ -1128,9 +1128,15 @@ static_assert(kListCap2 <= 32 * mask_words<2>() && kListCap3 <= 32 * mask_words<
               "a list's neighbour bits fit one lane's mask");
 constexpr int kListCapD = 24;     // density pass: near and far lists each
 constexpr int kTestBatch = 4;     // candidate loads issued together
-// Density pairs with q = r/h < kNearQ are evaluated in float-float, the others
-// (W below ~1% of W(0) each) in FP32.
-constexpr float kNearQ = 1.6f;
+// 2D density pairs with q = r/h < near_q() are evaluated in float-float, the
+// others (W below ~1% of W(0) each, ~8 of ~20 pairs) in FP32. In 3D every pair
+// is float-float: ~50 of ~80 pairs lie beyond q = 1.6, and the FP32 rounding of
+// their sum (a few 1e-7 of ~1% of rho each) would exceed 1e-5 of the pressure
+// of a quiescent flow, whose p is ~1e-5 of rho0 c0^2.
+template <int DIM>
+__host__ __device__ constexpr float near_q() {
+    return DIM == 2 ? 1.6f : 2.0f;
+}
 
 // Candidate rows: for each (dy, dz) in [-f, f]^(DIM-1) the cells cx-f..cx+f of
 // that row are consecutive keys, so one contiguous slot range. On a periodic x
@@ -1327,19 +1333,20 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     if (sub != 0) S = Wn = sph::ff{0.f, 0.f};
     const float ihf = ih_i.hi;
     const float kgih_i = __fmul_rn(P.kg, pow_grad<DIM>(ihf));
-    const float kwf = P.kw_hi * (DIM == 2 ? ihf * ihf : ihf * ihf * ihf);
     float divs = 0.f;
     constexpr int W = mask_words<DIM>() / TPP;  // mask words of this lane
     const size_t mlane = (size_t)s * TPP + sub;
     Cursor cu = cursor_begin<DIM>(g);
     bool done = !work;
-    const bool mask_on = work && fluid;
+    // (listed particles, LST, need no bits: the force pass re-tests their list)
+    bool mask_on = work && fluid;
     int ord = 0;  // candidate ordinal (cursor order, self included)
     int wb = 0;   // the accumulator holds the bits of ordinals 32 wb .. 32 wb + 63
     unsigned long long cur = 0ull;
     int shift = 0;  // staged index - slot in the cursor's row
     const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // list entries (-1: walk the cells)
     int lt = 0;
+    if (LST && lc >= 0) mask_on = false;
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
         // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
@@ -1390,10 +1397,12 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 const int k = kb[u];
                 if (u >= cnt || k == s || !pair_delta<DIM>(xi, xb[u], g, d, dr2)) continue;
                 pb |= 1u << u;
-                const float hs = xi.w + xb[u].w;  // near: q < kNearQ with h = hs/2
+                const float hs = xi.w + xb[u].w;  // near: q < near_q() with h = hs/2
                 const LT e = (LT)(STG ? k + shift : k);
-                if (dr2 < (0.25f * kNearQ * kNearQ) * hs * hs) s_near[nn++][tid] = e;
-                else s_far[nf++][tid] = e;
+                if (DIM == 3 || dr2 < (0.25f * near_q<DIM>() * near_q<DIM>()) * hs * hs)
+                    s_near[nn++][tid] = e;
+                else
+                    s_far[nf++][tid] = e;
             }
             if (ord - 32 * wb >= 32) {  // word wb is complete
                 if (mask_on && wb < W) B.nmask[mask_word_index<W>(wb, B.mstride, mlane)] = (unsigned)cur;
@@ -1447,18 +1456,33 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             float d[3], dr2;
             pair_delta<DIM>(xi, xj, g, d, dr2);
             refine_periodic<DIM>(xi, xj, g, d, dr2);
-            float ih = ihf, kgih = kgih_i, kwh = kwf;
+            // With uniform h and m every pair would share the rounding of
+            // K m / h^dim and of 1/h: a bias that adds up over the far pairs.
+            // So the prefactor and 1/h stay float-float, r is the
+            // Newton-corrected square root, and q is rounded once.
+            sph::ff ih = ih_i, al = al_i;
+            float kgih = kgih_i;
             if (xj.w != xi.w) {
-                ih = __fdividef(2.0f, xi.w + xj.w);
-                kgih = P.kg * pow_grad<DIM>(ih);
-                kwh = P.kw_hi * (DIM == 2 ? ih * ih : ih * ih * ih);
+                ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+                al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
+                kgih = P.kg * pow_grad<DIM>(ih.hi);
             }
-            const float q = __fmul_rn(fast_sqrt_pos(dr2), ih);
+            float r = 0.f;
+            if (dr2 > 0.f) {
+                const float rs = rsqrtf(dr2);
+                r = __fmul_rn(dr2, rs);
+                r = fmaf(fmaf(-r, r, dr2), 0.5f * rs, r);
+            }
+            // one rounding of r (ih.hi + ih.lo): rounding r ih.hi first and then
+            // adding r ih.lo would lose the correction, the same way for all pairs
+            const float q = fmaf(r, ih.hi, __fmul_rn(r, ih.lo));
             if (fluid) {
                 float tt = fmaf(-0.5f, q, 1.0f);
                 tt = tt * tt;
                 tt = tt * tt;
-                const float wm = kwh * mj * tt * fmaf(2.0f, q, 1.0f);
+                const float f = tt * fmaf(2.0f, q, 1.0f);
+                const sph::ff c = sph::ff_mul_f(al, mj);
+                const float wm = fmaf(c.hi, f, __fmul_rn(c.lo, f));
                 sph::ff_acc(S, sph::ff{wm, 0.f});
                 if (nor) sph::ff_acc(Wn, sph::ff{__fdiv_rn(wm, __ldg(B.q + k)), 0.f});
             }
@@ -1670,14 +1694,17 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     bool from_mask = false;
     uint4 ch = make_uint4(0u, 0u, 0u, 0u);  // mask chunk being decoded
     unsigned wbits = 0u;                    // bits left of word wi
-    if (work) {
+    // A listed particle walks its neighbour list (coalesced rows of entries)
+    // and re-tests each entry; the others decode the density pass's bits.
+    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;
+    int lt = 0;
+    if (work && !(LST && lc >= 0)) {
         ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, 0);
         wbits = ch.x;
         from_mask = !(ch.x == ~0u && (W == 1 || ch.y == ~0u));
     }
     int wi = 0, rbase = 0;  // index of wbits; ordinal of the cursor row's first slot
     int shift = 0;          // staged index - slot in the cursor's row
-    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // bits index list entries
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
         while (!done && from_mask) {
@@ -1693,10 +1720,6 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             }
             const int o = 32 * wi + __ffs(wbits) - 1;
             wbits &= wbits - 1u;
-            if (LST && lc >= 0) {
-                s_list[nl++][tid] = (LT)__ldg(B.nlist + (size_t)o * B.lstride + s);
-                continue;
-            }
             bool in_rows = true;
             while (o >= rbase + lane_len<TPP>(cu)) {  // move to the range holding ordinal o
                 rbase += lane_len<TPP>(cu);
@@ -1714,31 +1737,49 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
             s_list[nl++][tid] = (LT)(cu.k + TPP * (o - rbase) + (STG ? shift : 0));
         }
         while (!done && !from_mask) {
-            if (cu.k >= cu.ke) {
-                if (!cursor_next<DIM>(g, start, cc, cu)) {
+            int kb[kTestBatch];
+            int cnt;
+            float4 xb[kTestBatch];
+            if (LST && lc >= 0) {
+                if (lt >= lc) {
                     done = true;
                     break;
                 }
-                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
-                if (TPP > 1) {
-                    cu.k += sub;
-                    continue;
-                }
-            }
-            if (nl > kListCap - kTestBatch) break;
-            const int k0 = cu.k;
-            const int cnt = min(kTestBatch, lane_len<TPP>(cu));
-            float4 xb[kTestBatch];
+                if (nl > kListCap - kTestBatch) break;
+                cnt = min(kTestBatch, lc - lt);
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u) {
-                const int ku = min(k0 + u * TPP, cu.ke - 1);
-                xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                for (int u = 0; u < kTestBatch; ++u)
+                    kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
+#pragma unroll
+                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + kb[u]);
+                lt += cnt;
+            } else {
+                if (cu.k >= cu.ke) {
+                    if (!cursor_next<DIM>(g, start, cc, cu)) {
+                        done = true;
+                        break;
+                    }
+                    if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
+                    if (TPP > 1) {
+                        cu.k += sub;
+                        continue;
+                    }
+                }
+                if (nl > kListCap - kTestBatch) break;
+                const int k0 = cu.k;
+                cnt = min(kTestBatch, lane_len<TPP>(cu));
+#pragma unroll
+                for (int u = 0; u < kTestBatch; ++u) {
+                    const int ku = min(k0 + u * TPP, cu.ke - 1);
+                    kb[u] = k0 + u * TPP;
+                    xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                }
+                cu.k += cnt * TPP;
             }
-            cu.k += cnt * TPP;
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 float d[3], dr2;
-                const int k = k0 + u * TPP;
+                const int k = kb[u];
                 if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
                     s_list[nl++][tid] = (LT)(STG ? k + shift : k);
             }

@@ -203,3 +203,89 @@ def test_torch_autograd_wrapper(O):
     _, ref = gpu_gradients(c, spec, K=2)
     assert np.array_equal(v0.grad.numpy(), ref["v"])
     assert alpha.grad.item() == pytest.approx(ref["params"]["av_alpha"], rel=1e-6)
+
+
+def heat_case(dim):
+    """Artificial heat on (art_heat.f:42-97, g1 = 0.1, g2 = 1.0) with a
+    nonuniform energy field, so psi, the energy differences and the divergence
+    (compressing and expanding regions) all carry gradient."""
+    if dim == 2:
+        c = cases.perturbed(cases.dam_break(dx=0.05), seed=72, dv=0.3, du=200.0)
+    else:
+        c = cases.perturbed(cases.channel(n_x=16, n_yz=8, length=16 * 7.9e-4, width=8 * 7.9e-4,
+                                          layers=2, jitter=0.01), seed=73, dv=0.05, du=200.0)
+        c.params.heat_external = 0
+    c.params.heat_artificial = 1
+    c.params.ah_g1, c.params.ah_g2 = 0.1, 1.0
+    return c
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("steps,tol", [(1, TOL_ONE), (STEPS, TOL_GRAD)])
+def test_art_heat_gradients_match_tangent_linear(O, dim, steps, tol):
+    c = heat_case(dim)
+    spec = spec_for(O) if dim == 2 else O.LossSpec.make(
+        w_ke=1.0, w_p=1e-4, w_u=0.1, c=(0.006, 0.003, 0.003), radius=0.006, w_ref=1.0)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.forward_checkpointed(got, c.dt, 1, steps, 2)
+        _, cot = loss_and_cotangents(got.arrays(), c.dim, c.mass, c.itype, spec)
+        g = ctx.backward(**cot)
+    checks = {}
+    for k, name in enumerate(["av_alpha", "c0"]):
+        dp = [0.0] * 4
+        dp[2 * k] = 1.0
+        checks[name] = (g["params"][name], O.tangent(O.State(c), 1, steps, c.dt, spec, dparam=dp)[1])
+    for which in ("x", "v", "u"):
+        d = _direction(c, which)
+        checks[which] = (float(np.dot(g[which].astype(np.float64), d)),
+                         O.tangent(O.State(c), 1, steps, c.dt, spec, **_seed_kw(which, d))[1])
+    for k, (a, b) in checks.items():
+        e = _rel(a, b)
+        print(dim, steps, k, a, b, f"{e:.2e}")
+        assert e <= tol, (k, a, b, e)
+
+
+def test_full_size_c5_adjoint_against_tangent_linear(O):
+    """The benchmark's reverse-mode workload itself: the 2D dam break of
+    260,904 particles (cases.adjoint_dam_break, initial v ~ N(0, 0.01 m/s)),
+    checkpoint every 50 iterations over 51 iterations, so the backward sweep
+    replays the first segment from its checkpoint. The loss is the benchmark's
+    (final kinetic energy + mean pressure of a probe inside the column). alpha,
+    c0 and two initial-velocity directions against the FP64 tangent-linear:
+    within 1e-4, or within the FP64 gradient's own change when the inputs move
+    by one ulp where that is larger. The eight FP64 runs go in parallel."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    c = cases.adjoint_dam_break()
+    assert c.n == 260_904
+    steps, K = 51, 50
+    fl = c.itype > 0
+    (cx, cy, _), radius = cases.ADJOINT_PROBE
+    xx = c.x.reshape(-1, 2).astype(np.float64)
+    t = 1.0 - ((xx - np.array([cx, cy])) ** 2).sum(1) / radius ** 2
+    w_ref = float(np.where((t > 0) & fl, t ** 3, 0.0).sum())
+    spec = O.LossSpec.make(w_ke=1.0, w_p=1.0, w_u=0.0, c=(cx, cy), radius=radius, w_ref=w_ref)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.forward_checkpointed(got, c.dt, 1, steps, K)
+        _, cot = loss_and_cotangents(got.arrays(), c.dim, c.mass, c.itype, spec)
+        g = ctx.backward(**cot)
+    rng = np.random.default_rng(74)
+    dirs = [rng.standard_normal(c.n * 2) * np.repeat(fl, 2) for _ in range(2)]
+    twin = c.copy()
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    twin.x = np.where(np.repeat(fl, 2), np.nextafter(c.x, bump), c.x).astype(np.float32)
+    jobs = []
+    for case in (c, twin):
+        jobs += [(case, {"dparam": [1.0, 0.0, 0.0, 0.0]}), (case, {"dparam": [0.0, 0.0, 1.0, 0.0]})]
+        jobs += [(case, {"dv0": d}) for d in dirs]
+    with ThreadPoolExecutor(len(jobs)) as ex:
+        res = list(ex.map(lambda j: O.tangent(O.State(j[0]), 1, steps, c.dt, spec, **j[1])[1], jobs))
+    ref, ref2 = res[:4], res[4:]
+    got_vals = [g["params"]["av_alpha"], g["params"]["c0"]] + [
+        float(np.dot(g["v"].astype(np.float64), d)) for d in dirs]
+    for name, a, b, b2 in zip(("alpha", "c0", "v dir 1", "v dir 2"), got_vals, ref, ref2):
+        err, cond = _rel(a, b), _rel(b2, b)
+        print("C5", name, a, b, f"err {err:.2e} ulp-conditioning {cond:.2e}")
+        assert err <= max(TOL_GRAD, cond), (name, a, b, err, cond)
