@@ -372,6 +372,25 @@ class Batch(Context):
             self.sync()
         return s
 
+    def autotune_batch(self, s, dts, its0: int, steps_per_trial: int = 5):
+        """Times the candidate tunings that apply to a batch (one thread per
+        particle, skin 0: the reach) on the packed state `s` (not modified),
+        keeps the fastest; returns (best (reach, tpp, block, skin),
+        {tuning: ms per step})."""
+        a = s.arrays() if hasattr(s, "arrays") else s
+        self._validate(a)
+        d = np.ascontiguousarray(dts, np.float32)
+        if d.size != self.n_instances:
+            raise ValueError("one dt per instance")
+        best = Tuning()
+        ms = (C.c_float * N_TUNINGS)()
+        self._check(self._lib.armando_batch_autotune(
+            self._h, _ptr(a["x"]), _ptr(a["v"]), _ptr(a["mass"]), _ptr(a["rho"]), _ptr(a["p"]),
+            _ptr(a["u"]), _ptr(a["h"]), _ptr(a["itype"]), _ptr(a["dvdt"]), _ptr(a["dudt"]),
+            d.ctypes.data_as(C.c_void_p), int(its0), int(steps_per_trial), C.byref(best), ms))
+        cands = self.tuning_candidates()
+        return best.as_tuple(), {cands[k]: float(ms[k]) for k in range(N_TUNINGS) if ms[k] > 0}
+
 
 # ---- particle decks and snapshots (host only) ------------------------------------
 

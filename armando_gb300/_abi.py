@@ -262,6 +262,7 @@ EXPORTED = [
     "armando_batch_create", "armando_batch_integrate",
     "armando_forward_checkpointed", "armando_backward",
     "armando_get_tuning", "armando_set_tuning", "armando_tuning_candidate", "armando_autotune",
+    "armando_batch_autotune",
     "armando_deck_count", "armando_deck_read", "armando_deck_write", "armando_write_vtk",
     "armando_set_materials", "armando_get_hsml", "armando_set_open_boundaries",
     "armando_integrate_open", "armando_set_zones",
@@ -338,6 +339,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.armando_autotune.argtypes = [vp] * 11 + [C.c_float, C.c_int32, C.c_int32,
                                                  C.POINTER(Tuning), C.POINTER(C.c_float)]
     lib.armando_autotune.restype = C.c_int
+    lib.armando_batch_autotune.argtypes = [vp] * 12 + [C.c_int32, C.c_int32,
+                                                       C.POINTER(Tuning), C.POINTER(C.c_float)]
+    lib.armando_batch_autotune.restype = C.c_int
     lib.armando_cell_ids_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int64, vp, vp]
     lib.armando_cell_ids_noalloc.restype = C.c_int
     cp = C.c_char_p

@@ -42,8 +42,11 @@ void set_last_error(const char* msg) {
 struct GraphKey {
     float kdt, hdt, dt;
     int heat_on;
+    int par;  // 0: one state buffer; 1, 2: which of the two is current (fused predictor)
+    int lst;  // neighbour lists in use
     bool operator<(const GraphKey& o) const {
-        return std::tie(kdt, hdt, dt, heat_on) < std::tie(o.kdt, o.hdt, o.dt, o.heat_on);
+        return std::tie(kdt, hdt, dt, heat_on, par, lst) <
+               std::tie(o.kdt, o.hdt, o.dt, o.heat_on, o.par, o.lst);
     }
 };
 
@@ -80,6 +83,11 @@ struct armando_ctx {
     // Neighbour lists between sorts (ARMANDO_NEIGHBOUR_LISTS=0 at creation:
     // walk the cells every iteration; 2D results are the same bits).
     bool lists = true;
+    // Fused predictor on the iterations between sorts (ARMANDO_FUSED_PREDICTOR=0
+    // at creation: a reorder copy every iteration; the same bits).
+    bool fuse_ok = true;
+    // Inside armando_forward_checkpointed or a replay of armando_backward.
+    bool reverse_run = false;
     armando_params prm{};
     DevParams dp{};
     int dim = 2;
@@ -137,6 +145,7 @@ struct armando_ctx {
     int* d_queue = nullptr;                 // [4] work-queue heads, reset every step
     int* d_its = nullptr;
     int any_visc = 0;
+    bool batch_lean = false;  // every instance has lean physics: the lean passes
     int grid_density = 0, grid_shear = 0, grid_force = 0;  // persistent CTAs
     cudaGraphExec_t batch_graph = nullptr;
     // Reverse mode (armando_forward_checkpointed / armando_backward).
@@ -179,6 +188,10 @@ struct armando_ctx {
     std::vector<float> inlet_dist;
     OpenSpec open{};
     StateA A2{};
+    // Fused predictor (lazily sorting, lean physics, lists): the force pass
+    // writes the next state into A_alt, then the two swap; acur counts swaps.
+    StateA A_alt{};
+    int acur = 0;
     bool open_ready = false;
     int *open_keep = nullptr, *d_open_n = nullptr, *h_open_n = nullptr;
     unsigned *open_tc = nullptr, *open_to = nullptr;
@@ -403,9 +416,12 @@ bool lazy(const armando_ctx* ctx) { return ctx->tune.skin > 0 && ctx->n_inst == 
 // Neighbour lists: a lazily sorting CERN step with one lane per particle and
 // the lists allocated (ensure_lists); the iterations between sorts then read
 // the lists instead of walking the cells.
+// Not in reverse mode: its iterations sort every time, and the adjoint passes
+// decode the neighbour bits that the density pass leaves only for particles
+// walking their cells.
 bool use_lists(const armando_ctx* ctx) {
     return lazy(ctx) && ctx->tune.threads_per_particle == 1 && ctx->prm.scheme == 0 &&
-           ctx->B.nlist != nullptr;
+           ctx->B.nlist != nullptr && !ctx->reverse_run;
 }
 
 template <int DIM>
@@ -483,6 +499,29 @@ bool sorts_every_step(const armando_params& p) {
     return p.wall_model == 3 || p.sle != 0;
 }
 
+// The passes read the state themselves on iterations that do not sort (no
+// reorder copy) and write the next state into the other buffer: lists, lean
+// physics, no step option.
+bool fused_wanted(const armando_ctx* ctx) {
+    return ctx->fuse_ok && use_lists(ctx) && lean_physics(ctx->dp) && !step_options(ctx->prm);
+}
+bool fused(const armando_ctx* ctx) { return fused_wanted(ctx) && ctx->A_alt.xh != nullptr; }
+
+// After a fused iteration the next state is in A_alt: make it current.
+void swap_state(armando_ctx* ctx) {
+    StateA& a = ctx->A;
+    StateA& b = ctx->A_alt;
+    std::swap(a.xh, b.xh);
+    std::swap(a.vm, b.vm);
+    std::swap(a.u, b.u);
+    std::swap(a.ap, b.ap);
+    std::swap(a.rho, b.rho);
+    std::swap(a.p, b.p);
+    std::swap(a.itype, b.itype);
+    std::swap(a.id, b.id);
+    ctx->acur ^= 1;
+}
+
 // The staged passes serve one thread per particle, lean physics, no periodic
 // axis, no single_step option and no mirror ghosts (the other variants read
 // their candidates from global memory).
@@ -514,8 +553,10 @@ void launch_force_staged(armando_ctx* ctx, const unsigned* skeys, const StepArgs
 }
 
 template <int DIM>
-void launch_density(armando_ctx* ctx, const unsigned* skeys) {
+void launch_density(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     const int n = (int)ctx->n_work;
+    const bool fuse = fused(ctx);
+    const FusedSrc F{ctx->A, fuse ? resort_flags(ctx) : nullptr, S.hdt};
     if (staged_passes(ctx)) {
         if (ctx->tune.block == 256) launch_density_staged<DIM, 256>(ctx, skeys);
         else launch_density_staged<DIM, 128>(ctx, skeys);
@@ -526,14 +567,25 @@ void launch_density(armando_ctx* ctx, const unsigned* skeys) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
         constexpr bool OPT = decltype(opt)::value, LST = decltype(lst)::value;
-        k_density<DIM, T, BSZ, PER, LEAN, OPT, LST><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
-            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
+        constexpr bool FUS_OK = LST && LEAN && !OPT;
+        const int grid = blocks_for((int64_t)n * T, BSZ);
+        if constexpr (FUS_OK) {
+            if (fuse) {
+                k_density<DIM, T, BSZ, PER, LEAN, OPT, LST, true><<<grid, BSZ, 0, ctx->stream>>>(
+                    ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n, F);
+                return;
+            }
+        }
+        k_density<DIM, T, BSZ, PER, LEAN, OPT, LST><<<grid, BSZ, 0, ctx->stream>>>(
+            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n, F);
     });
 }
 
 template <int DIM>
 void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     const int n = (int)ctx->n_work;
+    const bool fuse = fused(ctx);
+    const FusedSrc F{ctx->A, fuse ? resort_flags(ctx) : nullptr, S.hdt};
     if (staged_passes(ctx)) {
         if (ctx->tune.block == 256) launch_force_staged<DIM, 256>(ctx, skeys, S);
         else launch_force_staged<DIM, 128>(ctx, skeys, S);
@@ -544,8 +596,17 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
         constexpr int T = decltype(tpp)::value, BSZ = decltype(bs)::value;
         constexpr bool PER = decltype(per)::value, LEAN = decltype(lean)::value && T == 1;
         constexpr bool OPT = decltype(opt)::value, LST = decltype(lst)::value;
-        k_force<DIM, T, BSZ, PER, LEAN, OPT, LST><<<blocks_for((int64_t)n * T, BSZ), BSZ, 0, ctx->stream>>>(
-            ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n);
+        constexpr bool FUS_OK = LST && LEAN && !OPT;
+        const int grid = blocks_for((int64_t)n * T, BSZ);
+        if constexpr (FUS_OK) {
+            if (fuse) {  // the next state into the other buffer
+                k_force<DIM, T, BSZ, PER, LEAN, OPT, LST, true><<<grid, BSZ, 0, ctx->stream>>>(
+                    ctx->B, ctx->A_alt, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n, F);
+                return;
+            }
+        }
+        k_force<DIM, T, BSZ, PER, LEAN, OPT, LST><<<grid, BSZ, 0, ctx->stream>>>(
+            ctx->B, ctx->A, skeys, ctx->start, ctx->grid, ctx->dp, S, ctx->flags, n, F);
     });
 }
 
@@ -556,8 +617,9 @@ int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     const int n = (int)ctx->n_work;
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
-    launch_density<DIM>(ctx, skeys);
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs,
+                                                           fused(ctx));
+    launch_density<DIM>(ctx, skeys, S);
     int L = 2;
     if (n > ctx->n) {  // mirror ghosts take their owners' density, pressure, energy
         k_invert_ids<<<blocks_for(n, 256), 256, 0, st>>>(ctx->B.id, ctx->g_slot, n);
@@ -768,9 +830,14 @@ int launch_batch_step(armando_ctx* ctx, cudaEvent_t* ev) {
     k_reorder_batch<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, ctx->d_params,
                                                              ctx->d_its, n);
     if (ev) cudaEventRecord(ev[3], st);
-    k_density_batch<DIM><<<ctx->grid_density, kPassThreads, 0, st>>>(
-        ctx->B, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_items, ctx->n_items,
-        ctx->d_queue + 0);
+    if (ctx->batch_lean)
+        k_density_batch<DIM, true><<<ctx->grid_density, kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_items, ctx->n_items,
+            ctx->d_queue + 0);
+    else
+        k_density_batch<DIM><<<ctx->grid_density, kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_items, ctx->n_items,
+            ctx->d_queue + 0);
     if (ev) cudaEventRecord(ev[4], st);
     L += 3;
     if (ctx->any_visc) {
@@ -780,9 +847,14 @@ int launch_batch_step(armando_ctx* ctx, cudaEvent_t* ev) {
         ++L;
     }
     if (ev) cudaEventRecord(ev[5], st);
-    k_force_batch<DIM><<<ctx->grid_force, kPassThreads, 0, st>>>(
-        ctx->B, ctx->A, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_its, ctx->flags,
-        ctx->d_items, ctx->n_items, ctx->d_queue + 2);
+    if (ctx->batch_lean)
+        k_force_batch<DIM, true><<<ctx->grid_force, kPassThreads, 0, st>>>(
+            ctx->B, ctx->A, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_its, ctx->flags,
+            ctx->d_items, ctx->n_items, ctx->d_queue + 2);
+    else
+        k_force_batch<DIM><<<ctx->grid_force, kPassThreads, 0, st>>>(
+            ctx->B, ctx->A, skeys, ctx->start, ctx->d_grids, ctx->d_params, ctx->d_its, ctx->flags,
+            ctx->d_items, ctx->n_items, ctx->d_queue + 2);
     k_advance_its<<<1, 1, 0, st>>>(ctx->d_its);
     if (ev) cudaEventRecord(ev[6], st);
     return L + 2;
@@ -828,9 +900,10 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     k_cell_start<<<blocks_for((int64_t)n + 1, kCellStartThreads), kCellStartThreads, 0, st>>>(skeys, n, &ctx->grid->ncells,
                                                                    (int)ctx->cell_cap, ctx->start, rs);
     if (use_lists(ctx)) L += launch_build_list<DIM>(ctx, rs, st);
-    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs);
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs,
+                                                           fused(ctx));
     cudaEventRecord(ev[3], st);
-    launch_density<DIM>(ctx, skeys);
+    launch_density<DIM>(ctx, skeys, S);
     cudaEventRecord(ev[4], st);
     L += 3;
     if (ctx->dp.visc) {
@@ -906,11 +979,19 @@ armando_status run_ghost_step(armando_ctx* ctx, const StepArgs& S) {
     return ARMANDO_OK;
 }
 
+armando_status alloc_stateA(armando_ctx* ctx, StateA& a);
+
 armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     if (ctx->n_inst > 1) return run_batch_step(ctx);
     if (ctx->prm.wall_model == 3)
         return ctx->dim == 2 ? run_ghost_step<2>(ctx, S) : run_ghost_step<3>(ctx, S);
-    GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on};
+    if (fused_wanted(ctx) && !ctx->A_alt.xh) {  // the second state buffer, on first use
+        armando_status as = alloc_stateA(ctx, ctx->A_alt);
+        if (as != ARMANDO_OK) return as;
+        free_graphs(ctx);
+    }
+    const bool fuse = fused(ctx);
+    GraphKey key{S.kdt, S.hdt, S.dt, S.heat_on, fuse ? 1 + ctx->acur : 0, use_lists(ctx) ? 1 : 0};
     auto itg = ctx->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
     if (itg == ctx->graphs.end() && lazy(ctx) && !ctx->no_conditional) {
@@ -957,6 +1038,7 @@ armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     ctx->launches += ctx->launches_per_step - ctx->lazy_body;
     ctx->steps_done += 1;
     if (!lazy(ctx)) ctx->sorts_host += 1;
+    if (fuse) swap_state(ctx);
     return ARMANDO_OK;
 }
 
@@ -1897,22 +1979,30 @@ armando_status alloc_batch(armando_ctx* ctx) {
     CK(cudaMemcpy(ctx->d_inst_items, inst_items.data(), sizeof(int) * (ni + 1), cudaMemcpyHostToDevice));
     if (ctx->n_items)
         CK(cudaMemcpy(ctx->d_items, items.data(), sizeof(WorkItem) * ctx->n_items, cudaMemcpyHostToDevice));
+    ctx->any_visc = 0;
+    ctx->batch_lean = true;
+    for (const auto& q : ctx->prm_inst) {
+        ctx->any_visc |= q.visc ? 1 : 0;
+        ctx->batch_lean = ctx->batch_lean && lean_physics(make_dev_params(q)) && !step_options(q);
+    }
     int sms = 0, bd = 0, bs = 0, bf = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+    auto occ = [&](auto kd, auto ks, auto kf) -> cudaError_t {
+        cudaError_t e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, kd, kPassThreads, 0);
+        if (e2 == cudaSuccess) e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, ks, kPassThreads, 0);
+        if (e2 == cudaSuccess) e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, kf, kPassThreads, 0);
+        return e2;
+    };
     if (ctx->dim == 2) {
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, k_density_batch<2>, kPassThreads, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_shear_batch<2>, kPassThreads, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_force_batch<2>, kPassThreads, 0));
+        CK(ctx->batch_lean ? occ(k_density_batch<2, true>, k_shear_batch<2>, k_force_batch<2, true>)
+                           : occ(k_density_batch<2>, k_shear_batch<2>, k_force_batch<2>));
     } else {
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bd, k_density_batch<3>, kPassThreads, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bs, k_shear_batch<3>, kPassThreads, 0));
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_force_batch<3>, kPassThreads, 0));
+        CK(ctx->batch_lean ? occ(k_density_batch<3, true>, k_shear_batch<3>, k_force_batch<3, true>)
+                           : occ(k_density_batch<3>, k_shear_batch<3>, k_force_batch<3>));
     }
     ctx->grid_density = std::max(1, std::min(sms * bd, ctx->n_items));
     ctx->grid_shear = std::max(1, std::min(sms * bs, ctx->n_items));
     ctx->grid_force = std::max(1, std::min(sms * bf, ctx->n_items));
-    ctx->any_visc = 0;
-    for (const auto& q : ctx->prm_inst) ctx->any_visc |= q.visc ? 1 : 0;
     return upload_batch_params(ctx);
 }
 
@@ -2135,6 +2225,7 @@ static armando_status create_impl(armando_ctx** out, int32_t n_inst, const arman
     ctx->stream = ctx->own_stream;
     if (const char* sv = std::getenv("ARMANDO_STAGING")) ctx->staging = std::strcmp(sv, "1") == 0;
     if (const char* lv = std::getenv("ARMANDO_NEIGHBOUR_LISTS")) ctx->lists = std::strcmp(lv, "0") != 0;
+    if (const char* fv = std::getenv("ARMANDO_FUSED_PREDICTOR")) ctx->fuse_ok = std::strcmp(fv, "0") != 0;
     armando_status st = alloc_state(ctx);
     if (st == ARMANDO_OK && n_inst > 1) st = alloc_batch(ctx);
     if (st != ARMANDO_OK) {
@@ -2411,6 +2502,87 @@ armando_status armando_batch_integrate(armando_ctx* ctx, float* x, float* vx, co
     return finish_call(ctx);
 }
 
+static_assert(kPassThreads == ARMANDO_BATCH_BLOCK, "the batched passes' CTA size");
+
+armando_status armando_batch_autotune(armando_ctx* ctx, const float* x, const float* vx,
+                                      const float* mass, const float* rho, const float* p,
+                                      const float* u, const float* hsml, const int32_t* itype,
+                                      const float* dvdt, const float* dudt, const float* dt,
+                                      int32_t its0, int32_t steps_per_trial, armando_tuning* best,
+                                      float* ms_per_step) {
+    if (!ctx) return fail(nullptr, ARMANDO_ERR_INVALID_ARG, "ctx is NULL");
+    if (!dt) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "dt is NULL");
+    if (ctx->n_inst == 1)
+        return armando_autotune(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt[0], its0,
+                                steps_per_trial, best, ms_per_step);
+    armando_status st = check_step_args(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt, dt[0], its0);
+    if (st != ARMANDO_OK) return st;
+    if (steps_per_trial < 1) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps_per_trial must be >= 1");
+    bool changed = false;
+    for (int k = 0; k < ctx->n_inst; ++k) {
+        if (!(dt[k] > 0.f) || !std::isfinite(dt[k]))
+            return fail(ctx, ARMANDO_ERR_INVALID_ARG, "every dt must be finite and > 0");
+        changed |= dt[k] != ctx->inst_dt[k];
+    }
+    CK(cudaSetDevice(ctx->device));
+    if (changed) {
+        for (int k = 0; k < ctx->n_inst; ++k) ctx->inst_dt[k] = dt[k];
+        if ((st = upload_batch_params(ctx)) != ARMANDO_OK) return st;
+    }
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    armando_tuning win = ctx->tune;
+    float win_ms = -1.f;
+    for (int k = 0; k < ARMANDO_N_TUNINGS; ++k) {
+        armando_tuning t;
+        armando_tuning_candidate(k, &t);
+        float ms = -1.f;
+        // The batched passes run one thread per particle in CTAs of one work
+        // item and sort every iteration: the candidates differ in reach.
+        if (k >= 18 || t.threads_per_particle != 1 || t.block != kPassThreads) {
+            if (ms_per_step) ms_per_step[k] = ms;
+            continue;
+        }
+        if ((st = apply_tuning(ctx, t)) != ARMANDO_OK) break;
+        if ((st = clear_flags(ctx)) != ARMANDO_OK) break;
+        st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+        if (st == ARMANDO_OK) st = plan_grid(ctx);
+        if (st == ARMANDO_OK) {
+            const int its = its0;
+            CK(cudaMemcpyAsync(ctx->d_its, &its, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+            st = run_batch_step(ctx);  // untimed: captures the step graph
+        }
+        if (st == ARMANDO_OK) {
+            CK(cudaEventRecord(e0, ctx->stream));
+            for (int q = 0; q < steps_per_trial && st == ARMANDO_OK; ++q) st = run_batch_step(ctx);
+            CK(cudaEventRecord(e1, ctx->stream));
+        }
+        if (st == ARMANDO_OK) st = check_flags(ctx);
+        if (st == ARMANDO_OK) {
+            float el = 0.f;
+            CK(cudaEventElapsedTime(&el, e0, e1));
+            ms = el / (float)steps_per_trial;
+            if (win_ms < 0.f || ms < win_ms) {
+                win_ms = ms;
+                win = t;
+            }
+        } else if (st == ARMANDO_ERR_CUDA) {
+            break;
+        }
+        st = ARMANDO_OK;
+        if (ms_per_step) ms_per_step[k] = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != ARMANDO_OK) return st;
+    if (win_ms < 0.f) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "no candidate tuning runs on this batch");
+    if ((st = apply_tuning(ctx, win)) != ARMANDO_OK) return st;
+    if (best) *best = win;
+    ctx->next_its = 0;  // the trials left the device state behind
+    return ARMANDO_OK;
+}
+
 armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const float* mass,
                                  float* rho, float* p, float* u, const float* hsml,
                                  const int32_t* itype, float* dvdt, float* dudt, float dt,
@@ -2641,6 +2813,13 @@ armando_status armando_neighbours(armando_ctx* ctx, const float* x, const float*
     return check_flags(ctx);
 }
 
+// Marks a reverse-mode forward run or replay for its duration.
+struct ReverseScope {
+    armando_ctx* c;
+    explicit ReverseScope(armando_ctx* ctx) : c(ctx) { c->reverse_run = true; }
+    ~ReverseScope() { c->reverse_run = false; }
+};
+
 armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* vx,
                                            const float* mass, float* rho, float* p, float* u,
                                            const float* hsml, const int32_t* itype, float* dvdt,
@@ -2653,6 +2832,7 @@ armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* v
         return fail(ctx, ARMANDO_ERR_INVALID_ARG, "steps and checkpoint_every must be >= 1");
     CK(cudaSetDevice(ctx->device));
     ctx->adj_ready = false;
+    ReverseScope rv(ctx);
     if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
     if ((st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt)) != ARMANDO_OK) return st;
     if ((st = plan_grid(ctx)) != ARMANDO_OK) return st;
@@ -2735,6 +2915,7 @@ armando_status armando_backward(armando_ctx* ctx, const float* x_bar, const floa
     for (int c = nck - 1; c >= 0; --c) {
         const int a0 = c * K, len = std::min(K, steps - a0);
         if (ctx->tape_seg != c) {  // replay the segment from its checkpoint, taping it
+            ReverseScope rv(ctx);
             ctx->tape_seg = -1;
             if ((st = copy_stateA(ctx, ctx->A, ctx->ckpts[c])) != ARMANDO_OK) return st;
             for (int t = 0; t < len; ++t) {
@@ -2812,6 +2993,7 @@ armando_status armando_profile_phases(armando_ctx* ctx, int32_t steps, float* ms
         ctx->launches += L;
         ctx->steps_done += 1;
         ctx->next_its += 1;
+        if (ctx->n_inst == 1 && fused(ctx)) swap_state(ctx);
         cudaError_t e = cudaEventSynchronize(ev[ARMANDO_N_PHASES]);
         if (e != cudaSuccess) {
             st = cuda_fail(ctx, e, "profile step");

@@ -805,11 +805,15 @@ __global__ void k_scatter_out(StateA A, int n, float* __restrict__ x, float* __r
 // Cell-ordered working set + leapfrog predictor (time_integration.f:136-154).
 template <int DIM>
 // An iteration that does not sort keeps the slot order (perm = identity).
+// only_sorted: an iteration that does not sort skips the copy (the passes of
+// such an iteration read A themselves, FusedSrc).
 __global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, StepArgs S,
-                              int n, const int* __restrict__ resort = nullptr) {
+                              int n, const int* __restrict__ resort = nullptr,
+                              bool only_sorted = false) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const bool sorted = !sort_skipped(resort);
+    if (only_sorted && !sorted) return;
     const int j = sorted ? perm[s] : s;
     const float4 xh = A.xh[j];
     if (sorted && B.xsort) B.xsort[s] = xh;
@@ -1275,6 +1279,17 @@ struct StageView {
     const int* shift;   // per stencil row, cursor order
 };
 
+// The integrated state A of a lazily sorting context with lean physics, read
+// by the passes on the iterations that do not sort: they skip the reorder
+// copy into B, apply the leapfrog predictor (time_integration.f:136-154) on
+// load, and the force pass writes the next state into the other A buffer.
+// rs: the context's lazy-sort flags (which iterations sort).
+struct FusedSrc {
+    StateA A;
+    const int* rs;
+    float hdt;  // predictor half step of this iteration
+};
+
 // Stencil row of the cursor's current range (non-periodic grids: one piece
 // per row), r = (dz + f) (2f + 1) + (dy + f).
 template <int DIM>
@@ -1292,23 +1307,43 @@ __device__ __forceinline__ int cursor_row(const Cursor& cu, int f) {
 // type, staged indices), else from global memory through L1.
 // LST: a lazily sorting context's neighbour lists (B.nlist) replace the cell
 // walk for slots whose list fits; the neighbour bits then index list entries.
+// FUS: on iterations that do not sort, read the state from F.A (FusedSrc).
 template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
-          bool STG = false, class LT = int, bool LST = false>
+          bool STG = false, class LT = int, bool LST = false, bool FUS = false>
 __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __restrict__ keys,
                                              const int* __restrict__ start, const DevGrid& g,
                                              const DevParams& P, const int s, const bool valid,
                                              LT (*s_near)[BS], LT (*s_far)[BS],
-                                             const StageView& SV = StageView{}) {
+                                             const StageView& SV = StageView{},
+                                             const FusedSrc& F = FusedSrc{}) {
     static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
     static_assert(!LST || (TPP == 1 && !STG), "lists: one lane per particle, unstaged");
+    static_assert(!FUS || (LST && LEAN && !OPT), "fused predictor: lists, lean physics");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
     const bool need_div = !LEAN && P.heat_art != 0;
+    const bool from_a = FUS && sort_skipped(F.rs);
+    const float4* __restrict__ xsrc = from_a ? F.A.xh : B.xh;
+    const float4* __restrict__ vsrc = from_a ? F.A.vm : B.vm;  // 3D masses (.w)
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rp = xi;
     float p = 0.f;
     int it_i = 0;
     bool fluid = false;
-    if (valid) {
+    if (valid && from_a) {
+        xi = F.A.xh[s];
+        it_i = F.A.itype[s];
+        fluid = it_i > 0;
+        vi = F.A.vm[s];
+        p = F.A.p[s];
+        rp = make_float4(F.A.rho[s], 0.f, 0.f, 0.f);
+        if (fluid && F.hdt != 0.f) {  // predictor (k_reorder_dim's, same operations)
+            const float4 ap = F.A.ap[s];
+            vi.x = fmaf(F.hdt, ap.x, vi.x);
+            vi.y = fmaf(F.hdt, ap.y, vi.y);
+            if (DIM == 3) vi.z = fmaf(F.hdt, ap.z, vi.z);
+        }
+        if (DIM == 3) B.vm[s] = vi;  // the force pass reads neighbours' predicted v here
+    } else if (valid) {
         xi = B.xh[s];
         rp = B.rp[s];
         p = B.p[s];
@@ -1365,7 +1400,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 for (int u = 0; u < kTestBatch; ++u)
                     kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
 #pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + kb[u]);
+                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(xsrc + kb[u]);
                 lt += cnt;
             } else {
                 if (cu.k >= cu.ke) {
@@ -1386,7 +1421,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 for (int u = 0; u < kTestBatch; ++u) {
                     const int ku = min(k0 + u * TPP, cu.ke - 1);
                     kb[u] = k0 + u * TPP;
-                    xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                    xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
                 }
                 cu.k += cnt * TPP;
             }
@@ -1419,9 +1454,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             if (t >= nn) continue;
             const int k = (int)s_near[t][tid];
             if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;  // push only
-            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
+            const float4 xj = STG ? SV.x[k] : __ldg(xsrc + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(B.vm + k);
+            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(vsrc + k);
             const float mj = mass_of<DIM>(xj, vj);
             float dh[3], dl[3];
             exact_delta<DIM>(xi, xj, g, dh, dl);
@@ -1449,9 +1484,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             if (t >= nf) continue;
             const int k = (int)s_far[t][tid];
             if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) continue;
-            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
+            const float4 xj = STG ? SV.x[k] : __ldg(xsrc + k);
             float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(B.vm + k);
+            if (DIM == 3 || need_div) vj = STG ? SV.v[k] : __ldg(vsrc + k);
             const float mj = mass_of<DIM>(xj, vj);
             float d[3], dr2;
             pair_delta<DIM>(xi, xj, g, d, dr2);
@@ -1630,22 +1665,39 @@ __device__ __forceinline__ void shear_body(const StateB& B, const unsigned* __re
 // Pass 2: forces, heat, leapfrog corrector. Reads B, writes the next state A.
 // ---------------------------------------------------------------------------
 // STG: neighbours from the CTA's staged copy SV (see density_body).
+// FUS: on iterations that do not sort, the state comes from F.A (FusedSrc);
+// A is then the other buffer, which receives the next state.
 template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
-          bool STG = false, class LT = int, bool LST = false>
+          bool STG = false, class LT = int, bool LST = false, bool FUS = false>
 __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                                            const unsigned* __restrict__ keys,
                                            const int* __restrict__ start, const DevGrid& g,
                                            const DevParams& P, const StepArgs& S,
                                            unsigned* __restrict__ flags, const int s,
                                            const bool valid, LT (*s_list)[BS],
-                                           const StageView& SV = StageView{}) {
+                                           const StageView& SV = StageView{},
+                                           const FusedSrc& F = FusedSrc{}) {
     static_assert(!STG || (TPP == 1 && LEAN && !OPT), "staged: one lane per particle, lean physics");
     static_assert(!LST || (TPP == 1 && !STG), "lists: one lane per particle, unstaged");
+    static_assert(!FUS || (LST && LEAN && !OPT), "fused predictor: lists, lean physics");
     const int tid = threadIdx.x;
     const int sub = (TPP == 1) ? 0 : (tid & (TPP - 1));
+    const bool from_a = FUS && sort_skipped(F.rs);
+    const float4* __restrict__ xsrc = from_a ? F.A.xh : B.xh;
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi;
     int it = 0;
-    if (valid) {
+    if (valid && from_a) {
+        xi = F.A.xh[s];
+        it = F.A.itype[s];
+        vi = F.A.vm[s];
+        rpi = B.rp[s];
+        if (it > 0 && F.hdt != 0.f) {  // predictor, as the density pass applied it
+            const float4 ap = F.A.ap[s];
+            vi.x = fmaf(F.hdt, ap.x, vi.x);
+            vi.y = fmaf(F.hdt, ap.y, vi.y);
+            if (DIM == 3) vi.z = fmaf(F.hdt, ap.z, vi.z);
+        }
+    } else if (valid) {
         xi = B.xh[s];
         it = B.itype[s];
         vi = B.vm[s];
@@ -1655,15 +1707,15 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     // (wall_model 3) to the particle's own index, the ghosts being dropped.
     const bool ghosts = !LEAN && P.wall_model == 3;
     if (valid && (it <= 0 || !g.ok) && sub == 0) {  // wall: fixed state, zero rates
-        const int id = B.id[s];
+        const int id = from_a ? F.A.id[s] : B.id[s];
         if (!ghosts || id < P.n_real) {
             const int o = ghosts ? id : s;
             A.xh[o] = xi;
             A.vm[o] = vi;
-            A.u[o] = B.vmin[s].w;
+            A.u[o] = from_a ? F.A.u[s] : B.vmin[s].w;
             A.ap[o] = make_float4(0.f, 0.f, 0.f, 0.f);
             A.rho[o] = rpi.x;
-            A.p[o] = B.p[s];
+            A.p[o] = from_a ? F.A.p[s] : B.p[s];
             A.itype[o] = it;
             A.id[o] = id;
             if (A.inst) A.inst[o] = B.inst[s];
@@ -1751,7 +1803,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 for (int u = 0; u < kTestBatch; ++u)
                     kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
 #pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xh + kb[u]);
+                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(xsrc + kb[u]);
                 lt += cnt;
             } else {
                 if (cu.k >= cu.ke) {
@@ -1772,7 +1824,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 for (int u = 0; u < kTestBatch; ++u) {
                     const int ku = min(k0 + u * TPP, cu.ke - 1);
                     kb[u] = k0 + u * TPP;
-                    xb[u] = STG ? SV.x[ku + shift] : __ldg(B.xh + ku);
+                    xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
                 }
                 cu.k += cnt * TPP;
             }
@@ -1788,7 +1840,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
         for (int t = 0; t < ml; ++t) {
             if (t >= nl) continue;
             const int k = (int)s_list[t][tid];
-            const float4 xj = STG ? SV.x[k] : __ldg(B.xh + k);
+            const float4 xj = STG ? SV.x[k] : __ldg(xsrc + k);
             float4 vj, rpj;
             if (DIM == 2) {  // {vx, vy, rho, P}; u and psi only for art_heat
                 const float4 vr = STG ? SV.v[k] : __ldg(B.vr + k);
@@ -1951,7 +2003,13 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     a1 += P.gravity[1];
     if (DIM == 3) a2 += P.gravity[2];
     // Corrector (time_integration.f:186-218).
-    const float4 vmin = B.vmin[s];
+    float4 vmin;
+    if (from_a) {
+        const float4 v0 = F.A.vm[s];
+        vmin = make_float4(v0.x, v0.y, v0.z, F.A.u[s]);
+    } else {
+        vmin = B.vmin[s];
+    }
     float4 vn = vi;
     vn.x = fmaf(S.kdt, a0, vmin.x);
     vn.y = fmaf(S.kdt, a1, vmin.y);
@@ -1989,7 +2047,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     const float chk = xn.x + xn.y + xn.z + vn.x + vn.y + vn.z + un + a0 + a1 + a2 + du;
     if (!isfinite(chk)) atomicOr(flags, (unsigned)FLAG_NONFINITE);
-    const int id = B.id[s];
+    const int id = from_a ? F.A.id[s] : B.id[s];
     const int o = ghosts ? id : s;
     A.xh[o] = xn;
     A.vm[o] = vn;
@@ -2016,16 +2074,17 @@ __device__ __forceinline__ DevGrid load_grid(const DevGrid* __restrict__ gp) {
 }
 
 // One CTA per BS / TPP consecutive slots.
-template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false,
+          bool FUS = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
-              const DevGrid* __restrict__ gp, DevParams P, int n) {
+              const DevGrid* __restrict__ gp, DevParams P, int n, FusedSrc F) {
     __shared__ int s_near[kListCapD][BS];
     __shared__ int s_far[kListCapD][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    density_body<DIM, TPP, BS, LEAN, OPT, false, int, LST>(B, keys, start, g, P, s, s < n, s_near,
-                                                           s_far);
+    density_body<DIM, TPP, BS, LEAN, OPT, false, int, LST, FUS>(B, keys, start, g, P, s, s < n,
+                                                                s_near, s_far, StageView{}, F);
 }
 
 // Neighbour lists of an iteration that sorts (lazy sorting), built in the
@@ -2085,16 +2144,17 @@ __global__ void __launch_bounds__(kPassThreads)
     shear_body<DIM>(B, keys, start, g, P, s, s < n);
 }
 
-template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false>
+template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool LST = false,
+          bool FUS = false>
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
-            int n) {
+            int n, FusedSrc F) {
     __shared__ int s_list[kListCap][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
-    force_body<DIM, TPP, BS, LEAN, OPT, false, int, LST>(B, A, keys, start, g, P, S, flags, s,
-                                                         s < n, s_list);
+    force_body<DIM, TPP, BS, LEAN, OPT, false, int, LST, FUS>(B, A, keys, start, g, P, S, flags, s,
+                                                              s < n, s_list, StageView{}, F);
 }
 
 // ---------------------------------------------------------------------------
@@ -2153,7 +2213,9 @@ __device__ __forceinline__ bool next_item(ItemCtx& c, const WorkItem* __restrict
     return true;
 }
 
-template <int DIM>
+// LEAN: no instance uses physical viscosity, artificial heat, a wall model
+// or a single_step option (the passes' lean variant).
+template <int DIM, bool LEAN = false>
 __global__ void __launch_bounds__(kPassThreads, 8)
     k_density_batch(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
                     const DevGrid* __restrict__ grids, const DevParams* __restrict__ params,
@@ -2163,7 +2225,8 @@ __global__ void __launch_bounds__(kPassThreads, 8)
     __shared__ ItemCtx c;
     while (next_item(c, items, n_items, queue, params, grids, nullptr)) {
         const int s = c.w.s0 + threadIdx.x;
-        density_body<DIM>(B, keys, start, c.g, c.P, s, s < c.w.s1, s_near, s_far);
+        density_body<DIM, 1, kPassThreads, LEAN>(B, keys, start, c.g, c.P, s, s < c.w.s1, s_near,
+                                                 s_far);
     }
 }
 
@@ -2179,7 +2242,7 @@ __global__ void __launch_bounds__(kPassThreads)
     }
 }
 
-template <int DIM>
+template <int DIM, bool LEAN = false>
 __global__ void __launch_bounds__(kPassThreads, 8)
     k_force_batch(StateB B, StateA A, const unsigned* __restrict__ keys,
                   const int* __restrict__ start, const DevGrid* __restrict__ grids,
@@ -2190,7 +2253,8 @@ __global__ void __launch_bounds__(kPassThreads, 8)
     __shared__ ItemCtx c;
     while (next_item(c, items, n_items, queue, params, grids, its)) {
         const int s = c.w.s0 + threadIdx.x;
-        force_body<DIM>(B, A, keys, start, c.g, c.P, c.S, flags, s, s < c.w.s1, s_list);
+        force_body<DIM, 1, kPassThreads, LEAN>(B, A, keys, start, c.g, c.P, c.S, flags, s,
+                                               s < c.w.s1, s_list);
     }
 }
 

@@ -648,6 +648,7 @@ def run_sweep(args):
     dev = {k: torch.from_numpy(v).cuda() for k, v in arrays.items()}
     with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
                   [c.n_wall for c in insts], mem=ag.MEM_DEVICE) as b:
+        best, table = b.autotune_batch(dev, dts, 1, 3)  # untimed; the state is not modified
         b.integrate_batch(dev, dts, 1, 3)
         launches0 = b.stats().gpu_launches
         ms_b = timed_integrate(b, dev, dts, 4, args.extra_steps, batch=True)
@@ -655,11 +656,13 @@ def run_sweep(args):
     del dev
     torch.cuda.empty_cache()
     batch_rate = ntot * args.extra_steps / (ms_b * 1e-3)
-    # Plain step, one instance after another (each its own context and graph).
+    # Plain step, one instance after another (each its own context and graph),
+    # at the batch's tuning.
     ms_p = 0.0
     for c in insts:
         d = {k: torch.from_numpy(v.copy()).cuda() for k, v in c.arrays().items()}
         with ag.Context(c.params, c.n_fluid, c.n_wall, mem=ag.MEM_DEVICE) as ctx:
+            ctx.set_tuning(*best)
             ctx.integrate(d, c.dt, 1, 3)
             ms_p += timed_integrate(ctx, d, c.dt, 4, args.plain_steps)
     plain_rate = ntot * args.plain_steps / (ms_p * 1e-3)
@@ -667,6 +670,8 @@ def run_sweep(args):
                         f"{ntot} particles, n_k log-uniform in [2e3, 2e5], alpha ~ U(0.005, 0.05), "
                         f"c0 ~ U(20, 80), seed 4",
             "particles": ntot, "instances": len(insts), "steps": args.extra_steps,
+            "tuning": list(best),
+            "tuning_ms_per_step": {",".join(map(str, k)): round(v, 4) for k, v in table.items()},
             "value": batch_rate, "unit": METRIC, "ms_per_step": ms_b / args.extra_steps,
             "gpu_launches_per_step": launches / args.extra_steps,
             "plain_per_instance": {"value": plain_rate, "steps": args.plain_steps,
@@ -933,7 +938,8 @@ def summary(out):
         s["channel3d"] = {"ms_per_step": round(c["ms_per_step"], 3), "value": c["value"],
                           "two_roof_frac": (c.get("two_roof") or {}).get("frac")}
     if "sweep" in w:
-        s["sweep"] = {"value": w["sweep"]["value"], "speedup_vs_plain": w["sweep"]["speedup_vs_plain"]}
+        s["sweep"] = {"value": w["sweep"]["value"], "speedup_vs_plain": w["sweep"]["speedup_vs_plain"],
+                      "tuning": w["sweep"]["tuning"]}
     if "adjoint" in w:
         a = w["adjoint"]
         s["adjoint"] = {"backward_over_forward": a["backward_over_forward"],

@@ -380,6 +380,24 @@ armando_status armando_autotune(armando_ctx* ctx, const float* x, const float* v
                                 float* ms_per_step);
 
 /*
+ * Autotuner of a batch (armando_batch_create): as armando_autotune, on the
+ * packed state of every instance with one time step per instance (dt[k], as
+ * for armando_batch_integrate). The batched passes run one thread per
+ * particle in CTAs of ARMANDO_BATCH_BLOCK threads and sort every iteration,
+ * so the candidates with threads_per_particle 1, that block and skin 0 are
+ * timed (they differ in reach, the cell size 2 max h / reach of every
+ * instance's grid); the others receive -1 in ms_per_step. On a single-system
+ * context this is armando_autotune with dt[0]. The fastest tuning is set.
+ */
+#define ARMANDO_BATCH_BLOCK 128
+armando_status armando_batch_autotune(armando_ctx* ctx, const float* x, const float* vx,
+                                      const float* mass, const float* rho, const float* p,
+                                      const float* u, const float* hsml, const int32_t* itype,
+                                      const float* dvdt, const float* dudt, const float* dt,
+                                      int32_t its0, int32_t steps_per_trial, armando_tuning* best,
+                                      float* ms_per_step);
+
+/*
  * Allocation-free form of armando_cell_ids. It has no counterpart in the
  * reference.
  * For callers that must not allocate device memory: a host code that hands

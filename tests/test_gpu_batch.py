@@ -145,3 +145,44 @@ def test_batch_of_boundary_models_matches_instances_alone():
         alone = _run_single(c, 1, 4)
         for f in FIELDS:
             assert np.array_equal(getattr(outs[k], f), getattr(alone, f)), (k, f)
+
+
+def _lean_sweep():
+    insts = cases.sweep(n_instances=8, seed=45, n_min=400, n_max=4000)
+    assert all(c.params.visc == 0 and c.params.heat_artificial == 0 for c in insts)
+    return insts
+
+
+def test_lean_batch_equals_instances_run_alone():
+    """Every instance lean (the sweep's physics): the batch runs the lean
+    passes, still bit-identical to each instance run alone."""
+    insts = _lean_sweep()
+    got = _run_batch(insts, 1, 5)
+    for c, g in zip(insts, got):
+        ref = _run_single(c, 1, 5)
+        for f in FIELDS:
+            assert np.array_equal(getattr(g, f), getattr(ref, f)), (c.name, f)
+
+
+def test_batch_autotune_times_the_reach_and_keeps_the_fastest():
+    insts = _lean_sweep()
+    arrays, offs = cases.pack(insts)
+    before = {k: v.copy() for k, v in arrays.items()}
+    dts = [c.dt for c in insts]
+    with ag.Batch([c.params for c in insts], [c.n_fluid for c in insts],
+                  [c.n_wall for c in insts]) as b:
+        best, table = b.autotune_batch(arrays, dts, 1, 3)
+        for k in before:  # the state is not modified
+            assert np.array_equal(arrays[k], before[k]), k
+        assert sorted(table) == [(1, 1, 128, 0), (2, 1, 128, 0), (3, 1, 128, 0)]
+        assert best == min(table, key=table.get)
+        assert b.tuning().as_tuple() == best
+        b.integrate_batch(arrays, dts, 1, 4)
+    got = cases.unpack(arrays, offs, insts)
+    for c, g in zip(insts, got):  # the tuned batch equals each instance alone at that tuning
+        ref = c.copy()
+        with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+            ctx.set_tuning(*best)
+            ctx.integrate(ref, c.dt, 1, 4)
+        for f in FIELDS:
+            assert np.array_equal(getattr(g, f), getattr(ref, f)), (c.name, best, f)
