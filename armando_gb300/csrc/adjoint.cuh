@@ -22,7 +22,14 @@
 // and turns psi_bar into the cotangent of each particle's divergence sum;
 // k_adj_density gathers that sum's reverse onto velocities and positions. |divv|
 // follows its sign (no gradient at divv = 0 from one side).
-// Supported: pa_sph = 1, no physical viscosity.
+// Physical viscosity (internal_force.f:75-171), when on: tau_i = eta/rho_i^2 T_i,
+// T_i = sum_j m_j/rho_j H(vh_j - vh_i, G_ij d_ij) (the shear tensor of every
+// particle, walls included), a_i += sum_j m_j (tau_i + tau_j) G_ij d_ij, du_i +=
+// eta/(2 rho_i) T_i:T_i. k_adj_force takes the tau cotangents of the pair
+// forces and turns them, with the heating term's, into cotangents of each
+// particle's shear tensor; k_adj_shear gathers the shear sums' reverse onto
+// velocities, positions and densities before the density reverse.
+// Supported: pa_sph = 1.
 #pragma once
 #include "kernels.cuh"
 
@@ -56,6 +63,8 @@ struct TapeSlot {
     int* start;
     DevGrid* grid;
     float* ulo;  // rounding residual of the predicted energy (artificial heat only)
+    float4* tau;   // physical viscosity: eta/rho^2 T {xx, yy, xy, zz}
+    float4* tau2;  // 3D: {xz, yz, -, -}
 };
 
 template <int DIM>
@@ -80,6 +89,8 @@ __global__ void k_tape_save(StateB B, const unsigned* __restrict__ keys,
     T.perm[s] = perm[s];
     T.du[s] = ap[s].w;
     if (T.ulo) T.ulo[s] = B.ulo ? B.ulo[s] : 0.f;
+    if (T.tau) T.tau[s] = B.tau[s];
+    if (T.tau2) T.tau2[s] = B.tau2[s];
 }
 
 // The working set of a taped iteration as the pass kernels see it.
@@ -93,6 +104,10 @@ inline StateB tape_view(StateB B, const TapeSlot& T, int n) {
     B.nmask = T.nmask;
     B.mstride = n;
     B.ulo = T.ulo;
+    if (T.tau) {
+        B.tau = T.tau;
+        B.tau2 = T.tau2;
+    }
     return B;
 }
 
@@ -304,6 +319,33 @@ __device__ __forceinline__ int nbr_fill(NbrStream<DIM>& ns, const StateB& B, con
     return nl;
 }
 
+// Symmetric tensors as stored by the shear pass: a {xx, yy, xy, zz}, b {xz, yz}.
+// H(dv, w) is the shear pass's pair term: diagonal (2/3)(2 dv_a w_a - sum of
+// the others), off-diagonal dv_a w_b + dv_b w_a. A . H(dv, w) = dv^T M(A) w,
+// M(A) symmetric with M_aa = (2/3)(2 A_aa - the other diagonal entries) and
+// M_ab = A_ab.
+template <int DIM>
+__device__ __forceinline__ void sym_apply(const float4& a, const float4& b, const float* x,
+                                          float* y) {  // y = S x, S = {a, b}
+    y[0] = a.x * x[0] + a.z * x[1];
+    y[1] = a.z * x[0] + a.y * x[1];
+    y[2] = 0.f;
+    if (DIM == 3) {
+        y[0] += b.x * x[2];
+        y[1] += b.y * x[2];
+        y[2] = b.x * x[0] + b.y * x[1] + a.w * x[2];
+    }
+}
+
+template <int DIM>
+__device__ __forceinline__ void shear_m(const float4& a, const float4& b, float4& ma, float4& mb) {
+    const float tr = (DIM == 3) ? a.x + a.y + a.w : a.x + a.y;
+    // (2/3)(2 A_aa - (tr - A_aa)) = (2/3)(3 A_aa - tr)
+    ma = make_float4((2.f / 3.f) * (3.f * a.x - tr), (2.f / 3.f) * (3.f * a.y - tr), a.z,
+                     DIM == 3 ? (2.f / 3.f) * (3.f * a.w - tr) : 0.f);
+    mb = b;
+}
+
 // Forward pair geometry shared by the adjoint gathers.
 template <int DIM>
 struct PairGeo {
@@ -330,7 +372,8 @@ __global__ void __launch_bounds__(kPassThreads)
                 const DevGrid* __restrict__ gp, DevParams P, StepArgs S,
                 const float4* __restrict__ abar, const float* __restrict__ pbar_loss,
                 float* __restrict__ rhobar, float4* __restrict__ xF, float4* __restrict__ vhb,
-                float* __restrict__ divsb, double* __restrict__ block_part, int n) {
+                float* __restrict__ divsb, float4* __restrict__ tbar, float4* __restrict__ tbar2,
+                double* __restrict__ block_part, int n) {
     __shared__ int s_list[kListCap][kPassThreads];
     __shared__ double s_red[ADJ_NPARAM][kPassThreads / 32];
     const int tid = threadIdx.x;
@@ -338,11 +381,12 @@ __global__ void __launch_bounds__(kPassThreads)
     const bool valid = s < n;
     const DevGrid g = *gp;
     const bool ah = P.heat_art != 0;
+    const bool vs = P.visc != 0;
     const int it = valid ? B.itype[s] : 0;
     const bool work = valid && g.ok && it > 0;
-    // walls take part for artificial heat only: their psi enters their
-    // neighbours' energy rates
-    const bool act = valid && g.ok && (it > 0 || ah);
+    // walls take part for artificial heat (their psi enters their neighbours'
+    // energy rates) and physical viscosity (their tau, their neighbours' forces)
+    const bool act = valid && g.ok && (it > 0 || ah || vs);
     float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi, rpi = xi, abi = make_float4(0.f, 0.f, 0.f, 0.f);
     float pi = 0.f, uloi = 0.f;
     if (act) {
@@ -356,6 +400,12 @@ __global__ void __launch_bounds__(kPassThreads)
     const float mi = mass_of<DIM>(xi, vi);
     CellCoord cc = {{0, 0, 0}};
     if (act) cc = decode_key<DIM>(keys[s], g);
+    float4 tai = make_float4(0.f, 0.f, 0.f, 0.f), tbi = tai;  // tau_i
+    float4 tba = tai, tbb = tai;                              // tau_bar_i
+    if (act && vs) {
+        tai = B.tau[s];
+        if (DIM == 3) tbi = B.tau2[s];
+    }
     float xb[3] = {0.f, 0.f, 0.f}, vb[3] = {0.f, 0.f, 0.f}, Pb = 0.f, rb = 0.f;
     float psib = 0.f, uhb = 0.f;  // artificial heat: psi_bar, u_half_bar of this particle
     // parameter cotangents, float-float (hi in pa, rounding residuals in palo):
@@ -431,7 +481,66 @@ __global__ void __launch_bounds__(kPassThreads)
 #pragma unroll
                 for (int k = 0; k < DIM; ++k) xb[k] = fmaf(cx, pg.d[k], xb[k]);
             }
+            if (vs) {
+                // a_s += m_j (tau_s + tau_j) w, a_j += m_s (tau_j + tau_s) (-w), w = G d:
+                // cotangent b = m_j a_bar_s - m_s a_bar_j on (tau_s + tau_j) w.
+                const float4 taj = __ldg(B.tau + j);
+                float4 tbj = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (DIM == 3) tbj = __ldg(B.tau2 + j);
+                const float bv[3] = {mj * abi.x - mi * abj.x, mj * abi.y - mi * abj.y,
+                                     DIM == 3 ? mj * abi.z - mi * abj.z : 0.f};
+                const float w0 = pg.G * pg.d[0], w1 = pg.G * pg.d[1];
+                const float w2 = (DIM == 3) ? pg.G * pg.d[2] : 0.f;
+                tba.x = fmaf(bv[0], w0, tba.x);
+                tba.y = fmaf(bv[1], w1, tba.y);
+                tba.z += bv[0] * w1 + bv[1] * w0;
+                if (DIM == 3) {
+                    tba.w = fmaf(bv[2], w2, tba.w);
+                    tbb.x += bv[0] * w2 + bv[2] * w0;
+                    tbb.y += bv[1] * w2 + bv[2] * w1;
+                }
+                if (work) {  // d_bar = J u, u = (tau_s + tau_j) b, J = G I + (G'/r) d d^T
+                    const float4 sa = make_float4(tai.x + taj.x, tai.y + taj.y, tai.z + taj.z,
+                                                  tai.w + taj.w);
+                    const float4 sb = make_float4(tbi.x + tbj.x, tbi.y + tbj.y, 0.f, 0.f);
+                    float u[3];
+                    sym_apply<DIM>(sa, sb, bv, u);
+                    float du_ = u[0] * pg.d[0] + u[1] * pg.d[1];
+                    if (DIM == 3) du_ += u[2] * pg.d[2];
+#pragma unroll
+                    for (int k = 0; k < DIM; ++k)
+                        xb[k] += pg.G * u[k] + pg.dGdr_r * du_ * pg.d[k];
+                }
+            }
         }
+    }
+    if (act && vs) {
+        // tau = sc T, sc = eta / rho^2; du += tds = eta/(2 rho) T:T (fluid only).
+        const float rho = rpi.x;
+        const float sc = P.eta / (rho * rho);
+        const float isc = P.eta != 0.f ? 1.f / sc : 0.f;
+        const float4 Ta = make_float4(tai.x * isc, tai.y * isc, tai.z * isc, tai.w * isc);
+        const float4 Tb = make_float4(tbi.x * isc, tbi.y * isc, 0.f, 0.f);
+        const float tdsb = work ? abi.w : 0.f;
+        const float k = tdsb * P.eta / rho;  // d tds / d T_aa = eta/rho T_aa, off-diagonal 2x
+        float4 Ga = make_float4(fmaf(sc, tba.x, k * Ta.x), fmaf(sc, tba.y, k * Ta.y),
+                                fmaf(sc, tba.z, 2.f * k * Ta.z), 0.f);
+        float4 Gb = make_float4(0.f, 0.f, 0.f, 0.f);
+        float q = Ta.x * Ta.x + Ta.y * Ta.y + 2.f * Ta.z * Ta.z;
+        float tt = tba.x * tai.x + tba.y * tai.y + tba.z * tai.z;
+        if (DIM == 3) {
+            Ga.w = fmaf(sc, tba.w, k * Ta.w);
+            Gb = make_float4(fmaf(sc, tbb.x, 2.f * k * Tb.x), fmaf(sc, tbb.y, 2.f * k * Tb.y), 0.f,
+                             0.f);
+            q += Ta.w * Ta.w + 2.f * (Tb.x * Tb.x + Tb.y * Tb.y);
+            tt += tba.w * tai.w + tbb.x * tbi.x + tbb.y * tbi.y;
+        }
+        if (work) rb += -2.f * tt / rho - tdsb * 0.5f * P.eta * q / (rho * rho);
+        tbar[s] = Ga;
+        if (DIM == 3) tbar2[s] = Gb;
+    } else if (valid && vs) {
+        tbar[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (DIM == 3) tbar2[s] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     float dsb = 0.f;  // cotangent of the divergence sum (artificial heat)
     if (act && ah) {
@@ -495,6 +604,99 @@ __global__ void __launch_bounds__(kPassThreads)
         for (int w2 = 0; w2 < kPassThreads / 32; ++w2) v += s_red[tid][w2];
         block_part[blockIdx.x * ADJ_NPARAM + tid] = v;
     }
+}
+
+// Shear-tensor reverse (physical viscosity): T_j = sum_k m_k/rho_k H(vh_k - vh_j,
+// G_jk d_jk) for every particle j, cotangents tbar. For a fluid particle i the
+// pair (i, j) enters T_i (weight m_j/rho_j) and T_j (weight m_i/rho_i, with
+// dv and w both reversed: the same H): with Ab = m_j/rho_j tbar_i + m_i/rho_i
+// tbar_j, vh_bar_i -= M(Ab) w, x_bar_i += J M(Ab) dv, and rho_i's weight in T_j
+// gives rho_bar_i -= m_i/rho_i^2 dv^T M(tbar_j) w. Added to the force reverse's
+// cotangents of i (the density's where the Tait clamp did not bind).
+template <int DIM>
+__global__ void __launch_bounds__(kPassThreads)
+    k_adj_shear(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
+                const DevGrid* __restrict__ gp, DevParams P, const float4* __restrict__ tbar,
+                const float4* __restrict__ tbar2, float* __restrict__ rhobar,
+                float4* __restrict__ xF, float4* __restrict__ vhb, int n) {
+    __shared__ int s_list[kListCap][kPassThreads];
+    const int tid = threadIdx.x;
+    const int s = blockIdx.x * blockDim.x + tid;
+    const bool valid = s < n;
+    const DevGrid g = *gp;
+    const bool work = valid && g.ok && B.itype[s] > 0;
+    float4 xi = make_float4(0.f, 0.f, 0.f, 1.f), vi = xi;
+    float4 tai = make_float4(0.f, 0.f, 0.f, 0.f), tbi = tai;
+    float rhoi = 1.f;
+    if (work) {
+        xi = B.xh[s];
+        vi = B.vm[s];
+        rhoi = B.rp[s].x;
+        tai = tbar[s];
+        if (DIM == 3) tbi = tbar2[s];
+    }
+    const float mi = mass_of<DIM>(xi, vi);
+    const float ci = mi / rhoi;
+    CellCoord cc = {{0, 0, 0}};
+    if (work) cc = decode_key<DIM>(keys[s], g);
+    float xb[3] = {0.f, 0.f, 0.f}, vb[3] = {0.f, 0.f, 0.f}, rb = 0.f;
+    NbrStream<DIM> ns;
+    nbr_init<DIM>(ns, B, g, s, work);
+    while (__any_sync(0xffffffffu, !ns.done)) {
+        const int nl = nbr_fill<DIM>(ns, B, g, start, cc, xi, s, s_list);
+        const int ml = __reduce_max_sync(0xffffffffu, nl);
+        for (int t = 0; t < ml; ++t) {
+            if (t >= nl) continue;
+            const int j = s_list[t][tid];
+            const float4 xj = __ldg(B.xh + j);
+            const float4 vj = __ldg(B.vm + j);
+            const float rhoj = __ldg(&B.rp[j].x);
+            const float4 taj = __ldg(tbar + j);
+            float4 tbj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 3) tbj = __ldg(tbar2 + j);
+            const float cj = mass_of<DIM>(xj, vj) / rhoj;
+            PairGeo<DIM> pg;
+            pair_geo<DIM>(xi, xj, g, P, pg);
+            const float w[3] = {pg.G * pg.d[0], pg.G * pg.d[1], DIM == 3 ? pg.G * pg.d[2] : 0.f};
+            const float dv[3] = {vj.x - vi.x, vj.y - vi.y, DIM == 3 ? vj.z - vi.z : 0.f};
+            const float4 Aa = make_float4(cj * tai.x + ci * taj.x, cj * tai.y + ci * taj.y,
+                                          cj * tai.z + ci * taj.z, cj * tai.w + ci * taj.w);
+            const float4 Ab = make_float4(cj * tbi.x + ci * tbj.x, cj * tbi.y + ci * tbj.y, 0.f, 0.f);
+            float4 ma, mb;
+            shear_m<DIM>(Aa, Ab, ma, mb);
+            float mw[3], mdv[3];
+            sym_apply<DIM>(ma, mb, w, mw);
+            sym_apply<DIM>(ma, mb, dv, mdv);
+            float dmd = mdv[0] * pg.d[0] + mdv[1] * pg.d[1];
+            if (DIM == 3) dmd += mdv[2] * pg.d[2];
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) {
+                vb[k] -= mw[k];
+                xb[k] += pg.G * mdv[k] + pg.dGdr_r * dmd * pg.d[k];
+            }
+            float4 mja, mjb;
+            shear_m<DIM>(taj, tbj, mja, mjb);
+            float mjw[3];
+            sym_apply<DIM>(mja, mjb, w, mjw);
+            float h = dv[0] * mjw[0] + dv[1] * mjw[1];
+            if (DIM == 3) h += dv[2] * mjw[2];
+            rb -= mi / (rhoi * rhoi) * h;
+        }
+    }
+    if (!work) return;
+    // the Tait clamp (p < pmin) set rho_i = rho0: no gradient reaches the sum
+    const bool clamped = (P.pmin > -FLT_MAX) && B.p[s] == 0.f && rhoi == P.rho0;
+    if (!clamped) rhobar[s] += rb;
+    float4 f = xF[s];
+    f.x += xb[0];
+    f.y += xb[1];
+    f.z += xb[2];
+    xF[s] = f;
+    float4 v = vhb[s];
+    v.x += vb[0];
+    v.y += vb[1];
+    v.z += vb[2];
+    vhb[s] = v;
 }
 
 // Density reverse (rho_i = m_i W(0) + sum m_j W_ij), the reverse of the

@@ -164,6 +164,7 @@ struct armando_ctx {
     float *adj_rhobar = nullptr, *adj_pbar = nullptr;
     double* adj_blk = nullptr;   // per-block parameter cotangents
     float* adj_divsb = nullptr;  // cotangents of the divergence sums (artificial heat)
+    float4 *adj_tbar = nullptr, *adj_tbar2 = nullptr;  // shear-tensor cotangents (viscosity)
     double* adj_pacc = nullptr;
     int adj_its0 = 0, adj_steps = 0, adj_K = 0;
     float adj_dt = 0.f;
@@ -611,16 +612,21 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
 }
 
 // Reorder/predictor, the pair passes and (lazy sorting) the flag advance.
+// reorder = false: the caller launched the reorder copy itself (the fused
+// predictor's step graph, where only iterations that sort need it).
 template <int DIM>
-int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
+int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs, bool reorder = true) {
     cudaStream_t st = ctx->stream;
     const int n = (int)ctx->n_work;
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
-    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs,
-                                                           fused(ctx));
+    int L = 1;
+    if (reorder) {
+        k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n, rs,
+                                                               fused(ctx));
+        ++L;
+    }
     launch_density<DIM>(ctx, skeys, S);
-    int L = 2;
     if (n > ctx->n) {  // mirror ghosts take their owners' density, pressure, energy
         k_invert_ids<<<blocks_for(n, 256), 256, 0, st>>>(ctx->B.id, ctx->g_slot, n);
         k_ghost_sync<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->B, ctx->g_slot, ctx->g_owner,
@@ -700,15 +706,24 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
                                            nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return fail_graph(e, "cudaStreamBeginCaptureToGraph(body)");
     body_cap = true;
-    const int body = launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2,
-                                               ctx->prm.scheme == 0 && use_lists(ctx));
+    int body = launch_grid_and_sort<DIM>(ctx, nullptr, ctx->stream2,
+                                         ctx->prm.scheme == 0 && use_lists(ctx));
+    // With the fused predictor only the iterations that sort copy the state
+    // into cell order: the copy joins the body.
+    const bool body_reorder = ctx->prm.scheme == 0 && fused(ctx);
+    if (body_reorder) {
+        const int n = (int)ctx->n_work;
+        k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, ctx->stream2>>>(
+            ctx->A, ctx->vals[ctx->passes & 1], ctx->B, S, n);
+        ++body;
+    }
     int L = 1 + body;
     cudaGraph_t body_out = nullptr;
     e = cudaStreamEndCapture(ctx->stream2, &body_out);
     body_cap = false;
     if (e != cudaSuccess) return fail_graph(e, "cudaStreamEndCapture(body)");
     L += ctx->prm.scheme != 0 ? launch_gpuc_passes<DIM>(ctx, S, resort_flags(ctx))
-                              : launch_passes<DIM>(ctx, S, resort_flags(ctx));
+                              : launch_passes<DIM>(ctx, S, resort_flags(ctx), !body_reorder);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail_graph(e, "kernel launch during capture");
     cudaGraph_t g_out = nullptr;
     e = cudaStreamEndCapture(ctx->stream, &g_out);
@@ -1824,10 +1839,14 @@ armando_status alloc_adjoint(armando_ctx* ctx) {
     ctx->adj_blk = dalloc<double>((size_t)blocks_for(ctx->n, kPassThreads) * ADJ_NPARAM + 4, e);
     ctx->adj_pacc = dalloc<double>(ADJ_NPARAM, e);
     if (ctx->prm.heat_artificial) ctx->adj_divsb = dalloc<float>(n, e);
+    if (ctx->prm.visc) {
+        ctx->adj_tbar = dalloc<float4>(n, e);
+        if (ctx->dim == 3) ctx->adj_tbar2 = dalloc<float4>(n, e);
+    }
     for (void* p : {(void*)ctx->adj_abar, (void*)ctx->adj_xpart, (void*)ctx->adj_vpart,
                     (void*)ctx->adj_xF, (void*)ctx->adj_vhb, (void*)ctx->adj_rhobar,
                     (void*)ctx->adj_pbar, (void*)ctx->adj_blk, (void*)ctx->adj_pacc,
-                    (void*)ctx->adj_divsb})
+                    (void*)ctx->adj_divsb, (void*)ctx->adj_tbar, (void*)ctx->adj_tbar2})
         ctx->owned.push_back(p);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(adjoint)");
     return ARMANDO_OK;
@@ -1851,9 +1870,13 @@ armando_status alloc_tape(armando_ctx* ctx, int count) {
         T.start = dalloc<int>((size_t)ctx->cell_cap + 1, e);
         T.grid = dalloc<DevGrid>(1, e);
         if (ctx->prm.heat_artificial) T.ulo = dalloc<float>(n, e);
+        if (ctx->prm.visc) {
+            T.tau = dalloc<float4>(n, e);
+            if (ctx->dim == 3) T.tau2 = dalloc<float4>(n, e);
+        }
         for (void* p : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
                         (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm, (void*)T.du,
-                        (void*)T.start, (void*)T.grid, (void*)T.ulo})
+                        (void*)T.start, (void*)T.grid, (void*)T.ulo, (void*)T.tau, (void*)T.tau2})
             ctx->owned.push_back(p);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "cudaMalloc(adjoint tape; a smaller checkpoint_every needs less)");
@@ -1894,13 +1917,20 @@ int launch_adjoint(armando_ctx* ctx, const StepArgs& S, const TapeSlot& T) {
     k_adj_force<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
                                                  ctx->adj_abar, ctx->adj_pbar, ctx->adj_rhobar,
                                                  ctx->adj_xF, ctx->adj_vhb, ctx->adj_divsb,
-                                                 ctx->adj_blk, n);
+                                                 ctx->adj_tbar, ctx->adj_tbar2, ctx->adj_blk, n);
+    int L = 4;
+    if (ctx->dp.visc) {
+        k_adj_shear<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp,
+                                                     ctx->adj_tbar, ctx->adj_tbar2,
+                                                     ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb, n);
+        ++L;
+    }
     k_adj_density<DIM><<<nb, kPassThreads, 0, st>>>(Bv, T.keys, T.start, T.grid, ctx->dp, S,
                                                    ctx->adj_rhobar, ctx->adj_xF, ctx->adj_vhb,
                                                    ctx->adj_xpart, ctx->adj_vpart, ctx->adj_divsb,
                                                    T.perm, ctx->adjGp, n);
     k_adj_params<<<1, 256, 0, st>>>(ctx->adj_blk, nb, ctx->adj_pacc);
-    return 4;
+    return L;
 }
 
 armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
@@ -1914,10 +1944,10 @@ armando_status run_adjoint(armando_ctx* ctx, const StepArgs& S, int t) {
 armando_status check_adjoint_support(armando_ctx* ctx) {
     if (ctx->n_inst > 1) return fail(ctx, ARMANDO_ERR_UNSUPPORTED, "reverse mode of one particle system only");
     const armando_params& p = ctx->prm;
-    if (p.pa_sph != 1 || p.visc || p.wall_model != 0 || p.scheme != 0 || step_options(p))
+    if (p.pa_sph != 1 || p.wall_model != 0 || p.scheme != 0 || step_options(p))
         return fail(ctx, ARMANDO_ERR_UNSUPPORTED,
                     "reverse mode supports pa_sph = 1, wall_model 0, summation density, without "
-                    "physical viscosity, XSPH or h evolution");
+                    "XSPH or h evolution");
     return ARMANDO_OK;
 }
 
@@ -2319,7 +2349,8 @@ armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
         for (const TapeSlot& T : ctx->tape)
             for (void* q : {(void*)T.xh, (void*)T.vm, (void*)T.vmin, (void*)T.rp, (void*)T.p,
                             (void*)T.itype, (void*)T.nmask, (void*)T.keys, (void*)T.perm,
-                            (void*)T.du, (void*)T.start, (void*)T.grid, (void*)T.ulo})
+                            (void*)T.du, (void*)T.start, (void*)T.grid, (void*)T.ulo,
+                            (void*)T.tau, (void*)T.tau2})
                 release(ctx, q);
         ctx->tape.clear();
     }

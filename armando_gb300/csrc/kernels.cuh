@@ -1132,6 +1132,23 @@ static_assert(kListCap2 <= 32 * mask_words<2>() && kListCap3 <= 32 * mask_words<
               "a list's neighbour bits fit one lane's mask");
 constexpr int kListCapD = 24;     // density pass: near and far lists each
 constexpr int kTestBatch = 4;     // candidate loads issued together
+// A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
+// at nlist + r * lstride + s0) requested into L2 at once, one row per lane, so
+// the walk's coalesced entry loads hit L2 instead of waiting on DRAM.
+// List entries whose loads a listed particle issues together (3D: fewer, the
+// passes' registers are taken by the float-float sums and the 3D state).
+template <int DIM>
+__host__ __device__ constexpr int list_batch() {
+    return DIM == 2 ? 4 : 2;
+}
+
+__device__ __forceinline__ void prefetch_list_rows(const int* nlist, int lstride, int s, int lc) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const int rows = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
+    const int s0 = __shfl_sync(0xffffffffu, s, 0);
+    for (int r = lane; r < rows; r += 32)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(nlist + (size_t)r * lstride + s0));
+}
 // 2D density pairs with q = r/h < near_q() are evaluated in float-float, the
 // others (W below ~1% of W(0) each, ~8 of ~20 pairs) in FP32. In 3D every pair
 // is float-float: ~50 of ~80 pairs lie beyond q = 1.6, and the FP32 rounding of
@@ -1306,7 +1323,8 @@ __device__ __forceinline__ int cursor_row(const Cursor& cu, int f) {
 // STG: the candidates come from the CTA's staged copy SV (LT: the list entry
 // type, staged indices), else from global memory through L1.
 // LST: a lazily sorting context's neighbour lists (B.nlist) replace the cell
-// walk for slots whose list fits; the neighbour bits then index list entries.
+// walk for slots whose list fits; those slots leave no neighbour bits (the
+// force pass re-tests their lists).
 // FUS: on iterations that do not sort, read the state from F.A (FusedSrc).
 template <int DIM, int TPP = 1, int BS = kPassThreads, bool LEAN = false, bool OPT = false,
           bool STG = false, class LT = int, bool LST = false, bool FUS = false>
@@ -1380,8 +1398,62 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     unsigned long long cur = 0ull;
     int shift = 0;  // staged index - slot in the cursor's row
     const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // list entries (-1: walk the cells)
-    int lt = 0;
     if (LST && lc >= 0) mask_on = false;
+    if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc);
+    // A listed particle evaluates every list entry in float-float as it is
+    // read (2D far pairs included) and keeps the terms of the entries that
+    // pass the pair test (a predicate, not a branch): no candidate lists in
+    // shared memory, no second load. The cell walk below serves the others.
+    if (LST) {
+        constexpr int NB = list_batch<DIM>();
+        const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
+        for (int t0 = 0; t0 < lcm; t0 += NB) {
+            int kb[NB];
+            float4 xb[NB], vb[NB];
+#pragma unroll
+            for (int u = 0; u < NB; ++u)
+                kb[u] = lc > 0 ? __ldg(B.nlist + (size_t)min(t0 + u, lc - 1) * B.lstride + s) : s;
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                xb[u] = __ldg(xsrc + kb[u]);
+                vb[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (DIM == 3 || need_div) vb[u] = __ldg(vsrc + kb[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                const int k = kb[u];
+                const float4 xj = xb[u];
+                float d[3], dr2;
+                bool in = t0 + u < lc && k != s && pair_delta<DIM>(xi, xj, g, d, dr2);
+                if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) in = false;  // push only
+                const float mj = mass_of<DIM>(xj, vb[u]);
+                float dh[3], dl[3];
+                exact_delta<DIM>(xi, xj, g, dh, dl);
+                sph::ff ih = ih_i, al = al_i;
+                if (xj.w != xi.w) {
+                    ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+                    al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
+                }
+                if (fluid) {
+                    const sph::ff wm = sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj);
+                    if (in) {
+                        sph::ff_acc(S, wm);
+                        if (nor) sph::ff_acc(Wn, sph::ff_mul(wm, sph::ff_recip(__ldg(B.q + k))));
+                    }
+                }
+                if (need_div && in) {
+                    const float4 vj = vb[u];
+                    const float r2 = sph::dist2_exact<DIM>(dh);
+                    const float gw = sph::wendland_grad_factor<DIM>(
+                        fast_sqrt_pos(r2), ih.hi, __fmul_rn(P.kg, pow_grad<DIM>(ih.hi)));
+                    float vd = fmaf(vj.y - vi.y, dh[1], __fmul_rn(vj.x - vi.x, dh[0]));
+                    if (DIM == 3) vd = fmaf(vj.z - vi.z, dh[2], vd);
+                    divs = fmaf(mj * gw, vd, divs);
+                }
+            }
+        }
+        if (lc >= 0) done = true;
+    }
     while (__any_sync(0xffffffffu, !done)) {
         int nn = 0, nf = 0;
         // Test phase: fill the near / far lists, kTestBatch candidate loads in flight.
@@ -1389,42 +1461,27 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             int kb[kTestBatch];
             int cnt;
             float4 xb[kTestBatch];
-            if (LST && lc >= 0) {
-                if (lt >= lc) {
+            if (cu.k >= cu.ke) {
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
                     done = true;
                     break;
                 }
-                if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
-                cnt = min(kTestBatch, lc - lt);
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u)
-                    kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(xsrc + kb[u]);
-                lt += cnt;
-            } else {
-                if (cu.k >= cu.ke) {
-                    if (!cursor_next<DIM>(g, start, cc, cu)) {
-                        done = true;
-                        break;
-                    }
-                    if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
-                    if (TPP > 1) {
-                        cu.k += sub;
-                        continue;
-                    }
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
+                if (TPP > 1) {
+                    cu.k += sub;
+                    continue;
                 }
-                if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
-                const int k0 = cu.k;
-                cnt = min(kTestBatch, lane_len<TPP>(cu));
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) {
-                    const int ku = min(k0 + u * TPP, cu.ke - 1);
-                    kb[u] = k0 + u * TPP;
-                    xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
-                }
-                cu.k += cnt * TPP;
             }
+            if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
+            const int k0 = cu.k;
+            cnt = min(kTestBatch, lane_len<TPP>(cu));
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                const int ku = min(k0 + u * TPP, cu.ke - 1);
+                kb[u] = k0 + u * TPP;
+                xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
+            }
+            cu.k += cnt * TPP;
             unsigned pb = 0u;  // pass bits of this batch
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
@@ -1749,7 +1806,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     // A listed particle walks its neighbour list (coalesced rows of entries)
     // and re-tests each entry; the others decode the density pass's bits.
     const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;
-    int lt = 0;
+    if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc);
     if (work && !(LST && lc >= 0)) {
         ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, 0);
         wbits = ch.x;
@@ -1757,106 +1814,24 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     }
     int wi = 0, rbase = 0;  // index of wbits; ordinal of the cursor row's first slot
     int shift = 0;          // staged index - slot in the cursor's row
-    while (__any_sync(0xffffffffu, !done)) {
-        int nl = 0;
-        while (!done && from_mask) {
-            if (nl == kListCap) break;
-            while (wbits == 0u && wi < W - 1) {
-                ++wi;
-                if (W > CW && wi % CW == 0) ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, wi / CW);
-                wbits = chunk_word(ch, wi % CW);
-            }
-            if (wbits == 0u) {
-                done = true;
-                break;
-            }
-            const int o = 32 * wi + __ffs(wbits) - 1;
-            wbits &= wbits - 1u;
-            bool in_rows = true;
-            while (o >= rbase + lane_len<TPP>(cu)) {  // move to the range holding ordinal o
-                rbase += lane_len<TPP>(cu);
-                if (!cursor_next<DIM>(g, start, cc, cu)) {
-                    in_rows = false;
-                    break;
-                }
-                cu.k += sub;
-                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
-            }
-            if (!in_rows) {  // cannot happen for a mask of this step's candidates
-                done = true;
-                break;
-            }
-            s_list[nl++][tid] = (LT)(cu.k + TPP * (o - rbase) + (STG ? shift : 0));
-        }
-        while (!done && !from_mask) {
-            int kb[kTestBatch];
-            int cnt;
-            float4 xb[kTestBatch];
-            if (LST && lc >= 0) {
-                if (lt >= lc) {
-                    done = true;
-                    break;
-                }
-                if (nl > kListCap - kTestBatch) break;
-                cnt = min(kTestBatch, lc - lt);
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u)
-                    kb[u] = __ldg(B.nlist + (size_t)(lt + min(u, cnt - 1)) * B.lstride + s);
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(xsrc + kb[u]);
-                lt += cnt;
-            } else {
-                if (cu.k >= cu.ke) {
-                    if (!cursor_next<DIM>(g, start, cc, cu)) {
-                        done = true;
-                        break;
-                    }
-                    if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
-                    if (TPP > 1) {
-                        cu.k += sub;
-                        continue;
-                    }
-                }
-                if (nl > kListCap - kTestBatch) break;
-                const int k0 = cu.k;
-                cnt = min(kTestBatch, lane_len<TPP>(cu));
-#pragma unroll
-                for (int u = 0; u < kTestBatch; ++u) {
-                    const int ku = min(k0 + u * TPP, cu.ke - 1);
-                    kb[u] = k0 + u * TPP;
-                    xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
-                }
-                cu.k += cnt * TPP;
-            }
-#pragma unroll
-            for (int u = 0; u < kTestBatch; ++u) {
-                float d[3], dr2;
-                const int k = kb[u];
-                if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
-                    s_list[nl++][tid] = (LT)(STG ? k + shift : k);
-            }
-        }
-        const int ml = __reduce_max_sync(0xffffffffu, nl);
-        for (int t = 0; t < ml; ++t) {
-            if (t >= nl) continue;
-            const int k = (int)s_list[t][tid];
-            const float4 xj = STG ? SV.x[k] : __ldg(xsrc + k);
+    // One pair's terms (pressure, viscosity, art_visc, art_heat, options).
+    // va, vb: the neighbour's 2D {vx, vy, rho, P} (vb unused) or 3D v and
+    // {rho, P, u, psi}; d, dr2 from the pair test.
+    auto pair_terms = [&](const int k, const float4& xj, const float4& va, const float4& vb,
+                          float* d, float dr2) {
             float4 vj, rpj;
-            if (DIM == 2) {  // {vx, vy, rho, P}; u and psi only for art_heat
-                const float4 vr = STG ? SV.v[k] : __ldg(B.vr + k);
-                vj = make_float4(vr.x, vr.y, 0.f, 0.f);
-                rpj = make_float4(vr.z, vr.w, 0.f, 0.f);
+            if (DIM == 2) {  // u and psi only for art_heat
+                vj = make_float4(va.x, va.y, 0.f, 0.f);
+                rpj = make_float4(va.z, va.w, 0.f, 0.f);
                 if (heat_art) {
                     const float4 r = __ldg(B.rp + k);
                     rpj.z = r.z;
                     rpj.w = r.w;
                 }
             } else {
-                vj = STG ? SV.v[k] : __ldg(B.vm + k);
-                rpj = STG ? SV.r[k] : __ldg(B.rp + k);
+                vj = va;
+                rpj = vb;
             }
-            float d[3], dr2;
-            pair_delta<DIM>(xi, xj, g, d, dr2);
             refine_periodic<DIM>(xi, xj, g, d, dr2);
             const float mj = mass_of<DIM>(xj, vj);
             float ih = ihf, kgih = kgih_i;
@@ -1887,7 +1862,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     a1 = fmaf(f, d[1], a1);
                     if (DIM == 3) a2 = fmaf(f, d[2], a2);
                 }
-                if (P.wall_model == 1) continue;  // no other interaction
+                if (P.wall_model == 1) return;  // no other interaction
             }
             const float t3 = q - 2.0f;
             const float gw = kgih * t3 * t3 * t3;
@@ -1970,6 +1945,119 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                 const float du_ij = (rpi.z - rpj.z) + (ulo_i - __ldg(B.ulo + k));
                 ah_du = fmaf(mj * psi, du_ij, ah_du);
             }
+    };
+    // A listed particle takes each entry's terms as the entry is read and
+    // passes the pair test, without a candidate list; the mask decoding and
+    // cell walk below serve the others.
+    if (LST) {
+        constexpr int NB = list_batch<DIM>();
+        const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
+        for (int t0 = 0; t0 < lcm; t0 += NB) {
+            int kb[NB];
+            float4 xb[NB];
+#pragma unroll
+            for (int u = 0; u < NB; ++u)
+                kb[u] = lc > 0 ? __ldg(B.nlist + (size_t)min(t0 + u, lc - 1) * B.lstride + s) : s;
+            // 2D: the neighbours' {vx, vy, rho, P} load with their positions; 3D
+            // loads v and {rho, P} once the pair test passed (registers).
+            float4 vr[NB];
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                xb[u] = __ldg(xsrc + kb[u]);
+                if (DIM == 2) vr[u] = __ldg(B.vr + kb[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < NB; ++u) {
+                float d[3], dr2;
+                if (t0 + u < lc && kb[u] != s && pair_delta<DIM>(xi, xb[u], g, d, dr2)) {
+                    if (DIM == 2)
+                        pair_terms(kb[u], xb[u], vr[u], vr[u], d, dr2);
+                    else
+                        pair_terms(kb[u], xb[u], __ldg(B.vm + kb[u]), __ldg(B.rp + kb[u]), d, dr2);
+                }
+            }
+        }
+        if (lc >= 0) done = true;
+    }
+    while (__any_sync(0xffffffffu, !done)) {
+        int nl = 0;
+        while (!done && from_mask) {
+            if (nl == kListCap) break;
+            while (wbits == 0u && wi < W - 1) {
+                ++wi;
+                if (W > CW && wi % CW == 0) ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, wi / CW);
+                wbits = chunk_word(ch, wi % CW);
+            }
+            if (wbits == 0u) {
+                done = true;
+                break;
+            }
+            const int o = 32 * wi + __ffs(wbits) - 1;
+            wbits &= wbits - 1u;
+            bool in_rows = true;
+            while (o >= rbase + lane_len<TPP>(cu)) {  // move to the range holding ordinal o
+                rbase += lane_len<TPP>(cu);
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
+                    in_rows = false;
+                    break;
+                }
+                cu.k += sub;
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
+            }
+            if (!in_rows) {  // cannot happen for a mask of this step's candidates
+                done = true;
+                break;
+            }
+            s_list[nl++][tid] = (LT)(cu.k + TPP * (o - rbase) + (STG ? shift : 0));
+        }
+        while (!done && !from_mask) {
+            int kb[kTestBatch];
+            int cnt;
+            float4 xb[kTestBatch];
+            if (cu.k >= cu.ke) {
+                if (!cursor_next<DIM>(g, start, cc, cu)) {
+                    done = true;
+                    break;
+                }
+                if (STG) shift = SV.shift[cursor_row<DIM>(cu, g.reach)];
+                if (TPP > 1) {
+                    cu.k += sub;
+                    continue;
+                }
+            }
+            if (nl > kListCap - kTestBatch) break;
+            const int k0 = cu.k;
+            cnt = min(kTestBatch, lane_len<TPP>(cu));
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                const int ku = min(k0 + u * TPP, cu.ke - 1);
+                kb[u] = k0 + u * TPP;
+                xb[u] = STG ? SV.x[ku + shift] : __ldg(xsrc + ku);
+            }
+            cu.k += cnt * TPP;
+#pragma unroll
+            for (int u = 0; u < kTestBatch; ++u) {
+                float d[3], dr2;
+                const int k = kb[u];
+                if (u < cnt && k != s && pair_delta<DIM>(xi, xb[u], g, d, dr2))
+                    s_list[nl++][tid] = (LT)(STG ? k + shift : k);
+            }
+        }
+        const int ml = __reduce_max_sync(0xffffffffu, nl);
+        for (int t = 0; t < ml; ++t) {
+            if (t >= nl) continue;
+            const int k = (int)s_list[t][tid];
+            const float4 xj = STG ? SV.x[k] : __ldg(xsrc + k);
+            float4 va, vb = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (DIM == 2) {
+                va = STG ? SV.v[k] : __ldg(B.vr + k);
+            } else {
+                va = STG ? SV.v[k] : __ldg(B.vm + k);
+                vb = STG ? SV.r[k] : __ldg(B.rp + k);
+            }
+            float d[3], dr2;
+            pair_delta<DIM>(xi, xj, g, d, dr2);
+            pair_terms(k, xj, va, vb, d, dr2);
         }
     }
     if (TPP > 1) {  // the particle's lanes reach this point together

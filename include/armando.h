@@ -275,8 +275,11 @@ typedef struct armando_param_grads {
  * Reverse mode, step 1: armando_integrate over `steps` iterations its0.., also
  * keeping the state before every checkpoint_every-th iteration on the device
  * for armando_backward. Outputs the final state like armando_integrate.
- * Supports pa_sph = 1 without physical viscosity and without artificial heat
- * (ARMANDO_ERR_UNSUPPORTED otherwise); one particle system (no batch).
+ * Supports pa_sph = 1 with artificial viscosity, artificial heat, physical
+ * viscosity and the external heat source, wall_model 0, summation density
+ * (ARMANDO_ERR_UNSUPPORTED otherwise: XSPH, h evolution, continuity or
+ * normalised density, the wall models, the GPU-C schemes); one particle
+ * system (no batch).
  */
 armando_status armando_forward_checkpointed(armando_ctx* ctx, float* x, float* vx,
                                            const float* mass, float* rho, float* p, float* u,

@@ -260,6 +260,57 @@ def test_art_heat_gradients_match_tangent_linear(O, dim, steps, tol):
         assert e <= tol, (k, a, b, e)
 
 
+def visc_case(dim):
+    """Physical viscosity on (internal_force.f:75-171): the lid-driven cavity
+    with a perturbed velocity field in 2D; in 3D a small channel section with
+    viscosity, artificial heat and nonuniform energy together."""
+    if dim == 2:
+        return cases.perturbed(cases.cavity(), seed=5, dv=2e-4)
+    c = cases.perturbed(cases.channel(n_x=16, n_yz=8, length=16 * 7.9e-4, width=8 * 7.9e-4,
+                                      layers=2, jitter=0.01), seed=77, dv=0.05, du=200.0)
+    c.params.heat_external = 0
+    c.params.visc = 1
+    c.params.eta = 1.0e-3
+    c.params.heat_artificial = 1
+    c.params.ah_g1, c.params.ah_g2 = 0.1, 1.0
+    return c
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("steps,tol", [(1, TOL_ONE), (STEPS, TOL_GRAD)])
+def test_viscosity_gradients_match_tangent_linear(O, dim, steps, tol):
+    """The reverse of the shear tensors (every particle's, walls included),
+    their pair forces and their heating: c0 (and alpha in 3D) and directions
+    of the initial x, v, u against the FP64 tangent-linear."""
+    c = visc_case(dim)
+    x = c.x.reshape(-1, dim)[c.itype > 0]
+    centre = 0.5 * (x.min(0) + x.max(0))
+    radius = 0.3 * float((x.max(0) - x.min(0)).min())
+    spec = O.LossSpec.make(w_ke=1.0, w_p=1e-6, w_u=1.0, c=tuple(centre), radius=radius,
+                           w_ref=1.0)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.forward_checkpointed(got, c.dt, 1, steps, 2)
+        _, cot = loss_and_cotangents(got.arrays(), c.dim, c.mass, c.itype, spec)
+        g = ctx.backward(**cot)
+    checks = {"c0": (g["params"]["c0"],
+                     O.tangent(O.State(c), 1, steps, c.dt, spec, dparam=[0.0, 0.0, 1.0, 0.0])[1])}
+    if dim == 3:
+        checks["av_alpha"] = (g["params"]["av_alpha"], O.tangent(
+            O.State(c), 1, steps, c.dt, spec, dparam=[1.0, 0.0, 0.0, 0.0])[1])
+    for which in ("x", "v", "u"):
+        # along the sign pattern of the gradient: on the cavity's lattice a
+        # Gaussian direction's dot product cancels to a part in ~1e3
+        gw = g[which].astype(np.float64)
+        d = np.abs(_direction(c, which)) * np.sign(gw)
+        checks[which] = (float(np.dot(gw, d)),
+                         O.tangent(O.State(c), 1, steps, c.dt, spec, **_seed_kw(which, d))[1])
+    for k, (a, b) in checks.items():
+        e = _rel(a, b)
+        print("visc", dim, steps, k, a, b, f"{e:.2e}")
+        assert e <= tol, (k, a, b, e)
+
+
 def _c5_setup(O):
     c = cases.adjoint_dam_break()
     assert c.n == 260_904

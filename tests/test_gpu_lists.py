@@ -2,12 +2,13 @@
 
 With a sort skin, the iterations that sort build, for every particle, the list
 of candidates within h_i + h_j + skin (k_build_list); until the next sort the
-passes read the lists instead of walking the cells, and the neighbour bits of
-the density pass index list entries. The lists hold the candidates in the cell
-walk's order, so in 2D (fewer than one round of near and far pairs) the
-results are the same bits as walking the cells (ARMANDO_NEIGHBOUR_LISTS=0); in
-3D the summation rounds differ and the gate is the oracle. Particles whose
-list would exceed its capacity walk their cells (a compressed clump).
+passes read the lists instead of walking the cells. A listed particle's
+density pass evaluates each entry in float-float as it reads it and keeps the
+terms of the entries that pass the pair test; its force pass does the same
+with the pair forces. The neighbour sets are the cell walk's; the summation
+order and (2D) the far pairs' arithmetic differ, so the gates are the oracle
+for one iteration and the cell walk to 1e-5 over many. Particles whose list
+would exceed its capacity walk their cells (a compressed clump).
 """
 import os
 
@@ -47,13 +48,49 @@ def _run(c, tuning, its0, steps, lists):
 
 
 @pytest.mark.parametrize("tuning", [(1, 1, 128, 10), (3, 1, 256, 10), (2, 1, 128, 40)])
-def test_lists_equal_cell_walk_2d(tuning):
+def test_lists_20_iterations_within_conditioning_2d(O, tuning):
+    """20 iterations on the lists (a few sort), against 20 FP64 oracle
+    iterations: within 20 times the oracle's own divergence when its FP32
+    inputs move by one ulp (the trajectory's conditioning; the perturbed dam
+    break amplifies rounding), or 1e-5. The cell walk is held to the same."""
     c = cases.perturbed(cases.dam_break(dx=0.01), seed=61, dv=0.2)
-    a, sa = _run(c, tuning, 1, 40, True)
-    b, sb = _run(c, tuning, 1, 40, False)
-    assert sa == sb and 1 <= sa < 40
+    a, sa = _run(c, tuning, 1, 20, True)
+    b, sb = _run(c, tuning, 1, 20, False)
+    assert 1 <= sa < 20
+    rng = np.random.default_rng(69)
+    twin = c.copy()
+    fl = np.repeat(c.itype > 0, 2)
+    bump = np.where(rng.random(c.x.size) < 0.5, np.inf, -np.inf).astype(np.float32)
+    twin.x = np.where(fl, np.nextafter(c.x, bump), c.x).astype(np.float32)
+    ref, pert = O.State(c), O.State(twin)
+    O.integrate_gather(ref, 1, 20, c.dt)
+    O.integrate_gather(pert, 1, 20, c.dt)
     for f in FIELDS:
-        assert np.array_equal(getattr(a, f), getattr(b, f)), (tuning, f)
+        cond = rel_err(getattr(pert, f), getattr(ref, f))
+        ea, eb = rel_err(getattr(a, f), getattr(ref, f)), rel_err(getattr(b, f), getattr(ref, f))
+        print(tuning, f, f"lists {ea:.1e} cell walk {eb:.1e} one-ulp twin {cond:.1e}")
+        assert ea <= max(20.0 * cond, 1e-5), (tuning, f, ea, cond)
+        assert eb <= max(20.0 * cond, 1e-5), (tuning, f, eb, cond)
+
+
+@pytest.mark.parametrize("tuning", [(1, 1, 128, 10), (3, 1, 256, 10)])
+def test_listed_iteration_parity_2d(O, tuning):
+    """One iteration on the lists (it does not sort) against one FP64 oracle
+    iteration from the same FP32 state, the output of a first one-step call."""
+    c = history_state(O, cases.perturbed(cases.dam_break(dx=0.01), seed=68, dv=0.05), steps=2)
+    mid = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(*tuning)
+        ctx.step(mid, c.dt, 3)
+    ref = O.State(mid)
+    O.step(ref, 4, c.dt)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(*tuning)
+        ctx.integrate(got, c.dt, 3, 2)
+        assert ctx.stats().sorts_done == 1
+    for f in FIELDS:
+        assert rel_err(getattr(got, f), getattr(ref, f)) <= 1e-5, (tuning, f)
 
 
 def _with_extra_copies(c, idx, offsets):
@@ -73,11 +110,11 @@ def _with_extra_copies(c, idx, offsets):
     return out
 
 
-def test_lists_with_overflow_patch_2d():
+def test_lists_with_overflow_patch_2d(O):
     """A patch at three times the lattice density (two shifted copies of 100
     particles): lists there exceed their capacity and those particles walk
-    their cells, beside listed ones; one iteration (it sorts and uses the
-    lists), against the cell walk bit for bit."""
+    their cells, beside listed ones. One iteration (it sorts and uses the
+    lists) against the FP64 oracle, and against the cell walk."""
     c = cases.perturbed(cases.dam_break(dx=0.01), seed=62, dv=0.05)
     fl = np.flatnonzero(c.itype > 0)
     x = c.x.reshape(-1, 2)
@@ -86,8 +123,11 @@ def test_lists_with_overflow_patch_2d():
     c = _with_extra_copies(c, patch, [0.33, 0.66])
     a, _ = _run(c, (1, 1, 128, 40), 1, 1, True)
     b, _ = _run(c, (1, 1, 128, 40), 1, 1, False)
+    ref = O.State(c)
+    O.step(ref, 1, c.dt)
     for f in FIELDS:
-        assert np.array_equal(getattr(a, f), getattr(b, f)), f
+        assert rel_err(getattr(a, f), getattr(ref, f)) <= 1e-5, f
+        assert rel_err(getattr(a, f), getattr(b, f)) <= 1e-5, f
 
 
 def test_lists_3d_channel_against_oracle(O):

@@ -46,3 +46,25 @@ def test_tangent_linear_matches_central_differences_velocity(O):
     s2.v = st.v - e * dv
     fd = (O.loss(s1, 1, 10, c.dt, spec) - O.loss(s2, 1, 10, c.dt, spec)) / (2 * e)
     assert abs(dL - fd) <= 1e-5 * abs(fd), (dL, fd)
+
+
+def visc_case():
+    """The lid-driven cavity (physical viscosity, internal_force.f:75-171) with
+    a perturbed velocity field, so the shear tensors and their heating carry
+    gradient everywhere."""
+    return cases.perturbed(cases.cavity(), seed=5, dv=2e-4)
+
+
+def test_tangent_linear_with_viscosity_matches_central_differences(O):
+    c = visc_case()
+    st = O.State(c)
+    spec = O.LossSpec.make(w_ke=1.0, w_p=1e-6, w_u=1.0, c=(5e-4, 5e-4), radius=3e-4)
+    rng = np.random.default_rng(1)
+    dv = rng.standard_normal(st.v.size) * np.repeat(c.itype > 0, 2)
+    _, dL = O.tangent(st, 1, 5, c.dt, spec, dv0=dv)
+    e = 1e-7
+    s1, s2 = O.State(c), O.State(c)
+    s1.v = st.v + e * dv
+    s2.v = st.v - e * dv
+    fd = (O.loss(s1, 1, 5, c.dt, spec) - O.loss(s2, 1, 5, c.dt, spec)) / (2 * e)
+    assert abs(dL - fd) <= 1e-5 * abs(fd), (dL, fd)
