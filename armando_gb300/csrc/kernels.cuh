@@ -126,6 +126,7 @@ struct StateB {  // working set of one step (cell order)
     float* q;      // density at the iteration's start (continuity and normalised density)
     float* rlo;    // rounding residual of the predicted density (continuity)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
+    float4* xv;    // 2D with lists: {x, y, m, h} and {vx, vy, rho, P} of a slot side by side
     float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour lists of a lazily sorting context (built on the iterations that
     // sort): entry t of slot s at nlist[t * n + s], the candidates within
@@ -1135,12 +1136,21 @@ constexpr int kTestBatch = 4;     // candidate loads issued together
 // A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
 // at nlist + r * lstride + s0) requested into L2 at once, one row per lane, so
 // the walk's coalesced entry loads hit L2 instead of waiting on DRAM.
+// The density pass's list walk loads the next batch's entries before
+// evaluating this one (the force pass's registers do not allow it).
+constexpr bool kListPipeline = true;
+constexpr bool kForceListPipeline = false;
+
 // List entries whose loads a listed particle issues together (3D: fewer, the
 // passes' registers are taken by the float-float sums and the 3D state).
 template <int DIM>
 __host__ __device__ constexpr int list_batch() {
     return DIM == 2 ? 4 : 2;
 }
+constexpr int kForceListBatch2 = 4;  // the force pass's batch in 2D
+// 2D with lists: the density pass writes each slot's position and {v, rho, P}
+// side by side (B.xv), which the force pass reads as one record per neighbour.
+constexpr bool kForceRecord = false;
 
 __device__ __forceinline__ void prefetch_list_rows(const int* nlist, int lstride, int s, int lc) {
     const int lane = (int)(threadIdx.x & 31u);
@@ -1407,12 +1417,22 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     if (LST) {
         constexpr int NB = list_batch<DIM>();
         const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
+        // (a lane past the last slot reads slot 0: its loads stay in bounds)
+        auto entry = [&](int t) {
+            return lc > 0 ? __ldg(B.nlist + (size_t)min(t, lc - 1) * B.lstride + s) : (valid ? s : 0);
+        };
+        int kn[NB];  // kListPipeline: the next batch's entries, loaded one batch ahead
+#pragma unroll
+        for (int u = 0; u < NB; ++u) kn[u] = kListPipeline ? entry(u) : 0;
         for (int t0 = 0; t0 < lcm; t0 += NB) {
             int kb[NB];
             float4 xb[NB], vb[NB];
 #pragma unroll
-            for (int u = 0; u < NB; ++u)
-                kb[u] = lc > 0 ? __ldg(B.nlist + (size_t)min(t0 + u, lc - 1) * B.lstride + s) : s;
+            for (int u = 0; u < NB; ++u) kb[u] = kListPipeline ? kn[u] : entry(t0 + u);
+            if (kListPipeline && t0 + NB < lcm) {
+#pragma unroll
+                for (int u = 0; u < NB; ++u) kn[u] = entry(t0 + NB + u);
+            }
 #pragma unroll
             for (int u = 0; u < NB; ++u) {
                 xb[u] = __ldg(xsrc + kb[u]);
@@ -1617,6 +1637,10 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
         B.rp[s] = rp;
         if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
+        if (LST && DIM == 2 && kForceRecord) {
+            B.xv[2 * (size_t)s] = xi;
+            B.xv[2 * (size_t)s + 1] = make_float4(vi.x, vi.y, rp.x, rp.y);
+        }
         return;
     }
     float rho = rp.x;
@@ -1649,6 +1673,10 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     }
     B.rp[s] = rp;
     if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
+    if (LST && DIM == 2 && kForceRecord) {
+        B.xv[2 * (size_t)s] = xi;
+        B.xv[2 * (size_t)s + 1] = make_float4(vi.x, vi.y, rp.x, rp.y);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1950,21 +1978,36 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     // passes the pair test, without a candidate list; the mask decoding and
     // cell walk below serve the others.
     if (LST) {
-        constexpr int NB = list_batch<DIM>();
+        constexpr int NB = DIM == 2 ? kForceListBatch2 : list_batch<DIM>();
         const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
+        // (a lane past the last slot reads slot 0: its loads stay in bounds)
+        auto entry = [&](int t) {
+            return lc > 0 ? __ldg(B.nlist + (size_t)min(t, lc - 1) * B.lstride + s) : (valid ? s : 0);
+        };
+        int kn[NB];  // kForceListPipeline: the next batch's entries, loaded one batch ahead
+#pragma unroll
+        for (int u = 0; u < NB; ++u) kn[u] = kForceListPipeline ? entry(u) : 0;
         for (int t0 = 0; t0 < lcm; t0 += NB) {
             int kb[NB];
             float4 xb[NB];
 #pragma unroll
-            for (int u = 0; u < NB; ++u)
-                kb[u] = lc > 0 ? __ldg(B.nlist + (size_t)min(t0 + u, lc - 1) * B.lstride + s) : s;
+            for (int u = 0; u < NB; ++u) kb[u] = kForceListPipeline ? kn[u] : entry(t0 + u);
+            if (kForceListPipeline && t0 + NB < lcm) {
+#pragma unroll
+                for (int u = 0; u < NB; ++u) kn[u] = entry(t0 + NB + u);
+            }
             // 2D: the neighbours' {vx, vy, rho, P} load with their positions; 3D
             // loads v and {rho, P} once the pair test passed (registers).
             float4 vr[NB];
 #pragma unroll
             for (int u = 0; u < NB; ++u) {
-                xb[u] = __ldg(xsrc + kb[u]);
-                if (DIM == 2) vr[u] = __ldg(B.vr + kb[u]);
+                if (DIM == 2 && kForceRecord) {  // one 32-byte record per neighbour
+                    xb[u] = __ldg(B.xv + 2 * (size_t)kb[u]);
+                    vr[u] = __ldg(B.xv + 2 * (size_t)kb[u] + 1);
+                } else {
+                    xb[u] = __ldg(xsrc + kb[u]);
+                    if (DIM == 2) vr[u] = __ldg(B.vr + kb[u]);
+                }
             }
 #pragma unroll
             for (int u = 0; u < NB; ++u) {
