@@ -2372,12 +2372,6 @@ armando_status apply_tuning(armando_ctx* ctx, const armando_tuning& t) {
         ctx->owned.push_back(nc);
         ctx->B.nlist = nl;
         ctx->B.ncount = nc;
-        if (ctx->dim == 2) {  // {x, y, m, h} and {vx, vy, rho, P} per slot
-            float4* xv = dalloc<float4>(2 * (size_t)std::max<int64_t>(ctx->cap, 1), e);
-            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(neighbour records)");
-            ctx->owned.push_back(xv);
-            ctx->B.xv = xv;
-        }
         ctx->B.lcap = lcap;
         ctx->B.lstride = (int)ctx->cap;
     }

@@ -126,7 +126,6 @@ struct StateB {  // working set of one step (cell order)
     float* q;      // density at the iteration's start (continuity and normalised density)
     float* rlo;    // rounding residual of the predicted density (continuity)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
-    float4* xv;    // 2D with lists: {x, y, m, h} and {vx, vy, rho, P} of a slot side by side
     float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour lists of a lazily sorting context (built on the iterations that
     // sort): entry t of slot s at nlist[t * n + s], the candidates within
@@ -1132,25 +1131,31 @@ constexpr int kListCap3 = 256;
 static_assert(kListCap2 <= 32 * mask_words<2>() && kListCap3 <= 32 * mask_words<3>(),
               "a list's neighbour bits fit one lane's mask");
 constexpr int kListCapD = 24;     // density pass: near and far lists each
+// With neighbour lists only the particles whose list overflowed fill these
+// candidate lists: smaller ones leave the SM's shared storage to L1.
+constexpr int kListCapLst = 4;
+template <bool LST>
+__host__ __device__ constexpr int cap_density() {
+    return LST ? kListCapLst : kListCapD;
+}
+template <bool LST>
+__host__ __device__ constexpr int cap_force() {
+    return LST ? kListCapLst : kListCap;
+}
 constexpr int kTestBatch = 4;     // candidate loads issued together
-// A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
-// at nlist + r * lstride + s0) requested into L2 at once, one row per lane, so
-// the walk's coalesced entry loads hit L2 instead of waiting on DRAM.
-// The density pass's list walk loads the next batch's entries before
-// evaluating this one (the force pass's registers do not allow it).
-constexpr bool kListPipeline = true;
-constexpr bool kForceListPipeline = false;
 
 // List entries whose loads a listed particle issues together (3D: fewer, the
-// passes' registers are taken by the float-float sums and the 3D state).
+// passes' registers are taken by the float-float sums and the 3D state). The
+// density pass loads the next batch's entries before evaluating this one (the
+// force pass's registers do not allow it).
 template <int DIM>
 __host__ __device__ constexpr int list_batch() {
     return DIM == 2 ? 4 : 2;
 }
-constexpr int kForceListBatch2 = 4;  // the force pass's batch in 2D
-// 2D with lists: the density pass writes each slot's position and {v, rho, P}
-// side by side (B.xv), which the force pass reads as one record per neighbour.
-constexpr bool kForceRecord = false;
+
+// A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
+// at nlist + r * lstride + s0) requested into L2 at once, one row per lane, so
+// the walk's coalesced entry loads hit L2 instead of waiting on DRAM.
 
 __device__ __forceinline__ void prefetch_list_rows(const int* nlist, int lstride, int s, int lc) {
     const int lane = (int)(threadIdx.x & 31u);
@@ -1421,15 +1426,15 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         auto entry = [&](int t) {
             return lc > 0 ? __ldg(B.nlist + (size_t)min(t, lc - 1) * B.lstride + s) : (valid ? s : 0);
         };
-        int kn[NB];  // kListPipeline: the next batch's entries, loaded one batch ahead
+        int kn[NB];  // the next batch's entries, loaded one batch ahead
 #pragma unroll
-        for (int u = 0; u < NB; ++u) kn[u] = kListPipeline ? entry(u) : 0;
+        for (int u = 0; u < NB; ++u) kn[u] = entry(u);
         for (int t0 = 0; t0 < lcm; t0 += NB) {
             int kb[NB];
             float4 xb[NB], vb[NB];
 #pragma unroll
-            for (int u = 0; u < NB; ++u) kb[u] = kListPipeline ? kn[u] : entry(t0 + u);
-            if (kListPipeline && t0 + NB < lcm) {
+            for (int u = 0; u < NB; ++u) kb[u] = kn[u];
+            if (t0 + NB < lcm) {
 #pragma unroll
                 for (int u = 0; u < NB; ++u) kn[u] = entry(t0 + NB + u);
             }
@@ -1492,7 +1497,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                     continue;
                 }
             }
-            if (nn > kListCapD - kTestBatch || nf > kListCapD - kTestBatch) break;
+            if (nn > cap_density<LST>() - kTestBatch || nf > cap_density<LST>() - kTestBatch) break;
             const int k0 = cu.k;
             cnt = min(kTestBatch, lane_len<TPP>(cu));
 #pragma unroll
@@ -1637,10 +1642,6 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
         rp.y = (P.pa_sph == 1) ? __fdiv_rn(p, __fmul_rn(rp.x, rp.x)) : p;
         B.rp[s] = rp;
         if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
-        if (LST && DIM == 2 && kForceRecord) {
-            B.xv[2 * (size_t)s] = xi;
-            B.xv[2 * (size_t)s + 1] = make_float4(vi.x, vi.y, rp.x, rp.y);
-        }
         return;
     }
     float rho = rp.x;
@@ -1673,10 +1674,6 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     }
     B.rp[s] = rp;
     if (DIM == 2) B.vr[s] = make_float4(vi.x, vi.y, rp.x, rp.y);
-    if (LST && DIM == 2 && kForceRecord) {
-        B.xv[2 * (size_t)s] = xi;
-        B.xv[2 * (size_t)s + 1] = make_float4(vi.x, vi.y, rp.x, rp.y);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1978,36 +1975,24 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     // passes the pair test, without a candidate list; the mask decoding and
     // cell walk below serve the others.
     if (LST) {
-        constexpr int NB = DIM == 2 ? kForceListBatch2 : list_batch<DIM>();
+        constexpr int NB = list_batch<DIM>();
         const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
         // (a lane past the last slot reads slot 0: its loads stay in bounds)
         auto entry = [&](int t) {
             return lc > 0 ? __ldg(B.nlist + (size_t)min(t, lc - 1) * B.lstride + s) : (valid ? s : 0);
         };
-        int kn[NB];  // kForceListPipeline: the next batch's entries, loaded one batch ahead
-#pragma unroll
-        for (int u = 0; u < NB; ++u) kn[u] = kForceListPipeline ? entry(u) : 0;
         for (int t0 = 0; t0 < lcm; t0 += NB) {
             int kb[NB];
             float4 xb[NB];
 #pragma unroll
-            for (int u = 0; u < NB; ++u) kb[u] = kForceListPipeline ? kn[u] : entry(t0 + u);
-            if (kForceListPipeline && t0 + NB < lcm) {
-#pragma unroll
-                for (int u = 0; u < NB; ++u) kn[u] = entry(t0 + NB + u);
-            }
+            for (int u = 0; u < NB; ++u) kb[u] = entry(t0 + u);
             // 2D: the neighbours' {vx, vy, rho, P} load with their positions; 3D
             // loads v and {rho, P} once the pair test passed (registers).
             float4 vr[NB];
 #pragma unroll
             for (int u = 0; u < NB; ++u) {
-                if (DIM == 2 && kForceRecord) {  // one 32-byte record per neighbour
-                    xb[u] = __ldg(B.xv + 2 * (size_t)kb[u]);
-                    vr[u] = __ldg(B.xv + 2 * (size_t)kb[u] + 1);
-                } else {
-                    xb[u] = __ldg(xsrc + kb[u]);
-                    if (DIM == 2) vr[u] = __ldg(B.vr + kb[u]);
-                }
+                xb[u] = __ldg(xsrc + kb[u]);
+                if (DIM == 2) vr[u] = __ldg(B.vr + kb[u]);
             }
 #pragma unroll
             for (int u = 0; u < NB; ++u) {
@@ -2025,7 +2010,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     while (__any_sync(0xffffffffu, !done)) {
         int nl = 0;
         while (!done && from_mask) {
-            if (nl == kListCap) break;
+            if (nl == cap_force<LST>()) break;
             while (wbits == 0u && wi < W - 1) {
                 ++wi;
                 if (W > CW && wi % CW == 0) ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, wi / CW);
@@ -2068,7 +2053,7 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
                     continue;
                 }
             }
-            if (nl > kListCap - kTestBatch) break;
+            if (nl > cap_force<LST>() - kTestBatch) break;
             const int k0 = cu.k;
             cnt = min(kTestBatch, lane_len<TPP>(cu));
 #pragma unroll
@@ -2210,8 +2195,8 @@ template <int DIM, int TPP, int BS, bool PER, bool LEAN, bool OPT = false, bool 
 __global__ void __launch_bounds__(BS, 1024 / BS)
     k_density(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
               const DevGrid* __restrict__ gp, DevParams P, int n, FusedSrc F) {
-    __shared__ int s_near[kListCapD][BS];
-    __shared__ int s_far[kListCapD][BS];
+    __shared__ int s_near[cap_density<LST>()][BS];
+    __shared__ int s_far[cap_density<LST>()][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
     density_body<DIM, TPP, BS, LEAN, OPT, false, int, LST, FUS>(B, keys, start, g, P, s, s < n,
@@ -2281,7 +2266,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
     k_force(StateB B, StateA A, const unsigned* __restrict__ keys, const int* __restrict__ start,
             const DevGrid* __restrict__ gp, DevParams P, StepArgs S, unsigned* __restrict__ flags,
             int n, FusedSrc F) {
-    __shared__ int s_list[kListCap][BS];
+    __shared__ int s_list[cap_force<LST>()][BS];
     const int s = blockIdx.x * (BS / TPP) + (int)threadIdx.x / TPP;
     const DevGrid g = load_grid<PER>(gp);
     force_body<DIM, TPP, BS, LEAN, OPT, false, int, LST, FUS>(B, A, keys, start, g, P, S, flags, s,
