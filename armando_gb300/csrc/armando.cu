@@ -430,13 +430,14 @@ int launch_build_list(armando_ctx* ctx, const int* rs, cudaStream_t st) {
     const int n = (int)ctx->n_work;
     const unsigned* skeys = ctx->keys[ctx->passes & 1];
     const int* perm = ctx->vals[ctx->passes & 1];
+    k_sorted_positions<<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, n, rs);
     if (ctx->dp.periodic[0] || ctx->dp.periodic[1] || ctx->dp.periodic[2])
         k_build_list<DIM, true><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-            ctx->A, perm, ctx->B, skeys, ctx->start, ctx->grid, n, rs);
+            ctx->B, skeys, ctx->start, ctx->grid, n, rs);
     else
         k_build_list<DIM, false><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
-            ctx->A, perm, ctx->B, skeys, ctx->start, ctx->grid, n, rs);
-    return 1;
+            ctx->B, skeys, ctx->start, ctx->grid, n, rs);
+    return 2;
 }
 
 // End of a lazily sorting iteration: the next one sorts if this one flagged

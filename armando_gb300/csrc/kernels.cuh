@@ -856,6 +856,16 @@ __global__ void k_reorder_dim(StateA A, const int* __restrict__ perm, StateB B, 
     B.id[s] = A.id[j];
 }
 
+// Positions in cell order on an iteration that sorts (B.xsort), read by the
+// list build as contiguous candidate ranges.
+__global__ void k_sorted_positions(StateA A, const int* __restrict__ perm, StateB B, int n,
+                                   const int* __restrict__ resort) {
+    if (sort_skipped(resort)) return;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    B.xsort[s] = A.xh[perm[s]];
+}
+
 // Positions only (neighbour entry point).
 __global__ void k_reorder_xh(StateA A, const int* __restrict__ perm, StateB B, int n) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2213,8 +2223,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
 // (r < h_i + h_j) on those iterations is in the list.
 template <int DIM, bool PER>
 __global__ void __launch_bounds__(kPassThreads)
-    k_build_list(StateA A, const int* __restrict__ perm, StateB B,
-                 const unsigned* __restrict__ keys, const int* __restrict__ start,
+    k_build_list(StateB B, const unsigned* __restrict__ keys, const int* __restrict__ start,
                  const DevGrid* __restrict__ gp, int n, const int* __restrict__ resort = nullptr) {
     if (sort_skipped(resort)) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2224,7 +2233,7 @@ __global__ void __launch_bounds__(kPassThreads)
         B.ncount[s] = 0;
         return;
     }
-    const float4 xi = A.xh[perm[s]];
+    const float4 xi = B.xsort[s];
     const CellCoord cc = decode_key<DIM>(keys[s], g);
     const float pad = (1.0f + 0x1p-14f);
     int cnt = 0;
@@ -2233,8 +2242,7 @@ __global__ void __launch_bounds__(kPassThreads)
         for (int k0 = cu.k; k0 < cu.ke; k0 += kTestBatch) {
             float4 xb[kTestBatch];
 #pragma unroll
-            for (int u = 0; u < kTestBatch; ++u)
-                xb[u] = __ldg(A.xh + __ldg(perm + min(k0 + u, cu.ke - 1)));
+            for (int u = 0; u < kTestBatch; ++u) xb[u] = __ldg(B.xsort + min(k0 + u, cu.ke - 1));
 #pragma unroll
             for (int u = 0; u < kTestBatch; ++u) {
                 const int k = k0 + u;
