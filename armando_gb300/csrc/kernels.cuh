@@ -1154,13 +1154,16 @@ __host__ __device__ constexpr int cap_force() {
 }
 constexpr int kTestBatch = 4;     // candidate loads issued together
 
-// List entries whose loads a listed particle issues together (3D: fewer, the
-// passes' registers are taken by the float-float sums and the 3D state). The
-// density pass loads the next batch's entries before evaluating this one (the
-// force pass's registers do not allow it).
+// List entries whose loads a listed particle issues together, measured best:
+// the force pass 4 in 2D, 2 in 3D (its registers); the density pass, which
+// also loads the next batch's entries before evaluating this one, 2.
 template <int DIM>
 __host__ __device__ constexpr int list_batch() {
     return DIM == 2 ? 4 : 2;
+}
+template <int DIM>
+__host__ __device__ constexpr int density_list_batch() {
+    return 2;
 }
 
 // A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
@@ -1426,11 +1429,11 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     if (LST && lc >= 0) mask_on = false;
     if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc);
     // A listed particle evaluates every list entry in float-float as it is
-    // read (2D far pairs included) and keeps the terms of the entries that
-    // pass the pair test (a predicate, not a branch): no candidate lists in
-    // shared memory, no second load. The cell walk below serves the others.
+    // read (2D far pairs included); the kernel is zero beyond its support, so
+    // the entries need no pair test: no candidate lists in shared memory, no
+    // second load. The cell walk below serves the others.
     if (LST) {
-        constexpr int NB = list_batch<DIM>();
+        constexpr int NB = density_list_batch<DIM>();
         const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
         // (a lane past the last slot reads slot 0: its loads stay in bounds)
         auto entry = [&](int t) {
@@ -1458,8 +1461,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
             for (int u = 0; u < NB; ++u) {
                 const int k = kb[u];
                 const float4 xj = xb[u];
-                float d[3], dr2;
-                bool in = t0 + u < lc && k != s && pair_delta<DIM>(xi, xj, g, d, dr2);
+                // no pair test: the kernel's support (W = 0 for q >= 2) drops the
+                // entries beyond it
+                bool in = t0 + u < lc;
                 if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) in = false;  // push only
                 const float mj = mass_of<DIM>(xj, vb[u]);
                 float dh[3], dl[3];
@@ -1470,7 +1474,7 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                     al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
                 }
                 if (fluid) {
-                    const sph::ff wm = sph::wendland_mw_ff<DIM>(dh, dl, ih, al, mj);
+                    const sph::ff wm = sph::wendland_mw_ff<DIM, true>(dh, dl, ih, al, mj);
                     if (in) {
                         sph::ff_acc(S, wm);
                         if (nor) sph::ff_acc(Wn, sph::ff_mul(wm, sph::ff_recip(__ldg(B.q + k))));
@@ -1479,8 +1483,9 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                 if (need_div && in) {
                     const float4 vj = vb[u];
                     const float r2 = sph::dist2_exact<DIM>(dh);
-                    const float gw = sph::wendland_grad_factor<DIM>(
+                    float gw = sph::wendland_grad_factor<DIM>(
                         fast_sqrt_pos(r2), ih.hi, __fmul_rn(P.kg, pow_grad<DIM>(ih.hi)));
+                    if (!(fast_sqrt_pos(r2) * ih.hi < 2.0f)) gw = 0.f;  // beyond the support
                     float vd = fmaf(vj.y - vi.y, dh[1], __fmul_rn(vj.x - vi.x, dh[0]));
                     if (DIM == 3) vd = fmaf(vj.z - vi.z, dh[2], vd);
                     divs = fmaf(mj * gw, vd, divs);

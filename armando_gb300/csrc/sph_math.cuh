@@ -119,7 +119,8 @@ SPH_HD float min_image(float dx, float L, float half) {
 // when the coordinates differ by more than a factor 2, e.g. near the origin),
 // h = (h_i + h_j)/2 passed as its reciprocal ih and the prefactor
 // alpha = K_dim * ih^dim (both float-float).
-template <int DIM>
+// CLAMP: zero beyond the support (q >= 2), so pairs need no separate test.
+template <int DIM, bool CLAMP = false>
 SPH_HD ff wendland_mw_ff(const float* dh, const float* dl, ff ih, ff alpha, float mj) {
     // dr^2 = sum (dh + dl)^2 as hi + lo (dl^2 is below the float-float unit).
     ff s0 = two_prod(dh[0], dh[0]);
@@ -147,6 +148,7 @@ SPH_HD ff wendland_mw_ff(const float* dh, const float* dl, ff ih, ff alpha, floa
     // t = 1 - q/2 (q < 2 so |1| >= |q/2|).
     ff t = fast_two_sum(1.0f, __fmul_rn(-0.5f, q.hi));
     t.lo = fmaf(-0.5f, q.lo, t.lo);
+    if (CLAMP && !(t.hi + t.lo > 0.0f)) t = ff{0.0f, 0.0f};
     ff t2 = ff_sqr(t);
     ff t4 = ff_sqr(t2);
     // g = 1 + 2q.
