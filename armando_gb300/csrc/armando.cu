@@ -371,7 +371,7 @@ const int* resort_flags(armando_ctx* ctx) { return reinterpret_cast<const int*>(
 // The next iteration rebuilds the grid and sorts (the state in A was loaded
 // or replaced since the last sort).
 armando_status force_sort(armando_ctx* ctx) {
-    CK(cudaMemsetAsync(ctx->flags + 1, 0x01, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->flags + 2, 0x01, sizeof(unsigned), ctx->stream));
     return ARMANDO_OK;
 }
 
@@ -440,11 +440,11 @@ int launch_build_list(armando_ctx* ctx, const int* rs, cudaStream_t st) {
     return 2;
 }
 
-// End of a lazily sorting iteration: the next one sorts if this one flagged
-// it; counts this iteration's sort.
-int launch_resort_advance(armando_ctx* ctx) {
-    k_resort_advance<<<1, 32, 0, ctx->stream>>>(reinterpret_cast<int*>(ctx->flags + 1),
-                                                reinterpret_cast<int*>(ctx->flags + 3));
+// Start of a lazily sorting iteration launched without the step graph's
+// head: it sorts if the last one (or the host) asked for it.
+int launch_resort_begin(armando_ctx* ctx) {
+    k_resort_begin<<<1, 32, 0, ctx->stream>>>(reinterpret_cast<int*>(ctx->flags + 1),
+                                              reinterpret_cast<int*>(ctx->flags + 3));
     return 1;
 }
 
@@ -612,7 +612,7 @@ void launch_force(armando_ctx* ctx, const unsigned* skeys, const StepArgs& S) {
     });
 }
 
-// Reorder/predictor, the pair passes and (lazy sorting) the flag advance.
+// Reorder/predictor and the pair passes.
 // reorder = false: the caller launched the reorder copy itself (the fused
 // predictor's step graph, where only iterations that sort need it).
 template <int DIM>
@@ -641,7 +641,6 @@ int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs, bool reord
     }
     launch_force<DIM>(ctx, skeys, S);
     ++L;
-    if (rs) L += launch_resort_advance(ctx);
     return L;
 }
 
@@ -650,8 +649,9 @@ int launch_passes(armando_ctx* ctx, const StepArgs& S, const int* rs, bool reord
 template <int DIM>
 int launch_step(armando_ctx* ctx, const StepArgs& S) {
     const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
+    const int L0 = rs ? launch_resort_begin(ctx) : 0;
     const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream, use_lists(ctx));
-    return L + launch_passes<DIM>(ctx, S, rs);
+    return L0 + L + launch_passes<DIM>(ctx, S, rs);
 }
 
 // One lazily sorting iteration as a graph whose grid and sort kernels sit in
@@ -686,7 +686,8 @@ armando_status build_lazy_graph(armando_ctx* ctx, const StepArgs& S, cudaGraphEx
                                            cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return fail_graph(e, "cudaStreamBeginCaptureToGraph");
     main_cap = true;
-    k_resort_cond<<<1, 32, 0, ctx->stream>>>(h, resort_flags(ctx));
+    k_resort_cond<<<1, 32, 0, ctx->stream>>>(h, reinterpret_cast<int*>(ctx->flags + 1),
+                                              reinterpret_cast<int*>(ctx->flags + 3));
     cudaStreamCaptureStatus cs;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
@@ -772,16 +773,15 @@ int launch_gpuc_passes(armando_ctx* ctx, const StepArgs& S, const int* rs) {
     }
     k_gpuc_scatter<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->gs, 1, ctx->A, n, ctx->grid,
                                                             ctx->flags);
-    int L = 5;
-    if (rs) L += launch_resort_advance(ctx);
-    return L;
+    return 5;
 }
 
 // rs: the lazy-sorting flags (nullptr: the step sorts).
 template <int DIM>
 int launch_gpuc_step(armando_ctx* ctx, const StepArgs& S, const int* rs) {
+    const int L0 = rs ? launch_resort_begin(ctx) : 0;
     const int L = launch_grid_and_sort<DIM>(ctx, rs, ctx->stream);
-    return L + launch_gpuc_passes<DIM>(ctx, S, rs);
+    return L0 + L + launch_gpuc_passes<DIM>(ctx, S, rs);
 }
 
 int launch_step_any(armando_ctx* ctx, const StepArgs& S) {
@@ -889,6 +889,7 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     int L = 0;
     cudaEventRecord(ev[0], st);
     const int* rs = lazy(ctx) ? resort_flags(ctx) : nullptr;
+    if (rs) L += launch_resort_begin(ctx);
     k_bbox_partial<<<kBBoxBlocks, 256, 0, st>>>(ctx->A.xh, n, DIM, ctx->bbox_part, rs);
     k_bbox_final<<<1, 256, 0, st>>>(ctx->bbox_part, kBBoxBlocks, ctx->dp, ctx->cell_cap, ctx->grid,
                                     ctx->flags, rs);
@@ -929,7 +930,6 @@ int launch_step_phased(armando_ctx* ctx, const StepArgs& S, cudaEvent_t* ev) {
     }
     cudaEventRecord(ev[5], st);
     launch_force<DIM>(ctx, skeys, S);
-    if (rs) L += launch_resort_advance(ctx);
     cudaEventRecord(ev[6], st);
     return L + 1;
 }

@@ -188,29 +188,38 @@ __device__ __forceinline__ float mass_of(const float4& xh, const float4& vm) {
     return DIM == 2 ? xh.z : vm.w;
 }
 
-// Lazy sorting (sort skin). resort[0] != 0: this iteration sorts; the force
-// pass sets resort[1] when a particle has moved more than half the skin from
-// where it was binned; k_resort_advance moves it to resort[0] for the next
-// iteration. The grid, hash, sort and cell-table kernels return at once on an
-// iteration that does not sort (their outputs from the last sort stay valid:
-// cells of 2 max(h) + skin hold every pair within 2 max(h) while no particle
-// is farther than skin / 2 from its binned position). resort == nullptr:
-// always sort.
+// Lazy sorting (sort skin). resort[1] != 0 asks for a sort: the force pass
+// sets it when a particle has moved more than half the skin from where it was
+// binned, the host after loading a state. The first kernel of an iteration
+// (resort_begin) turns it into resort[0] (this iteration sorts) and clears it.
+// The grid, hash, sort and cell-table kernels return at once on an iteration
+// that does not sort (their outputs from the last sort stay valid: cells of
+// 2 max(h) + skin hold every pair within 2 max(h) while no particle is farther
+// than skin / 2 from its binned position). resort == nullptr: always sort.
 __device__ __forceinline__ bool sort_skipped(const int* resort) {
     return resort != nullptr && *(volatile const int*)resort == 0;
 }
 
-__global__ void k_resort_advance(int* __restrict__ resort, int* __restrict__ sorts) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    if (resort[0] != 0) ++sorts[0];
-    resort[0] = resort[1];
+// Start of a lazily sorting iteration (one thread); counts the sorts.
+__device__ __forceinline__ unsigned resort_begin(int* resort, int* sorts) {
+    const unsigned sort = resort[1] != 0 ? 1u : 0u;
+    resort[0] = (int)sort;
     resort[1] = 0;
+    if (sort) ++sorts[0];
+    return sort;
 }
 
-// Head of a lazily sorting step graph: the IF node after it runs the grid,
-// hash, sort and cell-table kernels only when this iteration sorts.
-__global__ void k_resort_cond(cudaGraphConditionalHandle handle, const int* __restrict__ resort) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(handle, resort[0] != 0 ? 1u : 0u);
+__global__ void k_resort_begin(int* __restrict__ resort, int* __restrict__ sorts) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) resort_begin(resort, sorts);
+}
+
+// Head of a lazily sorting step graph: starts the iteration; the IF node
+// after it runs the grid, hash, sort and cell-table kernels only when this
+// iteration sorts.
+__global__ void k_resort_cond(cudaGraphConditionalHandle handle, int* __restrict__ resort,
+                              int* __restrict__ sorts) {
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        cudaGraphSetConditional(handle, resort_begin(resort, sorts));
 }
 
 // ---------------------------------------------------------------------------
