@@ -128,9 +128,11 @@ struct StateB {  // working set of one step (cell order)
     float4* vr;    // 2D: {vx, vy, rho, P} after the density pass (one neighbour load in the force pass)
     float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour lists of a lazily sorting context (built on the iterations that
-    // sort): entry t of slot s at nlist[t * n + s], the candidates within
-    // h_i + h_j + skin in cursor order; ncount[s] entries, -1 when more than
-    // lcap (that slot walks its cells instead).
+    // sort): row t of slot s at nlist[t * lstride + s], the candidates within
+    // h_i + h_j + skin, first the near ones (q < near_q() when sorted; in 3D
+    // all) in cursor order, then the far ones in reverse cursor order;
+    // ncount[s] = near | far << 16, -1 when more than lcap (that slot walks
+    // its cells instead).
     int* nlist;
     int* ncount;
     int lcap;      // list entries per slot
@@ -1174,6 +1176,10 @@ template <int DIM>
 __host__ __device__ constexpr int density_list_batch() {
     return 2;
 }
+// The 2D density pass's far entries (FP32 weights).
+__host__ __device__ constexpr int density_far_batch() {
+    return 2;
+}
 
 // A warp's neighbour-list rows (entry r of its 32 slots is one 128-byte run
 // at nlist + r * lstride + s0) requested into L2 at once, one row per lane, so
@@ -1186,6 +1192,11 @@ __device__ __forceinline__ void prefetch_list_rows(const int* nlist, int lstride
     for (int r = lane; r < rows; r += 32)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(nlist + (size_t)r * lstride + s0));
 }
+
+// A slot's list counts from ncount: near entries (-1: no list, walk the
+// cells) and far entries.
+__device__ __forceinline__ int list_near(int packed) { return packed >= 0 ? (packed & 0xffff) : -1; }
+__device__ __forceinline__ int list_far(int packed) { return packed >= 0 ? (packed >> 16) : 0; }
 // 2D density pairs with q = r/h < near_q() are evaluated in float-float, the
 // others (W below ~1% of W(0) each, ~8 of ~20 pairs) in FP32. In 3D every pair
 // is float-float: ~50 of ~80 pairs lie beyond q = 1.6, and the FP32 rounding of
@@ -1434,13 +1445,16 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
     int wb = 0;   // the accumulator holds the bits of ordinals 32 wb .. 32 wb + 63
     unsigned long long cur = 0ull;
     int shift = 0;  // staged index - slot in the cursor's row
-    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;  // list entries (-1: walk the cells)
+    const int lpk = (LST && work) ? __ldg(B.ncount + s) : -1;
+    const int lc = list_near(lpk);  // near list entries (-1: walk the cells)
+    const int lf = list_far(lpk);   // far list entries (2D)
     if (LST && lc >= 0) mask_on = false;
-    if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc);
-    // A listed particle evaluates every list entry in float-float as it is
-    // read (2D far pairs included); the kernel is zero beyond its support, so
-    // the entries need no pair test: no candidate lists in shared memory, no
-    // second load. The cell walk below serves the others.
+    if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc + lf);
+    // A listed particle evaluates each list entry as it is read, the near
+    // ones in float-float, the far ones (2D) like the cell walk's far pairs;
+    // the kernel is zero beyond its support, so the entries need no pair
+    // test: no candidate lists in shared memory, no second load. The cell
+    // walk below serves the others.
     if (LST) {
         constexpr int NB = density_list_batch<DIM>();
         const int lcm = __reduce_max_sync(0xffffffffu, lc > 0 ? lc : 0);
@@ -1498,6 +1512,77 @@ __device__ __forceinline__ void density_body(const StateB& B, const unsigned* __
                     float vd = fmaf(vj.y - vi.y, dh[1], __fmul_rn(vj.x - vi.x, dh[0]));
                     if (DIM == 3) vd = fmaf(vj.z - vi.z, dh[2], vd);
                     divs = fmaf(mj * gw, vd, divs);
+                }
+            }
+        }
+        // 2D far entries (the rows after the near ones): FP32 weights with
+        // the float-float prefactor, zero beyond the support.
+        if constexpr (DIM == 2) {
+            constexpr int NF = density_far_batch();
+            const int lfm = __reduce_max_sync(0xffffffffu, lf);
+            auto fentry = [&](int t) {
+                return lf > 0 ? __ldg(B.nlist + (size_t)(lc + min(t, lf - 1)) * B.lstride + s)
+                              : (valid ? s : 0);
+            };
+            int kf[NF];
+#pragma unroll
+            for (int u = 0; u < NF; ++u) kf[u] = fentry(u);
+            for (int t0 = 0; t0 < lfm; t0 += NF) {
+                int kb[NF];
+                float4 xb[NF], vb[NF];
+#pragma unroll
+                for (int u = 0; u < NF; ++u) kb[u] = kf[u];
+                if (t0 + NF < lfm) {
+#pragma unroll
+                    for (int u = 0; u < NF; ++u) kf[u] = fentry(t0 + NF + u);
+                }
+#pragma unroll
+                for (int u = 0; u < NF; ++u) {
+                    xb[u] = __ldg(xsrc + kb[u]);
+                    vb[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (need_div) vb[u] = __ldg(vsrc + kb[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < NF; ++u) {
+                    const int k = kb[u];
+                    const float4 xj = xb[u];
+                    bool in = t0 + u < lf;
+                    if (!LEAN && P.wall_model == 1 && __ldg(B.itype + k) != it_i) in = false;  // push only
+                    const float mj = mass_of<DIM>(xj, vb[u]);
+                    float d[3], dr2;
+                    pair_delta<DIM>(xi, xj, g, d, dr2);
+                    refine_periodic<DIM>(xi, xj, g, d, dr2);
+                    sph::ff ih = ih_i, al = al_i;
+                    float kgih = kgih_i;
+                    if (xj.w != xi.w) {
+                        ih = sph::ff_recip(__fmul_rn(0.5f, __fadd_rn(xi.w, xj.w)));
+                        al = sph::ff_mul(kw, ff_pow_dim<DIM>(ih));
+                        kgih = P.kg * pow_grad<DIM>(ih.hi);
+                    }
+                    float r = 0.f;
+                    if (dr2 > 0.f) {
+                        const float rs = rsqrtf(dr2);
+                        r = __fmul_rn(dr2, rs);
+                        r = fmaf(fmaf(-r, r, dr2), 0.5f * rs, r);
+                    }
+                    const float q = fmaf(r, ih.hi, __fmul_rn(r, ih.lo));
+                    if (fluid && in) {
+                        float tt = fmaxf(fmaf(-0.5f, q, 1.0f), 0.0f);  // 0 beyond the support
+                        tt = tt * tt;
+                        tt = tt * tt;
+                        const float f = tt * fmaf(2.0f, q, 1.0f);
+                        const sph::ff c = sph::ff_mul_f(al, mj);
+                        const float wm = fmaf(c.hi, f, __fmul_rn(c.lo, f));
+                        sph::ff_acc(S, sph::ff{wm, 0.f});
+                        if (nor) sph::ff_acc(Wn, sph::ff{__fdiv_rn(wm, __ldg(B.q + k)), 0.f});
+                    }
+                    if (need_div && in && q < 2.0f) {
+                        const float4 vj = vb[u];
+                        const float t3 = q - 2.0f;
+                        const float gw = kgih * t3 * t3 * t3;
+                        float vd = fmaf(vj.y - vi.y, d[1], __fmul_rn(vj.x - vi.x, d[0]));
+                        divs = fmaf(mj * gw, vd, divs);
+                    }
                 }
             }
         }
@@ -1854,7 +1939,8 @@ __device__ __forceinline__ void force_body(const StateB& B, const StateA& A,
     unsigned wbits = 0u;                    // bits left of word wi
     // A listed particle walks its neighbour list (coalesced rows of entries)
     // and re-tests each entry; the others decode the density pass's bits.
-    const int lc = (LST && work) ? __ldg(B.ncount + s) : -1;
+    const int lpk = (LST && work) ? __ldg(B.ncount + s) : -1;
+    const int lc = lpk >= 0 ? list_near(lpk) + list_far(lpk) : -1;  // entries (-1: no list)
     if (LST) prefetch_list_rows(B.nlist, B.lstride, s, lc);
     if (work && !(LST && lc >= 0)) {
         ch = mask_load_chunk<W>(B.nmask, B.mstride, mlane, 0);
@@ -2230,7 +2316,9 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
 // Neighbour lists of an iteration that sorts (lazy sorting), built in the
 // sort's conditional body after the cell table: for each slot s of the new
 // order, the candidates k != s (cursor order) within h_s + h_k + skin, the
-// bound widened by 2^-14 over the rounding of the FP32 distances. Positions
+// bound widened by 2^-14 over the rounding of the FP32 distances; in 2D the
+// pairs the density pass evaluates in FP32 (q >= near_q() at the sort) go
+// after the others (filled from the last row down, then moved up). Positions
 // are read through the sort's permutation (the reorder into cell order comes
 // later in the iteration). Until the next sort every particle stays within
 // half the skin of where it was binned, so every pair the exact test accepts
@@ -2250,7 +2338,7 @@ __global__ void __launch_bounds__(kPassThreads)
     const float4 xi = B.xsort[s];
     const CellCoord cc = decode_key<DIM>(keys[s], g);
     const float pad = (1.0f + 0x1p-14f);
-    int cnt = 0;
+    int cn = 0, cf = 0;  // near and far entries
     Cursor cu = cursor_begin<DIM>(g);
     while (cursor_next<DIM>(g, start, cc, cu)) {
         for (int k0 = cu.k; k0 < cu.ke; k0 += kTestBatch) {
@@ -2265,12 +2353,26 @@ __global__ void __launch_bounds__(kPassThreads)
                 pair_delta<DIM>(xi, xb[u], g, d, dr2);
                 const float lim = __fmul_rn(__fadd_rn(__fadd_rn(xi.w, xb[u].w), g.skin), pad);
                 if (!(dr2 < __fmul_rn(lim, lim))) continue;
-                if (cnt < B.lcap) B.nlist[(size_t)cnt * B.lstride + s] = k;
-                ++cnt;
+                const float hs = xi.w + xb[u].w;  // the density pass's near test
+                const bool near =
+                    DIM == 3 || dr2 < (0.25f * near_q<DIM>() * near_q<DIM>()) * hs * hs;
+                if (cn + cf < B.lcap) B.nlist[(size_t)(near ? cn : B.lcap - 1 - cf) * B.lstride + s] = k;
+                if (near) ++cn;
+                else ++cf;
             }
         }
     }
-    B.ncount[s] = cnt <= B.lcap ? cnt : -1;
+    if (cn + cf <= B.lcap) {
+        // the far entries, written from the last row down, moved up behind the
+        // near ones (rows in increasing order: each source row is read before
+        // a later copy could overwrite it)
+        for (int i = 0; i < cf; ++i)
+            B.nlist[(size_t)(cn + i) * B.lstride + s] =
+                B.nlist[(size_t)(B.lcap - cf + i) * B.lstride + s];
+        B.ncount[s] = cn | (cf << 16);
+    } else {
+        B.ncount[s] = -1;
+    }
 }
 
 template <int DIM>
