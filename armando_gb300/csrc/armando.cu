@@ -153,7 +153,12 @@ struct armando_ctx {
     armando_tuning tune{1, 1, 128, 0};   // neighbour-pass tuning (armando_set_tuning)
     int64_t sorts_done = 0;              // lazily sorting iterations that sorted (device count)
     int64_t sorts_host = 0;              // iterations that always sort
-    cudaStream_t stream2 = nullptr;      // captures the conditional sort body
+    cudaStream_t stream2 = nullptr;      // captures the conditional sort body; copies beside the step
+    // A host-memory call's copies beside the step (overlapped_call): events
+    // {inputs start, rest of the inputs loaded, density done, rho and p written}.
+    cudaEvent_t ev_ovl[4] = {nullptr, nullptr, nullptr, nullptr};
+    int ovl_ctas = 0;                    // CTAs of the copy kernels beside the step
+    bool split_in = false;               // load_inputs left the rest of the inputs on stream2
     bool no_conditional = false;         // conditional graphs failed to build here
     float4* xsort_buf = nullptr;
     std::vector<TapeSlot> tape;          // intermediates of each iteration of one segment
@@ -997,6 +1002,56 @@ armando_status run_ghost_step(armando_ctx* ctx, const StepArgs& S) {
 
 armando_status alloc_stateA(armando_ctx* ctx, StateA& a);
 
+template <class T>
+T* mapped_host(T* p);
+
+// One iteration of a host-memory call beside its copies (load_inputs left the
+// rest of the inputs loading on the second stream): the grid and sort run on
+// the positions meanwhile, the reorder waits for the rest; after the density
+// pass the second stream writes the output density and pressure (final then)
+// back while the force pass runs. Direct launches: the events belong to this
+// call. Same kernels, same order of operations as the step graph: the same
+// results.
+template <int DIM>
+int launch_overlapped_step(armando_ctx* ctx, const StepArgs& S, float* rho_out, float* p_out) {
+    cudaStream_t st = ctx->stream, s2 = ctx->stream2;
+    const int n = (int)ctx->n_work;
+    int L = launch_grid_and_sort<DIM>(ctx, nullptr, st);
+    cudaStreamWaitEvent(st, ctx->ev_ovl[1], 0);  // the rest of the inputs
+    const unsigned* skeys = ctx->keys[ctx->passes & 1];
+    const int* perm = ctx->vals[ctx->passes & 1];
+    k_reorder_dim<DIM><<<blocks_for(n, 256), 256, 0, st>>>(ctx->A, perm, ctx->B, S, n);
+    launch_density<DIM>(ctx, skeys, S);
+    cudaEventRecord(ctx->ev_ovl[2], st);
+    cudaStreamWaitEvent(s2, ctx->ev_ovl[2], 0);
+    k_invert_ids<<<blocks_for(n, 256), 256, 0, s2>>>(ctx->B.id, ctx->inv, n);
+    k_scatter_rp<<<ctx->ovl_ctas, 256, 0, s2>>>(ctx->B, ctx->inv, n, rho_out, p_out);
+    cudaEventRecord(ctx->ev_ovl[3], s2);
+    L += 4;
+    if (ctx->dp.visc) {
+        k_shear<DIM><<<blocks_for(n, kPassThreads), kPassThreads, 0, st>>>(
+            ctx->B, skeys, ctx->start, ctx->grid, ctx->dp, n);
+        ++L;
+    }
+    launch_force<DIM>(ctx, skeys, S);
+    cudaStreamWaitEvent(st, ctx->ev_ovl[3], 0);  // the inverse ids serve the other outputs
+    return L + 1;
+}
+
+armando_status run_overlapped_step(armando_ctx* ctx, const StepArgs& S, float* rho_out,
+                                   float* p_out) {
+    float* mr = mapped_host(rho_out);
+    float* mp = mapped_host(p_out);
+    if (!mr || !mp) return fail(ctx, ARMANDO_ERR_INVALID_ARG, "output arrays are not mapped");
+    const int L = ctx->dim == 2 ? launch_overlapped_step<2>(ctx, S, mr, mp)
+                                : launch_overlapped_step<3>(ctx, S, mr, mp);
+    CK(cudaGetLastError());
+    ctx->launches += L;
+    ctx->steps_done += 1;
+    ctx->sorts_host += 1;
+    return ARMANDO_OK;
+}
+
 armando_status run_step(armando_ctx* ctx, const StepArgs& S) {
     if (ctx->n_inst > 1) return run_batch_step(ctx);
     if (ctx->prm.wall_model == 3)
@@ -1666,9 +1721,54 @@ T* mapped_host(T* p) {
     return static_cast<T*>(a.devicePointer);
 }
 
+// Whether the step reads the input density / pressure of fluid particles: the
+// GPU-C schemes integrate both and the single_step options start from the
+// input density; summation density and the equation of state replace them
+// otherwise. Batches read all.
+bool fluid_rho_read(const armando_ctx* ctx) {
+    return ctx->n_inst > 1 || ctx->prm.scheme != 0 || step_options(ctx->prm) ||
+           ctx->prm.wall_model == 3;
+}
+bool fluid_p_read(const armando_ctx* ctx) { return ctx->n_inst > 1 || ctx->prm.scheme != 0; }
+
+// A one-iteration call on host memory that the device maps whose step can run
+// beside its copies (launch_overlapped_step): one CERN-scheme particle system
+// without mirror ghosts, single_step options or lazy sorting, outside reverse
+// mode.
+bool overlap_eligible(const armando_ctx* ctx, int steps) {
+    return steps == 1 && ctx->mem_kind == ARMANDO_MEM_HOST && ctx->n_inst == 1 &&
+           ctx->prm.scheme == 0 && ctx->prm.wall_model != 3 && !step_options(ctx->prm) &&
+           !lazy(ctx) && !ctx->reverse_run && ctx->n_work == ctx->n;
+}
+
+// The second stream, its events and the inverse ids, on first use.
+armando_status ensure_overlap(armando_ctx* ctx) {
+    cudaError_t e = cudaSuccess;
+    if (!ctx->stream2 && (e = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking)) != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaStreamCreate");
+    for (cudaEvent_t& ev : ctx->ev_ovl)
+        if (!ev && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaEventCreate");
+    if (!ctx->ovl_ctas) {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+        ctx->ovl_ctas = 2 * std::max(sms, 1);
+    }
+    if (!ctx->inv) {
+        ctx->inv = dalloc<int>((size_t)std::max<int64_t>(ctx->n, 1), e);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(inverse ids)");
+        ctx->owned.push_back(ctx->inv);
+    }
+    return ARMANDO_OK;
+}
+
+// split: the call may load the inputs in two parts (overlap_eligible); with
+// the arrays mapped it does, and sets ctx->split_in.
 armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, const float* mass,
                            const float* rho, const float* p, const float* u, const float* hsml,
-                           const int32_t* itype, const float* dvdt, const float* dudt) {
+                           const int32_t* itype, const float* dvdt, const float* dudt,
+                           bool split = false) {
+    ctx->split_in = false;
     const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
     cudaStream_t st = ctx->stream;
     const float *mx = nullptr, *mv = nullptr, *mm = nullptr, *mrho = nullptr, *mp = nullptr,
@@ -1715,20 +1815,48 @@ armando_status load_inputs(armando_ctx* ctx, const float* x, const float* vx, co
     // arrays on another stream passes it with armando_set_stream.
     if (dvdt && !dudt) dvdt = nullptr;
     const int nn = (int)ctx->n;
+    const int rfl = fluid_rho_read(ctx) ? 1 : 0, pfl = fluid_p_read(ctx) ? 1 : 0;
+    if (split && zero_copy) {
+        // positions and h now; the rest from a few CTAs on the second stream,
+        // which the step waits for before its reorder
+        armando_status os = ensure_overlap(ctx);
+        if (os != ARMANDO_OK) return os;
+        cudaStream_t s2 = ctx->stream2;
+        CK(cudaEventRecord(ctx->ev_ovl[0], st));
+        CK(cudaStreamWaitEvent(s2, ctx->ev_ovl[0], 0));
+        if (ctx->dim == 2) {
+            k_gather_pos<2><<<blocks_for(nn, 256), 256, 0, st>>>(x, mass, hsml, ctx->A, nn);
+            k_gather_rest<2><<<ctx->ovl_ctas, 256, 0, s2>>>(vx, mass, rho, p, u, itype, dvdt, dudt,
+                                                            ctx->A, nn, rfl, pfl);
+        } else {
+            k_gather_pos<3><<<blocks_for(nn, 256), 256, 0, st>>>(x, mass, hsml, ctx->A, nn);
+            k_gather_rest<3><<<ctx->ovl_ctas, 256, 0, s2>>>(vx, mass, rho, p, u, itype, dvdt, dudt,
+                                                            ctx->A, nn, rfl, pfl);
+        }
+        CK(cudaEventRecord(ctx->ev_ovl[1], s2));
+        ctx->launches += 2;
+        ctx->split_in = true;
+        CK(cudaGetLastError());
+        return force_sort(ctx);
+    }
     if (ctx->dim == 2)
         k_gather_in<2><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
-                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0);
+                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0,
+                                                            rfl, pfl);
     else
         k_gather_in<3><<<blocks_for(nn, 256), 256, 0, st>>>(x, vx, mass, rho, p, u, hsml, itype,
-                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0);
+                                                            dvdt, dudt, ctx->A, nn, ctx->d_inst0,
+                                                            rfl, pfl);
     ctx->launches += 1;
     CK(cudaGetLastError());
     return force_sort(ctx);  // A is in caller order now
 }
 
 // A -> caller arrays.
+// rp_done: an overlapped step wrote rho and p already (k_scatter_rp) and left
+// the inverse ids in ctx->inv.
 armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, float* p, float* u,
-                             float* dvdt, float* dudt) {
+                             float* dvdt, float* dudt, bool rp_done = false) {
     const size_t n = (size_t)ctx->n, nd = n * ctx->dim;
     cudaStream_t st = ctx->stream;
     const bool host = ctx->mem_kind == ARMANDO_MEM_HOST;
@@ -1744,14 +1872,19 @@ armando_status store_outputs(armando_ctx* ctx, float* x, float* vx, float* rho, 
                 if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(inverse ids)");
                 ctx->owned.push_back(ctx->inv);
             }
-            k_invert_ids<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.id, ctx->inv, nn);
+            if (rp_done) {
+                mrho = mp = nullptr;
+            } else {
+                k_invert_ids<<<blocks_for(nn, 256), 256, 0, st>>>(ctx->A.id, ctx->inv, nn);
+                ctx->launches += 1;
+            }
             if (ctx->dim == 2)
                 k_scatter_out_seq<2><<<blocks_for(nn, kScatterSeq), kScatterSeq, 0, st>>>(
                     ctx->A, ctx->inv, nn, mx, mv, mrho, mp, mu, mdv, mdu);
             else
                 k_scatter_out_seq<3><<<blocks_for(nn, kScatterSeq), kScatterSeq, 0, st>>>(
                     ctx->A, ctx->inv, nn, mx, mv, mrho, mp, mu, mdv, mdu);
-            ctx->launches += 2;
+            ctx->launches += 1;
             CK(cudaGetLastError());
             return ARMANDO_OK;
         }
@@ -2631,8 +2764,10 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     CK(cudaSetDevice(ctx->device));
     if (ctx->n == 0 || steps == 0) return ARMANDO_OK;
     if (armando_status cs = clear_flags(ctx); cs != ARMANDO_OK) return cs;
-    st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt);
+    st = load_inputs(ctx, x, vx, mass, rho, p, u, hsml, itype, dvdt, dudt,
+                     overlap_eligible(ctx, steps));
     if (st != ARMANDO_OK) return st;
+    const bool split = ctx->split_in;
     st = plan_grid(ctx);
     if (st != ARMANDO_OK) return st;
     st = build_wall_grid(ctx);
@@ -2642,14 +2777,15 @@ armando_status armando_integrate(armando_ctx* ctx, float* x, float* vx, const fl
     st = prepare_options(ctx);
     if (st != ARMANDO_OK) return st;
     for (int k = 0; k < steps; ++k) {
-        st = run_step(ctx, make_args(ctx, dt, its0 + k));
+        st = split ? run_overlapped_step(ctx, make_args(ctx, dt, its0 + k), rho, p)
+                   : run_step(ctx, make_args(ctx, dt, its0 + k));
         if (st != ARMANDO_OK) return st;
     }
     st = keep_options(ctx);
     if (st != ARMANDO_OK) return st;
     ctx->last_dt = dt;
     ctx->next_its = its0 + steps;
-    st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt);
+    st = store_outputs(ctx, x, vx, rho, p, u, dvdt, dudt, split);
     if (st != ARMANDO_OK) return st;
     return finish_call(ctx);
 }
@@ -3266,6 +3402,8 @@ armando_status armando_destroy(armando_ctx* ctx) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+    for (cudaEvent_t ev : ctx->ev_ovl)
+        if (ev) cudaEventDestroy(ev);
     delete ctx;
     return ARMANDO_OK;
 }

@@ -682,32 +682,75 @@ __global__ void __launch_bounds__(kCellStartThreads)
 // ---------------------------------------------------------------------------
 // State movement
 // ---------------------------------------------------------------------------
+// Caller arrays -> A, in two parts: what the grid and sort read (positions,
+// h; the 2D mass rides in xh.z) and the rest. The input density and pressure
+// of a fluid particle are read only where the step uses them (rho_fl, p_fl):
+// summation density and the equation of state replace them otherwise.
+template <int DIM>
+__device__ __forceinline__ void gather_pos_one(int i, const float* __restrict__ x,
+                                               const float* __restrict__ m,
+                                               const float* __restrict__ h, StateA& A) {
+    if (DIM == 2) A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], m[i], h[i]);
+    else A.xh[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], h[i]);
+    A.id[i] = i;
+}
+template <int DIM>
+__device__ __forceinline__ void gather_rest_one(int i, const float* __restrict__ v,
+                                                const float* __restrict__ m,
+                                                const float* __restrict__ rho,
+                                                const float* __restrict__ p,
+                                                const float* __restrict__ u,
+                                                const int* __restrict__ itype,
+                                                const float* __restrict__ dvdt,
+                                                const float* __restrict__ dudt, StateA& A,
+                                                bool rho_fl, bool p_fl) {
+    const int it = itype[i];
+    if (DIM == 2) {
+        A.vm[i] = make_float4(v[2 * i], v[2 * i + 1], 0.f, 0.f);
+        A.ap[i] = dvdt ? make_float4(dvdt[2 * i], dvdt[2 * i + 1], 0.f, dudt[i])
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+        A.vm[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], m[i]);
+        A.ap[i] = dvdt ? make_float4(dvdt[3 * i], dvdt[3 * i + 1], dvdt[3 * i + 2], dudt[i])
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    A.u[i] = u[i];
+    A.rho[i] = (rho_fl || it <= 0) ? rho[i] : 0.f;
+    A.p[i] = (p_fl || it <= 0) ? p[i] : 0.f;
+    A.itype[i] = it;
+}
+
 template <int DIM>
 __global__ void k_gather_in(const float* __restrict__ x, const float* __restrict__ v,
                             const float* __restrict__ m, const float* __restrict__ rho,
                             const float* __restrict__ p, const float* __restrict__ u,
                             const float* __restrict__ h, const int* __restrict__ itype,
                             const float* __restrict__ dvdt, const float* __restrict__ dudt,
-                            StateA A, int n, const int* __restrict__ inst0) {
+                            StateA A, int n, const int* __restrict__ inst0, int rho_fl,
+                            int p_fl) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (inst0) A.inst[i] = inst0[i];
-    if (DIM == 2) {
-        A.xh[i] = make_float4(x[2 * i], x[2 * i + 1], m[i], h[i]);
-        A.vm[i] = make_float4(v[2 * i], v[2 * i + 1], 0.f, 0.f);
-        A.ap[i] = dvdt ? make_float4(dvdt[2 * i], dvdt[2 * i + 1], 0.f, dudt[i])
-                       : make_float4(0.f, 0.f, 0.f, 0.f);
-    } else {
-        A.xh[i] = make_float4(x[3 * i], x[3 * i + 1], x[3 * i + 2], h[i]);
-        A.vm[i] = make_float4(v[3 * i], v[3 * i + 1], v[3 * i + 2], m[i]);
-        A.ap[i] = dvdt ? make_float4(dvdt[3 * i], dvdt[3 * i + 1], dvdt[3 * i + 2], dudt[i])
-                       : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    A.u[i] = u[i];
-    A.rho[i] = rho[i];
-    A.p[i] = p[i];
-    A.itype[i] = itype[i];
-    A.id[i] = i;
+    gather_pos_one<DIM>(i, x, m, h, A);
+    gather_rest_one<DIM>(i, v, m, rho, p, u, itype, dvdt, dudt, A, rho_fl, p_fl);
+}
+
+// The two parts apart: a host-memory call loads the positions first and the
+// rest from a few CTAs on a second stream while the sort runs.
+template <int DIM>
+__global__ void k_gather_pos(const float* __restrict__ x, const float* __restrict__ m,
+                             const float* __restrict__ h, StateA A, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) gather_pos_one<DIM>(i, x, m, h, A);
+}
+template <int DIM>
+__global__ void k_gather_rest(const float* __restrict__ v, const float* __restrict__ m,
+                              const float* __restrict__ rho, const float* __restrict__ p,
+                              const float* __restrict__ u, const int* __restrict__ itype,
+                              const float* __restrict__ dvdt, const float* __restrict__ dudt,
+                              StateA A, int n, int rho_fl, int p_fl) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        gather_rest_one<DIM>(i, v, m, rho, p, u, itype, dvdt, dudt, A, rho_fl, p_fl);
 }
 
 // Positions and h only (neighbour / cell-id entry points).
@@ -748,6 +791,19 @@ __global__ void k_invert_ids(const int* __restrict__ id, int* __restrict__ inv, 
 // the scattered side.
 constexpr int kScatterSeq = 256;
 
+// The output density and pressure of a summation-density iteration, final
+// after the density pass (the force pass copies them): written to the caller's
+// arrays from a few CTAs on a second stream while the force pass runs. inv is
+// the inverse of B.id.
+__global__ void k_scatter_rp(StateB B, const int* __restrict__ inv, int n, float* __restrict__ rho,
+                             float* __restrict__ p) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int s = inv[i];
+        rho[i] = B.rp[s].x;
+        p[i] = B.p[s];
+    }
+}
+
 template <int DIM>
 __global__ void __launch_bounds__(kScatterSeq)
     k_scatter_out_seq(StateA A, const int* __restrict__ inv, int n, float* __restrict__ x,
@@ -774,8 +830,8 @@ __global__ void __launch_bounds__(kScatterSeq)
         }
         dudt[i] = r.w;
         u[i] = A.u[s];
-        rho[i] = A.rho[s];
-        p[i] = A.p[s];
+        if (rho) rho[i] = A.rho[s];  // (null: written earlier, k_scatter_rp)
+        if (p) p[i] = A.p[s];
     }
     __syncthreads();
     const int cnt = DIM * min(kScatterSeq, n - i0);

@@ -1,6 +1,9 @@
 """Host-memory contexts with page-locked caller arrays: the copy kernels read
-and write the caller's arrays across the host link (no staging copies). The
-results must be bit-identical to the staged path taken for pageable arrays."""
+and write the caller's arrays across the host link (no staging copies); a
+one-iteration call (armando_step without a sort skin) loads the inputs other
+than the positions on a second stream while the sort runs, and writes the
+output density and pressure back while the force pass runs. The results must
+be bit-identical to the staged path taken for pageable arrays."""
 import numpy as np
 import pytest
 
@@ -37,12 +40,14 @@ def pinned_copy(case, only=None):
 def small(name):
     if name == "dambreak":
         return cases.perturbed(cases.dam_break(dx=0.02), seed=61, dv=0.05)
+    if name == "cavity":  # physical viscosity: the shear pass between the two
+        return cases.perturbed(cases.cavity(n_side=24), seed=65, dv=1e-4)
     return cases.perturbed(cases.channel(n_x=40, n_yz=12, length=40 * 7.9e-4,
                                          width=12 * 7.9e-4, layers=3, jitter=0.01),
                            seed=62, dv=0.02, du=50.0)
 
 
-@pytest.mark.parametrize("name", ["dambreak", "channel3d"])
+@pytest.mark.parametrize("name", ["dambreak", "channel3d", "cavity"])
 @pytest.mark.parametrize("only", [None, ("x", "v", "rho")], ids=["all", "some"])
 def test_pinned_host_arrays_match_pageable(name, only):
     c = small(name)
@@ -77,3 +82,40 @@ def test_pinned_batch_matches_pageable():
             b.integrate_batch(arr, dts, 1, 3)
     for k in plain:
         assert np.array_equal(plain[k], pinned[k]), k
+
+
+@pytest.mark.parametrize("name", ["dambreak", "channel3d"])
+def test_pinned_step_calls_match_pageable(name):
+    """Consecutive one-iteration calls (each loads, steps and stores) on
+    page-locked arrays against pageable ones."""
+    c = small(name)
+    a = c.copy()
+    b = pinned_copy(c)
+    for arr in (a, b):
+        with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+            for its in range(1, 7):
+                ctx.step(arr, c.dt, its)
+    for f in FIELDS:
+        assert np.array_equal(getattr(a, f), np.asarray(getattr(b, f))), f
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+@pytest.mark.parametrize("name", ["dambreak", "channel3d"])
+def test_fluid_input_density_and_pressure_unused(name, pinned):
+    """With summation density the step recomputes the fluid particles'
+    density and pressure: their input values (NaN here) are not read; the
+    walls' are."""
+    c = small(name)
+    assert c.params.density_form == 0 and c.params.scheme == 0
+    bad = c.copy()
+    fl = bad.itype > 0
+    bad.rho = np.where(fl, np.float32(np.nan), bad.rho).astype(np.float32)
+    bad.p = np.where(fl, np.float32(np.nan), bad.p).astype(np.float32)
+    a = pinned_copy(c) if pinned else c.copy()
+    b = pinned_copy(bad) if pinned else bad.copy()
+    for arr in (a, b):
+        with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+            ctx.step(arr, c.dt, 1)
+            ctx.step(arr, c.dt, 2)
+    for f in FIELDS:
+        assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f))), f
