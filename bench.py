@@ -936,9 +936,14 @@ def run_ours(args, rank, world, local_rank):
         td.all_reduce(t, op=td.ReduceOp.MAX)
         ems = float(t.item())
     if rank == 0:
-        h2d = sum(a.nbytes for a in (pinned["x"], pinned["v"], pinned["mass"], pinned["rho"],
-                                     pinned["p"], pinned["u"], pinned["h"], pinned["itype"],
-                                     pinned["dvdt"], pinned["dudt"]))
+        h2d = sum(a.nbytes for a in (pinned["x"], pinned["v"], pinned["mass"], pinned["u"],
+                                     pinned["h"], pinned["itype"], pinned["dvdt"], pinned["dudt"]))
+        # input rho and p: the walls' only under summation density (the step
+        # replaces the fluid particles'), all of them otherwise
+        sums = case.params.scheme == 0 and case.params.density_form == 0 and \
+            case.params.wall_model != 3 and not case.params.average_velocity and not case.params.sle
+        rp_read = int((pinned["itype"] <= 0).sum()) if sums else case.n
+        h2d += rp_read * (pinned["rho"].itemsize + pinned["p"].itemsize)
         d2h = sum(a.nbytes for a in (pinned["x"], pinned["v"], pinned["rho"], pinned["p"],
                                      pinned["u"], pinned["dvdt"], pinned["dudt"]))
         out["e2e"] = {"value": world * case.n * e2e_steps / (ems * 1e-3), "unit": METRIC,

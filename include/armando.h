@@ -215,8 +215,13 @@ armando_status armando_set_params(armando_ctx* ctx, const armando_params* params
  * for its > 1 the previous rates dvdt[n*dim], dudt[n]. Out: x, vx, u (fluid),
  * rho, p (fluid; from summation density and the Tait EOS of this step), and the
  * new rates dvdt, dudt (zero for walls). Walls keep every input value.
+ * Under summation density (density_form 0, scheme 0, no mirror ghosts) the
+ * fluid particles' input rho and p are not read: the step replaces them.
  * The call is stream-ordered; with ARMANDO_MEM_HOST it returns after the
- * results are back in the caller's arrays.
+ * results are back in the caller's arrays. With page-locked (mapped) host
+ * arrays and no sort skin, the copies run beside the step: the inputs other
+ * than x, mass and hsml load while the sort runs, and rho and p are written
+ * back while the force pass runs (a second stream of the context's).
  */
 armando_status armando_step(armando_ctx* ctx, float* x, float* vx,
                             const float* mass, float* rho, float* p, float* u,
