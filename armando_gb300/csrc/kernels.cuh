@@ -129,7 +129,7 @@ struct StateB {  // working set of one step (cell order)
     float4* xsort; // position of each slot when the particles were last sorted
     // Neighbour lists of a lazily sorting context (built on the iterations that
     // sort): row t of slot s at nlist[t * lstride + s], the candidates within
-    // h_i + h_j + skin, first the near ones (q < near_q() when sorted; in 3D
+    // h_i + h_j + skin, first the near ones (q < list_near_q2() when sorted; in 3D
     // all) in cursor order, then the far ones in reverse cursor order;
     // ncount[s] = near | far << 16, -1 when more than lcap (that slot walks
     // its cells instead).
@@ -1262,6 +1262,11 @@ template <int DIM>
 __host__ __device__ constexpr float near_q() {
     return DIM == 2 ? 1.6f : 2.0f;
 }
+// The 2D neighbour lists' split (at the sort): float-float below q = 1.5, under
+// a lattice's second neighbours (r = 2 dx, q = 1.54 at h = 1.3 dx), which take
+// the FP32 path with the farther ones: 2% of the step for a one-step pressure
+// error of 1.5e-6 instead of 5.7e-7 at the cell walk's 1.6 (gate 1e-5).
+__host__ __device__ constexpr float list_near_q2() { return 1.5f; }
 
 // Candidate rows: for each (dy, dz) in [-f, f]^(DIM-1) the cells cx-f..cx+f of
 // that row are consecutive keys, so one contiguous slot range. On a periodic x
@@ -2373,7 +2378,7 @@ __global__ void __launch_bounds__(BS, 1024 / BS)
 // sort's conditional body after the cell table: for each slot s of the new
 // order, the candidates k != s (cursor order) within h_s + h_k + skin, the
 // bound widened by 2^-14 over the rounding of the FP32 distances; in 2D the
-// pairs the density pass evaluates in FP32 (q >= near_q() at the sort) go
+// pairs the density pass evaluates in FP32 (q >= list_near_q2() at the sort) go
 // after the others (filled from the last row down, then moved up). Positions
 // are read through the sort's permutation (the reorder into cell order comes
 // later in the iteration). Until the next sort every particle stays within
@@ -2411,7 +2416,7 @@ __global__ void __launch_bounds__(kPassThreads)
                 if (!(dr2 < __fmul_rn(lim, lim))) continue;
                 const float hs = xi.w + xb[u].w;  // the density pass's near test
                 const bool near =
-                    DIM == 3 || dr2 < (0.25f * near_q<DIM>() * near_q<DIM>()) * hs * hs;
+                    DIM == 3 || dr2 < (0.25f * list_near_q2() * list_near_q2()) * hs * hs;
                 if (cn + cf < B.lcap) B.nlist[(size_t)(near ? cn : B.lcap - 1 - cf) * B.lstride + s] = k;
                 if (near) ++cn;
                 else ++cf;
