@@ -119,3 +119,25 @@ def test_fluid_input_density_and_pressure_unused(name, pinned):
             ctx.step(arr, c.dt, 2)
     for f in FIELDS:
         assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f))), f
+
+
+def test_pinned_step_calls_on_a_caller_stream():
+    """The overlapped one-iteration calls with the context on a caller's
+    stream: the second stream's copies are ordered by events after the
+    caller's earlier work and joined back before the call returns."""
+    import torch
+
+    c = small("dambreak")
+    a = pinned_copy(c)
+    b = pinned_copy(c)
+    s = torch.cuda.Stream()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        for its in range(1, 5):
+            ctx.step(a, c.dt, its)
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_stream(s.cuda_stream)
+        for its in range(1, 5):
+            ctx.step(b, c.dt, its)
+        ctx.set_stream(0)
+    for f in FIELDS:
+        assert np.array_equal(np.asarray(getattr(a, f)), np.asarray(getattr(b, f))), f
