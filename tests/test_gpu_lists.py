@@ -2,10 +2,12 @@
 
 With a sort skin, the iterations that sort build, for every particle, the list
 of candidates within h_i + h_j + skin (k_build_list); until the next sort the
-passes read the lists instead of walking the cells. A listed particle's
-density pass evaluates each entry in float-float as it reads it and keeps the
-terms of the entries that pass the pair test; its force pass does the same
-with the pair forces. The neighbour sets are the cell walk's; the summation
+passes read the lists instead of walking the cells. A 2D list holds its near
+entries (q < 1.5 at the sort) first and its far ones after them. A listed
+particle's density pass evaluates each near entry in float-float and each far
+one in FP32 with a float-float prefactor, as it reads it (the kernel is zero
+beyond its support); its force pass takes the pair forces of the entries that
+pass the pair test. The neighbour sets are the cell walk's; the summation
 order and (2D) the far pairs' arithmetic differ, so the gates are the oracle
 for one iteration and the cell walk to 1e-5 over many. Particles whose list
 would exceed its capacity walk their cells (a compressed clump).
