@@ -95,6 +95,35 @@ def test_listed_iteration_parity_2d(O, tuning):
         assert rel_err(getattr(got, f), getattr(ref, f)) <= 1e-5, (tuning, f)
 
 
+@pytest.mark.parametrize("tuning", [(1, 1, 128, 10), (3, 1, 256, 10)])
+def test_listed_iteration_parity_2d_variable_h(O, tuning):
+    """Lists over fluid particles whose h differ (seeded, +-10%): the near
+    entries' float-float path and the far entries' FP32 path with the pair's
+    own h = (h_i + h_j)/2 and prefactor. One iteration on the lists (it does not
+    sort) against one FP64 oracle iteration from the same FP32 state."""
+    c0 = cases.perturbed(cases.dam_break(dx=0.01), seed=72, dv=0.05)
+    rng = np.random.default_rng(73)
+    fl = c0.itype > 0
+    c0.h = np.where(fl, c0.h * (1.0 + 0.1 * (2.0 * rng.random(c0.n) - 1.0)),
+                    c0.h).astype(np.float32)
+    c = history_state(O, c0, steps=2)
+    mid = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(*tuning)
+        ctx.step(mid, c.dt, 3)
+    ref = O.State(mid)
+    O.step(ref, 4, c.dt)
+    got = c.copy()
+    with ag.Context(c.params, c.n_fluid, c.n_wall) as ctx:
+        ctx.set_tuning(*tuning)
+        ctx.integrate(got, c.dt, 3, 2)
+        assert ctx.stats().sorts_done == 1
+    for f in FIELDS:
+        err = rel_err(getattr(got, f), getattr(ref, f))
+        print(tuning, "variable h", f, f"{err:.2e}")
+        assert err <= 1e-5, (tuning, f, err)
+
+
 def _with_extra_copies(c, idx, offsets):
     """c with copies of particles idx added at each offset (in units of the
     lattice spacing): a locally two- or three-fold denser patch."""
