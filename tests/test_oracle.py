@@ -99,3 +99,31 @@ def test_first_step_half_kick(O):
     assert np.allclose(s.v[fl], v0[fl] + 0.5 * c.dt * s.dvdt[fl], rtol=0, atol=1e-14)
     assert np.allclose(s.x[fl], x0[fl] + c.dt * s.v[fl], rtol=0, atol=1e-14)
     assert np.array_equal(s.x[~fl], x0[~fl]) and np.array_equal(s.v[~fl], v0[~fl])
+
+
+@pytest.mark.parametrize("name", ["dambreak", "channel3d", "cavity"])
+def test_fluid_input_density_and_pressure_unused_under_summation(O, name):
+    """Under summation density (density.f:1-62) a step recomputes every fluid
+    particle's density and, by the equation of state, its pressure before any
+    term reads them: the oracle's step from NaN fluid inputs rho and p equals
+    the step from the real ones. (The device step therefore does not read
+    them; walls keep theirs.)"""
+    if name == "dambreak":
+        c = cases.perturbed(cases.dam_break(dx=0.04), seed=81, dv=0.05)
+    elif name == "cavity":
+        c = cases.perturbed(cases.cavity(n_side=16), seed=82, dv=1e-4)
+    else:
+        c = cases.perturbed(cases.channel(n_x=12, n_yz=5, length=12 * 7.9e-4,
+                                          width=5 * 7.9e-4, layers=2, jitter=0.05),
+                            seed=83, dv=0.02, du=50.0)
+    assert c.params.density_form == 0 and c.params.scheme == 0
+    bad = c.copy()
+    fl = bad.itype > 0
+    bad.rho = np.where(fl, np.float32(np.nan), bad.rho).astype(np.float32)
+    bad.p = np.where(fl, np.float32(np.nan), bad.p).astype(np.float32)
+    for its in (1, 2):
+        a, b = O.State(c), O.State(bad)
+        O.step(a, its, c.dt)
+        O.step(b, its, c.dt)
+        for f in ("x", "v", "rho", "p", "u", "dvdt", "dudt"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), (name, its, f)
